@@ -1,0 +1,133 @@
+"""ctypes front end of the C oracle (``oracle/walk_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py``.  The product never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, '_build', 'liboracle_walk.so')
+
+RECORD_DTYPE = np.dtype([
+    ('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float64),
+    ('theta_n', np.float64), ('phi_n', np.float64), ('path_length', np.float64),
+    ('snow_depth', np.float64), ('n_draws', np.int64), ('phi_undefined', np.int32),
+    ('pad', np.int32)])
+
+
+class Table(ctypes.Structure):
+    _fields_ = [('wvl', ctypes.c_void_p), ('ssa', ctypes.c_void_p), ('ext', ctypes.c_void_p),
+                ('asm_', ctypes.c_void_p), ('n', ctypes.c_int32)]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [('n_photon', ctypes.c_int64), ('wvl0', ctypes.c_double),
+                ('half_width', ctypes.c_double), ('theta0_deg', ctypes.c_double),
+                ('tau_tot', ctypes.c_double), ('imp_cnc', ctypes.c_double),
+                ('rho_snw', ctypes.c_double), ('rho_ice', ctypes.c_double),
+                ('lam_surface', ctypes.c_int32), ('lam_bottom', ctypes.c_int32),
+                ('R', ctypes.c_double), ('ssa_ice_override', ctypes.c_double),
+                ('g_override', ctypes.c_double), ('ext_ice_override', ctypes.c_double),
+                ('ssa_imp_override', ctypes.c_double), ('ext_imp_override', ctypes.c_double)]
+
+
+def build():
+    """Compile the oracle (make, gcc) into oracle/_build."""
+    subprocess.run(['make', '-s', '-C', HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_uniform.restype = ctypes.c_double
+        L.orc_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_wavelength.restype = ctypes.c_double
+        L.orc_wavelength.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double]
+        L.orc_philox4x32_10.argtypes = [ctypes.c_void_p] * 3
+        L.orc_walk_range.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Table),
+                                     ctypes.POINTER(Table), ctypes.c_uint64, ctypes.c_int64,
+                                     ctypes.c_int64, ctypes.c_void_p]
+        L.orc_walk_threads.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Table),
+                                       ctypes.POINTER(Table), ctypes.c_uint64, ctypes.c_int64,
+                                       ctypes.c_int, ctypes.c_void_p]
+        L.orc_walk_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def philox(ctr, key):
+    c = np.asarray(ctr, dtype=np.uint32)
+    k = np.asarray(key, dtype=np.uint32)
+    out = np.zeros(4, dtype=np.uint32)
+    lib().orc_philox4x32_10(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    return out
+
+
+class _Tables:
+    """Keeps the numpy arrays of two SSP tables alive while C reads them."""
+
+    def __init__(self, ice, imp):
+        self.arrays = []
+
+        def mk(t):
+            cols = [np.ascontiguousarray(t.wvl, dtype=np.float64),
+                    np.ascontiguousarray(t.ss_alb, dtype=np.float64),
+                    np.ascontiguousarray(t.ext_cff_mss, dtype=np.float64),
+                    np.ascontiguousarray(t.asm_prm, dtype=np.float64)]
+            self.arrays.extend(cols)
+            return Table(cols[0].ctypes.data, cols[1].ctypes.data, cols[2].ctypes.data,
+                         cols[3].ctypes.data, cols[0].size)
+        self.ice = mk(ice)
+        self.imp = mk(imp)
+
+
+def make_config(n_photon, wvl0, half_width, theta0_deg, tau_tot, imp_cnc=0.0, rho_snw=300.0,
+                rho_ice=917.0, lam_surface=False, lam_bottom=True, R=1.0,
+                ssa_ice_override=np.nan, g_override=np.nan, ext_ice_override=np.nan,
+                ssa_imp_override=np.nan, ext_imp_override=np.nan):
+    return Config(int(n_photon), wvl0, half_width, theta0_deg, tau_tot, imp_cnc, rho_snw, rho_ice,
+                  int(bool(lam_surface)), int(bool(lam_bottom)), R, ssa_ice_override,
+                  g_override, ext_ice_override, ssa_imp_override, ext_imp_override)
+
+
+def walk(cfg, ice, imp, seed, p0=0, p1=None, threads=1):
+    """FP64 replay walk of photons [p0, p1) -> structured array (RECORD_DTYPE)."""
+    if p1 is None:
+        p1 = cfg.n_photon
+    tabs = _Tables(ice, imp)
+    out = np.zeros(p1 - p0, dtype=RECORD_DTYPE)
+    if threads > 1 and p0 == 0:
+        rc = lib().orc_walk_threads(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
+                                    int(seed), int(p1), int(threads), out.ctypes.data)
+        if rc:
+            raise RuntimeError('oracle thread start failed')
+    else:
+        lib().orc_walk_range(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
+                             int(seed), int(p0), int(p1), out.ctypes.data)
+    return out
+
+
+def config_from_golden(g):
+    """Config of a golden fixture (tests/golden/*.npz)."""
+    p = lambda k: g['param_' + k].item()  # noqa: E731
+    return make_config(p('n_photon'), p('wvl0'), p('half_width'), p('theta0'), p('tau_tot'),
+                       p('imp_cnc'), p('rho_snw'), p('rho_ice'), p('lam_surface'),
+                       p('lam_bottom'), p('R'), ssa_ice_override=p('ssa_ice_override'),
+                       g_override=p('g_override'))
+
+
+def tables_from_golden(g):
+    from monte_carlompi_gb300.ssp import SSPTable
+    ice = SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'])
+    imp = SSPTable(g['imp_wvl'], g['imp_ssa'], g['imp_ext'], None)
+    return ice, imp

@@ -1,0 +1,357 @@
+/*
+ * CPU restatement of the reference photon random walk, in plain C (FP64).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests/, the smoke check
+ * and the CPU-baseline leg of bench.py load it (through ctypes) to check the
+ * CUDA kernels and to time a CPU implementation of the same path.  Nothing in
+ * the product links or calls it.
+ *
+ * Parity is pinned: the .npz fixtures under tests/golden hold per-photon answers of the
+ * unmodified reference (monte_carloMPI/monte_carlo3D.py) run on the same
+ * replay stream, and tests/test_oracle.py checks this file against them.
+ *
+ * Each function cites the reference lines it restates.  The arithmetic keeps
+ * the reference's operation order; compile with -ffp-contract=off so no
+ * multiply-add is fused.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_TAG_WALK 0u
+#define ORC_TAG_WVL 1u
+
+static const double ORC_PI = 3.141592653589793;
+static const double ORC_TWO_PI = 6.283185307179586; /* 2*np.pi, monte_carlo3D.py:26 */
+
+/* ---------------------------------------------------------------- Philox */
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* Uniform k of stream `tag` for `photon`: block k>>1, 64-bit word k&1,
+ * ((word >> 12) + 0.5) * 2^-52 in [2^-53, 1 - 2^-53]. */
+double orc_uniform(uint64_t seed, uint32_t tag, uint64_t photon, uint64_t k)
+{
+    uint32_t ctr[4] = {(uint32_t)(k >> 1), tag, (uint32_t)photon, (uint32_t)(photon >> 32)};
+    uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t x[4];
+    orc_philox4x32_10(ctr, key, x);
+    int j = (int)(k & 1u);
+    uint64_t w = ((uint64_t)x[2 * j + 1] << 32) | x[2 * j];
+    return ((double)(w >> 12) + 0.5) * 0x1p-52;
+}
+
+/* Sequential reader over one photon's walk stream. */
+typedef struct {
+    uint64_t seed, photon, k;
+    int have;             /* block index cached in x[] */
+    uint64_t block;
+    uint32_t x[4];
+} orc_stream;
+
+static double stream_next(orc_stream *s)
+{
+    uint64_t b = s->k >> 1;
+    if (!s->have || b != s->block) {
+        uint32_t ctr[4] = {(uint32_t)b, ORC_TAG_WALK, (uint32_t)s->photon, (uint32_t)(s->photon >> 32)};
+        uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
+        orc_philox4x32_10(ctr, key, s->x);
+        s->block = b;
+        s->have = 1;
+    }
+    int j = (int)(s->k & 1u);
+    uint64_t w = ((uint64_t)s->x[2 * j + 1] << 32) | s->x[2 * j];
+    s->k++;
+    return ((double)(w >> 12) + 0.5) * 0x1p-52;
+}
+
+/* ---------------------------------------------------------------- types */
+typedef struct {
+    const double *wvl;   /* metres */
+    const double *ssa;
+    const double *ext;
+    const double *asm_;  /* may be NULL (impurity) */
+    int32_t n;
+} orc_table;
+
+typedef struct {
+    int64_t n_photon;
+    double wvl0, half_width, theta0_deg, tau_tot, imp_cnc, rho_snw, rho_ice;
+    int32_t lam_surface, lam_bottom;
+    double R;
+    /* run(test=True) overrides (monte_carlo3D.py:1553-1573); NaN = from table */
+    double ssa_ice_override, g_override, ext_ice_override, ssa_imp_override, ext_imp_override;
+} orc_config;
+
+typedef struct {
+    int32_t condition, n_scat;
+    double wvn, theta_n, phi_n, path_length, snow_depth;
+    int64_t n_draws;      /* uniforms consumed from the walk stream */
+    int32_t phi_undefined;/* reference would raise: mux or muy exactly 0 (monte_carlo3D.py:1472-1485) */
+    int32_t pad;
+} orc_record;
+
+/* ---------------------------------------------------------------- lookups */
+
+/* Two nearest table points by |wvl - wvl_tab|, then scipy interp1d's linear
+ * form between them; nearest value when wvl lies outside that pair
+ * (interp1d raises ValueError).  monte_carlo3D.py:594-616 (ice) and :688-711
+ * (impurity); scipy interp1d._call_linear for the formula. */
+static void nearest_two(const orc_table *t, double wvl, int32_t *i0, int32_t *i1)
+{
+    int32_t a = -1, b = -1;
+    double da = INFINITY, db = INFINITY;
+    for (int32_t i = 0; i < t->n; ++i) {
+        double d = fabs(wvl - t->wvl[i]);
+        if (d < da) { b = a; db = da; a = i; da = d; }
+        else if (d < db) { b = i; db = d; }
+    }
+    *i0 = a; *i1 = b;
+}
+
+static double interp_two(const orc_table *t, const double *y, int32_t i0, int32_t i1, double wvl)
+{
+    double x0 = t->wvl[i0], x1 = t->wvl[i1], y0 = y[i0], y1 = y[i1];
+    double xl, xh, yl, yh;
+    if (x0 < x1) { xl = x0; xh = x1; yl = y0; yh = y1; }
+    else { xl = x1; xh = x0; yl = y1; yh = y0; }
+    if (wvl < xl || wvl > xh) return y0;            /* ValueError -> nearest */
+    return ((wvl - xl) / (xh - xl)) * yh + ((xh - wvl) / (xh - xl)) * yl;
+}
+
+/* Photon wavelength on the replay stream: monte_carlo3D.py:1516-1520.
+ * scale = FWHM / 2.355; np.around(x, 2) == rint(x * 100) / 100. */
+double orc_wavelength(uint64_t seed, uint64_t photon, double wvl0, double half_width)
+{
+    double scale = half_width / 2.355;
+    double u0 = orc_uniform(seed, ORC_TAG_WVL, photon, 0);
+    double u1 = orc_uniform(seed, ORC_TAG_WVL, photon, 1);
+    double z = sqrt(-2.0 * log(u0)) * cos(ORC_TWO_PI * u1);
+    double x = wvl0 + scale * z;
+    return nearbyint(x * 100.0) / 100.0;
+}
+
+/* Per-photon optics: monte_carlo3D.py:1524-1612. */
+typedef struct { double wvl, ssa_ice, ssa_imp, g, ext_cff_mss, P_ext_imp, snow_depth; } orc_optics;
+
+static orc_optics photon_optics(const orc_config *c, const orc_table *ice, const orc_table *imp, double wvl_um)
+{
+    orc_optics o;
+    double w = wvl_um * 1e-6;
+    int32_t i0, i1;
+    nearest_two(ice, w, &i0, &i1);
+    double ssa_ice = interp_two(ice, ice->ssa, i0, i1, w);
+    double ext_ice = interp_two(ice, ice->ext, i0, i1, w);
+    double g = interp_two(ice, ice->asm_, i0, i1, w);
+    nearest_two(imp, w, &i0, &i1);
+    double ssa_imp = interp_two(imp, imp->ssa, i0, i1, w);
+    double ext_imp = interp_two(imp, imp->ext, i0, i1, w);
+    if (!isnan(c->ssa_ice_override)) ssa_ice = c->ssa_ice_override;
+    if (!isnan(c->ext_ice_override)) ext_ice = c->ext_ice_override;
+    if (!isnan(c->g_override)) g = c->g_override;
+    if (!isnan(c->ssa_imp_override)) ssa_imp = c->ssa_imp_override;
+    if (!isnan(c->ext_imp_override)) ext_imp = c->ext_imp_override;
+    double cnc = c->imp_cnc;
+    o.wvl = wvl_um;
+    o.ssa_ice = ssa_ice;
+    o.ssa_imp = ssa_imp;
+    o.g = g;
+    o.ext_cff_mss = ext_ice * (1 - cnc) + ext_imp * cnc;                       /* :1577 */
+    o.P_ext_imp = (cnc * ext_imp) / (cnc * ext_imp + (1 - cnc) * ext_ice);     /* :1580-1581 */
+    o.snow_depth = c->tau_tot / (o.ext_cff_mss * c->rho_snw);                  /* :1612 */
+    return o;
+}
+
+/* Henyey_Greenstein2, monte_carlo3D.py:790-800. */
+static double hg2(double g, double r)
+{
+    if (g == 0) return 1 - 2 * r;
+    double q = (1 - g * g) / (1 - g + 2 * g * r);
+    return (1. / (2. * g)) * (1 + g * g - q * q);
+}
+
+/* ---------------------------------------------------------------- walk */
+
+/* One photon: MonteCarlo.monte_carlo3D, monte_carlo3D.py:1111-1490 (HG
+ * branch), with the draws of populate_pdfs (:905-1025) and initial_pdfs
+ * (:1027-1044) taken from the replay stream. */
+void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table *imp,
+                     uint64_t seed, uint64_t photon, orc_record *out)
+{
+    double wvl = orc_wavelength(seed, photon, c->wvl0, c->half_width);
+    orc_optics o = photon_optics(c, ice, imp, wvl);
+    double theta0 = (ORC_PI * c->theta0_deg) / 180.;                           /* :1508 */
+
+    orc_stream s = {seed, photon, 0, 0, 0, {0, 0, 0, 0}};
+    /* initial_pdfs: tau, ssa, ext (:1035-1038) */
+    double tau_rand = -log(stream_next(&s));
+    double ssa_rand = stream_next(&s);
+    double ext_rand = stream_next(&s);
+    double p_rand = 0, phi_rand = 0;
+
+    double mux_0 = sin(theta0), muy_0 = 0, muz_0 = -cos(theta0);              /* :1121-1124 */
+    double muz2_0 = muz_0 * muz_0;
+    double mux_n = 0, muy_n = 0, muz_n = 0;
+    double z_prev = 0, path_length = 0;
+    double ext_cff = o.ext_cff_mss * c->rho_snw;                               /* :1355-1356 */
+    int bottom_reflection = 0, condition = 0;
+    int64_t i = 0, i_rand = 0;
+
+    while (condition == 0) {                                                   /* :1212 */
+        i += 1;
+        i_rand += 1;
+        if (i_rand > 1) {                                                      /* :1215-1224 */
+            p_rand = hg2(o.g, stream_next(&s));
+            phi_rand = stream_next(&s) * ORC_TWO_PI;
+            tau_rand = -log(stream_next(&s));
+            ssa_rand = stream_next(&s);
+            ext_rand = stream_next(&s);
+            i_rand = 1;
+        }
+        double dtau = tau_rand;                                                /* :1227 */
+        if (c->lam_surface && i == 1) dtau = 0;
+        double costheta, sintheta, cosphi = 0, sinphi = 0;
+        if (i == 1) {                                                          /* :1232-1237 */
+            costheta = 1; sintheta = 0;
+        } else if (c->lam_surface || bottom_reflection) {                      /* :1238-1250 */
+            mux_0 = 0.; muy_0 = 0.; muz_0 = 1.;
+            for (;;) {
+                double theta_rand = 0 + (ORC_PI / 2 - 0) * stream_next(&s);
+                double r1 = stream_next(&s);
+                if (r1 < 2 * sin(theta_rand) * cos(theta_rand)) {
+                    costheta = cos(theta_rand);
+                    sintheta = sqrt(1 - costheta * costheta);
+                    break;
+                }
+            }
+        } else {                                                               /* :1251-1253 */
+            costheta = p_rand;
+            sintheta = sqrt(1 - costheta * costheta);
+        }
+        if (i > 1) {                                                           /* :1255-1281 */
+            cosphi = cos(phi_rand);
+            sinphi = sin(phi_rand);
+            if (muz_0 == 1) {
+                mux_n = sintheta * cosphi;
+                muy_n = sintheta * sinphi;
+                muz_n = costheta;
+            } else if (muz_0 == -1) {
+                mux_n = sintheta * cosphi;
+                muy_n = -sintheta * sinphi;
+                muz_n = -costheta;
+            } else {
+                double sq = sqrt(1 - muz2_0);
+                mux_n = (sintheta * (mux_0 * muz_0 * cosphi - muy_0 * sinphi)) / sq + mux_0 * costheta;
+                muy_n = (sintheta * (muy_0 * muz_0 * cosphi + mux_0 * sinphi)) / sq + muy_0 * costheta;
+                muz_n = -sq * sintheta * cosphi + muz_0 * costheta;
+            }
+            if (bottom_reflection) bottom_reflection = 0;                      /* :1283-1285 */
+        } else {                                                               /* :1344-1347 */
+            mux_n = mux_0; muy_n = muy_0; muz_n = muz_0;
+        }
+        double z_i = z_prev + dtau * muz_n;                                    /* :1352 */
+        if (i > 1) {                                                           /* :1364-1369 */
+            mux_0 = mux_n; muy_0 = muy_n; muz_0 = muz_n;
+            muz2_0 = muz_0 * muz_0;
+        }
+        path_length += dtau / ext_cff;                                         /* :1372 */
+        int ext_state;
+        double ssa_event;
+        if (ext_rand > o.P_ext_imp) { ext_state = 1; ssa_event = o.ssa_ice; }  /* :1375-1383 */
+        else { ext_state = 2; ssa_event = o.ssa_imp; }
+        if (c->lam_surface) ssa_event = c->R;                                  /* :1385-1387 */
+
+        if (z_i > 0) {                                                         /* :1390-1397 */
+            condition = 1;
+            path_length += -((z_i * dtau) / ((z_i - z_prev) * ext_cff));
+        } else if (z_i < -c->tau_tot) {                                        /* :1399-1459 */
+            path_length += -(((z_i + c->tau_tot) * dtau) / ((z_i - z_prev) * ext_cff));
+            double dtau_correction = -(((z_i + c->tau_tot) / (z_prev - z_i)) * dtau);
+            z_i = z_i - (muz_n * dtau_correction);
+            int direct = (i == 1);
+            if (c->lam_bottom) {
+                double reflectance_rand = stream_next(&s);
+                if (reflectance_rand <= c->R) bottom_reflection = 1;
+                else condition = direct ? 3 : 2;
+            } else {
+                condition = direct ? 3 : 2;
+            }
+        } else if (ssa_rand >= ssa_event) {                                    /* :1461-1466 */
+            condition = (ext_state == 1) ? 4 : 5;
+        }
+        z_prev = z_i;
+    }
+
+    out->condition = condition;
+    out->wvn = 1. / wvl;                                                       /* :1468 */
+    out->theta_n = acos(muz_0);                                                /* :1469 */
+    out->phi_undefined = 0;
+    if (i == 1) out->phi_n = 0.;                                               /* :1472-1485 */
+    else if (mux_0 > 0 && muy_0 > 0) out->phi_n = atan(muy_0 / mux_0);
+    else if (mux_0 < 0 && muy_0 > 0) out->phi_n = atan(muy_0 / mux_0) + ORC_PI;
+    else if (mux_0 < 0 && muy_0 < 0) out->phi_n = atan(muy_0 / mux_0) + ORC_PI;
+    else if (mux_0 > 0 && muy_0 < 0) out->phi_n = atan(muy_0 / mux_0) + ORC_TWO_PI;
+    else { out->phi_n = NAN; out->phi_undefined = 1; }
+    out->n_scat = (int32_t)(i - 1);                                            /* :1487 */
+    out->path_length = path_length;
+    out->snow_depth = o.snow_depth;
+    out->n_draws = (int64_t)s.k;
+    out->pad = 0;
+}
+
+/* Photons [p0, p1) of one run, in order (the loop of monte_carlo3D.py:1613-1616). */
+void orc_walk_range(const orc_config *c, const orc_table *ice, const orc_table *imp,
+                    uint64_t seed, int64_t p0, int64_t p1, orc_record *out)
+{
+    for (int64_t p = p0; p < p1; ++p) orc_walk_photon(c, ice, imp, seed, (uint64_t)p, out + (p - p0));
+}
+
+/* ---------------------------------------------------------------- threads */
+typedef struct {
+    const orc_config *c; const orc_table *ice, *imp; uint64_t seed;
+    int64_t p0, p1; orc_record *out;
+} orc_job;
+
+static void *job_main(void *arg)
+{
+    orc_job *j = (orc_job *)arg;
+    orc_walk_range(j->c, j->ice, j->imp, j->seed, j->p0, j->p1, j->out + j->p0);
+    return NULL;
+}
+
+/* Photons [0, n) split across n_threads like np.array_split (parallelize.py:14-15):
+ * the first n % n_threads shares get one extra photon.  Returns 0 on success. */
+int orc_walk_threads(const orc_config *c, const orc_table *ice, const orc_table *imp,
+                     uint64_t seed, int64_t n, int n_threads, orc_record *out)
+{
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > 1024) n_threads = 1024;
+    pthread_t th[1024];
+    orc_job jobs[1024];
+    int64_t base = n / n_threads, extra = n % n_threads, p = 0;
+    int started = 0, rc = 0;
+    for (int t = 0; t < n_threads; ++t) {
+        int64_t len = base + (t < extra ? 1 : 0);
+        jobs[t] = (orc_job){c, ice, imp, seed, p, p + len, out};
+        p += len;
+        if (pthread_create(&th[t], NULL, job_main, &jobs[t]) != 0) { rc = -1; break; }
+        started++;
+    }
+    for (int t = 0; t < started; ++t) pthread_join(th[t], NULL);
+    if (rc) return rc;
+    return 0;
+}
