@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Throughput of the photon random walk on GB300 (one JSON line on rank 0).
+
+Workload: 1,000,000 photons per GPU, r_eff 250 um, centre wavelength 1.55 um,
+FWHM 0.085 um, incident zenith 60 deg, 0.10 m slab (tau 196.29), Lambertian
+bottom R = 0.5, synthetic sphere SSPs, FP32 Philox walk, 18 x 36 exit
+histogram, per-photon records.  One step = one walk of those photons
+(mcw_walk: SSP lookup table, walk kernel, tallies).
+
+* ``value``: photons/s with the SSP tables and config resident on the device
+  and records written to device memory; per-step device time from CUDA
+  events on the library's stream; L2 flushed (256 MB write) between steps.
+* ``e2e``: the same walk through the public API with host buffers
+  (Walker.walk -> mcw_walk, records copied into pinned host memory), host
+  wall clock per call.
+* ``roofline``: the walk kernel is bound by SM instruction issue (integer
+  Philox rounds, FP32 rotation, SFU), not by HBM or tensor cores.
+* ``cpu_baseline``: the C oracle (an FP64 port of the reference's walk) on all
+  host cores, on a bounded sample of the same workload.
+
+``--impl reference`` times the CPU implementation of the path (the oracle
+port; the reference itself is Python and is not present on the GPU host) on
+all host cores and prints the same line with ``"impl": "reference"``.
+Multi-GPU (torchrun): replicas, each walking its own photon range (weak
+scaling, no data-path collective).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'photons/s & scatter-events/s (1 GB300) vs plain; surrogate BRF/s at ≤2% err'
+N_PER_GPU = 1000000
+SEED = 0x5EED0002
+# algorithmic thread-instructions per scatter event of the FP32 walk: Philox4x32-10
+# (10 rounds x 2 wide multiplies + 2 three-input XORs = 40), four uniform
+# conversions (8), HG inversion (6), sin/cos/sqrt of the angles (6), rotation and
+# renormalisation (25), move, compensated path sum and boundary tests (15).
+ALG_INST_PER_EVENT = 100
+RECORD_BYTES = 32
+
+
+def workload(n=N_PER_GPU):
+    from monte_carlompi_gb300 import ssp
+    from monte_carlompi_gb300.config import WalkConfig
+    lo, hi = ssp.grid_for(1.55, 0.085)
+    ice = ssp.synthetic_ice_table(250.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = 0.10 * ssp.ext_cff_mss_sphere(250.0) * 300.0
+    cfg = WalkConfig(n_photon=n, wvl0=1.55, half_width=0.085, theta0_deg=60.0, tau_tot=tau,
+                     lambertian_reflectance=0.5, rds_snw=250.0)
+    return cfg, ice, imp
+
+
+CONFIG_DESC = {'workload': 'photon walk, 1e6 photons/GPU: r_eff 250 um, lambda0 1.55 um, '
+                           'FWHM 0.085 um, theta0 60 deg, depth 0.10 m (tau 196.29), '
+                           'Lambertian bottom R 0.5, synthetic sphere SSPs, 18x36 BRF bins',
+               'photons_per_gpu': N_PER_GPU, 'mode': 'FP32 Philox4x32-10',
+               'l2': 'flushed between timed steps (256 MB write); records 32 MB/step'}
+
+
+def dist_env():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_sample(n, threads, seed=SEED):
+    """Time the C oracle (FP64 port) on n photons of the workload."""
+    from oracle import oracle
+    cfg, ice, imp = workload(n)
+    c = oracle.make_config(n, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot, R=0.5)
+    t0 = time.perf_counter()
+    rec = oracle.walk(c, ice, imp, seed, threads=threads)
+    dt = time.perf_counter() - t0
+    return dt, int(rec['n_scat'].astype(np.int64).sum())
+
+
+def cpu_baseline(target_s=8.0):
+    from oracle import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    cores = cpu_cores()
+    pilot_n = 20000
+    dt, _ = oracle_sample(pilot_n, cores, seed=SEED + 1)
+    n = int(min(N_PER_GPU, max(pilot_n, pilot_n * target_s / max(dt, 1e-3))))
+    dt, ev = oracle_sample(n, cores)
+    return {'value': n / dt, 'unit': 'photons/s', 'cores': cores, 'kind': 'port',
+            'events_per_s': ev / dt,
+            'sample': '%d of the 1e6 photons (FP64 C oracle, %d threads, %.2f s wall)' % (n, cores, dt)}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith('active'):
+                    reasons.add(name)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), 'measured'
+    return {'hbm_gbs': 6800.0, 'sm_max_mhz': 2070.0}, 'fallback'
+
+
+def committed_traffic():
+    """DRAM bytes per walk launch from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, 'profiles', 'walk_f32_traffic.json')
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get('dram_bytes_per_photon')
+    return None
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    cores = cpu_cores()
+    from oracle import oracle
+    if not os.path.exists(oracle.LIB_PATH):
+        oracle.build()
+    n = 100000
+    for _ in range(args.warmup):
+        oracle_sample(20000, cores, seed=SEED + 7)
+    times, events = [], 0
+    for k in range(args.steps):
+        dt, ev = oracle_sample(n, cores, seed=SEED + k)
+        times.append(dt)
+        events += ev
+    tot = sum(times)
+    value = n * args.steps / tot
+    line = {
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': 'photons/s',
+        'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': 1e3 * tot / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': dict(CONFIG_DESC, sample_photons_per_step=n),
+        'scatter_events_per_s': events / tot,
+        'cpu_baseline': {'value': value, 'unit': 'photons/s', 'cores': cores, 'kind': 'port',
+                         'sample': '%d photons per step of the workload (FP64 C oracle, '
+                                   '%d threads)' % (n, cores)},
+        'e2e': {'value': value, 'unit': 'photons/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    from monte_carlompi_gb300 import replicas
+    from monte_carlompi_gb300.walker import Walker
+
+    full, ice, imp = workload(N_PER_GPU * world)
+    cfg = replicas.shard_configs([full], rank, world)[0]
+    n = cfg.n_photon
+    w = Walker(dev)
+    w.set_tables([ice], imp)
+    dev_records = torch.empty(n * RECORD_BYTES, dtype=torch.uint8, device='cuda')
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device='cuda')
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def step():
+        return w.walk([cfg], SEED, mode='f32', records='device', device_ptr=dev_records.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(dev)
+    clocks.start()
+    barrier()
+    dev_ms, kern_ms, events, launches = [], [], 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        r = step()
+        dev_ms.append(r.stats['device_ms'])
+        kern_ms.append(r.stats['kernel_ms'])
+        events += r.stats['n_events']
+        launches += 2                       # SSP lookup table + walk kernel
+    barrier()
+    clk = clocks.stop()
+    t_dev = sum(dev_ms) / 1e3
+    t_kern = sum(kern_ms) / 1e3
+
+    # e2e: public API, host buffers (pinned), host wall clock per call
+    from monte_carlompi_gb300 import _abi
+    import ctypes
+    host_ptr = ctypes.c_void_p()
+    _abi.check(_abi.load().mcw_host_alloc(n * RECORD_BYTES, ctypes.byref(host_ptr)), what='host alloc')
+    host_buf = (ctypes.c_char * (n * RECORD_BYTES)).from_address(host_ptr.value)
+    host_rec = np.frombuffer(host_buf, dtype=_abi.RECORD32, count=n)
+    for _ in range(max(1, args.warmup)):
+        w.walk([cfg], SEED, mode='f32', records='host', out=host_rec)
+    barrier()
+    e2e_t, h2d, d2h = [], 0, 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = w.walk([cfg], SEED, mode='f32', records='host', out=host_rec)
+        e2e_t.append(time.perf_counter() - t0)
+        h2d, d2h = r.stats['h2d_bytes'], r.stats['d2h_bytes']
+    barrier()
+    _abi.load().mcw_host_free(host_ptr)
+
+    local_stats = np.array([t_dev, t_kern, sum(e2e_t), events], dtype=np.float64)
+    if world > 1:
+        t = torch.tensor(local_stats[:3], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ev = torch.tensor([events], dtype=torch.float64, device='cuda')
+        torch.distributed.all_reduce(ev)
+        local_stats[:3] = t.cpu().numpy()
+        local_stats[3] = float(ev.item())
+    t_dev, t_kern, t_e2e, events_all = local_stats
+    photons_all = N_PER_GPU * world * args.steps
+    value = photons_all / t_dev
+    if rank == 0:
+        peaks, src = measured_peaks()
+        sm_max = float(peaks.get('sm_max_mhz') or 2070.0)
+        ev_per_launch = events_all / args.steps / world
+        kern_s = t_kern / args.steps
+        achieved = ev_per_launch * ALG_INST_PER_EVENT / kern_s / 1e12
+        peak = 152 * 4 * 32 * sm_max * 1e6 / 1e12
+        rec_gbs = (n * RECORD_BYTES) / kern_s / 1e9
+        tb = committed_traffic()
+        line = {
+            'metric': METRIC, 'value': value, 'unit': 'photons/s', 'n_gpus': world,
+            'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t_dev / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+            'data': 'synthetic', 'config': dict(CONFIG_DESC, parallelism='replicas x%d' % world),
+            'scatter_events_per_s': events_all / t_dev,
+            'kernel_ms_per_step': 1e3 * kern_s,
+            'clocks': clk,
+            'gpu_launches': launches,
+            'e2e': {'value': photons_all / t_e2e, 'unit': 'photons/s',
+                    'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
+            'roofline': {
+                'bound': 'issue', 'achieved': achieved, 'peak': peak, 'unit': 'Tinst/s',
+                'frac': achieved / peak,
+                'traffic': (tb * n) if tb else None,
+                'basis': '%d algorithmic thread-instructions per scatter event; peak = 152 SMs x '
+                         '4 schedulers x 32 lanes x %.0f MHz (sm_max_mhz, %s)' % (
+                             ALG_INST_PER_EVENT, sm_max, src),
+                'hbm': {'achieved': rec_gbs, 'peak': peaks.get('hbm_gbs'), 'unit': 'GB/s',
+                        'frac': rec_gbs / float(peaks.get('hbm_gbs') or 6800.0),
+                        'bytes': 'records, 32 B/photon'},
+            },
+        }
+        if not args.no_cpu_baseline:
+            line['cpu_baseline'] = cpu_baseline()
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    w.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -1,0 +1,152 @@
+"""ctypes binding of libmcwalk.so (declarations in include/mcwalk.h).
+
+The library is the only compute path: if it is missing or no CUDA device is
+present, these functions raise instead of falling back to anything else.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, '_lib', 'libmcwalk.so')
+
+MCW_OK = 0
+ERRORS = {-1: 'MCW_ERR_ARG', -2: 'MCW_ERR_CUDA', -3: 'MCW_ERR_BUDGET', -4: 'MCW_ERR_STREAM',
+          -5: 'MCW_ERR_OOM', -6: 'MCW_ERR_STATE'}
+MODE_F32 = 0
+MODE_REPLAY64 = 1
+RECORDS_NONE, RECORDS_HOST, RECORDS_DEVICE = 0, 1, 2
+HIST_NTHETA, HIST_NPHI, HIST_BINS = 18, 36, 648
+WVN_FX_SCALE = 4294967296.0
+
+# names every build of the library must export (the entry points of mcwalk.h)
+EXPORTS = ['mcw_abi_version', 'mcw_version', 'mcw_create', 'mcw_destroy', 'mcw_last_error',
+           'mcw_set_tables', 'mcw_set_launch', 'mcw_get_launch', 'mcw_set_budget', 'mcw_walk',
+           'mcw_brf', 'mcw_autotune', 'mcw_graph_create', 'mcw_graph_launch',
+           'mcw_graph_destroy', 'mcw_host_alloc', 'mcw_host_free', 'mcw_write_csv',
+           'mcw_format_csv']
+
+
+class McwError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__('%s (%d): %s' % (ERRORS.get(code, 'MCW_ERR'), code, msg))
+        self.code = code
+
+
+class BudgetExceeded(McwError):
+    pass
+
+
+class SSPTableC(ctypes.Structure):
+    _fields_ = [('wvl', ctypes.c_void_p), ('ss_alb', ctypes.c_void_p),
+                ('ext_cff_mss', ctypes.c_void_p), ('asm_prm', ctypes.c_void_p),
+                ('n', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+
+
+class ConfigC(ctypes.Structure):
+    _fields_ = [('n_photon', ctypes.c_int64), ('first_photon', ctypes.c_int64),
+                ('wvl0', ctypes.c_double),
+                ('half_width', ctypes.c_double), ('theta0_deg', ctypes.c_double),
+                ('tau_tot', ctypes.c_double), ('imp_cnc', ctypes.c_double),
+                ('rho_snw', ctypes.c_double), ('rho_ice', ctypes.c_double),
+                ('lambertian_reflectance', ctypes.c_double),
+                ('lambertian_surface', ctypes.c_int32), ('lambertian_bottom', ctypes.c_int32),
+                ('ice_table', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('ssa_ice_override', ctypes.c_double), ('g_override', ctypes.c_double),
+                ('ext_ice_override', ctypes.c_double), ('ssa_imp_override', ctypes.c_double),
+                ('ext_imp_override', ctypes.c_double)]
+
+
+class StatsC(ctypes.Structure):
+    _fields_ = [('kernel_ms', ctypes.c_double), ('total_ms', ctypes.c_double),
+                ('device_ms', ctypes.c_double), ('h2d_bytes', ctypes.c_uint64),
+                ('d2h_bytes', ctypes.c_uint64),
+                ('n_photon', ctypes.c_uint64), ('n_events', ctypes.c_uint64),
+                ('max_n_scat', ctypes.c_uint32), ('status', ctypes.c_uint32),
+                ('block_size', ctypes.c_int32), ('blocks_per_sm', ctypes.c_int32),
+                ('regen_chunk', ctypes.c_int32), ('grid', ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class LaunchC(ctypes.Structure):
+    _fields_ = [('block_size', ctypes.c_int32), ('blocks_per_sm', ctypes.c_int32),
+                ('regen_chunk', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+
+
+RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
+                     ('theta_n', np.float32), ('phi_n', np.float32),
+                     ('path_length', np.float32), ('snow_depth', np.float32),
+                     ('config', np.uint32)])
+RECORD64 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float64),
+                     ('theta_n', np.float64), ('phi_n', np.float64),
+                     ('path_length', np.float64), ('snow_depth', np.float64),
+                     ('config', np.uint32), ('flags', np.uint32)])
+TALLY = np.dtype([('n_cond', np.uint64, 6), ('q_cond_fx', np.uint64, 6), ('n_events', np.uint64),
+                  ('max_n_scat', np.uint32), ('reserved', np.uint32),
+                  ('bin_wvn_fx', np.uint64, HIST_BINS), ('bin_count', np.uint32, HIST_BINS)])
+assert RECORD32.itemsize == 32 and RECORD64.itemsize == 56
+assert ctypes.sizeof(ConfigC) == 136 and ctypes.sizeof(StatsC) == 80
+
+_lib = None
+
+
+def load(path=None):
+    """Load libmcwalk.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError('libmcwalk.so is not built (%s); run '
+                           '`python -m monte_carlompi_gb300.build`' % p)
+    L = ctypes.CDLL(p)
+    vp, i32, i64, u64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double
+    sig = {
+        'mcw_abi_version': ([], ctypes.c_int),
+        'mcw_version': ([], ctypes.c_char_p),
+        'mcw_create': ([ctypes.c_int, ctypes.POINTER(vp)], ctypes.c_int),
+        'mcw_destroy': ([vp], ctypes.c_int),
+        'mcw_last_error': ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+        'mcw_set_tables': ([vp, ctypes.POINTER(SSPTableC), i32, ctypes.POINTER(SSPTableC)], ctypes.c_int),
+        'mcw_set_launch': ([vp, ctypes.POINTER(LaunchC)], ctypes.c_int),
+        'mcw_get_launch': ([vp, ctypes.POINTER(LaunchC)], ctypes.c_int),
+        'mcw_set_budget': ([vp, dbl], ctypes.c_int),
+        'mcw_walk': ([vp, ctypes.POINTER(ConfigC), i32, u64, i32, vp, i32, vp,
+                      ctypes.POINTER(StatsC)], ctypes.c_int),
+        'mcw_brf': ([vp, i32, vp, vp], ctypes.c_int),
+        'mcw_autotune': ([vp, ctypes.POINTER(ConfigC), i32, u64, ctypes.POINTER(LaunchC),
+                          ctypes.POINTER(dbl)], ctypes.c_int),
+        'mcw_graph_create': ([vp, ctypes.POINTER(ConfigC), i32, vp, ctypes.POINTER(vp)], ctypes.c_int),
+        'mcw_graph_launch': ([vp, u64, vp, ctypes.POINTER(StatsC)], ctypes.c_int),
+        'mcw_graph_destroy': ([vp], ctypes.c_int),
+        'mcw_host_alloc': ([ctypes.c_size_t, ctypes.POINTER(vp)], ctypes.c_int),
+        'mcw_host_free': ([vp], ctypes.c_int),
+        'mcw_write_csv': ([ctypes.c_char_p, vp, i32, i64, i32], ctypes.c_int),
+        'mcw_format_csv': ([vp, i32, i64, i32, vp, ctypes.c_size_t,
+                            ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = L
+    return L
+
+
+def last_error(ctx):
+    buf = ctypes.create_string_buffer(512)
+    load().mcw_last_error(ctx, buf, 512)
+    return buf.value.decode(errors='replace')
+
+
+def check(rc, ctx=None, what=''):
+    if rc == MCW_OK:
+        return
+    msg = last_error(ctx) if ctx else what
+    if rc == -3:
+        raise BudgetExceeded(rc, msg)
+    raise McwError(rc, msg or what)

@@ -1,0 +1,96 @@
+"""Build libmcwalk.so (CUDA sm_103a + host C++) in-tree with nvcc and g++.
+
+    python -m monte_carlompi_gb300.build [--force] [--verbose]
+
+Objects go to ``monte_carlompi_gb300/_build/``, the library to
+``monte_carlompi_gb300/_lib/libmcwalk.so``.  Translation units compile in
+parallel; a unit is rebuilt when any source or header is newer than its object.
+"""
+import argparse
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, 'csrc')
+BUILD = os.path.join(PKG, '_build')
+LIBDIR = os.path.join(PKG, '_lib')
+LIB = os.path.join(LIBDIR, 'libmcwalk.so')
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+
+# units whose FP64 arithmetic must keep the reference's rounding: no contraction
+NO_FMAD = {'walk_replay.cu', 'ssp_lut.cu'}
+
+
+def nvcc():
+    for cand in (os.environ.get('NVCC'), shutil.which('nvcc'), '/usr/local/cuda/bin/nvcc'):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError('nvcc not found')
+
+
+def _headers():
+    return glob.glob(os.path.join(CSRC, '*.cuh')) + [os.path.join(ROOT, 'include', 'mcwalk.h')]
+
+
+def _stale(obj, src):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(p) > t for p in [src] + _headers())
+
+
+def _compile(src, verbose):
+    name = os.path.basename(src)
+    obj = os.path.join(BUILD, name + '.o')
+    if not _stale(obj, src):
+        return obj, None
+    if name.endswith('.cu'):
+        cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
+        if name in NO_FMAD:
+            cmd.insert(-4, '--fmad=false')
+        if verbose:
+            cmd.insert(-4, '-Xptxas=-v')
+    else:
+        cmd = [os.environ.get('CXX', 'g++'), '-O2', '-std=c++17', '-fPIC', '-Wall', '-c', src, '-o', obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('compile failed: %s\n%s%s' % (' '.join(cmd), r.stdout, r.stderr))
+    return obj, (r.stdout + r.stderr) if verbose else None
+
+
+def build(force=False, verbose=False):
+    """Compile every unit under csrc/ and link libmcwalk.so.  Returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    srcs = sorted(glob.glob(os.path.join(CSRC, '*.cu')) + glob.glob(os.path.join(CSRC, '*.cpp')))
+    if force:
+        for s in srcs:
+            o = os.path.join(BUILD, os.path.basename(s) + '.o')
+            if os.path.exists(o):
+                os.remove(o)
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        results = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    objs = [o for o, _ in results]
+    if verbose:
+        for _, log in results:
+            if log:
+                print(log, file=sys.stderr)
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        cmd = [nvcc(), *ARCH, '-shared', '-o', LIB, *objs, '-lpthread']
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('link failed: %s\n%s%s' % (' '.join(cmd), r.stdout, r.stderr))
+    return LIB
+
+
+if __name__ == '__main__':
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--force', action='store_true')
+    ap.add_argument('--verbose', action='store_true')
+    a = ap.parse_args()
+    print(build(a.force, a.verbose))

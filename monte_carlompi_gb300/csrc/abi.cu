@@ -1,0 +1,742 @@
+// C ABI of libmcwalk: context, tables, walk dispatch, autotuner, CUDA graphs.
+// Declarations and the reference interface each entry point replaces are in
+// include/mcwalk.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mcw_internal.cuh"
+
+using namespace mcw;
+
+static_assert(sizeof(mcw_config) == 136, "mcw_config layout");
+static_assert(sizeof(mcw_record32) == 32, "mcw_record32 layout");
+static_assert(sizeof(mcw_record64) == 56, "mcw_record64 layout");
+static_assert(sizeof(mcw_stats) == 80, "mcw_stats layout");
+static_assert(sizeof(mcw_tally) == 13 * 8 + 8 + 648 * 12, "mcw_tally layout");
+
+namespace {
+
+const char kVersion[] = "libmcwalk 0.1 (sm_103a)";
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap && p) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+        if (e == cudaSuccess) cap = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// Host-side plan of one walk: per-config launch data and the LUT layout.
+struct Plan {
+    std::vector<DevConfig> cfgs;
+    std::vector<int64_t> prefix;
+    std::vector<int32_t> lut_cfg;
+    int64_t total = 0;
+    int32_t lut_total = 0;
+};
+
+struct Counters {
+    unsigned long long work;
+    unsigned int status;
+    unsigned int pad;
+};
+
+}  // namespace
+
+struct mcw_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evs = nullptr, eve = nullptr;
+    char err[512] = {0};
+    // tables
+    DevBuf tabdata, ice_tables;
+    DevTable imp{};
+    int32_t n_ice = 0;
+    bool have_tables = false;
+    // workspace
+    DevBuf cfgs, prefix, lut, lut_cfg, tallies, counters, records;
+    HostBuf h_stage, h_tallies, h_counters;
+    mcw_launch launch{256, 0, 8, 0};
+    double budget_s = 300.0;
+};
+
+struct mcw_graph {
+    mcw_ctx *ctx = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t walk_node = nullptr;
+    cudaKernelNodeParams walk_params{};
+    WalkArgs args{};
+    int32_t n_cfg = 0;
+    int64_t total = 0;
+    int grid = 0, block = 0;
+    DevBuf cfgs, prefix, lut, lut_cfg, tallies, counters;
+    HostBuf h_tallies, h_counters;
+};
+
+namespace {
+
+int set_err(mcw_ctx *ctx, int code, const char *fmt, ...) {
+    if (ctx) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(ctx->err, sizeof(ctx->err), fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+
+#define CUDA_TRY(ctx, call)                                                                      \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess)                                                                   \
+            return set_err((ctx), _e == cudaErrorMemoryAllocation ? MCW_ERR_OOM : MCW_ERR_CUDA,  \
+                           "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
+    } while (0)
+
+bool finite_pos(double x) { return std::isfinite(x) && x > 0; }
+
+// Validate one config the way MonteCarlo.run's inputs must be for the HG
+// sphere path.  Returns nullptr when valid.
+const char *check_config(const mcw_config &c, int32_t n_ice) {
+    if (c.n_photon < 0) return "n_photon < 0";
+    if (c.first_photon < 0 || c.first_photon > (int64_t(1) << kRngConfigShift) - c.n_photon)
+        return "first_photon + n_photon must lie in [0, 2^40]";
+    if (!finite_pos(c.wvl0)) return "wvl0 must be finite and > 0";
+    if (!std::isfinite(c.half_width) || c.half_width < 0) return "half_width must be finite and >= 0";
+    if (!std::isfinite(c.theta0_deg) || c.theta0_deg < 0 || c.theta0_deg >= 90) return "theta0_deg must be in [0, 90)";
+    if (!finite_pos(c.tau_tot)) return "tau_tot must be finite and > 0";
+    if (!std::isfinite(c.imp_cnc) || c.imp_cnc < 0 || c.imp_cnc > 1) return "imp_cnc must be in [0, 1]";
+    if (!finite_pos(c.rho_snw)) return "rho_snw must be finite and > 0";
+    if (!std::isfinite(c.lambertian_reflectance) || c.lambertian_reflectance < 0 || c.lambertian_reflectance > 1)
+        return "lambertian_reflectance must be in [0, 1]";
+    if (c.ice_table < 0 || c.ice_table >= n_ice) return "ice_table out of range";
+    if (!std::isnan(c.ssa_ice_override) && !(c.ssa_ice_override >= 0 && c.ssa_ice_override <= 1)) return "ssa_ice_override must be in [0, 1]";
+    if (!std::isnan(c.ssa_imp_override) && !(c.ssa_imp_override >= 0 && c.ssa_imp_override <= 1)) return "ssa_imp_override must be in [0, 1]";
+    if (!std::isnan(c.g_override) && !(c.g_override > -1 && c.g_override < 1)) return "g_override must be in (-1, 1)";
+    if (!std::isnan(c.ext_ice_override) && !finite_pos(c.ext_ice_override)) return "ext_ice_override must be > 0";
+    if (!std::isnan(c.ext_imp_override) && !(std::isfinite(c.ext_imp_override) && c.ext_imp_override >= 0)) return "ext_imp_override must be >= 0";
+    return nullptr;
+}
+
+constexpr int32_t kMaxLutPerConfig = 1 << 16;
+
+int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
+    if (!cfgs || n_cfg <= 0) return set_err(ctx, MCW_ERR_ARG, "need at least one config");
+    if (n_cfg > (1 << 23)) return set_err(ctx, MCW_ERR_ARG, "at most 2^23 configs per call");
+    plan.cfgs.resize(n_cfg);
+    plan.prefix.resize(n_cfg + 1);
+    plan.lut_cfg.clear();
+    int64_t off = 0;
+    int32_t lut_off = 0;
+    for (int32_t i = 0; i < n_cfg; ++i) {
+        const mcw_config &c = cfgs[i];
+        if (const char *why = check_config(c, ctx->n_ice)) return set_err(ctx, MCW_ERR_ARG, "config %d: %s", i, why);
+        DevConfig d{};
+        d.offset = off;
+        d.n_photon = c.n_photon;
+        d.rng_base = ((uint64_t)i << kRngConfigShift) | (uint64_t)c.first_photon;
+        plan.prefix[i] = off;
+        if (off > INT64_MAX - c.n_photon) return set_err(ctx, MCW_ERR_ARG, "total photon count overflows");
+        off += c.n_photon;
+        const double sigma = c.half_width / 2.355;
+        // wavelength grid of the LUT: lambda = k / 100 um over wvl0 +- 6.5 sigma
+        int64_t klo, khi;
+        if (sigma > 0) {
+            klo = (int64_t)std::floor((c.wvl0 - 6.5 * sigma) * 100.0) - 1;
+            khi = (int64_t)std::ceil((c.wvl0 + 6.5 * sigma) * 100.0) + 1;
+        } else {
+            klo = khi = (int64_t)std::nearbyint(c.wvl0 * 100.0);
+        }
+        klo = std::max<int64_t>(klo, 1);
+        khi = std::max<int64_t>(khi, klo);
+        if (khi - klo + 1 > kMaxLutPerConfig) return set_err(ctx, MCW_ERR_ARG, "config %d: half_width too wide", i);
+        d.k_lo = (int32_t)klo;
+        d.lut_n = (int32_t)(khi - klo + 1);
+        d.lut_off = lut_off;
+        for (int32_t k = 0; k < d.lut_n; ++k) plan.lut_cfg.push_back(i);
+        lut_off += d.lut_n;
+        d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
+                  (c.imp_cnc > 0 ? kFlagImpurity : 0u);
+        d.ice_table = c.ice_table;
+        const double theta0 = (kPi * c.theta0_deg) / 180.;  // monte_carlo3D.py:1508
+        d.wvl0_100 = (float)(c.wvl0 * 100.0);
+        d.sigma_100 = (float)(sigma * 100.0);
+        d.mux0 = (float)std::sin(theta0);
+        d.muz0 = (float)(-std::cos(theta0));
+        d.tau_tot = (float)c.tau_tot;
+        d.R = (float)c.lambertian_reflectance;
+        d.wvl0 = c.wvl0;
+        d.scale = sigma;
+        d.theta0 = theta0;
+        d.mux0_d = std::sin(theta0);
+        d.muz0_d = -std::cos(theta0);
+        d.tau_tot_d = c.tau_tot;
+        d.R_d = c.lambertian_reflectance;
+        d.imp_cnc = c.imp_cnc;
+        d.rho_snw = c.rho_snw;
+        d.ov_ssa_ice = c.ssa_ice_override;
+        d.ov_g = c.g_override;
+        d.ov_ext_ice = c.ext_ice_override;
+        d.ov_ssa_imp = c.ssa_imp_override;
+        d.ov_ext_imp = c.ext_imp_override;
+        plan.cfgs[i] = d;
+    }
+    plan.prefix[n_cfg] = off;
+    plan.total = off;
+    plan.lut_total = lut_off;
+    return MCW_OK;
+}
+
+struct Shape {
+    int grid, block, chunk, bps;
+};
+
+Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, int64_t total) {
+    Shape s;
+    s.block = l.block_size;
+    int occ = walk_f32_max_blocks_per_sm(s.block);
+    if (occ <= 0) occ = 1;
+    s.bps = (l.blocks_per_sm > 0) ? std::min(l.blocks_per_sm, occ) : occ;
+    s.chunk = l.regen_chunk;
+    int64_t grid = (int64_t)ctx->sm_count * s.bps;
+    const int64_t needed = (total + s.block - 1) / s.block;
+    grid = std::max<int64_t>(1, std::min(grid, needed));
+    s.grid = (int)grid;
+    return s;
+}
+
+// Upload a plan into the given buffers through a pinned staging buffer.
+int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &prefix, DevBuf &lut, DevBuf &lut_cfg,
+                DevBuf &tallies, DevBuf &counters, cudaStream_t st, cudaEvent_t start = nullptr,
+                uint64_t *h2d = nullptr) {
+    const size_t n_cfg = plan.cfgs.size();
+    const size_t b_cfg = n_cfg * sizeof(DevConfig);
+    const size_t b_pre = (n_cfg + 1) * sizeof(int64_t);
+    const size_t b_lc = std::max<size_t>(1, plan.lut_cfg.size()) * sizeof(int32_t);
+    CUDA_TRY(ctx, cfgs.ensure(b_cfg));
+    CUDA_TRY(ctx, prefix.ensure(b_pre));
+    CUDA_TRY(ctx, lut.ensure(std::max<size_t>(1, plan.lut_total) * sizeof(LutEntry)));
+    CUDA_TRY(ctx, lut_cfg.ensure(b_lc));
+    CUDA_TRY(ctx, tallies.ensure(n_cfg * sizeof(mcw_tally)));
+    CUDA_TRY(ctx, counters.ensure(sizeof(Counters)));
+    // the staging buffer must not be rewritten while a previous copy reads it
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    CUDA_TRY(ctx, ctx->h_stage.ensure(b_cfg + b_pre + b_lc));
+    char *h = (char *)ctx->h_stage.p;
+    memcpy(h, plan.cfgs.data(), b_cfg);
+    memcpy(h + b_cfg, plan.prefix.data(), b_pre);
+    if (!plan.lut_cfg.empty()) memcpy(h + b_cfg + b_pre, plan.lut_cfg.data(), plan.lut_cfg.size() * sizeof(int32_t));
+    if (start) CUDA_TRY(ctx, cudaEventRecord(start, st));
+    if (h2d) *h2d = b_cfg + b_pre + (plan.lut_cfg.empty() ? 0 : plan.lut_cfg.size() * sizeof(int32_t));
+    CUDA_TRY(ctx, cudaMemcpyAsync(cfgs.p, h, b_cfg, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(ctx, cudaMemcpyAsync(prefix.p, h + b_cfg, b_pre, cudaMemcpyHostToDevice, st));
+    if (!plan.lut_cfg.empty())
+        CUDA_TRY(ctx, cudaMemcpyAsync(lut_cfg.p, h + b_cfg + b_pre, plan.lut_cfg.size() * sizeof(int32_t),
+                                      cudaMemcpyHostToDevice, st));
+    return MCW_OK;
+}
+
+LutArgs lut_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &lut_cfg) {
+    LutArgs la;
+    la.cfgs = (const DevConfig *)cfgs.p;
+    la.n_cfg = (int32_t)plan.cfgs.size();
+    la.lut_total = plan.lut_total;
+    la.lut = (LutEntry *)lut.p;
+    la.lut_cfg = (const int32_t *)lut_cfg.p;
+    la.imp = ctx->imp;
+    la.ice = (const DevTable *)ctx->ice_tables.p;
+    return la;
+}
+
+WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &prefix, DevBuf &lut,
+                   DevBuf &tallies, DevBuf &counters, mcw_record32 *records, int chunk, uint64_t seed) {
+    WalkArgs wa;
+    wa.cfgs = (const DevConfig *)cfgs.p;
+    wa.prefix = (const int64_t *)prefix.p;
+    wa.lut = (const LutEntry *)lut.p;
+    wa.n_cfg = (int32_t)plan.cfgs.size();
+    wa.regen_chunk = chunk;
+    wa.total = plan.total;
+    Counters *cn = (Counters *)counters.p;
+    wa.work = &cn->work;
+    wa.status = &cn->status;
+    wa.records = records;
+    wa.tallies = (mcw_tally *)tallies.p;
+    wa.budget_ns = (unsigned long long)(ctx->budget_s * 1e9);
+    wa.keys = philox_schedule(seed);
+    return wa;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcw_abi_version(void) { return MCW_ABI_VERSION; }
+const char *mcw_version(void) { return kVersion; }
+
+int mcw_create(int device, mcw_ctx **out) {
+    if (!out) return MCW_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return MCW_ERR_CUDA;
+    if (device < 0 || device >= n) return MCW_ERR_ARG;
+    mcw_ctx *ctx = new (std::nothrow) mcw_ctx();
+    if (!ctx) return MCW_ERR_OOM;
+    ctx->device = device;
+    int rc = MCW_OK;
+    do {
+        if (cudaSetDevice(device) != cudaSuccess) { rc = MCW_ERR_CUDA; break; }
+        if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) { rc = MCW_ERR_CUDA; break; }
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = MCW_ERR_CUDA; break; }
+        if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+            cudaEventCreate(&ctx->evs) != cudaSuccess || cudaEventCreate(&ctx->eve) != cudaSuccess) { rc = MCW_ERR_CUDA; break; }
+        if (ctx->h_counters.ensure(sizeof(Counters)) != cudaSuccess) { rc = MCW_ERR_OOM; break; }
+    } while (0);
+    if (rc != MCW_OK) {
+        mcw_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return MCW_OK;
+}
+
+int mcw_destroy(mcw_ctx *ctx) {
+    if (!ctx) return MCW_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->tabdata, &ctx->ice_tables, &ctx->cfgs, &ctx->prefix, &ctx->lut, &ctx->lut_cfg,
+                      &ctx->tallies, &ctx->counters, &ctx->records})
+        b->release();
+    ctx->h_stage.release();
+    ctx->h_tallies.release();
+    ctx->h_counters.release();
+    for (cudaEvent_t e : {ctx->ev0, ctx->ev1, ctx->evs, ctx->eve})
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MCW_OK;
+}
+
+int mcw_last_error(const mcw_ctx *ctx, char *buf, size_t len) {
+    if (!ctx || !buf || len == 0) return MCW_ERR_ARG;
+    snprintf(buf, len, "%s", ctx->err);
+    return MCW_OK;
+}
+
+int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const mcw_ssp_table *imp) {
+    if (!ctx) return MCW_ERR_ARG;
+    if (!ice || n_ice <= 0 || !imp) return set_err(ctx, MCW_ERR_ARG, "need >= 1 ice table and an impurity table");
+    auto check = [](const mcw_ssp_table &t, bool need_asm) -> const char * {
+        if (t.n < 2) return "a table needs at least 2 wavelengths";
+        if (!t.wvl || !t.ss_alb || !t.ext_cff_mss || (need_asm && !t.asm_prm)) return "missing table column";
+        for (int32_t i = 0; i < t.n; ++i) {
+            if (!std::isfinite(t.wvl[i]) || !std::isfinite(t.ss_alb[i]) || !std::isfinite(t.ext_cff_mss[i]))
+                return "non-finite table value";
+            if (need_asm && !std::isfinite(t.asm_prm[i])) return "non-finite table value";
+        }
+        return nullptr;
+    };
+    size_t total = 0;
+    for (int32_t i = 0; i < n_ice; ++i) {
+        if (const char *why = check(ice[i], true)) return set_err(ctx, MCW_ERR_ARG, "ice table %d: %s", i, why);
+        total += 4 * (size_t)ice[i].n;
+    }
+    if (const char *why = check(*imp, false)) return set_err(ctx, MCW_ERR_ARG, "impurity table: %s", why);
+    total += 4 * (size_t)imp->n;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<double> host(total);
+    std::vector<DevTable> tabs(n_ice);
+    CUDA_TRY(ctx, ctx->tabdata.ensure(total * sizeof(double)));
+    CUDA_TRY(ctx, ctx->ice_tables.ensure(n_ice * sizeof(DevTable)));
+    const double *dbase = (const double *)ctx->tabdata.p;
+    size_t o = 0;
+    auto put = [&](const mcw_ssp_table &t, DevTable &d) {
+        const int32_t n = t.n;
+        memcpy(&host[o], t.wvl, n * sizeof(double));
+        memcpy(&host[o + n], t.ss_alb, n * sizeof(double));
+        memcpy(&host[o + 2 * n], t.ext_cff_mss, n * sizeof(double));
+        if (t.asm_prm) memcpy(&host[o + 3 * n], t.asm_prm, n * sizeof(double));
+        else std::fill(host.begin() + o + 3 * n, host.begin() + o + 4 * n, 0.0);
+        d.wvl = dbase + o;
+        d.ssa = dbase + o + n;
+        d.ext = dbase + o + 2 * n;
+        d.asm_ = dbase + o + 3 * n;
+        d.n = n;
+        d.pad = 0;
+        o += 4 * (size_t)n;
+    };
+    for (int32_t i = 0; i < n_ice; ++i) put(ice[i], tabs[i]);
+    DevTable dimp{};
+    put(*imp, dimp);
+    CUDA_TRY(ctx, cudaMemcpy(ctx->tabdata.p, host.data(), total * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(ctx->ice_tables.p, tabs.data(), n_ice * sizeof(DevTable), cudaMemcpyHostToDevice));
+    ctx->imp = dimp;
+    ctx->n_ice = n_ice;
+    ctx->have_tables = true;
+    return MCW_OK;
+}
+
+int mcw_set_launch(mcw_ctx *ctx, const mcw_launch *l) {
+    if (!ctx || !l) return MCW_ERR_ARG;
+    if (l->block_size < 32 || l->block_size > 256 || l->block_size % 32)
+        return set_err(ctx, MCW_ERR_ARG, "block_size must be a multiple of 32 in [32, 256]");
+    if (l->blocks_per_sm < 0 || l->blocks_per_sm > 64) return set_err(ctx, MCW_ERR_ARG, "blocks_per_sm must be in [0, 64]");
+    if (l->regen_chunk < 1 || l->regen_chunk > 32) return set_err(ctx, MCW_ERR_ARG, "regen_chunk must be in [1, 32]");
+    ctx->launch = *l;
+    return MCW_OK;
+}
+
+int mcw_get_launch(const mcw_ctx *ctx, mcw_launch *l) {
+    if (!ctx || !l) return MCW_ERR_ARG;
+    *l = ctx->launch;
+    return MCW_OK;
+}
+
+int mcw_set_budget(mcw_ctx *ctx, double seconds) {
+    if (!ctx) return MCW_ERR_ARG;
+    if (!(seconds > 0) || !std::isfinite(seconds)) return set_err(ctx, MCW_ERR_ARG, "budget must be > 0 s");
+    ctx->budget_s = seconds;
+    return MCW_OK;
+}
+
+int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed, int32_t mode, void *records,
+             int32_t records_where, mcw_tally *tallies, mcw_stats *stats) {
+    if (!ctx) return MCW_ERR_ARG;
+    const auto t_start = std::chrono::steady_clock::now();
+    if (!ctx->have_tables) return set_err(ctx, MCW_ERR_STATE, "mcw_set_tables has not been called");
+    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
+    if (records_where < MCW_RECORDS_NONE || records_where > MCW_RECORDS_DEVICE)
+        return set_err(ctx, MCW_ERR_ARG, "unknown records_where %d", records_where);
+    if (records_where != MCW_RECORDS_NONE && !records) return set_err(ctx, MCW_ERR_ARG, "records is NULL");
+    if (records_where == MCW_RECORDS_DEVICE && ((uintptr_t)records % 16) != 0)
+        return set_err(ctx, MCW_ERR_ARG, "device records must be 16-byte aligned");
+    Plan plan;
+    int rc = make_plan(ctx, cfgs, n_cfg, plan);
+    if (rc) return rc;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    uint64_t h2d = 0;
+    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->lut_cfg, ctx->tallies, ctx->counters, st,
+                     ctx->evs, &h2d);
+    if (rc) return rc;
+    const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
+    void *dev_records = nullptr;
+    if (records_where == MCW_RECORDS_DEVICE) dev_records = records;
+    if (records_where == MCW_RECORDS_HOST && plan.total > 0) {
+        CUDA_TRY(ctx, ctx->records.ensure((size_t)plan.total * rec_size));
+        dev_records = ctx->records.p;
+    }
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->tallies.p, 0, n_cfg * sizeof(mcw_tally), st));
+    CUDA_TRY(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(Counters), st));
+
+    Shape shape{0, 0, 0, 0};
+    if (mode == MCW_MODE_F32) {
+        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->lut_cfg), st));
+        shape = pick_shape(ctx, ctx->launch, plan.total);
+        WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->tallies, ctx->counters,
+                                (mcw_record32 *)dev_records, shape.chunk, seed);
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
+        if (plan.total > 0) CUDA_TRY(ctx, launch_walk_f32(wa, shape.grid, shape.block, st));
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
+    } else {
+        ReplayArgs ra;
+        ra.cfgs = (const DevConfig *)ctx->cfgs.p;
+        ra.prefix = (const int64_t *)ctx->prefix.p;
+        ra.n_cfg = n_cfg;
+        ra.pad = 0;
+        ra.total = plan.total;
+        ra.imp = ctx->imp;
+        ra.ice = (const DevTable *)ctx->ice_tables.p;
+        Counters *cn = (Counters *)ctx->counters.p;
+        ra.status = &cn->status;
+        ra.records = (mcw_record64 *)dev_records;
+        ra.tallies = (mcw_tally *)ctx->tallies.p;
+        ra.budget_ns = (unsigned long long)(ctx->budget_s * 1e9);
+        ra.seed = seed;
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
+        CUDA_TRY(ctx, launch_walk_replay(ra, st));
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
+        shape.block = 128;
+        shape.grid = (int)((plan.total + 127) / 128);
+    }
+    if (records_where == MCW_RECORDS_HOST && plan.total > 0)
+        CUDA_TRY(ctx, cudaMemcpyAsync(records, dev_records, (size_t)plan.total * rec_size, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, ctx->h_tallies.ensure(n_cfg * sizeof(mcw_tally)));
+    CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_tallies.p, ctx->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_counters.p, ctx->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, cudaEventRecord(ctx->eve, st));
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    const mcw_tally *ht = (const mcw_tally *)ctx->h_tallies.p;
+    if (tallies) memcpy(tallies, ht, n_cfg * sizeof(mcw_tally));
+    const Counters *hc = (const Counters *)ctx->h_counters.p;
+    float ms = 0.f, dev_ms = 0.f;
+    CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    CUDA_TRY(ctx, cudaEventElapsedTime(&dev_ms, ctx->evs, ctx->eve));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->kernel_ms = ms;
+        stats->device_ms = dev_ms;
+        stats->h2d_bytes = h2d;
+        stats->d2h_bytes = n_cfg * sizeof(mcw_tally) + sizeof(Counters) +
+                           ((records_where == MCW_RECORDS_HOST) ? (uint64_t)plan.total * rec_size : 0);
+        for (int32_t c = 0; c < n_cfg; ++c) {
+            for (int k = 1; k < 6; ++k) stats->n_photon += ht[c].n_cond[k];
+            stats->n_events += ht[c].n_events;
+            stats->max_n_scat = std::max(stats->max_n_scat, ht[c].max_n_scat);
+        }
+        stats->status = hc->status;
+        stats->block_size = shape.block;
+        stats->blocks_per_sm = shape.bps;
+        stats->regen_chunk = shape.chunk;
+        stats->grid = shape.grid;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    }
+    if (hc->status & kStatusBudget)
+        return set_err(ctx, MCW_ERR_BUDGET, "walk stopped by the %.3g s time budget; results are partial", ctx->budget_s);
+    if (hc->status & kStatusStream)
+        return set_err(ctx, MCW_ERR_STREAM, "a replay photon exhausted its 2^33-uniform stream");
+    return MCW_OK;
+}
+
+int mcw_brf(const mcw_tally *t, int32_t n_cfg, double *brf, double *albedo) {
+    if (!t || n_cfg <= 0) return MCW_ERR_ARG;
+    double w[MCW_HIST_NTHETA], wsum = 0;
+    for (int i = 0; i < MCW_HIST_NTHETA; ++i) {
+        const double mid = (i + 0.5) * (kPi / 2) / MCW_HIST_NTHETA;
+        w[i] = std::sin(mid) * std::cos(mid);
+        wsum += w[i];
+    }
+    for (int32_t c = 0; c < n_cfg; ++c) {
+        double q_down = 0;
+        for (int k = 1; k < 6; ++k) q_down += (double)t[c].q_cond_fx[k];
+        if (albedo) albedo[c] = q_down > 0 ? (double)t[c].q_cond_fx[1] / q_down : 0.0;
+        if (brf) {
+            for (int i = 0; i < MCW_HIST_NTHETA; ++i)
+                for (int j = 0; j < MCW_HIST_NPHI; ++j) {
+                    const int b = i * MCW_HIST_NPHI + j;
+                    const double wt = w[i] / (MCW_HIST_NPHI * wsum);
+                    brf[(size_t)c * MCW_HIST_BINS + b] = q_down > 0 ? (double)t[c].bin_wvn_fx[b] / (q_down * wt) : 0.0;
+                }
+        }
+    }
+    return MCW_OK;
+}
+
+int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed, mcw_launch *best,
+                 double *best_ms) {
+    if (!ctx || !cfgs || n_cfg <= 0) return MCW_ERR_ARG;
+    const mcw_launch saved = ctx->launch;
+    const int blocks[] = {128, 256};
+    const int chunks[] = {1, 4, 8, 16, 32};
+    mcw_launch win = saved;
+    double win_ms = 1e300;
+    for (int b : blocks) {
+        const int occ = std::max(1, walk_f32_max_blocks_per_sm(b));
+        const int bps_opts[] = {occ, std::max(1, occ / 2)};
+        for (int bi = 0; bi < 2; ++bi) {
+            if (bi == 1 && bps_opts[1] == bps_opts[0]) continue;
+            for (int ch : chunks) {
+                mcw_launch l{b, bps_opts[bi], ch, 0};
+                ctx->launch = l;
+                mcw_stats s;
+                double t = 0;
+                for (int rep = 0; rep < 2; ++rep) {
+                    int rc = mcw_walk(ctx, cfgs, n_cfg, seed + rep, MCW_MODE_F32, nullptr, MCW_RECORDS_NONE, nullptr, &s);
+                    if (rc) {
+                        ctx->launch = saved;
+                        return rc;
+                    }
+                    if (rep) t = s.kernel_ms;
+                }
+                if (t < win_ms) {
+                    win_ms = t;
+                    win = l;
+                }
+            }
+        }
+    }
+    ctx->launch = win;
+    if (best) *best = win;
+    if (best_ms) *best_ms = win_ms;
+    return MCW_OK;
+}
+
+int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_record32 *device_records,
+                     mcw_graph **out) {
+    if (!ctx || !out) return MCW_ERR_ARG;
+    *out = nullptr;
+    if (!ctx->have_tables) return set_err(ctx, MCW_ERR_STATE, "mcw_set_tables has not been called");
+    if (device_records && ((uintptr_t)device_records % 16) != 0)
+        return set_err(ctx, MCW_ERR_ARG, "device records must be 16-byte aligned");
+    Plan plan;
+    int rc = make_plan(ctx, cfgs, n_cfg, plan);
+    if (rc) return rc;
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    mcw_graph *g = new (std::nothrow) mcw_graph();
+    if (!g) return set_err(ctx, MCW_ERR_OOM, "out of host memory");
+    g->ctx = ctx;
+    g->n_cfg = n_cfg;
+    g->total = plan.total;
+    cudaStream_t st = ctx->stream;
+    auto fail = [&](int code) {
+        mcw_graph_destroy(g);
+        return code;
+    };
+    rc = upload_plan(ctx, plan, g->cfgs, g->prefix, g->lut, g->lut_cfg, g->tallies, g->counters, st);
+    if (rc) return fail(rc);
+    if (g->h_tallies.ensure(n_cfg * sizeof(mcw_tally)) != cudaSuccess || g->h_counters.ensure(sizeof(Counters)) != cudaSuccess)
+        return fail(set_err(ctx, MCW_ERR_OOM, "pinned allocation failed"));
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_err(ctx, MCW_ERR_CUDA, "upload failed"));
+    const Shape shape = pick_shape(ctx, ctx->launch, plan.total);
+    g->grid = shape.grid;
+    g->block = shape.block;
+    g->args = walk_args(ctx, plan, g->cfgs, g->prefix, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);
+    const LutArgs la = lut_args(ctx, plan, g->cfgs, g->lut, g->lut_cfg);
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(set_err(ctx, MCW_ERR_CUDA, "stream capture failed to start"));
+    cudaError_t e = cudaMemsetAsync(g->counters.p, 0, sizeof(Counters), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(g->tallies.p, 0, n_cfg * sizeof(mcw_tally), st);
+    if (e == cudaSuccess) e = launch_lut(la, st);
+    if (e == cudaSuccess && plan.total > 0) e = launch_walk_f32(g->args, g->grid, g->block, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->h_tallies.p, g->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->h_counters.p, g->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &g->graph);
+    if (e != cudaSuccess || e2 != cudaSuccess)
+        return fail(set_err(ctx, MCW_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2)));
+    // locate the walk kernel node so each launch can set its seed
+    size_t n_nodes = 0;
+    cudaGraphGetNodes(g->graph, nullptr, &n_nodes);
+    std::vector<cudaGraphNode_t> nodes(n_nodes);
+    cudaGraphGetNodes(g->graph, nodes.data(), &n_nodes);
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
+        cudaKernelNodeParams p;
+        if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) continue;
+        if (p.func == walk_f32_kernel_fn()) {
+            g->walk_node = nd;
+            g->walk_params = p;
+        }
+    }
+    if (plan.total > 0 && !g->walk_node) return fail(set_err(ctx, MCW_ERR_CUDA, "walk node not found in graph"));
+    if (cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess)
+        return fail(set_err(ctx, MCW_ERR_CUDA, "graph instantiation failed"));
+    *out = g;
+    return MCW_OK;
+}
+
+int mcw_graph_launch(mcw_graph *g, uint64_t seed, mcw_tally *tallies, mcw_stats *stats) {
+    if (!g || !g->ctx) return MCW_ERR_ARG;
+    mcw_ctx *ctx = g->ctx;
+    const auto t_start = std::chrono::steady_clock::now();
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    if (g->walk_node) {
+        g->args.keys = philox_schedule(seed);
+        void *kp[1] = {&g->args};
+        cudaKernelNodeParams p = g->walk_params;
+        p.kernelParams = kp;
+        p.extra = nullptr;
+        CUDA_TRY(ctx, cudaGraphExecKernelNodeSetParams(g->exec, g->walk_node, &p));
+    }
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
+    CUDA_TRY(ctx, cudaGraphLaunch(g->exec, st));
+    CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    const mcw_tally *ht = (const mcw_tally *)g->h_tallies.p;
+    if (tallies) memcpy(tallies, ht, g->n_cfg * sizeof(mcw_tally));
+    const Counters *hc = (const Counters *)g->h_counters.p;
+    if (stats) {
+        float ms = 0.f;
+        CUDA_TRY(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        memset(stats, 0, sizeof(*stats));
+        stats->kernel_ms = ms;
+        for (int32_t c = 0; c < g->n_cfg; ++c) {
+            for (int k = 1; k < 6; ++k) stats->n_photon += ht[c].n_cond[k];
+            stats->n_events += ht[c].n_events;
+            stats->max_n_scat = std::max(stats->max_n_scat, ht[c].max_n_scat);
+        }
+        stats->status = hc->status;
+        stats->block_size = g->block;
+        stats->grid = g->grid;
+        stats->regen_chunk = g->args.regen_chunk;
+        stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+    }
+    if (hc->status & kStatusBudget)
+        return set_err(ctx, MCW_ERR_BUDGET, "walk stopped by the %.3g s time budget; results are partial", ctx->budget_s);
+    return MCW_OK;
+}
+
+int mcw_graph_destroy(mcw_graph *g) {
+    if (!g) return MCW_OK;
+    if (g->ctx) {
+        cudaSetDevice(g->ctx->device);
+        cudaStreamSynchronize(g->ctx->stream);
+    }
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    for (DevBuf *b : {&g->cfgs, &g->prefix, &g->lut, &g->lut_cfg, &g->tallies, &g->counters}) b->release();
+    g->h_tallies.release();
+    g->h_counters.release();
+    delete g;
+    return MCW_OK;
+}
+
+int mcw_host_alloc(size_t bytes, void **out) {
+    if (!out || bytes == 0) return MCW_ERR_ARG;
+    *out = nullptr;
+    cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? MCW_ERR_OOM : MCW_ERR_CUDA;
+    return MCW_OK;
+}
+
+int mcw_host_free(void *p) {
+    if (!p) return MCW_OK;
+    return cudaFreeHost(p) == cudaSuccess ? MCW_OK : MCW_ERR_CUDA;
+}
+
+}  // extern "C"

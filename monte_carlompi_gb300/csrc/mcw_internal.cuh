@@ -1,0 +1,149 @@
+// Internal device-side types of libmcwalk.
+#pragma once
+#include <cstdint>
+
+#include "../../include/mcwalk.h"
+#include "philox.cuh"
+
+namespace mcw {
+
+// Philox counter word 1 ("tag") separates the streams of one photon.
+constexpr uint32_t kTagWalk = 0;    // replay: the walk's uniforms
+constexpr uint32_t kTagWvl = 1;     // replay: wavelength Box-Muller
+constexpr uint32_t kTagStep = 2;    // F32: per-step HG, azimuth, path, albedo draws
+constexpr uint32_t kTagSpecies = 3; // F32: ice/impurity draw (only when imp_cnc > 0)
+constexpr uint32_t kTagBottom = 4;  // F32: Lambertian-bottom reflectance draw
+constexpr uint32_t kTagBirth = 5;   // F32: wavelength Box-Muller at photon birth
+
+// Device status bits.
+constexpr uint32_t kStatusBudget = 1u;
+constexpr uint32_t kStatusStream = 2u;
+
+// Config flags.
+constexpr uint32_t kFlagLamSurface = 1u;
+constexpr uint32_t kFlagLamBottom = 2u;
+constexpr uint32_t kFlagImpurity = 4u;  // imp_cnc > 0: the species draw matters
+
+constexpr double kPi = 3.141592653589793;
+constexpr double kTwoPi = 6.283185307179586;  // 2*np.pi (monte_carlo3D.py:26)
+
+// One SSP table as device pointers.
+struct DevTable {
+    const double *wvl, *ssa, *ext, *asm_;
+    int32_t n;
+    int32_t pad;
+};
+
+// Per-config launch data computed on the host from mcw_config.
+struct DevConfig {
+    int64_t offset;       // record index of the config's first photon
+    int64_t n_photon;
+    uint64_t rng_base;    // stream id of photon 0: config << 40 | first_photon
+    int32_t lut_off;      // first LUT entry of this config
+    int32_t lut_n;        // LUT entries (wavelength grid points k_lo .. k_lo+lut_n-1)
+    int32_t k_lo;         // lambda = k / 100 um for LUT entry 0
+    uint32_t flags;
+    int32_t ice_table;
+    int32_t pad;
+    // FP32 walk
+    float wvl0_100;       // wvl0 * 100
+    float sigma_100;      // sigma * 100, sigma = FWHM / 2.355
+    float mux0, muz0;     // initial direction (sin theta0, 0, -cos theta0)
+    float tau_tot, R;
+    // FP64 replay walk
+    double wvl0, scale, theta0, tau_tot_d, R_d, imp_cnc, rho_snw;
+    double mux0_d, muz0_d;  // sin(theta0), -cos(theta0), evaluated on the host
+    double ov_ssa_ice, ov_g, ov_ext_ice, ov_ssa_imp, ov_ext_imp;  // NaN = table
+};
+
+// Optics of one wavelength grid point, FP32 walk.  32 bytes + fixed-point wvn.
+// Co-albedos (1 - ss_alb) are stored so small absorption keeps full precision.
+struct LutEntry {
+    float wvn;        // 1 / lambda [um^-1]
+    float coalb_ice;  // 1 - ssa_ice
+    float coalb_imp;  // 1 - ssa_imp
+    float g;
+    float inv_ext;    // 1 / (ext_cff_mss * rho_snw) [m]
+    float p_imp;      // P_ext_imp
+    float snow_depth; // [m]
+    float pad;
+    unsigned long long wvn_fx;  // wvn * 2^32, rounded
+    unsigned long long pad2;
+};
+
+// Per-warp running totals for the warp's current config (shared memory).
+struct WarpTally {
+    int32_t cfg;          // -1 = empty
+    uint32_t max_n_scat;
+    uint32_t n_cond[6];
+    unsigned long long q_cond_fx[6];
+    unsigned long long n_events;
+};
+
+struct WalkArgs {
+    const DevConfig *cfgs;
+    const int64_t *prefix;       // n_cfg + 1 global photon offsets
+    const LutEntry *lut;
+    int32_t n_cfg;
+    int32_t regen_chunk;
+    int64_t total;               // photons over all configs
+    unsigned long long *work;    // next unclaimed global photon id
+    unsigned int *status;
+    mcw_record32 *records;       // may be null
+    mcw_tally *tallies;          // n_cfg device tallies
+    unsigned long long budget_ns;
+    PhiloxKeys keys;
+};
+
+struct ReplayArgs {
+    const DevConfig *cfgs;
+    const int64_t *prefix;
+    int32_t n_cfg;
+    int32_t pad;
+    int64_t total;
+    DevTable imp;
+    const DevTable *ice;         // device array of ice tables
+    unsigned int *status;
+    mcw_record64 *records;
+    mcw_tally *tallies;
+    unsigned long long budget_ns;
+    uint64_t seed;
+};
+
+struct LutArgs {
+    const DevConfig *cfgs;
+    int32_t n_cfg;
+    int32_t lut_total;
+    LutEntry *lut;
+    const int32_t *lut_cfg;      // config of each LUT entry
+    DevTable imp;
+    const DevTable *ice;
+};
+
+// Kernel launchers (defined in the .cu files).
+cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
+cudaError_t launch_walk_f32(const WalkArgs &a, int grid, int block, cudaStream_t s);
+cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);
+int walk_f32_max_blocks_per_sm(int block);
+const void *walk_f32_kernel_fn();
+size_t walk_f32_smem_bytes(int block);
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+constexpr int kRngConfigShift = 40;  // stream id = config << 40 | photon index
+
+// Config of a global photon id: largest c with prefix[c] <= gid.
+__device__ __forceinline__ int find_config(const int64_t *prefix, int n_cfg, int64_t gid) {
+    int lo = 0, hi = n_cfg - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= gid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+}  // namespace mcw

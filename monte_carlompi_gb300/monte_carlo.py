@@ -1,0 +1,155 @@
+"""Drop-in ``MonteCarlo`` with the reference's constructor and ``run`` signature.
+
+Mirrors monte_carloMPI/monte_carlo3D.py's ``MonteCarlo`` for the
+Henyey-Greenstein sphere path:
+
+* ``MonteCarlo(**model_kwargs)`` reads ``config.ini`` from the working
+  directory when present, then applies keyword overrides (monte_carlo3D.py:
+  43-94).  Command-line arguments are not parsed (a library does not own
+  ``sys.argv``).
+* ``run(n_photon, wvl0, half_width, rds_snw, theta_0=0., ...)`` walks every
+  photon on the GPU through libmcwalk, writes the per-photon CSV under
+  ``output_dir/sphere/`` and prints its path, as :1492-1648 do.  It returns
+  None like the reference; the records, tallies and stats stay on the
+  instance (``records``, ``tallies``, ``stats``, ``output_file``).
+
+Extra keyword arguments (not in the reference): ``device`` (CUDA device),
+``seed`` (None draws one from os.urandom, like the reference's unseeded RNG),
+``mode`` ('f32' production walk or 'replay64' FP64 replay), ``ssp``
+('auto' reads the netCDF tables and falls back to the synthetic tables when
+they are missing, 'file' requires them, 'synthetic' never reads them) and
+``write_csv`` (False skips the file).
+
+Not available (raise): non-sphere shapes and polarised Stokes input (the
+Yang et al. 2013 data are not part of the reference archive), ``debug`` and
+``phase_functions`` (matplotlib figures).
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+from . import csv_io, ssp
+from .config import WalkConfig, read_model_args
+from .walker import Walker
+
+
+class MonteCarlo(object):
+    def __init__(self, **model_kwargs):
+        args = read_model_args('config.ini')
+        extras = dict(device=0, seed=None, mode='f32', ssp='auto', write_csv=True)
+        for k, v in model_kwargs.items():
+            if k in extras:
+                extras[k] = v
+            else:
+                args[k] = v
+        for k, v in args.items():
+            setattr(self, k, v)
+        self.device = extras['device']
+        self.seed = extras['seed']
+        self.mode = extras['mode']
+        self.ssp_source = extras['ssp']
+        self.write_csv = extras['write_csv']
+        if self.mode not in ('f32', 'replay64'):
+            raise ValueError("mode must be 'f32' or 'replay64'")
+        self._walker = None
+        self.records = None
+        self.tallies = None
+        self.stats = None
+        self.output_file = None
+
+    # -- SSP tables (get_optical_properties :498-514, get_impurity_optics :661-671)
+    def _tables(self, wvl0, half_width, rds_snw):
+        base = os.path.join(self.optics_dir, 'mie', 'snicar')
+        ice_path = os.path.join(base, ssp.ice_file_name(rds_snw))
+        imp_path = os.path.join(base, self.fi_imp)
+        have = os.path.exists(ice_path) and os.path.exists(imp_path)
+        if self.ssp_source == 'file' or (self.ssp_source == 'auto' and have):
+            return ssp.read_netcdf(ice_path), ssp.read_netcdf(imp_path)
+        if self.ssp_source == 'auto':
+            sys.stderr.write('SSP tables not found under %s; using the synthetic sphere '
+                             'tables\n' % base)
+        lo, hi = ssp.grid_for(wvl0, half_width)
+        return (ssp.synthetic_ice_table(rds_snw, lo, hi, self.rho_ice),
+                ssp.synthetic_impurity_table(lo, hi))
+
+    def _overrides(self, test):
+        ov = {}
+        if test:  # run(test=True) broadcasts attributes set on the instance (:1553-1573)
+            for attr, key in (('ssa_ice', 'ssa_ice_override'), ('g', 'g_override'),
+                              ('ext_cff_mss_ice', 'ext_ice_override'),
+                              ('ssa_imp', 'ssa_imp_override'),
+                              ('ext_cff_mss_imp', 'ext_imp_override')):
+                v = getattr(self, attr, None)
+                if v is not None and np.ndim(v) == 0:
+                    ov[key] = float(v)
+        return ov
+
+    def walker(self):
+        if self._walker is None:
+            self._walker = Walker(self.device)
+        return self._walker
+
+    def run(self, n_photon, wvl0, half_width, rds_snw, theta_0=0.,
+            stokes_params=np.array([1, 0, 0, 0]), shape='sphere', roughness='smooth', test=False,
+            debug=False, Lambertian_surface=False, Lambertian_bottom=True,
+            Lambertian_reflectance=1.):
+        """Walk n_photon photons and write the per-photon CSV.  ALL VALUES IN MICRONS."""
+        if shape != 'sphere' and not self.HG:
+            raise NotImplementedError('only the Henyey-Greenstein path is built: shape=%r needs '
+                                      'the Yang et al. (2013) phase matrices' % shape)
+        if shape != 'sphere':
+            raise NotImplementedError('aspherical SSP tables are not available')
+        if not np.array_equal(np.asarray(stokes_params), [1, 0, 0, 0]):
+            raise NotImplementedError('HG mode carries the Stokes vector [1, 0, 0, 0] only')
+        if debug:
+            raise NotImplementedError('debug trajectories are matplotlib figures')
+        if self.phase_functions:
+            raise NotImplementedError('phase-function plots are matplotlib figures')
+        self.Lambertian_surface = Lambertian_surface
+        self.Lambertian_bottom = Lambertian_bottom
+        self.R_Lambertian = Lambertian_reflectance
+        self.theta_0 = (np.pi * theta_0) / 180.
+        self.shape = shape
+        self.roughness = roughness
+        self.wvl0 = wvl0
+        self.snow_effective_radius = rds_snw
+
+        ice, imp = self._tables(wvl0, half_width, rds_snw)
+        w = self.walker()
+        w.set_tables([ice], imp)
+        cfg = WalkConfig(n_photon=int(n_photon), wvl0=float(wvl0), half_width=float(half_width),
+                         theta0_deg=float(theta_0), tau_tot=float(self.tau_tot),
+                         imp_cnc=float(self.imp_cnc), rho_snw=float(self.rho_snw),
+                         rho_ice=float(self.rho_ice),
+                         lambertian_reflectance=float(Lambertian_reflectance),
+                         lambertian_surface=bool(Lambertian_surface),
+                         lambertian_bottom=bool(Lambertian_bottom), rds_snw=float(rds_snw),
+                         **self._overrides(test))
+        seed = self.seed
+        if seed is None:
+            seed = int.from_bytes(os.urandom(8), 'little')
+        self.last_seed = seed
+        res = w.walk([cfg], seed, mode=self.mode, records='host')
+        self.records, self.tallies, self.stats = res.records, res.tallies, res.stats
+        if self.write_csv:
+            path = csv_io.output_path(self.output_dir, wvl0, half_width, rds_snw, n_photon,
+                                      csv_io.theta0_label(theta_0))
+            csv_io.write_csv(path, res.records)
+            self.output_file = path
+            print('%s' % path)
+        return None
+
+    def calculate_albedo(self, answers=None):
+        """Black-sky albedo Q_up / Q_down (monte_carlo3D.py:1659-1671) of the last run
+        (or of ``answers``, a record array)."""
+        rec = self.records if answers is None else answers
+        wvn = np.asarray(rec['wvn'], dtype=np.float64)
+        up = wvn[np.asarray(rec['condition']) == 1].sum()
+        down = wvn.sum()
+        return up / down if down > 0 else math.nan
+
+    @classmethod
+    def flatten_list(klass, l):
+        return [item for sublist in l for item in sublist]

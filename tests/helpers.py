@@ -1,0 +1,85 @@
+"""Comparison helpers shared by the parity tests."""
+import numpy as np
+
+from monte_carlompi_gb300 import ssp
+from monte_carlompi_gb300.config import WalkConfig
+
+FLOAT_RTOL = 1e-12   # FP64 replay: float fields, relative
+ANGLE_ATOL = 1e-12   # FP64 replay: direction cosines rebuilt from theta_n / phi_n
+
+
+def compare_replay(got, ref, skip_phi_undefined=True):
+    """Replay parity: condition and n_scat bit-exact; wvn, path_length and
+    snow_depth within FLOAT_RTOL; angles compared through the direction they
+    encode (cos theta, sin theta cos phi, sin theta sin phi), because arccos
+    and the quadrant arctan are ill-conditioned near the poles and axes.
+    Returns a dict of maximum errors; raises AssertionError on failure."""
+    assert np.array_equal(np.asarray(got['condition']), np.asarray(ref['condition']))
+    assert np.array_equal(np.asarray(got['n_scat']), np.asarray(ref['n_scat']))
+    err = {}
+    for k in ('wvn', 'path_length', 'snow_depth'):
+        a = np.asarray(got[k], np.float64)
+        b = np.asarray(ref[k], np.float64)
+        e = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+        err[k] = float(e.max()) if e.size else 0.0
+        assert err[k] <= FLOAT_RTOL, (k, err[k])
+    th_a, th_b = np.asarray(got['theta_n'], np.float64), np.asarray(ref['theta_n'], np.float64)
+    ph_a, ph_b = np.asarray(got['phi_n'], np.float64), np.asarray(ref['phi_n'], np.float64)
+    ok = np.isfinite(ph_a) & np.isfinite(ph_b)
+    da = np.stack([np.cos(th_a), np.sin(th_a) * np.cos(ph_a), np.sin(th_a) * np.sin(ph_a)])
+    db = np.stack([np.cos(th_b), np.sin(th_b) * np.cos(ph_b), np.sin(th_b) * np.sin(ph_b)])
+    e = np.abs(da - db)[:, ok]
+    err['direction'] = float(e.max()) if e.size else 0.0
+    assert err['direction'] <= ANGLE_ATOL, err
+    return err
+
+
+def golden_config(g):
+    p = lambda k: g['param_' + k].item()  # noqa: E731
+    return WalkConfig(n_photon=int(p('n_photon')), wvl0=p('wvl0'), half_width=p('half_width'),
+                      theta0_deg=p('theta0'), tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'),
+                      rho_snw=p('rho_snw'), rho_ice=p('rho_ice'),
+                      lambertian_reflectance=p('R'), lambertian_surface=bool(p('lam_surface')),
+                      lambertian_bottom=bool(p('lam_bottom')),
+                      ssa_ice_override=p('ssa_ice_override'), g_override=p('g_override'))
+
+
+def golden_tables(g):
+    ice = ssp.SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'])
+    imp = ssp.SSPTable(g['imp_wvl'], g['imp_ssa'], g['imp_ext'], None)
+    return ice, imp
+
+
+def condition_fractions_agree(c1, c2, n_sigma=4.0):
+    """Two-sample binomial test of the fraction of each end condition."""
+    n1, n2 = len(c1), len(c2)
+    out = {}
+    for k in range(1, 6):
+        p1, p2 = np.mean(c1 == k), np.mean(c2 == k)
+        p = (p1 * n1 + p2 * n2) / (n1 + n2)
+        sd = np.sqrt(max(p * (1 - p), 1e-300) * (1.0 / n1 + 1.0 / n2))
+        z = abs(p1 - p2) / sd if sd > 0 else 0.0
+        out[k] = (p1, p2, z)
+        assert z <= n_sigma, (k, p1, p2, z)
+    return out
+
+
+def exit_histogram(theta, phi, weights=None):
+    """18 x 36 (theta, phi) histogram of condition-1 exits, 5 x 10 degree bins."""
+    t = np.clip((np.asarray(theta, np.float64) * (36.0 / np.pi)).astype(np.int64), 0, 17)
+    p = np.clip((np.asarray(phi, np.float64) * (18.0 / np.pi)).astype(np.int64), 0, 35)
+    return np.bincount(t * 36 + p, weights=weights, minlength=648)
+
+
+def chi2_two_sample(a, b):
+    """Two-sample chi-square of two count histograms (equal totals not required).
+    Returns (chi2, dof, p-value)."""
+    from scipy.stats import chi2
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = (a + b) > 0
+    a, b = a[m], b[m]
+    ka, kb = np.sqrt(b.sum() / a.sum()), np.sqrt(a.sum() / b.sum())
+    x2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
+    dof = int(m.sum()) - 1
+    return x2, dof, float(chi2.sf(x2, dof))

@@ -1,0 +1,85 @@
+"""The reference-shaped API end to end on the GPU: MonteCarlo(...).run writes the
+per-photon CSV the reference writes."""
+import os
+
+import numpy as np
+import pytest
+
+from monte_carlompi_gb300 import csv_io, ssp
+from monte_carlompi_gb300.monte_carlo import MonteCarlo
+from tests.conftest import GOLDEN, load_golden
+from tests.helpers import compare_replay
+
+pytestmark = pytest.mark.gpu
+
+
+def _write_tables(optics, g, rds):
+    from tests.helpers import golden_tables
+    ice, imp = golden_tables(g)
+    base = os.path.join(optics, 'mie', 'snicar')
+    ssp.write_netcdf(os.path.join(base, ssp.ice_file_name(rds)), ice)
+    ssp.write_netcdf(os.path.join(base, 'imp.nc'), imp, with_asm=False)
+
+
+@pytest.mark.parametrize('name', ['cfg1', 'cfg2'])
+def test_run_replay_reproduces_reference_csv(tmp_path, monkeypatch, capsys, name):
+    """Same tables, same replay stream: the CSV holds the reference's photons."""
+    g = load_golden(name)
+    p = lambda k: g['param_' + k].item()  # noqa: E731
+    monkeypatch.chdir(tmp_path)
+    _write_tables(str(tmp_path / 'optics'), g, p('rds'))
+    mc = MonteCarlo(tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'), rho_snw=p('rho_snw'),
+                    rho_ice=p('rho_ice'), output_dir=str(tmp_path / 'out'),
+                    optics_dir=str(tmp_path / 'optics'), fi_imp='imp.nc', ssp='file',
+                    mode='replay64', seed=int(p('seed')))
+    mc.run(int(p('n_photon')), p('wvl0'), p('half_width'), p('rds'), theta_0=p('theta0'),
+           Lambertian_bottom=bool(p('lam_bottom')), Lambertian_reflectance=p('R'))
+    printed = capsys.readouterr().out.strip()
+    assert os.path.basename(printed) == str(g['csv_name'])
+    got = csv_io.read_csv(printed)
+    compare_replay(got, g)
+    ref = csv_io.read_csv(os.path.join(GOLDEN, name + '.csv'))
+    compare_replay(got, ref)
+    text = open(printed, 'rb').read()
+    assert text.startswith(csv_io.HEADER.encode())
+    assert text.count(b'\n') == int(p('n_photon')) + 1
+
+
+def test_run_f32_synthetic_and_albedo(tmp_path, monkeypatch, capsys):
+    monkeypatch.chdir(tmp_path)
+    mc = MonteCarlo(tau_tot=196.29, output_dir=str(tmp_path / 'out'), ssp='synthetic', seed=5)
+    mc.run(20000, 1.55, 0.085, 250.0, theta_0=60.0, Lambertian_reflectance=0.5)
+    path = capsys.readouterr().out.strip()
+    d = csv_io.read_csv(path)
+    assert d['condition'].size == 20000
+    assert set(np.unique(d['condition'])) <= {1, 2, 3, 4}
+    a = mc.calculate_albedo()
+    t = mc.tallies[0]
+    q = t['q_cond_fx'].astype(np.float64)
+    assert abs(a - q[1] / q[1:].sum()) < 1e-5
+    assert 0.2 < a < 0.9
+
+
+def test_run_test_mode_overrides(tmp_path, monkeypatch):
+    """run(test=True) uses ssa_ice / g set on the instance (the KAT set-up)."""
+    monkeypatch.chdir(tmp_path)
+    mc = MonteCarlo(tau_tot=2.0, imp_cnc=0, output_dir=str(tmp_path / 'o'), ssp='synthetic',
+                    seed=3, write_csv=False)
+    mc.ssa_ice = 0.9
+    mc.g = 0.75
+    mc.run(200000, 0.5, 0.085, 100, test=True, Lambertian_bottom=False)
+    t = mc.tallies[0]
+    n = int(t['n_cond'][1:].sum())
+    assert abs(int(t['n_cond'][1]) / n - 0.09739) < 4 * np.sqrt(0.0974 * 0.9026 / n)
+
+
+def test_unsupported_paths_raise(tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    mc = MonteCarlo(output_dir=str(tmp_path), ssp='synthetic', write_csv=False)
+    with pytest.raises(NotImplementedError):
+        mc.run(10, 1.3, 0.085, 100, shape='droxtal')
+    with pytest.raises(NotImplementedError):
+        mc.run(10, 1.3, 0.085, 100, stokes_params=np.array([1, 1, 0, 0]))
+    with pytest.raises(FileNotFoundError):
+        MonteCarlo(output_dir=str(tmp_path), ssp='file', optics_dir=str(tmp_path / 'none'),
+                   write_csv=False).run(10, 1.3, 0.085, 100)

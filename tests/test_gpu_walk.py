@@ -1,0 +1,295 @@
+"""Parity of the CUDA walk with the oracle and the reference (GPU, through the C ABI).
+
+* FP64 replay: per-photon condition and n_scat bit-exact, float fields within
+  1e-12 relative, against the reference's golden runs and the C oracle.
+* FP32 production walk: condition fractions within 4 sigma (two-sample
+  binomial) and a two-sample chi-square of the 18 x 36 exit histogram
+  (p > 1e-4) against the oracle at the same N.
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+from monte_carlompi_gb300 import _abi, replicas, ssp
+from monte_carlompi_gb300.config import WalkConfig
+from oracle import oracle
+from tests.conftest import golden_names, load_golden
+from tests.helpers import (chi2_two_sample, compare_replay, condition_fractions_agree,
+                           exit_histogram, golden_config, golden_tables)
+
+pytestmark = pytest.mark.gpu
+
+
+def cfg2_geometry(n, depth=0.10, rds=250.0):
+    lo, hi = ssp.grid_for(1.55, 0.085)
+    ice = ssp.synthetic_ice_table(rds, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = depth * ssp.ext_cff_mss_sphere(rds) * 300.0
+    cfg = WalkConfig(n_photon=n, wvl0=1.55, half_width=0.085, theta0_deg=60.0, tau_tot=tau,
+                     lambertian_reflectance=0.5)
+    return cfg, ice, imp
+
+
+def oracle_run(cfg, ice, imp, seed, threads=16):
+    c = oracle.make_config(cfg.n_photon, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot,
+                           cfg.imp_cnc, cfg.rho_snw, cfg.rho_ice, cfg.lambertian_surface,
+                           cfg.lambertian_bottom, cfg.lambertian_reflectance,
+                           ssa_ice_override=cfg.ssa_ice_override, g_override=cfg.g_override)
+    return oracle.walk(c, ice, imp, seed, p0=cfg.first_photon,
+                       p1=cfg.first_photon + cfg.n_photon, threads=threads if cfg.first_photon == 0 else 1)
+
+
+# ---------------------------------------------------------------- FP64 replay
+
+@pytest.mark.parametrize('name', golden_names())
+def test_replay_matches_reference(walker, name):
+    g = load_golden(name)
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    res = walker.walk([golden_config(g)], int(g['param_seed']), mode='replay64')
+    compare_replay(res.records, g)
+    assert not np.any(res.records['flags'])
+
+
+def test_replay_config2_first_10k_matches_oracle(walker):
+    cfg, ice, imp = cfg2_geometry(10000)
+    walker.set_tables([ice], imp)
+    res = walker.walk([cfg], 0x5EED0002, mode='replay64')
+    ref = oracle_run(cfg, ice, imp, 0x5EED0002)
+    err = compare_replay(res.records, ref)
+    assert err['path_length'] < 1e-12
+
+
+def test_replay_shard_equals_slice(walker):
+    g = load_golden('thin')
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    whole = walker.walk([golden_config(g)], 11, mode='replay64').records
+    part = dataclasses.replace(golden_config(g), first_photon=500, n_photon=700)
+    got = walker.walk([part], 11, mode='replay64').records
+    compare_replay(got, whole[500:1200])
+
+
+# ---------------------------------------------------------------- FP32 statistics
+
+STAT_CASES = {
+    # name: (config builder, N)
+    'cfg2': (lambda: cfg2_geometry(0), 200000),
+    'thin': (lambda: cfg2_geometry(0, depth=0.02, rds=1500.0), 200000),
+}
+
+
+def _golden_case(name, n):
+    g = load_golden(name)
+    ice, imp = golden_tables(g)
+    return dataclasses.replace(golden_config(g), n_photon=n), ice, imp
+
+
+@pytest.mark.parametrize('case,n', [('cfg2', 200000), ('thin', 200000), ('kat', 200000),
+                                    ('imp', 100000), ('lamsurf', 50000), ('edge', 50000),
+                                    ('cfg1', 20000)])
+def test_f32_statistics_match_oracle(walker, case, n):
+    if case in STAT_CASES:
+        cfg, ice, imp = STAT_CASES[case][0]()
+        cfg = dataclasses.replace(cfg, n_photon=n)
+    else:
+        cfg, ice, imp = _golden_case(case, n)
+    walker.set_tables([ice], imp)
+    res = walker.walk([cfg], 1234, mode='f32')
+    ref = oracle_run(cfg, ice, imp, 98765)
+    rec = res.records
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    top_g, top_r = rec['condition'] == 1, ref['condition'] == 1
+    h_g = exit_histogram(rec['theta_n'][top_g], rec['phi_n'][top_g])
+    h_r = exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r])
+    x2, dof, p = chi2_two_sample(h_g, h_r)
+    assert p > 1e-4, (x2, dof, p)
+    # mean scatter count and path length within 4 sigma
+    for k in ('n_scat', 'path_length'):
+        a = rec[k].astype(np.float64)
+        b = ref[k].astype(np.float64)
+        sd = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) <= 4 * sd + 1e-6 * abs(b.mean()), (k, a.mean(), b.mean())
+
+
+def test_f32_known_answer_slab(walker):
+    cfg, ice, imp = _golden_case('kat', 1000000)
+    walker.set_tables([ice], imp)
+    res = walker.walk([cfg], 2024, mode='f32', records=None)
+    t = res.tallies[0]
+    n = int(t['n_cond'][1:].sum())
+    assert n == 1000000
+    albedo = res.albedo()[0]
+    trans = (int(t['n_cond'][2]) + int(t['n_cond'][3])) / n
+    assert abs(albedo - 0.09739) < 4 * np.sqrt(0.09739 * 0.90261 / n)
+    assert abs(trans - 0.66096) < 4 * np.sqrt(0.66096 * 0.33904 / n)
+    assert abs(int(t['n_cond'][3]) / n - np.exp(-2)) < 4 * np.sqrt(np.exp(-2) / n)
+
+
+# ---------------------------------------------------------------- FP32 invariants
+
+def test_f32_same_records_for_any_launch_shape(walker):
+    cfg, ice, imp = cfg2_geometry(100000)
+    walker.set_tables([ice], imp)
+    saved = walker.get_launch()
+    try:
+        walker.set_launch(256, 0, 8)
+        a = walker.walk([cfg], 77, mode='f32')
+        walker.set_launch(128, 2, 1)
+        b = walker.walk([cfg], 77, mode='f32')
+        walker.set_launch(64, 1, 32)
+        c = walker.walk([cfg], 77, mode='f32')
+    finally:
+        walker.set_launch(**saved)
+    assert np.array_equal(a.records, b.records) and np.array_equal(a.records, c.records)
+    assert np.array_equal(a.tallies, b.tallies) and np.array_equal(a.tallies, c.tallies)
+
+
+def test_f32_tallies_agree_with_records(walker):
+    cfg, ice, imp = cfg2_geometry(300000, depth=0.02, rds=1500.0)
+    walker.set_tables([ice], imp)
+    res = walker.walk([cfg], 5, mode='f32')
+    rec, t = res.records, res.tallies[0]
+    counts = np.bincount(rec['condition'], minlength=6)
+    assert np.array_equal(counts[1:], t['n_cond'][1:].astype(np.int64))
+    assert int(t['n_events']) == int(rec['n_scat'].astype(np.int64).sum())
+    assert int(t['max_n_scat']) == int(rec['n_scat'].max())
+    top = rec['condition'] == 1
+    th = rec['theta_n'][top].astype(np.float32)
+    ph = rec['phi_n'][top].astype(np.float32)
+    tb = np.clip((th * np.float32(36.0 / np.pi)).astype(np.int64), 0, 17)
+    pb = np.clip((ph * np.float32(18.0 / np.pi)).astype(np.int64), 0, 35)
+    hist = np.bincount(tb * 36 + pb, minlength=648)
+    assert np.array_equal(hist, t['bin_count'].astype(np.int64))
+    q = t['q_cond_fx'].astype(np.float64) / _abi.WVN_FX_SCALE
+    for k in range(1, 6):
+        s = rec['wvn'][rec['condition'] == k].astype(np.float64).sum()
+        assert abs(q[k] - s) <= 1e-6 * max(s, 1.0)
+    assert np.all((rec['phi_n'] >= 0) & (rec['phi_n'] < 2 * np.pi))
+    assert np.all(rec['theta_n'][top] <= np.pi / 2 + 1e-6)
+
+
+def test_f32_shards_equal_whole_run(walker):
+    cfg, ice, imp = cfg2_geometry(99999)
+    walker.set_tables([ice], imp)
+    whole = walker.walk([cfg], 31, mode='f32')
+    world = 3
+    parts, tallies = [], []
+    for r in range(world):
+        res = walker.walk(replicas.shard_configs([cfg], r, world), 31, mode='f32')
+        parts.append(res.records)
+        tallies.append(res.tallies)
+    merged = replicas.merge_records(parts, [cfg], world)
+    keep = [n for n in _abi.RECORD32.names if n != 'config']
+    for k in keep:
+        assert np.array_equal(merged[k], whole.records[k]), k
+    m = replicas.merge_tallies(tallies)
+    for k in ('n_cond', 'q_cond_fx', 'n_events', 'bin_count', 'bin_wvn_fx', 'max_n_scat'):
+        assert np.array_equal(m[k], whole.tallies[k]), k
+
+
+def test_batch_first_config_equals_single_run(walker):
+    a, ice, imp = cfg2_geometry(50000)
+    b = dataclasses.replace(a, theta0_deg=0.0, n_photon=30000)
+    c = dataclasses.replace(a, wvl0=1.45, n_photon=0)
+    d = dataclasses.replace(a, tau_tot=a.tau_tot / 5, n_photon=40000)
+    walker.set_tables([ice], imp)
+    batch = walker.walk([a, b, c, d], 9, mode='f32')
+    alone = walker.walk([a], 9, mode='f32')
+    assert np.array_equal(batch.records[:50000], alone.records)
+    assert np.array_equal(batch.records['config'],
+                          np.repeat(np.arange(4, dtype=np.uint32), [50000, 30000, 0, 40000]))
+    assert int(batch.tallies[2]['n_cond'].sum()) == 0
+    for i, cf in ((1, b), (3, d)):
+        single = walker.walk([cf], 10 + i, mode='f32')
+        lo = 50000 + (30000 if i == 3 else 0)
+        condition_fractions_agree(batch.records['condition'][lo:lo + cf.n_photon],
+                                  single.records['condition'])
+
+
+def test_graph_replays_equal_walks(walker):
+    cfg, ice, imp = cfg2_geometry(200000)
+    cfgs = [cfg, dataclasses.replace(cfg, theta0_deg=30.0, n_photon=100000)]
+    walker.set_tables([ice], imp)
+    g = walker.graph(cfgs)
+    try:
+        for seed in (3, 4):
+            gr = g.launch(seed)
+            wr = walker.walk(cfgs, seed, mode='f32', records=None)
+            assert np.array_equal(gr.tallies, wr.tallies)
+    finally:
+        g.close()
+
+
+def test_device_records(walker):
+    torch = pytest.importorskip('torch')
+    cfg, ice, imp = cfg2_geometry(50000)
+    walker.set_tables([ice], imp)
+    host = walker.walk([cfg], 8, mode='f32').records
+    buf = torch.empty(50000 * 32, dtype=torch.uint8, device='cuda')
+    walker.walk([cfg], 8, mode='f32', records='device', device_ptr=buf.data_ptr())
+    torch.cuda.synchronize()
+    dev = buf.cpu().numpy().view(_abi.RECORD32)
+    assert np.array_equal(dev, host)
+
+
+def test_autotune_picks_a_valid_shape(walker):
+    cfg, ice, imp = cfg2_geometry(50000)
+    walker.set_tables([ice], imp)
+    saved = walker.get_launch()
+    try:
+        best = walker.autotune([cfg])
+        assert best['block_size'] in (128, 256) and 1 <= best['regen_chunk'] <= 32
+        assert best['ms'] > 0
+        assert walker.get_launch()['block_size'] == best['block_size']
+    finally:
+        walker.set_launch(**saved)
+
+
+# ---------------------------------------------------------------- errors
+
+def test_budget_stops_the_kernel_and_context_survives(walker):
+    g = load_golden('cfg1')
+    ice, imp = golden_tables(g)
+    cfg = dataclasses.replace(golden_config(g), n_photon=200000)
+    walker.set_tables([ice], imp)
+    walker.set_budget(1e-4)
+    try:
+        with pytest.raises(_abi.BudgetExceeded):
+            walker.walk([cfg], 1, mode='f32', records=None)
+        with pytest.raises(_abi.BudgetExceeded):
+            walker.walk([dataclasses.replace(cfg, n_photon=2000)], 1, mode='replay64', records=None)
+    finally:
+        walker.set_budget(300.0)
+    ok = walker.walk([dataclasses.replace(cfg, n_photon=1000)], 1, mode='f32')
+    assert int(ok.tallies[0]['n_cond'][1:].sum()) == 1000
+
+
+@pytest.mark.parametrize('bad', [dict(n_photon=-1), dict(wvl0=0.0), dict(half_width=-0.1),
+                                 dict(theta0_deg=90.0), dict(tau_tot=0.0), dict(imp_cnc=1.5),
+                                 dict(lambertian_reflectance=1.5), dict(ice_table=3),
+                                 dict(g_override=1.0), dict(first_photon=-2),
+                                 dict(rho_snw=float('nan'))])
+def test_invalid_config_rejected(walker, bad):
+    cfg, ice, imp = cfg2_geometry(10)
+    walker.set_tables([ice], imp)
+    with pytest.raises(_abi.McwError) as e:
+        walker.walk([dataclasses.replace(cfg, **bad)], 1)
+    assert e.value.code == -1
+
+
+def test_walk_without_tables_is_a_state_error():
+    from monte_carlompi_gb300.walker import Walker
+    with Walker(0) as w:
+        cfg, _, _ = cfg2_geometry(10)
+        with pytest.raises(_abi.McwError) as e:
+            w.walk([cfg], 1)
+        assert e.value.code == -6
+
+
+def test_empty_run(walker):
+    cfg, ice, imp = cfg2_geometry(0)
+    walker.set_tables([ice], imp)
+    res = walker.walk([cfg], 1)
+    assert res.records.size == 0 and int(res.tallies[0]['n_cond'].sum()) == 0
