@@ -111,7 +111,7 @@ class Walker:
         dtype = _abi.RECORD32 if mode_c == _abi.MODE_F32 else _abi.RECORD64
         cfg = configs_to_c(configs)
         n = len(configs)
-        total = int(sum(int(c.n_photon) for c in configs))
+        total = int(sum(max(int(c.n_photon), 0) for c in configs))
         tallies = np.zeros(n, _abi.TALLY)
         stats = _abi.StatsC()
         rec = None

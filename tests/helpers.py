@@ -10,17 +10,23 @@ ANGLE_ATOL = 1e-12   # FP64 replay: direction cosines rebuilt from theta_n / phi
 
 def compare_replay(got, ref, skip_phi_undefined=True):
     """Replay parity: condition and n_scat bit-exact; wvn, path_length and
-    snow_depth within FLOAT_RTOL; angles compared through the direction they
+    snow_depth within FLOAT_RTOL (path_length relative to max(|path|, depth));
+    angles compared through the direction they
     encode (cos theta, sin theta cos phi, sin theta sin phi), because arccos
     and the quadrant arctan are ill-conditioned near the poles and axes.
     Returns a dict of maximum errors; raises AssertionError on failure."""
     assert np.array_equal(np.asarray(got['condition']), np.asarray(ref['condition']))
     assert np.array_equal(np.asarray(got['n_scat']), np.asarray(ref['n_scat']))
     err = {}
+    depth = np.abs(np.asarray(ref['snow_depth'], np.float64))
     for k in ('wvn', 'path_length', 'snow_depth'):
         a = np.asarray(got[k], np.float64)
         b = np.asarray(ref[k], np.float64)
-        e = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+        # path_length: the exit correction cancels the last step, so a path that is
+        # exactly 0 (Lambertian surface) carries rounding residue of the step length;
+        # it is compared relative to max(|path|, slab depth)
+        scale = np.maximum(np.abs(b), depth) if k == 'path_length' else np.abs(b)
+        e = np.abs(a - b) / np.maximum(scale, 1e-300)
         err[k] = float(e.max()) if e.size else 0.0
         assert err[k] <= FLOAT_RTOL, (k, err[k])
     th_a, th_b = np.asarray(got['theta_n'], np.float64), np.asarray(ref['theta_n'], np.float64)
