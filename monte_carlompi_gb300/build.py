@@ -24,6 +24,8 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 
 # units whose FP64 arithmetic must keep the reference's rounding: no contraction
 NO_FMAD = {'walk_replay.cu', 'ssp_lut.cu'}
+# the FP32 production walk: flush denormals, approximate division and square root
+FAST_F32 = {'walk_f32.cu': ['-ftz=true', '-prec-div=false', '-prec-sqrt=false']}
 
 
 def nvcc():
@@ -53,6 +55,8 @@ def _compile(src, verbose):
         cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
         if name in NO_FMAD:
             cmd.insert(-4, '--fmad=false')
+        for flag in FAST_F32.get(name, []):
+            cmd.insert(-4, flag)
         if verbose:
             cmd.insert(-4, '-Xptxas=-v')
     else:

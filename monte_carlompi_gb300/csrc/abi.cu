@@ -233,10 +233,10 @@ struct Shape {
     int grid, block, chunk, bps;
 };
 
-Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, int64_t total) {
+Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, int64_t total, int32_t n_cfg) {
     Shape s;
     s.block = l.block_size;
-    int occ = walk_f32_max_blocks_per_sm(s.block);
+    int occ = walk_f32_max_blocks_per_sm(s.block, n_cfg);
     if (occ <= 0) occ = 1;
     s.bps = (l.blocks_per_sm > 0) ? std::min(l.blocks_per_sm, occ) : occ;
     s.chunk = l.regen_chunk;
@@ -384,22 +384,49 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
         total += 4 * (size_t)ice[i].n;
     }
     if (const char *why = check(*imp, false)) return set_err(ctx, MCW_ERR_ARG, "impurity table: %s", why);
+    {
+        std::vector<int32_t> tmp;
+        auto distinct = [&](const mcw_ssp_table &t) {
+            tmp.resize(t.n);
+            for (int32_t i = 0; i < t.n; ++i) tmp[i] = i;
+            std::stable_sort(tmp.begin(), tmp.end(), [&](int32_t a, int32_t b) { return t.wvl[a] < t.wvl[b]; });
+            for (int32_t i = 1; i < t.n; ++i)
+                if (!(t.wvl[tmp[i]] > t.wvl[tmp[i - 1]])) return false;
+            return true;
+        };
+        for (int32_t i = 0; i < n_ice; ++i)
+            if (!distinct(ice[i])) return set_err(ctx, MCW_ERR_ARG, "ice table %d: repeated wavelength", i);
+        if (!distinct(*imp)) return set_err(ctx, MCW_ERR_ARG, "impurity table: repeated wavelength");
+    }
     total += 4 * (size_t)imp->n;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    // device lookups binary-search the wavelengths: store every table sorted
+    // ascending and require distinct wavelengths
+    auto order_of = [](const mcw_ssp_table &t, std::vector<int32_t> &ord) -> bool {
+        ord.resize(t.n);
+        for (int32_t i = 0; i < t.n; ++i) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return t.wvl[a] < t.wvl[b]; });
+        for (int32_t i = 1; i < t.n; ++i)
+            if (!(t.wvl[ord[i]] > t.wvl[ord[i - 1]])) return false;
+        return true;
+    };
     std::vector<double> host(total);
     std::vector<DevTable> tabs(n_ice);
     CUDA_TRY(ctx, ctx->tabdata.ensure(total * sizeof(double)));
     CUDA_TRY(ctx, ctx->ice_tables.ensure(n_ice * sizeof(DevTable)));
     const double *dbase = (const double *)ctx->tabdata.p;
     size_t o = 0;
+    std::vector<int32_t> ord;
     auto put = [&](const mcw_ssp_table &t, DevTable &d) {
         const int32_t n = t.n;
-        memcpy(&host[o], t.wvl, n * sizeof(double));
-        memcpy(&host[o + n], t.ss_alb, n * sizeof(double));
-        memcpy(&host[o + 2 * n], t.ext_cff_mss, n * sizeof(double));
-        if (t.asm_prm) memcpy(&host[o + 3 * n], t.asm_prm, n * sizeof(double));
-        else std::fill(host.begin() + o + 3 * n, host.begin() + o + 4 * n, 0.0);
+        order_of(t, ord);
+        for (int32_t i = 0; i < n; ++i) {
+            host[o + i] = t.wvl[ord[i]];
+            host[o + n + i] = t.ss_alb[ord[i]];
+            host[o + 2 * n + i] = t.ext_cff_mss[ord[i]];
+            host[o + 3 * n + i] = t.asm_prm ? t.asm_prm[ord[i]] : 0.0;
+        }
         d.wvl = dbase + o;
         d.ssa = dbase + o + n;
         d.ext = dbase + o + 2 * n;
@@ -475,7 +502,7 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     Shape shape{0, 0, 0, 0};
     if (mode == MCW_MODE_F32) {
         CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->lut_cfg), st));
-        shape = pick_shape(ctx, ctx->launch, plan.total);
+        shape = pick_shape(ctx, ctx->launch, plan.total, n_cfg);
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
@@ -574,7 +601,7 @@ int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t s
     mcw_launch win = saved;
     double win_ms = 1e300;
     for (int b : blocks) {
-        const int occ = std::max(1, walk_f32_max_blocks_per_sm(b));
+        const int occ = std::max(1, walk_f32_max_blocks_per_sm(b, n_cfg));
         const int bps_opts[] = {occ, std::max(1, occ / 2)};
         for (int bi = 0; bi < 2; ++bi) {
             if (bi == 1 && bps_opts[1] == bps_opts[0]) continue;
@@ -630,7 +657,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     if (g->h_tallies.ensure(n_cfg * sizeof(mcw_tally)) != cudaSuccess || g->h_counters.ensure(sizeof(Counters)) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_OOM, "pinned allocation failed"));
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_err(ctx, MCW_ERR_CUDA, "upload failed"));
-    const Shape shape = pick_shape(ctx, ctx->launch, plan.total);
+    const Shape shape = pick_shape(ctx, ctx->launch, plan.total, n_cfg);
     g->grid = shape.grid;
     g->block = shape.block;
     g->args = walk_args(ctx, plan, g->cfgs, g->prefix, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);

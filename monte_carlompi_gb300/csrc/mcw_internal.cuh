@@ -124,9 +124,9 @@ struct LutArgs {
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
 cudaError_t launch_walk_f32(const WalkArgs &a, int grid, int block, cudaStream_t s);
 cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);
-int walk_f32_max_blocks_per_sm(int block);
+int walk_f32_max_blocks_per_sm(int block, int n_cfg);
 const void *walk_f32_kernel_fn();
-size_t walk_f32_smem_bytes(int block);
+size_t walk_f32_smem_bytes(int block, int n_cfg);
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;

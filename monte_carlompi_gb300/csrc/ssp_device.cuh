@@ -7,11 +7,23 @@
 namespace mcw {
 
 // The two table points nearest to w (metres); ties keep the lower index.
-// monte_carlo3D.py:594-597 (argsort of |wvl - wvl_in|, first two).
+// monte_carlo3D.py:594-597 (argsort of |wvl - wvl_in|, first two).  Tables are
+// strictly increasing (mcw_set_tables sorts and checks them), so the two
+// nearest points are among the two on either side of w: a binary search finds
+// them, and scanning those four in index order picks the same pair a scan of
+// the whole table would.
 __device__ inline void ssp_nearest_two(const DevTable &t, double w, int &i0, int &i1) {
+    int lo = 0, hi = t.n - 1;  // largest i with wvl[i] <= w, or -1
+    int k = -1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        if (t.wvl[mid] <= w) { k = mid; lo = mid + 1; }
+        else hi = mid - 1;
+    }
     int a = -1, b = -1;
     double da = __longlong_as_double(0x7ff0000000000000LL), db = da;
-    for (int i = 0; i < t.n; ++i) {
+    const int j0 = max(k - 1, 0), j1 = min(k + 2, t.n - 1);
+    for (int i = j0; i <= j1; ++i) {
         double d = fabs(w - t.wvl[i]);
         if (d < da) { b = a; db = da; a = i; da = d; }
         else if (d < db) { b = i; db = d; }

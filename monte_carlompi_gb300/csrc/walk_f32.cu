@@ -3,13 +3,22 @@
 // refills its idle lanes (photon regeneration) so lanes whose photons leave
 // early keep working instead of idling until the warp's longest walk ends.
 //
+// Births and finishes are batched through per-warp shared-memory queues so
+// their expensive parts run with all 32 lanes busy:
+//  * births: when the warp's queue of ready photons runs short, every lane
+//    starts one new photon (Philox + Box-Muller wavelength + SSP lookup) into
+//    the queue; idle lanes then pop a ready photon (a few shared loads);
+//  * finishes: a lane whose photon ends pushes its final state to the warp's
+//    finish queue; once 32 are queued the warp computes theta_n / phi_n,
+//    writes the 32 records and folds the tallies with warp reductions.
+//
 // Per step (monte_carloMPI/monte_carlo3D.py:1212-1466, HG branch) one
 // Philox4x32-10 block keyed by (step, photon) supplies the four uniforms the
 // step needs: HG cosine (:915), azimuth (:921), optical path (:1014) and the
 // absorption draw (:1020).  The ice/impurity draw (:1023) and the bottom
 // reflectance draw (:1422/:1453) take their own blocks only when the config
-// needs them.  Results depend only on (seed, photon id): any launch shape,
-// any number of GPUs or replicas gives the same records.
+// needs them.  Results depend only on (seed, photon stream id): any launch
+// shape, any number of GPUs or replicas gives the same records.
 //
 // Statistically equivalent restatements (identical distributions):
 //  * the Lambertian direction (p(theta) ~ sin 2 theta, :1238-1250) is drawn by
@@ -35,8 +44,9 @@ constexpr float kTwo32Inv = 2.3283064365386963e-10f;  // 2^-32
 constexpr float kTwo33Inv = 1.16415321826934814e-10f; // 2^-33
 constexpr uint32_t kFlagReflect = 8u;                  // bottom reflection pending
 constexpr int kSmemCfgMax = 256;                       // configs staged in shared memory
+constexpr int kFinishCap = 64;                         // finish queue entries per warp
 
-// Per-config values the FP32 walk reads at photon birth (staged in shared memory).
+// Per-config values the FP32 walk reads at photon birth.
 struct CfgF32 {
     int32_t lut_off, lut_n, k_lo;
     uint32_t flags;
@@ -61,6 +71,7 @@ __device__ __forceinline__ CfgF32 make_cfg(const DevConfig &c) {
     return f;
 }
 
+// Live state of a walking photon (registers).
 struct Photon {
     uint64_t rid;      // stream id: config << 40 | photon index
     int32_t cfg;       // -1: lane idle
@@ -72,9 +83,42 @@ struct Photon {
     float hg_a, hg_b, hg_c, hg_d, hg_e;  // 1+g^2, 1-g^2, 1-g, 2g, 1/(2g); hg_d == 0: isotropic
 };
 
-// Start photon p (index within its config) of config ci.
-__device__ __forceinline__ void birth(Photon &P, int64_t p, int ci, const CfgF32 &c,
-                                      const WalkArgs &a) {
+// A born photon waiting in the queue: 20 words = 5 x float4.
+struct __align__(16) BirthSlot {
+    uint32_t rid_lo, rid_hi, cfg, lut;
+    uint32_t flags;
+    float mux, muz, tau;
+    float R, inv_ext, coalb_ice, coalb_imp;
+    float p_imp, hg_a, hg_b, hg_c;
+    float hg_d, hg_e, pad0, pad1;
+};
+
+// A finished photon waiting for the batched epilogue: 12 words = 3 x float4.
+struct __align__(16) FinishSlot {
+    uint32_t rid_lo, rid_hi, cfg, lut;
+    int32_t n_step, cond;
+    float mux, muy;
+    float muz, path, pad0, pad1;
+};
+
+struct WarpQueues {
+    BirthSlot birth[32];
+    FinishSlot fin[kFinishCap];
+    WarpTally tally;
+    int32_t n_birth;
+    int32_t n_fin;
+};
+
+template <int N>
+__device__ __forceinline__ void copy_f4(void *dst, const void *src) {
+    float4 *d = reinterpret_cast<float4 *>(dst);
+    const float4 *s = reinterpret_cast<const float4 *>(src);
+#pragma unroll
+    for (int q = 0; q < N; ++q) d[q] = s[q];
+}
+
+// Start photon p (index within its config) of config ci into a queue slot.
+__device__ __forceinline__ void birth(BirthSlot &b, int64_t p, int ci, const CfgF32 &c, const WalkArgs &a) {
     const uint64_t rid = c.rng_base + (uint64_t)p;
     const uint4 r = philox10(make_uint4(0u, kTagBirth, (uint32_t)rid, (uint32_t)(rid >> 32)), a.keys);
     // Box-Muller normal for the wavelength (monte_carlo3D.py:1516-1520)
@@ -84,38 +128,63 @@ __device__ __forceinline__ void birth(Photon &P, int64_t p, int ci, const CfgF32
     const float zn = sqrtf(-2.f * __logf(u0)) * co;
     const int k = __float2int_rn(fmaf(c.sigma_100, zn, c.wvl0_100));
     const int idx = min(max(k - c.k_lo, 0), c.lut_n - 1);
-    P.rid = rid;
-    P.cfg = ci;
-    P.lut = c.lut_off + idx;
-    const LutEntry *e = a.lut + P.lut;
-    const float4 e0 = __ldg(reinterpret_cast<const float4 *>(e));
-    const float4 e1 = __ldg(reinterpret_cast<const float4 *>(e) + 1);
-    // e0 = (wvn, coalb_ice, coalb_imp, g), e1 = (inv_ext, p_imp, snow_depth, -)
-    P.coalb_ice = e0.y;
-    P.coalb_imp = e0.z;
+    const int lut = c.lut_off + idx;
+    const LutEntry *e = a.lut + lut;
+    const float4 e0 = __ldg(reinterpret_cast<const float4 *>(e));      // wvn, coalb_ice, coalb_imp, g
+    const float4 e1 = __ldg(reinterpret_cast<const float4 *>(e) + 1);  // inv_ext, p_imp, snow_depth, -
     const float g = e0.w;
-    P.inv_ext = e1.x;
-    P.p_imp = e1.y;
+    BirthSlot o;
+    o.rid_lo = (uint32_t)rid;
+    o.rid_hi = (uint32_t)(rid >> 32);
+    o.cfg = (uint32_t)ci;
+    o.lut = (uint32_t)lut;
+    o.flags = c.flags;
+    o.mux = c.mux0;
+    o.muz = c.muz0;
+    o.tau = c.tau_tot;
+    o.R = c.R;
+    o.inv_ext = e1.x;
+    o.coalb_ice = e0.y;
+    o.coalb_imp = e0.z;
+    o.p_imp = e1.y;
     if (fabsf(g) > 1e-6f) {
-        P.hg_a = 1.f + g * g;
-        P.hg_b = 1.f - g * g;
-        P.hg_c = 1.f - g;
-        P.hg_d = 2.f * g;
-        P.hg_e = 1.f / (2.f * g);
+        o.hg_a = 1.f + g * g;
+        o.hg_b = 1.f - g * g;
+        o.hg_c = 1.f - g;
+        o.hg_d = 2.f * g;
+        o.hg_e = 0.5f / g;
     } else {
-        P.hg_a = P.hg_b = P.hg_c = P.hg_e = 0.f;
-        P.hg_d = 0.f;
+        o.hg_a = o.hg_b = o.hg_c = o.hg_d = o.hg_e = 0.f;
     }
-    P.flags = c.flags;
-    P.tau = c.tau_tot;
-    P.R = c.R;
-    P.mux = c.mux0;
+    o.pad0 = o.pad1 = 0.f;
+    copy_f4<5>(&b, &o);
+}
+
+__device__ __forceinline__ void pop(Photon &P, const BirthSlot &b) {
+    BirthSlot o;
+    copy_f4<5>(&o, &b);
+    P.rid = ((uint64_t)o.rid_hi << 32) | o.rid_lo;
+    P.cfg = (int32_t)o.cfg;
+    P.lut = (int32_t)o.lut;
+    P.i = 0;
+    P.flags = o.flags;
+    P.mux = o.mux;
     P.muy = 0.f;
-    P.muz = c.muz0;
+    P.muz = o.muz;
     P.z = 0.f;
     P.path = 0.f;
     P.pathc = 0.f;
-    P.i = 0;
+    P.tau = o.tau;
+    P.R = o.R;
+    P.inv_ext = o.inv_ext;
+    P.coalb_ice = o.coalb_ice;
+    P.coalb_imp = o.coalb_imp;
+    P.p_imp = o.p_imp;
+    P.hg_a = o.hg_a;
+    P.hg_b = o.hg_b;
+    P.hg_c = o.hg_c;
+    P.hg_d = o.hg_d;
+    P.hg_e = o.hg_e;
 }
 
 // One scatter event (monte_carlo3D.py:1213-1466).  Returns the end condition
@@ -194,9 +263,9 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a) {
     int cond = 0;
     if (zn > 0.f) {                                         // :1390-1397
         cond = 1;
-        P.path -= (zn / (zn - z0)) * inc;
+        P.path -= __fdividef(zn, zn - z0) * inc;
     } else if (zn < -P.tau) {                               // :1399-1459
-        P.path -= ((zn + P.tau) / (zn - z0)) * inc;
+        P.path -= __fdividef(zn + P.tau, zn - z0) * inc;
         zn = -P.tau;
         bool leave = true;
         if (P.flags & kFlagLamBottom) {
@@ -217,16 +286,93 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a) {
     return cond;
 }
 
-__global__ void __launch_bounds__(256) walk_f32_kernel(const WalkArgs a) {
+// Exact warp sum of 64-bit values below 2^47.
+__device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
+    const unsigned lo = __reduce_add_sync(0xffffffffu, (unsigned)(v & 0xffffu));
+    const unsigned mid = __reduce_add_sync(0xffffffffu, (unsigned)((v >> 16) & 0xffffffu));
+    const unsigned hi = __reduce_add_sync(0xffffffffu, (unsigned)(v >> 40));
+    return (unsigned long long)lo + ((unsigned long long)mid << 16) + ((unsigned long long)hi << 40);
+}
+
+// Epilogue of up to 32 finished photons (entries [base, base + n) of the
+// finish queue): records, histogram bins and the warp's running totals.
+// Warp-collective.
+__device__ __noinline__ void finish_batch(WarpQueues &q, int base, int n, const WalkArgs &a,
+                                          const CfgF32 *scfg, const int64_t *prefix, bool staged,
+                                          int lane) {
+    const bool have = lane < n;
+    int cfg = -1, cond = 0, nscat = 0;
+    unsigned long long wfx = 0;
+    if (have) {
+        FinishSlot f;
+        copy_f4<3>(&f, &q.fin[base + lane]);
+        cfg = (int)f.cfg;
+        cond = f.cond;
+        nscat = f.n_step - 1;
+        const LutEntry *e = a.lut + f.lut;
+        const float wvn = __ldg(&e->wvn);
+        const float depth = __ldg(&e->snow_depth);
+        wfx = __ldg(&e->wvn_fx);
+        const float theta = acosf(fminf(fmaxf(f.muz, -1.f), 1.f));
+        float phi = 0.f;
+        if (f.n_step > 1) {
+            phi = atan2f(f.muy, f.mux);
+            if (phi < 0.f) phi += kTwoPiF;
+            if (phi >= kTwoPiF) phi = 0.f;
+        }
+        if (a.records) {
+            const uint64_t rid = ((uint64_t)f.rid_hi << 32) | f.rid_lo;
+            const uint64_t rbase = staged ? scfg[cfg].rng_base : a.cfgs[cfg].rng_base;
+            const int64_t gid = prefix[cfg] + (int64_t)(rid - rbase);
+            float4 *dst = reinterpret_cast<float4 *>(a.records + gid);
+            dst[0] = make_float4(__int_as_float(cond), __int_as_float(nscat), wvn, theta);
+            dst[1] = make_float4(phi, f.path, depth, __uint_as_float((uint32_t)cfg));
+        }
+        if (cond == 1) tally_bin(a.tallies + cfg, wfx, theta, phi);
+    }
+    // running totals per config (normally one config per batch)
+    unsigned pending = __ballot_sync(0xffffffffu, have);
+    while (pending) {
+        const int c = __shfl_sync(0xffffffffu, cfg, __ffs(pending) - 1);
+        const bool mine = have && cfg == c;
+        pending &= ~__ballot_sync(0xffffffffu, mine);
+        if (q.tally.cfg != c) {
+            warp_tally_flush(q.tally, a.tallies, lane);
+            if (lane == 0) q.tally.cfg = c;
+            __syncwarp();
+        }
+        const unsigned ev = __reduce_add_sync(0xffffffffu, mine ? (unsigned)nscat : 0u);
+        const unsigned mx = __reduce_max_sync(0xffffffffu, mine ? (unsigned)nscat : 0u);
+        unsigned cnt[6];
+        unsigned long long qs[6];
+#pragma unroll
+        for (int k = 1; k < 6; ++k) {
+            const bool hit = mine && cond == k;
+            cnt[k] = __popc(__ballot_sync(0xffffffffu, hit));
+            qs[k] = cnt[k] ? warp_sum_u64(hit ? wfx : 0ull) : 0ull;
+        }
+        if (lane == 0) {
+            q.tally.n_events += ev;
+            q.tally.max_n_scat = max(q.tally.max_n_scat, mx);
+#pragma unroll
+            for (int k = 1; k < 6; ++k) {
+                q.tally.n_cond[k] += cnt[k];
+                q.tally.q_cond_fx[k] += qs[k];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    WarpTally *wtally = reinterpret_cast<WarpTally *>(smem);
-    CfgF32 *scfg = reinterpret_cast<CfgF32 *>(smem + sizeof(WarpTally) * 32);
-    int64_t *sprefix = reinterpret_cast<int64_t *>(smem + sizeof(WarpTally) * 32 + sizeof(CfgF32) * kSmemCfgMax);
-
-    // stage configs in shared memory when they fit, else read them from global
+    const int nwarps = blockDim.x >> 5;
+    WarpQueues *queues = reinterpret_cast<WarpQueues *>(smem);
     const bool staged = a.n_cfg <= kSmemCfgMax;
+    CfgF32 *scfg = reinterpret_cast<CfgF32 *>(smem + sizeof(WarpQueues) * nwarps);
+    int64_t *sprefix = reinterpret_cast<int64_t *>(scfg + (staged ? a.n_cfg : 0));
     if (staged) {
         for (int c = threadIdx.x; c < a.n_cfg; c += blockDim.x) {
             scfg[c] = make_cfg(a.cfgs[c]);
@@ -234,8 +380,12 @@ __global__ void __launch_bounds__(256) walk_f32_kernel(const WalkArgs a) {
         }
     }
     const int64_t *prefix = staged ? sprefix : a.prefix;
-    WarpTally &wt = wtally[warp];
-    warp_tally_reset(wt, lane);
+    WarpQueues &q = queues[warp];
+    warp_tally_reset(q.tally, lane);
+    if (lane == 0) {
+        q.n_birth = 0;
+        q.n_fin = 0;
+    }
     __syncthreads();
 
     Photon P;
@@ -248,86 +398,73 @@ __global__ void __launch_bounds__(256) walk_f32_kernel(const WalkArgs a) {
     const unsigned lt_mask = (1u << lane) - 1u;
 
     for (uint32_t iter = 0;; ++iter) {
-        // ---- regeneration: refill idle lanes from the global photon counter
+        // ---- regeneration: idle lanes pop ready photons; refill the queue in batches
         const unsigned idle = __ballot_sync(0xffffffffu, P.cfg < 0);
         const int nidle = __popc(idle);
-        if (!exhausted && nidle > 0 && (nidle >= a.regen_chunk || nidle == 32)) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(a.work, (unsigned long long)nidle);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base + (unsigned long long)nidle >= (unsigned long long)a.total) exhausted = true;
-            if (P.cfg < 0) {
-                const int64_t g = (int64_t)base + __popc(idle & lt_mask);
-                if (g < a.total) {
+        if (nidle > 0 && (nidle >= a.regen_chunk || nidle == 32)) {
+            int cnt = q.n_birth;
+            if (cnt < nidle && !exhausted) {
+                const int want = 32 - cnt;
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(a.work, (unsigned long long)want);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                const int64_t left = a.total - (int64_t)base;
+                const int valid = (int)max((int64_t)0, min((int64_t)want, left));
+                if (left <= want) exhausted = true;
+                if (lane < valid) {
+                    const int64_t g = (int64_t)base + lane;
                     const int ci = find_config(prefix, a.n_cfg, g);
                     const CfgF32 c = staged ? scfg[ci] : make_cfg(a.cfgs[ci]);
-                    birth(P, g - prefix[ci], ci, c, a);
+                    birth(q.birth[cnt + lane], g - prefix[ci], ci, c, a);
                 }
+                cnt += valid;
+                __syncwarp();
             }
+            const int take = min(nidle, cnt);
+            if (idle & (1u << lane)) {
+                const int r = __popc(idle & lt_mask);
+                if (r < take) pop(P, q.birth[cnt - 1 - r]);
+            }
+            __syncwarp();
+            if (lane == 0) q.n_birth = cnt - take;
+            __syncwarp();
         }
         const unsigned active = __ballot_sync(0xffffffffu, P.cfg >= 0);
-        if (active == 0) break;  // nothing left: counter exhausted and all walks done
+        if (active == 0 && exhausted && q.n_birth == 0) break;
 
         // ---- one scatter event per active lane
         int cond = 0;
         if (P.cfg >= 0) cond = step(P, a);
 
-        // ---- finished photons: record, tallies
+        // ---- finished photons go to the finish queue
         const unsigned fin_mask = __ballot_sync(0xffffffffu, cond != 0);
         if (fin_mask) {
-            const bool fin = cond != 0;
-            float wvn = 0.f, depth = 0.f, theta = 0.f, phi = 0.f;
-            unsigned long long wfx = 0;
-            const int nscat = P.i - 1;
-            if (fin) {
-                const LutEntry *e = a.lut + P.lut;
-                wvn = __ldg(&e->wvn);
-                depth = __ldg(&e->snow_depth);
-                wfx = __ldg(&e->wvn_fx);
-                theta = acosf(fminf(fmaxf(P.muz, -1.f), 1.f));
-                if (P.i > 1) {
-                    phi = atan2f(P.muy, P.mux);
-                    if (phi < 0.f) phi += kTwoPiF;
-                    if (phi >= kTwoPiF) phi = 0.f;
-                }
-                if (a.records) {
-                    const uint64_t base_rid = staged ? scfg[P.cfg].rng_base : a.cfgs[P.cfg].rng_base;
-                    const int64_t gid = prefix[P.cfg] + (int64_t)(P.rid - base_rid);
-                    float4 *dst = reinterpret_cast<float4 *>(a.records + gid);
-                    dst[0] = make_float4(__int_as_float(cond), __int_as_float(nscat), wvn, theta);
-                    dst[1] = make_float4(phi, P.path, depth, __uint_as_float((uint32_t)P.cfg));
-                }
-                if (cond == 1) tally_bin(a.tallies + P.cfg, wfx, theta, phi);
+            const int nf = q.n_fin;
+            if (cond != 0) {
+                FinishSlot f;
+                f.rid_lo = (uint32_t)P.rid;
+                f.rid_hi = (uint32_t)(P.rid >> 32);
+                f.cfg = (uint32_t)P.cfg;
+                f.lut = (uint32_t)P.lut;
+                f.n_step = P.i;
+                f.cond = cond;
+                f.mux = P.mux;
+                f.muy = P.muy;
+                f.muz = P.muz;
+                f.path = P.path;
+                f.pad0 = f.pad1 = 0.f;
+                copy_f4<3>(&q.fin[nf + __popc(fin_mask & lt_mask)], &f);
+                P.cfg = -1;
             }
-            // warp running totals (shared memory), flushed when the config changes
-            const unsigned other = __ballot_sync(0xffffffffu, fin && P.cfg != wt.cfg);
-            if (other) {
-                unsigned pending = fin_mask;
-                while (pending) {
-                    const int leader = __ffs(pending) - 1;
-                    const int c = __shfl_sync(0xffffffffu, P.cfg, leader);
-                    const unsigned m = __ballot_sync(0xffffffffu, fin && P.cfg == c);
-                    if (wt.cfg != c) {
-                        warp_tally_flush(wt, a.tallies, lane);
-                        if (lane == 0) wt.cfg = c;
-                        __syncwarp();
-                    }
-                    if (m & (1u << lane)) {
-                        atomicAdd(&wt.n_cond[cond], 1u);
-                        atomicAdd(&wt.q_cond_fx[cond], wfx);
-                        atomicAdd(&wt.n_events, (unsigned long long)nscat);
-                        atomicMax(&wt.max_n_scat, (uint32_t)nscat);
-                    }
-                    __syncwarp();
-                    pending &= ~m;
-                }
-            } else if (fin) {
-                atomicAdd(&wt.n_cond[cond], 1u);
-                atomicAdd(&wt.q_cond_fx[cond], wfx);
-                atomicAdd(&wt.n_events, (unsigned long long)nscat);
-                atomicMax(&wt.max_n_scat, (uint32_t)nscat);
+            __syncwarp();
+            const int total_fin = nf + __popc(fin_mask);
+            if (total_fin >= 32) {
+                finish_batch(q, total_fin - 32, 32, a, scfg, prefix, staged, lane);
+                if (lane == 0) q.n_fin = total_fin - 32;
+            } else if (lane == 0) {
+                q.n_fin = total_fin;
             }
-            if (fin) P.cfg = -1;
+            __syncwarp();
         }
 
         // ---- time budget (watchdog; never a truncation in normal runs)
@@ -345,20 +482,30 @@ __global__ void __launch_bounds__(256) walk_f32_kernel(const WalkArgs a) {
             if (__shfl_sync(0xffffffffu, stop, 0)) break;
         }
     }
-    warp_tally_flush(wt, a.tallies, lane);
+    __syncwarp();
+    const int left = q.n_fin;
+    if (left > 0) finish_batch(q, 0, left, a, scfg, prefix, staged, lane);
+    warp_tally_flush(q.tally, a.tallies, lane);
+}
+
+size_t smem_bytes(int block, int n_cfg) {
+    const size_t cfg = n_cfg <= kSmemCfgMax ? (size_t)n_cfg * (sizeof(CfgF32) + sizeof(int64_t)) : 0;
+    return sizeof(WarpQueues) * (size_t)(block / 32) + cfg;
+}
+
+cudaError_t allow_smem() {
+    return cudaFuncSetAttribute(walk_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 }  // namespace
 
-size_t walk_f32_smem_bytes(int block) {
-    (void)block;
-    return sizeof(WarpTally) * 32 + sizeof(CfgF32) * kSmemCfgMax + sizeof(int64_t) * kSmemCfgMax;
-}
+size_t walk_f32_smem_bytes(int block, int n_cfg) { return smem_bytes(block, n_cfg); }
 
-int walk_f32_max_blocks_per_sm(int block) {
+int walk_f32_max_blocks_per_sm(int block, int n_cfg) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel, block,
-                                                      walk_f32_smem_bytes(block)) != cudaSuccess)
+    if (allow_smem() != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel, block, smem_bytes(block, n_cfg)) !=
+        cudaSuccess)
         return 0;
     return n;
 }
@@ -366,8 +513,9 @@ int walk_f32_max_blocks_per_sm(int block) {
 const void *walk_f32_kernel_fn() { return reinterpret_cast<const void *>(walk_f32_kernel); }
 
 cudaError_t launch_walk_f32(const WalkArgs &a, int grid, int block, cudaStream_t s) {
-    const size_t smem = walk_f32_smem_bytes(block);
-    walk_f32_kernel<<<grid, block, smem, s>>>(a);
+    cudaError_t e = allow_smem();
+    if (e != cudaSuccess) return e;
+    walk_f32_kernel<<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
     return cudaGetLastError();
 }
 
