@@ -105,12 +105,15 @@ def test_f32_statistics_match_oracle(walker, case, n):
     h_r = exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r])
     x2, dof, p = chi2_two_sample(h_g, h_r)
     assert p > 1e-4, (x2, dof, p)
-    # mean scatter count and path length within 4 sigma
+    # mean scatter count and path length within 4 sigma (+ 1e-6 of the slab depth:
+    # on a Lambertian surface the exact path is 0 and FP32 leaves rounding residue)
+    depth = float(ref['snow_depth'].mean())
     for k in ('n_scat', 'path_length'):
         a = rec[k].astype(np.float64)
         b = ref[k].astype(np.float64)
         sd = np.sqrt(a.var() / a.size + b.var() / b.size)
-        assert abs(a.mean() - b.mean()) <= 4 * sd + 1e-6 * abs(b.mean()), (k, a.mean(), b.mean())
+        floor = 1e-6 * max(abs(b.mean()), depth if k == 'path_length' else 0.0)
+        assert abs(a.mean() - b.mean()) <= 4 * sd + floor, (k, a.mean(), b.mean())
 
 
 def test_f32_known_answer_slab(walker):
