@@ -73,6 +73,7 @@ struct Plan {
     std::vector<int32_t> lut_cfg;
     int64_t total = 0;
     int32_t lut_total = 0;
+    bool impurity = false;  // some config has imp_cnc > 0
 };
 
 struct Counters {
@@ -200,6 +201,7 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
         d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
                   (c.imp_cnc > 0 ? kFlagImpurity : 0u);
         d.ice_table = c.ice_table;
+        if (c.imp_cnc > 0) plan.impurity = true;
         const double theta0 = (kPi * c.theta0_deg) / 180.;  // monte_carlo3D.py:1508
         d.wvl0_100 = (float)(c.wvl0 * 100.0);
         d.sigma_100 = (float)(sigma * 100.0);
@@ -233,10 +235,11 @@ struct Shape {
     int grid, block, chunk, bps;
 };
 
-Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, int64_t total, int32_t n_cfg) {
+Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, const Plan &plan) {
+    const int64_t total = plan.total;
     Shape s;
     s.block = l.block_size;
-    int occ = walk_f32_max_blocks_per_sm(s.block, n_cfg);
+    int occ = walk_f32_max_blocks_per_sm(s.block, (int)plan.cfgs.size(), plan.impurity);
     if (occ <= 0) occ = 1;
     s.bps = (l.blocks_per_sm > 0) ? std::min(l.blocks_per_sm, occ) : occ;
     s.chunk = l.regen_chunk;
@@ -502,11 +505,11 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     Shape shape{0, 0, 0, 0};
     if (mode == MCW_MODE_F32) {
         CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->lut_cfg), st));
-        shape = pick_shape(ctx, ctx->launch, plan.total, n_cfg);
+        shape = pick_shape(ctx, ctx->launch, plan);
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
-        if (plan.total > 0) CUDA_TRY(ctx, launch_walk_f32(wa, shape.grid, shape.block, st));
+        if (plan.total > 0) CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
     } else {
         ReplayArgs ra;
@@ -596,12 +599,14 @@ int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t s
                  double *best_ms) {
     if (!ctx || !cfgs || n_cfg <= 0) return MCW_ERR_ARG;
     const mcw_launch saved = ctx->launch;
+    bool imp_any = false;
+    for (int32_t i = 0; i < n_cfg; ++i) imp_any = imp_any || cfgs[i].imp_cnc > 0;
     const int blocks[] = {128, 256};
     const int chunks[] = {1, 4, 8, 16, 32};
     mcw_launch win = saved;
     double win_ms = 1e300;
     for (int b : blocks) {
-        const int occ = std::max(1, walk_f32_max_blocks_per_sm(b, n_cfg));
+        const int occ = std::max(1, walk_f32_max_blocks_per_sm(b, n_cfg, imp_any));
         const int bps_opts[] = {occ, std::max(1, occ / 2)};
         for (int bi = 0; bi < 2; ++bi) {
             if (bi == 1 && bps_opts[1] == bps_opts[0]) continue;
@@ -657,7 +662,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     if (g->h_tallies.ensure(n_cfg * sizeof(mcw_tally)) != cudaSuccess || g->h_counters.ensure(sizeof(Counters)) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_OOM, "pinned allocation failed"));
     if (cudaStreamSynchronize(st) != cudaSuccess) return fail(set_err(ctx, MCW_ERR_CUDA, "upload failed"));
-    const Shape shape = pick_shape(ctx, ctx->launch, plan.total, n_cfg);
+    const Shape shape = pick_shape(ctx, ctx->launch, plan);
     g->grid = shape.grid;
     g->block = shape.block;
     g->args = walk_args(ctx, plan, g->cfgs, g->prefix, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);
@@ -667,7 +672,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     cudaError_t e = cudaMemsetAsync(g->counters.p, 0, sizeof(Counters), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(g->tallies.p, 0, n_cfg * sizeof(mcw_tally), st);
     if (e == cudaSuccess) e = launch_lut(la, st);
-    if (e == cudaSuccess && plan.total > 0) e = launch_walk_f32(g->args, g->grid, g->block, st);
+    if (e == cudaSuccess && plan.total > 0) e = launch_walk_f32(g->args, plan.impurity, g->grid, g->block, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(g->h_tallies.p, g->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->h_counters.p, g->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, st);
@@ -684,7 +689,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
         if (cudaGraphNodeGetType(nd, &ty) != cudaSuccess || ty != cudaGraphNodeTypeKernel) continue;
         cudaKernelNodeParams p;
         if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) continue;
-        if (p.func == walk_f32_kernel_fn()) {
+        if (walk_f32_is_kernel(p.func)) {
             g->walk_node = nd;
             g->walk_params = p;
         }

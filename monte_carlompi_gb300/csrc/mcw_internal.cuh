@@ -12,7 +12,6 @@ constexpr uint32_t kTagWalk = 0;    // replay: the walk's uniforms
 constexpr uint32_t kTagWvl = 1;     // replay: wavelength Box-Muller
 constexpr uint32_t kTagStep = 2;    // F32: per-step HG, azimuth, path, albedo draws
 constexpr uint32_t kTagSpecies = 3; // F32: ice/impurity draw (only when imp_cnc > 0)
-constexpr uint32_t kTagBottom = 4;  // F32: Lambertian-bottom reflectance draw
 constexpr uint32_t kTagBirth = 5;   // F32: wavelength Box-Muller at photon birth
 
 // Device status bits.
@@ -122,10 +121,11 @@ struct LutArgs {
 
 // Kernel launchers (defined in the .cu files).
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
-cudaError_t launch_walk_f32(const WalkArgs &a, int grid, int block, cudaStream_t s);
+// impurity: some config has imp_cnc > 0 (the kernel instance with the species draw)
+cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, cudaStream_t s);
 cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);
-int walk_f32_max_blocks_per_sm(int block, int n_cfg);
-const void *walk_f32_kernel_fn();
+int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity);
+bool walk_f32_is_kernel(const void *fn);
 size_t walk_f32_smem_bytes(int block, int n_cfg);
 
 __device__ __forceinline__ unsigned long long global_ns() {

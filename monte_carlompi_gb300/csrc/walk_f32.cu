@@ -45,6 +45,12 @@ constexpr float kTwo33Inv = 1.16415321826934814e-10f; // 2^-33
 constexpr uint32_t kFlagReflect = 8u;                  // bottom reflection pending
 constexpr int kSmemCfgMax = 256;                       // configs staged in shared memory
 constexpr int kFinishCap = 64;                         // finish queue entries per warp
+#ifndef MCW_STEPS_PER_ROUND
+#define MCW_STEPS_PER_ROUND 4
+#endif
+// scatter events per loop round: their Philox blocks are computed together so
+// the ten dependent Philox rounds of one overlap those of the others
+constexpr int kStepsPerRound = MCW_STEPS_PER_ROUND;
 
 // Per-config values the FP32 walk reads at photon birth.
 struct CfgF32 {
@@ -105,8 +111,6 @@ struct WarpQueues {
     BirthSlot birth[32];
     FinishSlot fin[kFinishCap];
     WarpTally tally;
-    int32_t n_birth;
-    int32_t n_fin;
 };
 
 template <int N>
@@ -153,8 +157,9 @@ __device__ __forceinline__ void birth(BirthSlot &b, int64_t p, int ci, const Cfg
         o.hg_c = 1.f - g;
         o.hg_d = 2.f * g;
         o.hg_e = 0.5f / g;
-    } else {
-        o.hg_a = o.hg_b = o.hg_c = o.hg_d = o.hg_e = 0.f;
+    } else {  // isotropic: keep the HG expression finite (t = 0); the step selects 1 - 2u
+        o.hg_a = o.hg_b = o.hg_d = o.hg_e = 0.f;
+        o.hg_c = 1.f;
     }
     o.pad0 = o.pad1 = 0.f;
     copy_f4<5>(&b, &o);
@@ -187,98 +192,87 @@ __device__ __forceinline__ void pop(Photon &P, const BirthSlot &b) {
     P.hg_e = o.hg_e;
 }
 
-// One scatter event (monte_carlo3D.py:1213-1466).  Returns the end condition
-// (0 = still walking).
-__device__ __forceinline__ int step(Photon &P, const WalkArgs &a) {
+// One scatter event (monte_carlo3D.py:1213-1466) with its step block r =
+// Philox(step P.i + 1, photon) already computed.  Returns the end condition
+// (0 = still walking).  The alternatives of the reference's branches (first
+// step, Lambertian direction, pole, general rotation; top, bottom, absorption)
+// are evaluated together and selected, so the step is one straight dependency
+// chain; only the rare bottom-reflection draw branches.
+template <bool kImpurity>
+__device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm) {
     P.i += 1;
-    const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
-    const uint4 r = philox10(make_uint4((uint32_t)P.i, kTagStep, glo, ghi), a.keys);
     const float u1 = u01_f32(r.x);
     const float u2 = u01_f32(r.y);
     const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
     const bool first = (P.i == 1);
     const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
-
-    float dtau = -__logf(u3);
-    if (first && lam_surface) dtau = 0.f;
-
-    // scattering angle: HG inversion, or Lambertian after a bottom reflection
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
-    float ct;
-    if (lamb) {
-        ct = sqrtf(u1);
-    } else if (P.hg_d != 0.f) {
-        const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
-        ct = P.hg_e * (P.hg_a - t * t);
-        ct = fminf(fmaxf(ct, -1.f), 1.f);
-    } else {
-        ct = 1.f - 2.f * u1;
-    }
-    const float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+
+    const float dtau = (first && lam_surface) ? 0.f : -__logf(u3);
+
+    // scattering cosine: HG inversion (isotropic when hg_d == 0), or the
+    // Lambertian cos = sqrt(u) after a bottom reflection
+    const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
+    float ct = (P.hg_d != 0.f) ? P.hg_e * (P.hg_a - t * t) : fmaf(-2.f, u1, 1.f);
+    ct = lamb ? sqrtf(u1) : ct;
+    const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
     float sp, cp;
     __sincosf(kTwoPiF * (u2 - 0.5f), &sp, &cp);
 
-    float mx = P.mux, my = P.muy, mz = P.muz;
-    if (lamb) { mx = 0.f; my = 0.f; mz = 1.f; }
-    float nx, ny, nz;
-    if (first) {
-        nx = mx; ny = my; nz = mz;
-    } else if (fabsf(mz) > 0.99999f) {
-        const float sg = copysignf(1.f, mz);
-        nx = st * cp;
-        ny = sg * st * sp;
-        nz = sg * ct;
-    } else {
-        const float s2 = 1.f - mz * mz;
-        const float rs = rsqrtf(s2);
-        const float tq = st * rs;
-        nx = tq * (mx * mz * cp - my * sp) + mx * ct;
-        ny = tq * (my * mz * cp + mx * sp) + my * ct;
-        nz = -(s2 * rs) * st * cp + mz * ct;
-        const float inv = rsqrtf(nx * nx + ny * ny + nz * nz);
-        nx *= inv; ny *= inv; nz *= inv;
+    const float mx = lamb ? 0.f : P.mux;
+    const float my = lamb ? 0.f : P.muy;
+    const float mz = lamb ? 1.f : P.muz;
+    // general rotation (monte_carlo3D.py:1270-1281)
+    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
+    const float rs = rsqrtf(s2);
+    const float tq = st * rs;
+    float gx = fmaf(tq, mx * mz * cp - my * sp, mx * ct);
+    float gy = fmaf(tq, my * mz * cp + mx * sp, my * ct);
+    float gz = fmaf(-(s2 * rs) * st, cp, mz * ct);
+    if (renorm) {
+        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
+        gx *= inv; gy *= inv; gz *= inv;
     }
-    P.flags &= ~kFlagReflect;
+    // pole (monte_carlo3D.py:1262-1269), taken for |mu_z| > 0.99999
+    const float sg = copysignf(1.f, mz);
+    const bool pole = fabsf(mz) > 0.99999f;
+    const float nx = first ? mx : (pole ? st * cp : gx);
+    const float ny = first ? my : (pole ? sg * st * sp : gy);
+    const float nz = first ? mz : (pole ? sg * ct : gz);
 
     const float z0 = P.z;
-    float zn = z0 + dtau * nz;
+    float zn = fmaf(dtau, nz, z0);
     // path length, compensated sum
     const float inc = dtau * P.inv_ext;
     {
         const float y = inc - P.pathc;
-        const float t = P.path + y;
-        P.pathc = (t - P.path) - y;
-        P.path = t;
+        const float tt = P.path + y;
+        P.pathc = (tt - P.path) - y;
+        P.path = tt;
     }
 
-    // ice or impurity (monte_carlo3D.py:1375-1383)
+    // ice or impurity (monte_carlo3D.py:1375-1383); the draw exists only when imp_cnc > 0
     bool imp = false;
-    if (P.flags & kFlagImpurity) {
-        const uint4 r2 = philox10(make_uint4((uint32_t)P.i, kTagSpecies, glo, ghi), a.keys);
+    if (kImpurity && (P.flags & kFlagImpurity)) {
+        const uint4 r2 = philox10(make_uint4((uint32_t)P.i, kTagSpecies, (uint32_t)P.rid,
+                                             (uint32_t)(P.rid >> 32)), a.keys);
         imp = ((float)r2.x * kTwo32Inv) < P.p_imp;
     }
-    float coalb = imp ? P.coalb_imp : P.coalb_ice;
-    if (lam_surface) coalb = 1.f - P.R;
+    const float coalb = lam_surface ? 1.f - P.R : (imp ? P.coalb_imp : P.coalb_ice);
 
-    int cond = 0;
-    if (zn > 0.f) {                                         // :1390-1397
-        cond = 1;
-        P.path -= __fdividef(zn, zn - z0) * inc;
-    } else if (zn < -P.tau) {                               // :1399-1459
-        P.path -= __fdividef(zn + P.tau, zn - z0) * inc;
-        zn = -P.tau;
-        bool leave = true;
-        if (P.flags & kFlagLamBottom) {
-            const uint4 r3 = philox10(make_uint4((uint32_t)P.i, kTagBottom, glo, ghi), a.keys);
-            if ((float)r3.x * kTwo32Inv < P.R) {
-                leave = false;
-                P.flags |= kFlagReflect;
-            }
-        }
-        if (leave) cond = first ? 3 : 2;
-    } else if ((float)r.w * kTwo32Inv < coalb) {           // :1461-1466
-        cond = imp ? 5 : 4;
-    }
+    const bool top = zn > 0.f;                                  // :1390-1397
+    const bool bot = zn < -P.tau;                               // :1399-1459
+    const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
+    if (top || bot) P.path -= frac * inc;
+    zn = bot ? -P.tau : zn;
+    // r.w is the absorption draw; a step that reaches the bottom is never tested
+    // for absorption (the reference's elif chain), so there it is the
+    // Lambertian-bottom reflectance draw (:1422, :1453)
+    const float u4 = (float)r.w * kTwo32Inv;
+    const bool refl = bot && (P.flags & kFlagLamBottom) && u4 < P.R;
+    P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
+    const bool absorb = u4 < coalb;                             // :1461-1466
+    const int cond = top ? 1 : (bot ? (refl ? 0 : (first ? 3 : 2)) : (absorb ? (imp ? 5 : 4) : 0));
     P.mux = nx;
     P.muy = ny;
     P.muz = nz;
@@ -364,7 +358,8 @@ __device__ __noinline__ void finish_batch(WarpQueues &q, int base, int n, const 
     }
 }
 
-__global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
+template <bool kImpurity>
+__global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -382,10 +377,6 @@ __global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
     const int64_t *prefix = staged ? sprefix : a.prefix;
     WarpQueues &q = queues[warp];
     warp_tally_reset(q.tally, lane);
-    if (lane == 0) {
-        q.n_birth = 0;
-        q.n_fin = 0;
-    }
     __syncthreads();
 
     Photon P;
@@ -394,15 +385,16 @@ __global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
     P.lut = 0;
     P.i = 0;
     bool exhausted = false;
+    int n_birth = 0, n_fin = 0;        // queue fill, warp-uniform (kept in registers)
     const unsigned long long t0 = global_ns();
     const unsigned lt_mask = (1u << lane) - 1u;
+    unsigned idle = 0xffffffffu;       // lanes without a photon, warp-uniform
 
     for (uint32_t iter = 0;; ++iter) {
         // ---- regeneration: idle lanes pop ready photons; refill the queue in batches
-        const unsigned idle = __ballot_sync(0xffffffffu, P.cfg < 0);
         const int nidle = __popc(idle);
-        if (nidle > 0 && (nidle >= a.regen_chunk || nidle == 32)) {
-            int cnt = q.n_birth;
+        if (nidle > 0 && (nidle >= a.regen_chunk || nidle == 32) && !(exhausted && n_birth == 0)) {
+            int cnt = n_birth;
             if (cnt < nidle && !exhausted) {
                 const int want = 32 - cnt;
                 unsigned long long base = 0;
@@ -421,25 +413,50 @@ __global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
                 __syncwarp();
             }
             const int take = min(nidle, cnt);
+            bool popped = false;
             if (idle & (1u << lane)) {
                 const int r = __popc(idle & lt_mask);
-                if (r < take) pop(P, q.birth[cnt - 1 - r]);
+                if (r < take) {
+                    pop(P, q.birth[cnt - 1 - r]);
+                    popped = true;
+                }
             }
-            __syncwarp();
-            if (lane == 0) q.n_birth = cnt - take;
+            idle &= ~__ballot_sync(0xffffffffu, popped);
+            n_birth = cnt - take;
             __syncwarp();
         }
-        const unsigned active = __ballot_sync(0xffffffffu, P.cfg >= 0);
-        if (active == 0 && exhausted && q.n_birth == 0) break;
+        if (idle == 0xffffffffu && exhausted && n_birth == 0) break;
 
-        // ---- one scatter event per active lane
+        // ---- kStepsPerRound scatter events per active lane; their Philox blocks
+        // are independent of the walk, so they are computed together first
         int cond = 0;
-        if (P.cfg >= 0) cond = step(P, a);
+        if (P.cfg >= 0) {
+            uint4 rb[kStepsPerRound];
+            const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
+#pragma unroll
+            for (int k = 0; k < kStepsPerRound; ++k)
+                rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
+#pragma unroll
+            for (int k = 0; k < kStepsPerRound; ++k) {
+                // a lane whose photon ended earlier in the round keeps its final state
+                const bool alive = cond == 0;
+                Photon Q = P;
+                const int c = step<kImpurity>(Q, a, rb[k], k == kStepsPerRound - 1);
+                P.i = alive ? Q.i : P.i;
+                P.flags = alive ? Q.flags : P.flags;
+                P.mux = alive ? Q.mux : P.mux;
+                P.muy = alive ? Q.muy : P.muy;
+                P.muz = alive ? Q.muz : P.muz;
+                P.z = alive ? Q.z : P.z;
+                P.path = alive ? Q.path : P.path;
+                P.pathc = alive ? Q.pathc : P.pathc;
+                cond = alive ? c : cond;
+            }
+        }
 
         // ---- finished photons go to the finish queue
         const unsigned fin_mask = __ballot_sync(0xffffffffu, cond != 0);
         if (fin_mask) {
-            const int nf = q.n_fin;
             if (cond != 0) {
                 FinishSlot f;
                 f.rid_lo = (uint32_t)P.rid;
@@ -453,22 +470,20 @@ __global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
                 f.muz = P.muz;
                 f.path = P.path;
                 f.pad0 = f.pad1 = 0.f;
-                copy_f4<3>(&q.fin[nf + __popc(fin_mask & lt_mask)], &f);
+                copy_f4<3>(&q.fin[n_fin + __popc(fin_mask & lt_mask)], &f);
                 P.cfg = -1;
             }
+            idle |= fin_mask;
             __syncwarp();
-            const int total_fin = nf + __popc(fin_mask);
-            if (total_fin >= 32) {
-                finish_batch(q, total_fin - 32, 32, a, scfg, prefix, staged, lane);
-                if (lane == 0) q.n_fin = total_fin - 32;
-            } else if (lane == 0) {
-                q.n_fin = total_fin;
+            n_fin += __popc(fin_mask);
+            if (n_fin >= 32) {
+                finish_batch(q, n_fin - 32, 32, a, scfg, prefix, staged, lane);
+                n_fin -= 32;
             }
-            __syncwarp();
         }
 
         // ---- time budget (watchdog; never a truncation in normal runs)
-        if ((iter & 255u) == 255u) {
+        if ((iter & 63u) == 63u) {
             int stop = 0;
             if (lane == 0) {
                 const unsigned long long now = global_ns();
@@ -483,8 +498,7 @@ __global__ void __launch_bounds__(256, 4) walk_f32_kernel(const WalkArgs a) {
         }
     }
     __syncwarp();
-    const int left = q.n_fin;
-    if (left > 0) finish_batch(q, 0, left, a, scfg, prefix, staged, lane);
+    if (n_fin > 0) finish_batch(q, 0, n_fin, a, scfg, prefix, staged, lane);
     warp_tally_flush(q.tally, a.tallies, lane);
 }
 
@@ -494,28 +508,35 @@ size_t smem_bytes(int block, int n_cfg) {
 }
 
 cudaError_t allow_smem() {
-    return cudaFuncSetAttribute(walk_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(walk_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(walk_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 }
 
 }  // namespace
 
 size_t walk_f32_smem_bytes(int block, int n_cfg) { return smem_bytes(block, n_cfg); }
 
-int walk_f32_max_blocks_per_sm(int block, int n_cfg) {
+int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity) {
     int n = 0;
     if (allow_smem() != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel, block, smem_bytes(block, n_cfg)) !=
-        cudaSuccess)
-        return 0;
-    return n;
+    const size_t smem = smem_bytes(block, n_cfg);
+    const cudaError_t e = impurity
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<true>, block, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<false>, block, smem);
+    return e == cudaSuccess ? n : 0;
 }
 
-const void *walk_f32_kernel_fn() { return reinterpret_cast<const void *>(walk_f32_kernel); }
+bool walk_f32_is_kernel(const void *fn) {
+    return fn == reinterpret_cast<const void *>(walk_f32_kernel<false>) ||
+           fn == reinterpret_cast<const void *>(walk_f32_kernel<true>);
+}
 
-cudaError_t launch_walk_f32(const WalkArgs &a, int grid, int block, cudaStream_t s) {
+cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, cudaStream_t s) {
     cudaError_t e = allow_smem();
     if (e != cudaSuccess) return e;
-    walk_f32_kernel<<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
+    if (impurity) walk_f32_kernel<true><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
+    else walk_f32_kernel<false><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
     return cudaGetLastError();
 }
 
