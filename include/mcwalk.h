@@ -222,6 +222,27 @@ int mcw_write_csv(const char *path, const void *records, int32_t mode, int64_t n
 int mcw_format_csv(const void *records, int32_t mode, int64_t n, int32_t header, char *buf,
                    size_t cap, size_t *used);
 
+/* Largest wavelength lookup table mcw_walk_noalloc holds: grid points of
+ * lambda = k / 100 um over wvl0 +- 6.5 sigma, so FWHM up to about 3.6 um. */
+#define MCW_NOALLOC_MAX_LUT 2048
+
+/* The F32 walk of one config for callers that cannot allocate device memory
+ * (a plugin given buffers by a framework's own pool, a real-time loop that
+ * must not reach the allocator).  No counterpart in the reference.  The caller
+ * passes device buffers only: ice_dev / imp_dev hold DEVICE pointers to
+ * ascending tables with distinct wavelengths (asm_prm may be NULL for the
+ * impurity), records_dev (cfg->n_photon mcw_record32, 16-byte aligned) and
+ * tally_dev may be NULL; stream is a cudaStream_t (NULL = default stream).
+ * Allocates nothing: its scratch is a fixed device array of this library
+ * (about 115 KB per GPU, held until the process exits) shared by all calls on
+ * a device, so calls that overlap on the GPU race; the first call on a device
+ * resolves the array's address and should come before any stream capture.
+ * Sizes beyond MCW_NOALLOC_MAX_LUT and unsorted tables return MCW_ERR_ARG.
+ * Same records and tally as mcw_walk with one config and this seed.
+ * Synchronises the stream before returning. */
+int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_dev, const mcw_ssp_table *imp_dev,
+                     uint64_t seed, mcw_record32 *records_dev, mcw_tally *tally_dev, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

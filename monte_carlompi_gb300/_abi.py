@@ -25,7 +25,7 @@ EXPORTS = ['mcw_abi_version', 'mcw_version', 'mcw_create', 'mcw_destroy', 'mcw_l
            'mcw_set_tables', 'mcw_set_launch', 'mcw_get_launch', 'mcw_set_budget', 'mcw_walk',
            'mcw_brf', 'mcw_autotune', 'mcw_graph_create', 'mcw_graph_launch',
            'mcw_graph_destroy', 'mcw_host_alloc', 'mcw_host_free', 'mcw_write_csv',
-           'mcw_format_csv']
+           'mcw_format_csv', 'mcw_walk_noalloc']
 
 
 class McwError(RuntimeError):
@@ -127,6 +127,8 @@ def load(path=None):
         'mcw_write_csv': ([ctypes.c_char_p, vp, i32, i64, i32], ctypes.c_int),
         'mcw_format_csv': ([vp, i32, i64, i32, vp, ctypes.c_size_t,
                             ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+        'mcw_walk_noalloc': ([ctypes.POINTER(ConfigC), ctypes.POINTER(SSPTableC),
+                              ctypes.POINTER(SSPTableC), u64, vp, vp, vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

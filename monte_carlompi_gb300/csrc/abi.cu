@@ -314,6 +314,11 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &p
 
 }  // namespace
 
+namespace mcw {
+// Validation of one config, shared with entry points in other units.
+const char *config_problem(const mcw_config &c, int32_t n_ice) { return check_config(c, n_ice); }
+}  // namespace mcw
+
 extern "C" {
 
 int mcw_abi_version(void) { return MCW_ABI_VERSION; }

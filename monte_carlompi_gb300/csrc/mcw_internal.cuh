@@ -119,6 +119,9 @@ struct LutArgs {
     const DevTable *ice;
 };
 
+// Why a config is invalid (nullptr when valid); n_ice = number of ice tables.
+const char *config_problem(const mcw_config &c, int32_t n_ice);
+
 // Kernel launchers (defined in the .cu files).
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
 // impurity: some config has imp_cnc > 0 (the kernel instance with the species draw)
