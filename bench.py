@@ -166,6 +166,73 @@ def committed_traffic():
     return None
 
 
+def sweep_workload():
+    """BASELINE config 3: 64 configs from r_eff x lambda0 x theta0 x depth, photon counts
+    log-uniform over 1e4-1e6, seeded (0x5EED0003)."""
+    from monte_carlompi_gb300 import ssp
+    from monte_carlompi_gb300.config import WalkConfig
+    rng = np.random.default_rng(0x5EED0003)
+    radii = [50.0, 100.0, 200.0, 400.0, 800.0, 1500.0]
+    tables = [ssp.synthetic_ice_table(r, 600, 2100) for r in radii]
+    imp = ssp.synthetic_impurity_table(600, 2100)
+    cfgs = []
+    for _ in range(64):
+        ri = int(rng.integers(len(radii)))
+        wvl0 = float(np.round(rng.uniform(0.9, 1.8), 3))
+        theta0 = float(rng.choice([0.0, 30.0, 45.0, 60.0]))
+        depth = float(rng.choice([0.02, 0.10, 1.0]))
+        n = int(10 ** rng.uniform(4, 6))
+        tau = depth * ssp.ext_cff_mss_sphere(radii[ri]) * 300.0
+        cfgs.append(WalkConfig(n_photon=n, wvl0=wvl0, half_width=0.085, theta0_deg=theta0,
+                               tau_tot=tau, lambertian_reflectance=0.5, ice_table=ri,
+                               rds_snw=radii[ri]))
+    return cfgs, tables, imp
+
+
+def run_sweep(args):
+    """Batched sweep in one graph-captured launch vs one launch per config."""
+    import torch
+    from monte_carlompi_gb300.walker import Walker
+    cfgs, tables, imp = sweep_workload()
+    total = sum(c.n_photon for c in cfgs)
+    w = Walker(0)
+    w.set_tables(tables, imp)
+    best = w.autotune(cfgs, seed=11)
+    recs = torch.empty(total * RECORD_BYTES, dtype=torch.uint8, device='cuda')
+    g = w.graph(cfgs, device_ptr=recs.data_ptr())
+    for k in range(args.warmup):
+        g.launch(SEED + k)
+    t_batch, events = [], 0
+    for k in range(args.steps):
+        r = g.launch(SEED + 100 + k)
+        t_batch.append(r.stats['kernel_ms'])
+        events += r.stats['n_events']
+    # per-config launches (same photons, same statistical error)
+    for k in range(max(1, args.warmup // 2)):
+        w.walk([cfgs[0]], SEED, mode='f32', records=None)
+    t_plain = []
+    for k in range(args.steps):
+        t = 0.0
+        for c in cfgs:
+            t += w.walk([c], SEED + 100 + k, mode='f32', records='device',
+                        device_ptr=recs.data_ptr()).stats['device_ms']
+        t_plain.append(t)
+    g.close()
+    w.close()
+    tb, tp = float(np.median(t_batch)), float(np.median(t_plain))
+    line = {'metric': METRIC, 'workload': 'sweep', 'value': total / (tb / 1e3), 'unit': 'photons/s',
+            'n_gpus': 1, 'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': tb,
+            'higher_is_better': True, 'dtype': 'f32', 'data': 'synthetic',
+            'config': {'workload': '64 configs: r_eff {50..1500} um x lambda0 U(0.9,1.8) um x '
+                                   'theta0 {0,30,45,60} x depth {0.02,0.10,1.0} m, N log-U(1e4,1e6), '
+                                   'seed 0x5EED0003', 'photons': total,
+                       'launch': best},
+            'scatter_events_per_s': events / args.steps / (tb / 1e3),
+            'per_config_launches_ms': tp, 'batched_graph_ms': tb, 'speedup_vs_per_config': tp / tb}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -328,9 +395,12 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep'])
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.workload == 'sweep':
+        return run_sweep(args)
     return run_ours(args)
 
 

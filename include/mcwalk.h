@@ -234,7 +234,7 @@ int mcw_format_csv(const void *records, int32_t mode, int64_t n, int32_t header,
  * impurity), records_dev (cfg->n_photon mcw_record32, 16-byte aligned) and
  * tally_dev may be NULL; stream is a cudaStream_t (NULL = default stream).
  * Allocates nothing: its scratch is a fixed device array of this library
- * (about 115 KB per GPU, held until the process exits) shared by all calls on
+ * (about 107 KB per GPU, held until the process exits) shared by all calls on
  * a device, so calls that overlap on the GPU race; the first call on a device
  * resolves the array's address and should come before any stream capture.
  * Sizes beyond MCW_NOALLOC_MAX_LUT and unsorted tables return MCW_ERR_ARG.

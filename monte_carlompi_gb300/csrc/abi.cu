@@ -70,7 +70,6 @@ struct HostBuf {
 struct Plan {
     std::vector<DevConfig> cfgs;
     std::vector<int64_t> prefix;
-    std::vector<int32_t> lut_cfg;
     int64_t total = 0;
     int32_t lut_total = 0;
     bool impurity = false;  // some config has imp_cnc > 0
@@ -96,8 +95,9 @@ struct mcw_ctx {
     int32_t n_ice = 0;
     bool have_tables = false;
     // workspace
-    DevBuf cfgs, prefix, lut, lut_cfg, tallies, counters, records;
+    DevBuf cfgs, lut, tallies, counters, records;
     HostBuf h_stage, h_tallies, h_counters;
+    int32_t max_ice_n = 0;
     mcw_launch launch{256, 0, 8, 0};
     double budget_s = 300.0;
 };
@@ -112,7 +112,7 @@ struct mcw_graph {
     int32_t n_cfg = 0;
     int64_t total = 0;
     int grid = 0, block = 0;
-    DevBuf cfgs, prefix, lut, lut_cfg, tallies, counters;
+    DevBuf cfgs, lut, tallies, counters;
     HostBuf h_tallies, h_counters;
 };
 
@@ -168,7 +168,6 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
     if (n_cfg > (1 << 23)) return set_err(ctx, MCW_ERR_ARG, "at most 2^23 configs per call");
     plan.cfgs.resize(n_cfg);
     plan.prefix.resize(n_cfg + 1);
-    plan.lut_cfg.clear();
     int64_t off = 0;
     int32_t lut_off = 0;
     for (int32_t i = 0; i < n_cfg; ++i) {
@@ -196,7 +195,6 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
         d.k_lo = (int32_t)klo;
         d.lut_n = (int32_t)(khi - klo + 1);
         d.lut_off = lut_off;
-        for (int32_t k = 0; k < d.lut_n; ++k) plan.lut_cfg.push_back(i);
         lut_off += d.lut_n;
         d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
                   (c.imp_cnc > 0 ? kFlagImpurity : 0u);
@@ -250,54 +248,54 @@ Shape pick_shape(const mcw_ctx *ctx, const mcw_launch &l, const Plan &plan) {
     return s;
 }
 
-// Upload a plan into the given buffers through a pinned staging buffer.
-int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &prefix, DevBuf &lut, DevBuf &lut_cfg,
-                DevBuf &tallies, DevBuf &counters, cudaStream_t st, cudaEvent_t start = nullptr,
-                uint64_t *h2d = nullptr) {
+// Byte offset of the prefix array inside the plan buffer (after the configs).
+size_t prefix_offset(size_t n_cfg) { return (n_cfg * sizeof(DevConfig) + 255) & ~size_t(255); }
+
+// Upload a plan (configs then prefix, one copy) through a pinned staging buffer.
+int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &tallies, DevBuf &counters,
+                cudaStream_t st, cudaEvent_t start = nullptr, uint64_t *h2d = nullptr) {
     const size_t n_cfg = plan.cfgs.size();
     const size_t b_cfg = n_cfg * sizeof(DevConfig);
-    const size_t b_pre = (n_cfg + 1) * sizeof(int64_t);
-    const size_t b_lc = std::max<size_t>(1, plan.lut_cfg.size()) * sizeof(int32_t);
-    CUDA_TRY(ctx, cfgs.ensure(b_cfg));
-    CUDA_TRY(ctx, prefix.ensure(b_pre));
+    const size_t off = prefix_offset(n_cfg);
+    const size_t b_all = off + (n_cfg + 1) * sizeof(int64_t);
+    CUDA_TRY(ctx, cfgs.ensure(b_all));
     CUDA_TRY(ctx, lut.ensure(std::max<size_t>(1, plan.lut_total) * sizeof(LutEntry)));
-    CUDA_TRY(ctx, lut_cfg.ensure(b_lc));
     CUDA_TRY(ctx, tallies.ensure(n_cfg * sizeof(mcw_tally)));
     CUDA_TRY(ctx, counters.ensure(sizeof(Counters)));
     // the staging buffer must not be rewritten while a previous copy reads it
     CUDA_TRY(ctx, cudaStreamSynchronize(st));
-    CUDA_TRY(ctx, ctx->h_stage.ensure(b_cfg + b_pre + b_lc));
+    CUDA_TRY(ctx, ctx->h_stage.ensure(b_all));
     char *h = (char *)ctx->h_stage.p;
     memcpy(h, plan.cfgs.data(), b_cfg);
-    memcpy(h + b_cfg, plan.prefix.data(), b_pre);
-    if (!plan.lut_cfg.empty()) memcpy(h + b_cfg + b_pre, plan.lut_cfg.data(), plan.lut_cfg.size() * sizeof(int32_t));
+    memset(h + b_cfg, 0, off - b_cfg);
+    memcpy(h + off, plan.prefix.data(), (n_cfg + 1) * sizeof(int64_t));
     if (start) CUDA_TRY(ctx, cudaEventRecord(start, st));
-    if (h2d) *h2d = b_cfg + b_pre + (plan.lut_cfg.empty() ? 0 : plan.lut_cfg.size() * sizeof(int32_t));
-    CUDA_TRY(ctx, cudaMemcpyAsync(cfgs.p, h, b_cfg, cudaMemcpyHostToDevice, st));
-    CUDA_TRY(ctx, cudaMemcpyAsync(prefix.p, h + b_cfg, b_pre, cudaMemcpyHostToDevice, st));
-    if (!plan.lut_cfg.empty())
-        CUDA_TRY(ctx, cudaMemcpyAsync(lut_cfg.p, h + b_cfg + b_pre, plan.lut_cfg.size() * sizeof(int32_t),
-                                      cudaMemcpyHostToDevice, st));
+    if (h2d) *h2d = b_all;
+    CUDA_TRY(ctx, cudaMemcpyAsync(cfgs.p, h, b_all, cudaMemcpyHostToDevice, st));
     return MCW_OK;
 }
 
-LutArgs lut_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &lut_cfg) {
+LutArgs lut_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &tallies,
+                 DevBuf &counters) {
     LutArgs la;
     la.cfgs = (const DevConfig *)cfgs.p;
     la.n_cfg = (int32_t)plan.cfgs.size();
-    la.lut_total = plan.lut_total;
+    la.stage_doubles = ctx->max_ice_n + ctx->imp.n;
+    la.stage = la.stage_doubles <= 12288 ? 1 : 0;  // up to 96 KB of shared memory
+    la.counters_words = (int32_t)(sizeof(Counters) / 4);
     la.lut = (LutEntry *)lut.p;
-    la.lut_cfg = (const int32_t *)lut_cfg.p;
     la.imp = ctx->imp;
     la.ice = (const DevTable *)ctx->ice_tables.p;
+    la.tallies = (mcw_tally *)tallies.p;
+    la.counters = (uint32_t *)counters.p;
     return la;
 }
 
-WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &prefix, DevBuf &lut,
-                   DevBuf &tallies, DevBuf &counters, mcw_record32 *records, int chunk, uint64_t seed) {
+WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &tallies,
+                   DevBuf &counters, mcw_record32 *records, int chunk, uint64_t seed) {
     WalkArgs wa;
     wa.cfgs = (const DevConfig *)cfgs.p;
-    wa.prefix = (const int64_t *)prefix.p;
+    wa.prefix = (const int64_t *)((const char *)cfgs.p + prefix_offset(plan.cfgs.size()));
     wa.lut = (const LutEntry *)lut.p;
     wa.n_cfg = (int32_t)plan.cfgs.size();
     wa.regen_chunk = chunk;
@@ -354,8 +352,8 @@ int mcw_destroy(mcw_ctx *ctx) {
     if (!ctx) return MCW_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->tabdata, &ctx->ice_tables, &ctx->cfgs, &ctx->prefix, &ctx->lut, &ctx->lut_cfg,
-                      &ctx->tallies, &ctx->counters, &ctx->records})
+    for (DevBuf *b : {&ctx->tabdata, &ctx->ice_tables, &ctx->cfgs, &ctx->lut, &ctx->tallies, &ctx->counters,
+                      &ctx->records})
         b->release();
     ctx->h_stage.release();
     ctx->h_tallies.release();
@@ -450,6 +448,8 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     CUDA_TRY(ctx, cudaMemcpy(ctx->ice_tables.p, tabs.data(), n_ice * sizeof(DevTable), cudaMemcpyHostToDevice));
     ctx->imp = dimp;
     ctx->n_ice = n_ice;
+    ctx->max_ice_n = 0;
+    for (int32_t i = 0; i < n_ice; ++i) ctx->max_ice_n = std::max(ctx->max_ice_n, ice[i].n);
     ctx->have_tables = true;
     return MCW_OK;
 }
@@ -494,8 +494,7 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     uint64_t h2d = 0;
-    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->lut_cfg, ctx->tallies, ctx->counters, st,
-                     ctx->evs, &h2d);
+    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
     if (rc) return rc;
     const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
     void *dev_records = nullptr;
@@ -504,22 +503,22 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         CUDA_TRY(ctx, ctx->records.ensure((size_t)plan.total * rec_size));
         dev_records = ctx->records.p;
     }
-    CUDA_TRY(ctx, cudaMemsetAsync(ctx->tallies.p, 0, n_cfg * sizeof(mcw_tally), st));
-    CUDA_TRY(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(Counters), st));
-
     Shape shape{0, 0, 0, 0};
     if (mode == MCW_MODE_F32) {
-        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->lut_cfg), st));
+        // the lookup-table kernel also clears the counters and tallies
+        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
         shape = pick_shape(ctx, ctx->launch, plan);
-        WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->prefix, ctx->lut, ctx->tallies, ctx->counters,
+        WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
         if (plan.total > 0) CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
     } else {
+        CUDA_TRY(ctx, cudaMemsetAsync(ctx->tallies.p, 0, n_cfg * sizeof(mcw_tally), st));
+        CUDA_TRY(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(Counters), st));
         ReplayArgs ra;
         ra.cfgs = (const DevConfig *)ctx->cfgs.p;
-        ra.prefix = (const int64_t *)ctx->prefix.p;
+        ra.prefix = (const int64_t *)((const char *)ctx->cfgs.p + prefix_offset(plan.cfgs.size()));
         ra.n_cfg = n_cfg;
         ra.pad = 0;
         ra.total = plan.total;
@@ -662,7 +661,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
         mcw_graph_destroy(g);
         return code;
     };
-    rc = upload_plan(ctx, plan, g->cfgs, g->prefix, g->lut, g->lut_cfg, g->tallies, g->counters, st);
+    rc = upload_plan(ctx, plan, g->cfgs, g->lut, g->tallies, g->counters, st);
     if (rc) return fail(rc);
     if (g->h_tallies.ensure(n_cfg * sizeof(mcw_tally)) != cudaSuccess || g->h_counters.ensure(sizeof(Counters)) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_OOM, "pinned allocation failed"));
@@ -670,13 +669,11 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     const Shape shape = pick_shape(ctx, ctx->launch, plan);
     g->grid = shape.grid;
     g->block = shape.block;
-    g->args = walk_args(ctx, plan, g->cfgs, g->prefix, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);
-    const LutArgs la = lut_args(ctx, plan, g->cfgs, g->lut, g->lut_cfg);
+    g->args = walk_args(ctx, plan, g->cfgs, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);
+    const LutArgs la = lut_args(ctx, plan, g->cfgs, g->lut, g->tallies, g->counters);
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_CUDA, "stream capture failed to start"));
-    cudaError_t e = cudaMemsetAsync(g->counters.p, 0, sizeof(Counters), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(g->tallies.p, 0, n_cfg * sizeof(mcw_tally), st);
-    if (e == cudaSuccess) e = launch_lut(la, st);
+    cudaError_t e = launch_lut(la, st);  // clears counters and tallies too
     if (e == cudaSuccess && plan.total > 0) e = launch_walk_f32(g->args, plan.impurity, g->grid, g->block, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(g->h_tallies.p, g->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st);
@@ -756,7 +753,7 @@ int mcw_graph_destroy(mcw_graph *g) {
     }
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
-    for (DevBuf *b : {&g->cfgs, &g->prefix, &g->lut, &g->lut_cfg, &g->tallies, &g->counters}) b->release();
+    for (DevBuf *b : {&g->cfgs, &g->lut, &g->tallies, &g->counters}) b->release();
     g->h_tallies.release();
     g->h_counters.release();
     delete g;

@@ -112,11 +112,14 @@ struct ReplayArgs {
 struct LutArgs {
     const DevConfig *cfgs;
     int32_t n_cfg;
-    int32_t lut_total;
+    int32_t stage;               // stage table wavelengths in shared memory
+    int32_t stage_doubles;       // largest ice table + impurity table length
+    int32_t counters_words;      // 32-bit words of *counters to clear
     LutEntry *lut;
-    const int32_t *lut_cfg;      // config of each LUT entry
     DevTable imp;
     const DevTable *ice;
+    mcw_tally *tallies;          // n_cfg tallies to clear, or null
+    uint32_t *counters;          // work counter and status to clear, or null
 };
 
 // Why a config is invalid (nullptr when valid); n_ice = number of ice tables.

@@ -45,7 +45,6 @@ struct __align__(256) NoAllocScratch {
     alignas(256) int64_t prefix[2];
     alignas(256) DevTable ice;
     alignas(256) mcw_tally tally;       // used when the caller passes no tally
-    alignas(256) int32_t lut_cfg[kNoAllocLutMax];
     alignas(256) LutEntry lut[kNoAllocLutMax];
 };
 
@@ -69,7 +68,6 @@ __global__ void noalloc_setup(NoAllocScratch *s, const DevConfig cfg, const DevT
         s->prefix[1] = cfg.n_photon;
         s->ice = ice;
     }
-    for (int i = t; i < lut_n; i += blockDim.x) s->lut_cfg[i] = 0;
     uint32_t *tw = reinterpret_cast<uint32_t *>(tally);
     for (int i = t; i < (int)(sizeof(mcw_tally) / 4); i += blockDim.x) tw[i] = 0u;
     __syncthreads();
@@ -169,11 +167,14 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     LutArgs la;
     la.cfgs = &s->cfg;
     la.n_cfg = 1;
-    la.lut_total = d.lut_n;
+    la.stage = 0;
+    la.stage_doubles = 0;
+    la.counters_words = 0;
     la.lut = s->lut;
-    la.lut_cfg = s->lut_cfg;
     la.imp = imp;
     la.ice = &s->ice;
+    la.tallies = nullptr;   // cleared by noalloc_setup
+    la.counters = nullptr;
     if (launch_lut(la, st) != cudaSuccess) return MCW_ERR_CUDA;
     if (c.n_photon > 0) {
         WalkArgs wa;

@@ -16,35 +16,58 @@ namespace mcw {
 
 namespace {
 
+// One block per config: clears the call's counters and the config's tally
+// (they must start at zero), stages the wavelength columns of its tables in
+// shared memory when they fit, then fills the config's grid points.
 __global__ void lut_kernel(const LutArgs a) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= a.lut_total) return;
-    const int ci = a.lut_cfg[e];
+    extern __shared__ double s_wvl[];
+    const int ci = blockIdx.x;
     const DevConfig c = a.cfgs[ci];
-    const int k = c.k_lo + (e - c.lut_off);
-    const double wvl = (double)k / 100.0;
-    const Optics o = photon_optics(c, a.ice[c.ice_table], a.imp, wvl);
-    const double wvn = 1.0 / wvl;
-    LutEntry L;
-    L.wvn = (float)wvn;
-    L.coalb_ice = (float)(1.0 - o.ssa_ice);
-    L.coalb_imp = (float)(1.0 - o.ssa_imp);
-    L.g = (float)o.g;
-    L.inv_ext = (float)(1.0 / (o.ext_cff_mss * c.rho_snw));
-    L.p_imp = (float)o.p_imp;
-    L.snow_depth = (float)o.snow_depth;
-    L.pad = 0.f;
-    L.wvn_fx = (unsigned long long)llrint(wvn * 4294967296.0);
-    L.pad2 = 0;
-    a.lut[e] = L;
+    if (a.tallies) {
+        uint32_t *t = reinterpret_cast<uint32_t *>(a.tallies + ci);
+        for (int i = threadIdx.x; i < (int)(sizeof(mcw_tally) / 4); i += blockDim.x) t[i] = 0u;
+    }
+    if (a.counters && ci == 0)
+        for (int i = threadIdx.x; i < a.counters_words; i += blockDim.x) a.counters[i] = 0u;
+    DevTable ice = a.ice[c.ice_table];
+    DevTable imp = a.imp;
+    if (a.stage) {
+        for (int i = threadIdx.x; i < ice.n; i += blockDim.x) s_wvl[i] = ice.wvl[i];
+        for (int i = threadIdx.x; i < imp.n; i += blockDim.x) s_wvl[ice.n + i] = imp.wvl[i];
+        __syncthreads();
+        ice.wvl = s_wvl;
+        imp.wvl = s_wvl + ice.n;
+    }
+    for (int j = threadIdx.x; j < c.lut_n; j += blockDim.x) {
+        const int k = c.k_lo + j;
+        const double wvl = (double)k / 100.0;
+        const Optics o = photon_optics(c, ice, imp, wvl);
+        const double wvn = 1.0 / wvl;
+        LutEntry L;
+        L.wvn = (float)wvn;
+        L.coalb_ice = (float)(1.0 - o.ssa_ice);
+        L.coalb_imp = (float)(1.0 - o.ssa_imp);
+        L.g = (float)o.g;
+        L.inv_ext = (float)(1.0 / (o.ext_cff_mss * c.rho_snw));
+        L.p_imp = (float)o.p_imp;
+        L.snow_depth = (float)o.snow_depth;
+        L.pad = 0.f;
+        L.wvn_fx = (unsigned long long)llrint(wvn * 4294967296.0);
+        L.pad2 = 0;
+        a.lut[c.lut_off + j] = L;
+    }
 }
 
 }  // namespace
 
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s) {
-    if (a.lut_total <= 0) return cudaSuccess;
-    const int block = 128;
-    lut_kernel<<<(a.lut_total + block - 1) / block, block, 0, s>>>(a);
+    if (a.n_cfg <= 0) return cudaSuccess;
+    const size_t smem = a.stage ? (size_t)a.stage_doubles * sizeof(double) : 0;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(lut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    lut_kernel<<<a.n_cfg, 128, smem, s>>>(a);
     return cudaGetLastError();
 }
 
