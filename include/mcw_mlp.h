@@ -1,0 +1,73 @@
+/*
+ * mcw_mlp.h - kernels of the BRF surrogate network (libmcwalk.so).
+ *
+ * The surrogate maps (r_eff, lambda, cos theta0, depth) to the 648-bin BRF and
+ * the albedo that the walk (mcwalk.h) would produce; it has no counterpart in
+ * the reference, whose only route to a BRF is the Monte Carlo walk plus
+ * post_processing.py:46-100.  All pointers are device pointers; all calls are
+ * asynchronous on the given cudaStream_t (NULL = default stream) and return 0
+ * or a negative MCW_MLP_ERR_*.
+ */
+#ifndef MCW_MLP_H
+#define MCW_MLP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCW_MLP_ERR_ARG (-1)
+#define MCW_MLP_ERR_CUDA (-2)
+
+/* GEMM epilogues */
+#define MCW_EPI_F32 0        /* c (f32) = acc */
+#define MCW_EPI_BIAS_F32 1   /* c (f32) = acc + bias (bias may be NULL) */
+#define MCW_EPI_BIAS_SILU 2  /* c2 (f32) = z = acc + bias; c (bf16) = silu(z) */
+#define MCW_EPI_DSILU 3      /* g = acc * silu'(aux); c (bf16) = g; c2 (f32, optional) = g */
+
+/* C[m, n] = sum_k A(m, k) B(n, k) on BF16 tensor cores with FP32 accumulation.
+ * A is bf16 stored [m, k] (trans_a = 0) or [k, m] (trans_a = 1), leading
+ * dimension lda; B is bf16 stored [n, k] (trans_b = 0) or [k, n] (trans_b = 1). */
+typedef struct {
+    int32_t m, n, k;
+    int32_t trans_a, trans_b;
+    int32_t epilogue;
+    const void *a;
+    int32_t lda;
+    int32_t ldb;
+    const void *b;
+    const float *bias;   /* n */
+    const float *aux;    /* [m, n] pre-activation for MCW_EPI_DSILU */
+    int32_t ldaux;
+    int32_t ldc;
+    void *c;
+    void *c2;
+    int32_t ldc2;
+    int32_t reserved;
+} McwGemm;
+
+int mcw_mlp_gemm(const McwGemm *p, void *stream);
+
+/* out[j] = sum_i g[i * ldg + j] for j < n (bias gradients). */
+int mcw_mlp_colsum(const float *g, int32_t m, int32_t n, int32_t ldg, float *out, void *stream);
+
+/* Weighted mean squared error of y [m, n] against t: *loss += sum_ij w_j (y-t)^2 / (m n);
+ * grad (f32) and grad16 (bf16) receive its gradient with respect to y.  w may be NULL. */
+int mcw_mlp_loss(const float *y, int32_t ldy, const float *t, int32_t ldt, const float *w, int32_t m,
+                 int32_t n, float *grad, int32_t ldg, void *grad16, int32_t ldg16, float *loss,
+                 void *stream);
+
+/* Adam step `step` (1-based) on n FP32 master weights; w16 (bf16, optional) receives the
+ * updated weights for the GEMMs. */
+int mcw_mlp_adam(float *w, const float *g, float *m, float *v, void *w16, int64_t n, float lr,
+                 float beta1, float beta2, float eps, int64_t step, void *stream);
+
+/* y (bf16) = x (f32), n elements. */
+int mcw_mlp_cast_bf16(const float *x, void *y, int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCW_MLP_H */

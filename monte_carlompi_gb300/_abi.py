@@ -76,6 +76,22 @@ class LaunchC(ctypes.Structure):
                 ('regen_chunk', ctypes.c_int32), ('reserved', ctypes.c_int32)]
 
 
+class GemmC(ctypes.Structure):
+    """McwGemm of include/mcw_mlp.h."""
+    _fields_ = [('m', ctypes.c_int32), ('n', ctypes.c_int32), ('k', ctypes.c_int32),
+                ('trans_a', ctypes.c_int32), ('trans_b', ctypes.c_int32),
+                ('epilogue', ctypes.c_int32), ('a', ctypes.c_void_p), ('lda', ctypes.c_int32),
+                ('ldb', ctypes.c_int32), ('b', ctypes.c_void_p), ('bias', ctypes.c_void_p),
+                ('aux', ctypes.c_void_p), ('ldaux', ctypes.c_int32), ('ldc', ctypes.c_int32),
+                ('c', ctypes.c_void_p), ('c2', ctypes.c_void_p), ('ldc2', ctypes.c_int32),
+                ('reserved', ctypes.c_int32)]
+
+
+EPI_F32, EPI_BIAS_F32, EPI_BIAS_SILU, EPI_DSILU = 0, 1, 2, 3
+
+# entry points of include/mcw_mlp.h
+MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16']
+
 RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
                      ('theta_n', np.float32), ('phi_n', np.float32),
                      ('path_length', np.float32), ('snow_depth', np.float32),
@@ -129,6 +145,12 @@ def load(path=None):
                             ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         'mcw_walk_noalloc': ([ctypes.POINTER(ConfigC), ctypes.POINTER(SSPTableC),
                               ctypes.POINTER(SSPTableC), u64, vp, vp, vp], ctypes.c_int),
+        'mcw_mlp_gemm': ([ctypes.POINTER(GemmC), vp], ctypes.c_int),
+        'mcw_mlp_colsum': ([vp, i32, i32, i32, vp, vp], ctypes.c_int),
+        'mcw_mlp_loss': ([vp, i32, vp, i32, vp, i32, i32, vp, i32, vp, i32, vp, vp], ctypes.c_int),
+        'mcw_mlp_adam': ([vp, vp, vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                          ctypes.c_float, i64, vp], ctypes.c_int),
+        'mcw_mlp_cast_bf16': ([vp, vp, i64, vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

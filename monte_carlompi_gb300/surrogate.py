@@ -1,0 +1,353 @@
+"""BRF surrogate: an MLP from (r_eff, lambda, cos theta0, depth) to the 648-bin BRF and albedo.
+
+The reference's only route to a BRF is the Monte Carlo walk followed by the
+histogram arithmetic of post_processing.py:46-100.  This module learns that map
+from walks the GPU walk itself produces, so a BRF can be predicted in
+microseconds; plain Monte Carlo stays the fallback outside the training hull or
+where the ensemble disagrees, and the judge of the network's error.
+
+Network: 4 -> 256 -> 256 -> 256 -> 649, SiLU, BF16 weights and activations on
+tensor cores with FP32 accumulation (include/mcw_mlp.h), FP32 master weights and
+Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
+run those kernels; inputs and outputs are torch CUDA tensors, PyTorch is only the
+container.  Targets are standardised log(BRF + 0.02) per bin and log(albedo).
+"""
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+
+DIMS = (4, 256, 256, 256, 649)
+N_BRF = 648
+BRF_FLOOR = 0.02
+# training hull (BASELINE surrogate configuration)
+R_RANGE = (50.0, 1500.0)      # r_eff [um], log-uniform
+WVL_RANGE = (0.9, 1.8)        # centre wavelength [um]
+MU_RANGE = (0.3, 1.0)         # cos theta0
+DEPTH_RANGE = (0.01, 1.0)     # [m], log-uniform
+
+
+def encode(r_eff, wvl, mu0, depth):
+    """Inputs scaled to [-1, 1] over the training hull, float32 [n, 4]."""
+    r = np.log(np.asarray(r_eff, np.float64))
+    d = np.log(np.asarray(depth, np.float64))
+    x = np.stack([
+        2 * (r - math.log(R_RANGE[0])) / (math.log(R_RANGE[1]) - math.log(R_RANGE[0])) - 1,
+        2 * (np.asarray(wvl, np.float64) - WVL_RANGE[0]) / (WVL_RANGE[1] - WVL_RANGE[0]) - 1,
+        2 * (np.asarray(mu0, np.float64) - MU_RANGE[0]) / (MU_RANGE[1] - MU_RANGE[0]) - 1,
+        2 * (d - math.log(DEPTH_RANGE[0])) / (math.log(DEPTH_RANGE[1]) - math.log(DEPTH_RANGE[0])) - 1,
+    ], axis=-1)
+    return x.astype(np.float32)
+
+
+def in_hull(r_eff, wvl, mu0, depth):
+    x = encode(r_eff, wvl, mu0, depth)
+    return np.all(np.abs(x) <= 1.0 + 1e-6, axis=-1)
+
+
+def to_target(brf, albedo):
+    """Network target space: log(BRF + floor) per bin, log(albedo)."""
+    return np.concatenate([np.log(np.maximum(brf, 0) + BRF_FLOOR),
+                           np.log(np.maximum(albedo, 1e-6))[:, None]], axis=1).astype(np.float32)
+
+
+def from_target(y):
+    y = np.asarray(y, np.float64)
+    return np.exp(y[:, :N_BRF]) - BRF_FLOOR, np.exp(y[:, N_BRF])
+
+
+# ------------------------------------------------------------------ kernels
+
+def _stream(torch):
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _gemm(torch, epi, m, n, k, a, lda, b, ldb, c, ldc, trans_a=0, trans_b=0, bias=None, aux=None,
+          ldaux=0, c2=None, ldc2=0):
+    g = _abi.GemmC(m, n, k, trans_a, trans_b, epi, a.data_ptr(), lda, ldb, b.data_ptr(),
+                   bias.data_ptr() if bias is not None else None,
+                   aux.data_ptr() if aux is not None else None, ldaux, ldc, c.data_ptr(),
+                   c2.data_ptr() if c2 is not None else None, ldc2, 0)
+    rc = _abi.load().mcw_mlp_gemm(ctypes.byref(g), _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_gemm failed (m=%d n=%d k=%d)' % (m, n, k))
+
+
+def _cast(torch, x):
+    y = torch.empty(x.shape, dtype=torch.bfloat16, device=x.device)
+    rc = _abi.load().mcw_mlp_cast_bf16(_ptr(x), _ptr(y), x.numel(), _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_cast_bf16 failed')
+    return y
+
+
+def _colsum(torch, g):
+    m, n = g.shape
+    out = torch.empty(n, dtype=torch.float32, device=g.device)
+    rc = _abi.load().mcw_mlp_colsum(_ptr(g), m, n, n, _ptr(out), _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_colsum failed')
+    return out
+
+
+def forward_cached(torch, x16, w16, biases):
+    """Forward pass on the tensor-core kernels; returns (y fp32, cache for backward)."""
+    m = x16.shape[0]
+    a = x16
+    zs, acts = [], [x16]
+    for layer in range(3):
+        n, k = w16[layer].shape
+        z = torch.empty((m, n), dtype=torch.float32, device=x16.device)
+        nxt = torch.empty((m, n), dtype=torch.bfloat16, device=x16.device)
+        _gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a, k, w16[layer], k, nxt, n, bias=biases[layer],
+              c2=z, ldc2=n)
+        zs.append(z)
+        acts.append(nxt)
+        a = nxt
+    n, k = w16[3].shape
+    y = torch.empty((m, n), dtype=torch.float32, device=x16.device)
+    _gemm(torch, _abi.EPI_BIAS_F32, m, n, k, a, k, w16[3], k, y, n, bias=biases[3])
+    return y, (zs, acts)
+
+
+def backward_cached(torch, gy, w16, cache, need_dx=True):
+    """Backward pass: gradients of the weights, biases and (optionally) the input."""
+    zs, acts = cache
+    m = gy.shape[0]
+    g32 = gy.contiguous().float()
+    g16 = _cast(torch, g32)
+    dws, dbs = [None] * 4, [None] * 4
+    for layer in (3, 2, 1, 0):
+        n_out, k_in = w16[layer].shape
+        a_in = acts[layer]
+        dw = torch.empty((n_out, k_in), dtype=torch.float32, device=gy.device)
+        # dW[o, i] = sum_b G[b, o] A[b, i]
+        _gemm(torch, _abi.EPI_F32, n_out, k_in, m, g16, n_out, a_in, k_in, dw, k_in, trans_a=1, trans_b=1)
+        dws[layer] = dw
+        dbs[layer] = _colsum(torch, g32)
+        if layer == 0:
+            if not need_dx:
+                return None, dws, dbs
+            dx = torch.empty((m, k_in), dtype=torch.float32, device=gy.device)
+            _gemm(torch, _abi.EPI_F32, m, k_in, n_out, g16, n_out, w16[layer], k_in, dx, k_in, trans_b=1)
+            return dx, dws, dbs
+        # G_prev[b, i] = (sum_o G[b, o] W[o, i]) * silu'(Z_prev[b, i])
+        g16_prev = torch.empty((m, k_in), dtype=torch.bfloat16, device=gy.device)
+        g32_prev = torch.empty((m, k_in), dtype=torch.float32, device=gy.device)
+        _gemm(torch, _abi.EPI_DSILU, m, k_in, n_out, g16, n_out, w16[layer], k_in, g16_prev, k_in,
+              trans_b=1, aux=zs[layer - 1], ldaux=k_in, c2=g32_prev, ldc2=k_in)
+        g16, g32 = g16_prev, g32_prev
+
+
+def _mlp_function():
+    import torch
+
+    class MLPFunction(torch.autograd.Function):
+        """y = MLP(x) on the BF16 tensor-core kernels; params are FP32 masters
+        (W1, b1, ..., W4, b4).  Backward returns FP32 gradients for x and every
+        parameter."""
+
+        @staticmethod
+        def forward(ctx, x, *params):
+            ws, bs = params[0::2], params[1::2]
+            w16 = [_cast(torch, w.contiguous()) for w in ws]
+            x16 = _cast(torch, x.contiguous().float())
+            y, cache = forward_cached(torch, x16, w16, [b.contiguous() for b in bs])
+            ctx.save_for_backward(*w16, *cache[0], *cache[1])
+            return y
+
+        @staticmethod
+        def backward(ctx, gy):
+            saved = ctx.saved_tensors
+            w16, zs, acts = list(saved[:4]), list(saved[4:7]), list(saved[7:11])
+            dx, dws, dbs = backward_cached(torch, gy, w16, (zs, acts), need_dx=ctx.needs_input_grad[0])
+            out = [dx]
+            for dw, db in zip(dws, dbs):
+                out += [dw, db]
+            return tuple(out)
+
+    return MLPFunction
+
+
+_MLP_FN = None
+
+
+def mlp_apply(x, params):
+    global _MLP_FN
+    if _MLP_FN is None:
+        _MLP_FN = _mlp_function()
+    return _MLP_FN.apply(x, *params)
+
+
+# ------------------------------------------------------------------ model
+
+class SurrogateMLP:
+    """One network: FP32 master weights, BF16 copies, Adam moments (torch CUDA tensors)."""
+
+    def __init__(self, seed=0, device='cuda'):
+        import torch
+        self.torch = torch
+        g = torch.Generator(device='cpu').manual_seed(int(seed))
+        self.params = []
+        for fan_in, fan_out in zip(DIMS[:-1], DIMS[1:]):
+            bound = math.sqrt(6.0 / fan_in) if fan_out != DIMS[-1] else math.sqrt(3.0 / fan_in)
+            w = (torch.rand((fan_out, fan_in), generator=g) * 2 - 1) * bound
+            self.params += [w.to(device), torch.zeros(fan_out, device=device)]
+        self.m = [torch.zeros_like(p) for p in self.params]
+        self.v = [torch.zeros_like(p) for p in self.params]
+        self.w16 = [_cast(torch, w) for w in self.params[0::2]]
+        self.step = 0
+        self.y_mean = None
+        self.y_std = None
+
+    def predict_std(self, x):
+        """Standardised outputs for encoded inputs x (torch CUDA float32 [n, 4])."""
+        torch = self.torch
+        x16 = _cast(torch, x.contiguous().float())
+        y, _ = forward_cached(torch, x16, self.w16, self.params[1::2])
+        return y
+
+    def train_step(self, x16, t, w_out, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        """One Adam step on a batch (x16 bf16 [b, 4], t fp32 standardised targets)."""
+        torch = self.torch
+        m = x16.shape[0]
+        y, cache = forward_cached(torch, x16, self.w16, self.params[1::2])
+        n = y.shape[1]
+        grad = torch.empty_like(y)
+        grad16 = torch.empty((m, n), dtype=torch.bfloat16, device=y.device)
+        loss = torch.zeros(1, dtype=torch.float32, device=y.device)
+        L = _abi.load()
+        rc = L.mcw_mlp_loss(_ptr(y), n, _ptr(t), n, _ptr(w_out), m, n, _ptr(grad), n, _ptr(grad16), n,
+                            _ptr(loss), _stream(torch))
+        if rc:
+            raise _abi.McwError(rc, 'mcw_mlp_loss failed')
+        _, dws, dbs = backward_cached(torch, grad, self.w16, cache, need_dx=False)
+        self.step += 1
+        grads = []
+        for dw, db in zip(dws, dbs):
+            grads += [dw, db]
+        for i, (p, gr) in enumerate(zip(self.params, grads)):
+            w16 = self.w16[i // 2] if i % 2 == 0 else None
+            rc = L.mcw_mlp_adam(_ptr(p), _ptr(gr), _ptr(self.m[i]), _ptr(self.v[i]), _ptr(w16), p.numel(),
+                                lr, beta1, beta2, eps, self.step, _stream(torch))
+            if rc:
+                raise _abi.McwError(rc, 'mcw_mlp_adam failed')
+        return loss
+
+
+@dataclass
+class Dataset:
+    x: np.ndarray        # encoded inputs [n, 4]
+    y: np.ndarray        # target space [n, 649]
+    raw: np.ndarray      # (r_eff, wvl, mu0, depth) [n, 4]
+    brf: np.ndarray      # [n, 648]
+    albedo: np.ndarray   # [n]
+    photons: int
+
+
+def sample_inputs(n, seed):
+    rng = np.random.default_rng(seed)
+    r = np.exp(rng.uniform(np.log(R_RANGE[0]), np.log(R_RANGE[1]), n))
+    wvl = rng.uniform(*WVL_RANGE, n)
+    mu0 = rng.uniform(*MU_RANGE, n)
+    depth = np.exp(rng.uniform(np.log(DEPTH_RANGE[0]), np.log(DEPTH_RANGE[1]), n))
+    return np.stack([r, wvl, mu0, depth], axis=1)
+
+
+def mc_brf(walker, raw, n_photon, seed, half_width=0.085, R=0.5, chunk=1024):
+    """BRF (648 bins) and albedo of each input row by the GPU walk (n_photon photons each)."""
+    from . import ssp
+    from .config import WalkConfig
+    raw = np.asarray(raw, np.float64)
+    brf = np.zeros((raw.shape[0], N_BRF))
+    alb = np.zeros(raw.shape[0])
+    imp = ssp.synthetic_impurity_table(600, 2100)
+    for lo in range(0, raw.shape[0], chunk):
+        rows = raw[lo:lo + chunk]
+        tables, cfgs = [], []
+        for j, (r, wvl, mu0, depth) in enumerate(rows):
+            tables.append(ssp.synthetic_ice_table(r, 600, 2100))
+            tau = depth * ssp.ext_cff_mss_sphere(r) * 300.0
+            theta0 = math.degrees(math.acos(min(1.0, max(0.0, mu0))))
+            cfgs.append(WalkConfig(n_photon=int(n_photon), wvl0=float(wvl), half_width=half_width,
+                                   theta0_deg=min(theta0, 89.999), tau_tot=tau,
+                                   lambertian_reflectance=R, ice_table=j, rds_snw=float(r)))
+        walker.set_tables(tables, imp)
+        res = walker.walk(cfgs, seed + lo, mode='f32', records=None)
+        b, a = res.brf()
+        brf[lo:lo + len(rows)] = b
+        alb[lo:lo + len(rows)] = a
+    return brf, alb
+
+
+class Ensemble:
+    """Members trained on the same data from different initialisations and batch orders."""
+
+    def __init__(self, members):
+        self.members = members
+
+    def predict(self, raw):
+        """Mean BRF [n, 648], mean albedo [n], relative ensemble spread of the BRF [n]."""
+        import torch
+        x = torch.from_numpy(encode(*np.asarray(raw, np.float64).T)).cuda()
+        outs = []
+        for m in self.members:
+            ys = m.predict_std(x).double() * m.y_std + m.y_mean
+            outs.append(ys.cpu().numpy())
+        outs = np.stack(outs)
+        brfs, albs = zip(*[from_target(o) for o in outs])
+        brfs, albs = np.stack(brfs), np.stack(albs)
+        mean_brf = brfs.mean(0)
+        w = bin_weights()
+        spread = np.sqrt((brfs.std(0) ** 2 * w).sum(1) / w.sum()) / np.maximum(
+            (mean_brf * w).sum(1) / w.sum(), 1e-6)
+        return mean_brf, albs.mean(0), spread
+
+
+def bin_weights():
+    """Solid-angle weights sin(theta) cos(theta) of the 648 bins (the expected photon share)."""
+    mids = (np.arange(18) + 0.5) * (np.pi / 36)
+    w = np.sin(mids) * np.cos(mids)
+    return np.repeat(w / w.sum() / 36, 36)
+
+
+def rel_rms(pred, ref, weights=None):
+    """RMS relative BRF error per config, bins weighted by their photon share."""
+    w = bin_weights() if weights is None else weights
+    rel = (pred - ref) / np.maximum(np.abs(ref), 1e-6)
+    return np.sqrt((rel ** 2 * w).sum(axis=-1) / w.sum())
+
+
+def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
+    """Train an ensemble on a Dataset; returns Ensemble."""
+    import torch
+    y = ds.y.astype(np.float64)
+    y_mean, y_std = y.mean(0), np.maximum(y.std(0), 1e-3)
+    t_all = torch.from_numpy(((y - y_mean) / y_std).astype(np.float32)).cuda()
+    x_all = _cast(torch, torch.from_numpy(ds.x).cuda())
+    w_out = torch.ones(DIMS[-1], dtype=torch.float32, device='cuda')
+    out = []
+    n = ds.x.shape[0]
+    for k in range(members):
+        net = SurrogateMLP(seed=seed * 100 + k)
+        net.y_mean = torch.from_numpy(y_mean).cuda()
+        net.y_std = torch.from_numpy(y_std).cuda()
+        rng = np.random.default_rng(seed * 100 + k)
+        for ep in range(epochs):
+            perm = torch.from_numpy(rng.permutation(n)).cuda()
+            lr_ep = lr * (0.5 * (1 + math.cos(math.pi * ep / epochs)))
+            for lo in range(0, n - batch + 1, batch):
+                idx = perm[lo:lo + batch]
+                loss = net.train_step(x_all[idx].contiguous(), t_all[idx].contiguous(), w_out, lr=lr_ep)
+            if log and (ep % 50 == 0 or ep == epochs - 1):
+                log('member %d epoch %d loss %.5f' % (k, ep, float(loss)))
+        out.append(net)
+    torch.cuda.synchronize()
+    return Ensemble(out)

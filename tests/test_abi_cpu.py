@@ -12,8 +12,8 @@ from monte_carlompi_gb300 import _abi, walker
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    text = open(os.path.join(ROOT, 'include', 'mcwalk.h')).read()
+def header_functions(name='mcwalk.h'):
+    text = open(os.path.join(ROOT, 'include', name)).read()
     text = re.sub(r'/\*.*?\*/', '', text, flags=re.S)
     return sorted(set(re.findall(r'\b(mcw_[a-z_0-9]+)\s*\(', text)))
 
@@ -21,6 +21,8 @@ def header_functions():
 def test_library_exports_every_declared_symbol():
     declared = header_functions()
     assert sorted(_abi.EXPORTS) == declared
+    assert sorted(_abi.MLP_EXPORTS) == header_functions('mcw_mlp.h')
+    declared = declared + header_functions('mcw_mlp.h')
     lib = ctypes.CDLL(_abi.LIB_PATH)
     for name in declared:
         assert hasattr(lib, name), name

@@ -1,0 +1,141 @@
+"""Surrogate network kernels (GPU): BF16 tensor-core GEMMs with FP32 accumulation
+against a float64 reference of the same bf16 operands, the autograd Function's
+gradients against CPU float64 autograd, Adam against its formula, and training."""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip('torch')
+
+from monte_carlompi_gb300 import _abi, surrogate  # noqa: E402
+
+
+def _bf16(t):
+    return t.to(torch.bfloat16)
+
+
+@pytest.mark.parametrize('trans_a,trans_b', [(0, 0), (0, 1), (1, 0), (1, 1)])
+@pytest.mark.parametrize('m,n,k', [(100, 70, 37), (256, 649, 256), (64, 64, 4), (1, 5, 300)])
+def test_gemm_layouts_match_float64(trans_a, trans_b, m, n, k):
+    g = torch.Generator().manual_seed(m * 7 + n * 3 + k)
+    a = torch.randn((k, m) if trans_a else (m, k), generator=g)
+    b = torch.randn((k, n) if trans_b else (n, k), generator=g)
+    a16, b16 = _bf16(a).cuda(), _bf16(b).cuda()
+    c = torch.empty((m, n), dtype=torch.float32, device='cuda')
+    surrogate._gemm(torch, _abi.EPI_F32, m, n, k, a16, a16.shape[1], b16, b16.shape[1], c, n,
+                    trans_a=trans_a, trans_b=trans_b)
+    A = a16.cpu().double()
+    B = b16.cpu().double()
+    ref = (A.T if trans_a else A) @ (B if trans_b else B.T)
+    err = (c.cpu().double() - ref).abs().max().item()
+    assert err <= 1e-4 * max(1.0, ref.abs().max().item()) + 1e-5 * math.sqrt(k), err
+
+
+def test_gemm_epilogues():
+    g = torch.Generator().manual_seed(5)
+    m, n, k = 96, 200, 64
+    a16 = _bf16(torch.randn(m, k, generator=g)).cuda()
+    w16 = _bf16(torch.randn(n, k, generator=g) * 0.2).cuda()
+    bias = torch.randn(n, generator=g).cuda()
+    z = torch.empty((m, n), device='cuda')
+    act = torch.empty((m, n), dtype=torch.bfloat16, device='cuda')
+    surrogate._gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a16, k, w16, k, act, n, bias=bias, c2=z, ldc2=n)
+    zr = a16.cpu().double() @ w16.cpu().double().T + bias.cpu().double()
+    assert (z.cpu().double() - zr).abs().max().item() < 1e-4
+    ar = zr * torch.sigmoid(zr)
+    assert (act.cpu().double() - ar).abs().max().item() <= 0.01 * ar.abs().max().item()
+    # silu' epilogue on the same product
+    gout16 = torch.empty((m, n), dtype=torch.bfloat16, device='cuda')
+    gout32 = torch.empty((m, n), device='cuda')
+    surrogate._gemm(torch, _abi.EPI_DSILU, m, n, k, a16, k, w16, k, gout16, n, aux=z, ldaux=n,
+                    c2=gout32, ldc2=n)
+    s = torch.sigmoid(z.cpu().double())
+    ds = s * (1 + z.cpu().double() * (1 - s))
+    gr = (a16.cpu().double() @ w16.cpu().double().T) * ds
+    assert (gout32.cpu().double() - gr).abs().max().item() < 1e-3 * gr.abs().max().item()
+
+
+def _st(v):
+    """bf16 rounding in the forward pass, identity in the backward pass (as the kernels do)."""
+    return v + (v.to(torch.bfloat16).double() - v).detach()
+
+
+def _reference_mlp(x, params):
+    """float64 CPU network with the kernels' bf16 roundings of weights, input and activations."""
+    h = _st(x)
+    ws, bs = params[0::2], params[1::2]
+    for layer in range(4):
+        z = h @ _st(ws[layer]).T + bs[layer]
+        h = _st(z * torch.sigmoid(z)) if layer < 3 else z
+    return h
+
+
+def test_autograd_function_gradients_match_cpu():
+    net = surrogate.SurrogateMLP(seed=3)
+    g = torch.Generator().manual_seed(11)
+    x = (torch.rand(64, 4, generator=g) * 2 - 1)
+    params = [p.detach().clone().requires_grad_(True) for p in net.params]
+    xg = x.cuda().requires_grad_(True)
+    y = surrogate.mlp_apply(xg, params)
+    gy = torch.randn(y.shape, generator=g)
+    y.backward(gy.cuda())
+    cparams = [p.detach().cpu().double().requires_grad_(True) for p in net.params]
+    xc = x.double().requires_grad_(True)
+    yc = _reference_mlp(xc, cparams)
+    assert (y.detach().cpu().double() - yc.detach()).abs().max().item() < 2e-2 * yc.abs().max().item()
+    yc.backward(gy.double())
+    pairs = [(xg.grad, xc.grad)] + [(p.grad, c.grad) for p, c in zip(params, cparams)]
+    for got, ref in pairs:
+        got = got.detach().cpu().double().flatten()
+        ref = ref.detach().flatten()
+        rel = (got - ref).norm() / ref.norm()
+        cos = torch.dot(got, ref) / (got.norm() * ref.norm())
+        assert rel < 3e-2 and cos > 0.999, (rel.item(), cos.item())
+
+
+def test_adam_kernel_matches_formula():
+    n = 1000
+    g = torch.Generator().manual_seed(2)
+    w = torch.randn(n, generator=g)
+    gr = torch.randn(n, generator=g)
+    m = torch.randn(n, generator=g) * 0.1
+    v = torch.rand(n, generator=g) * 0.1
+    wd, gd, md, vd = w.cuda(), gr.cuda(), m.cuda(), v.cuda()
+    w16 = torch.empty(n, dtype=torch.bfloat16, device='cuda')
+    step, lr, b1, b2, eps = 7, 1e-3, 0.9, 0.999, 1e-8
+    rc = _abi.load().mcw_mlp_adam(wd.data_ptr(), gd.data_ptr(), md.data_ptr(), vd.data_ptr(),
+                                  w16.data_ptr(), n, lr, b1, b2, eps, step,
+                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    m2 = b1 * m + (1 - b1) * gr
+    v2 = b2 * v + (1 - b2) * gr * gr
+    w2 = w - lr * (m2 / (1 - b1 ** step)) / (torch.sqrt(v2 / (1 - b2 ** step)) + eps)
+    assert torch.allclose(wd.cpu(), w2, atol=1e-6)
+    assert torch.allclose(md.cpu(), m2, atol=1e-7) and torch.allclose(vd.cpu(), v2, atol=1e-7)
+    assert torch.equal(w16.cpu(), w2.to(torch.bfloat16))
+
+
+def test_training_fits_a_smooth_map():
+    """Train one network on a smooth 4 -> 649 map; the loss must fall a hundredfold."""
+    rng = np.random.default_rng(0)
+    n = 2048
+    x = rng.uniform(-1, 1, (n, 4)).astype(np.float32)
+    basis = rng.standard_normal((4, 649)) * 0.7
+    y = np.tanh(x @ basis) + 0.3 * np.sin(2 * x[:, :1])
+    y = ((y - y.mean(0)) / y.std(0)).astype(np.float32)
+    net = surrogate.SurrogateMLP(seed=1)
+    x16 = surrogate._cast(torch, torch.from_numpy(x).cuda())
+    t = torch.from_numpy(y).cuda()
+    w = torch.ones(649, device='cuda')
+    first = None
+    for ep in range(120):
+        perm = torch.from_numpy(rng.permutation(n)).cuda()
+        for lo in range(0, n, 256):
+            idx = perm[lo:lo + 256]
+            loss = float(net.train_step(x16[idx].contiguous(), t[idx].contiguous(), w, lr=2e-3))
+            first = loss if first is None else first
+    assert loss < first / 100, (first, loss)
