@@ -233,6 +233,54 @@ def run_sweep(args):
     return 0
 
 
+def run_surrogate(args):
+    """BASELINE surrogate configuration: 4,096 configs x 2e5 photons walked on the GPU,
+    5-member ensemble trained on the tensor-core kernels, 512 held-out configs judged by
+    1e6-photon Monte Carlo; BRF/s of the network against plain Monte Carlo."""
+    import time as _t
+    import torch
+    from monte_carlompi_gb300 import surrogate as S
+    from monte_carlompi_gb300.walker import Walker
+    n_cfg, n_train_photons = args.surrogate_configs, 200000
+    w = Walker(0)
+    t0 = _t.perf_counter()
+    ds = S.make_dataset(w, n_cfg, n_train_photons, seed=0x5EED0004)
+    t_data = _t.perf_counter() - t0
+    n_hold = min(512, n_cfg // 8)
+    train_ds = S.Dataset(ds.x[n_hold:], ds.y[n_hold:], ds.raw[n_hold:], ds.brf[n_hold:],
+                         ds.albedo[n_hold:], ds.photons)
+    t0 = _t.perf_counter()
+    ens = S.train(train_ds, members=5, epochs=args.surrogate_epochs, batch=256, lr=1e-3, seed=4)
+    t_train = _t.perf_counter() - t0
+    hold = ds.raw[:n_hold]
+    t0 = _t.perf_counter()
+    ref_brf, ref_alb = S.mc_brf(w, hold, 1000000, seed=0x5EED0044)
+    t_ref = _t.perf_counter() - t0
+    ref2_brf, _ = S.mc_brf(w, hold, 1000000, seed=0x5EED0045)
+    pred_brf, pred_alb, spread = ens.predict(hold)
+    err = S.rel_rms(pred_brf, ref_brf)
+    floor = S.rel_rms(ref2_brf, ref_brf) / np.sqrt(2)
+    err_small_mc = S.rel_rms(ds.brf[:n_hold], ref_brf)
+    rate_net = S.inference_rate(ens)
+    rate_mc = n_hold / t_ref
+    line = {'metric': METRIC, 'workload': 'surrogate', 'value': rate_net, 'unit': 'BRF/s',
+            'higher_is_better': True, 'dtype': 'bf16 (fp32 accumulate)', 'data': 'synthetic',
+            'config': {'configs': n_cfg, 'held_out': n_hold, 'train_photons': n_train_photons,
+                       'judge_photons': 1000000, 'members': 5, 'epochs': args.surrogate_epochs,
+                       'batch': 256, 'net': '4-256-256-256-649 SiLU'},
+            'mc_brf_per_s': rate_mc, 'speedup_vs_mc': rate_net / rate_mc,
+            'rms_rel_brf_err_vs_1e6_mc': {'median': float(np.median(err)), 'mean': float(np.mean(err)),
+                                          'p90': float(np.percentile(err, 90))},
+            'mc_1e6_noise_floor': float(np.median(floor)),
+            'mc_2e5_err_vs_1e6_mc': float(np.median(err_small_mc)),
+            'albedo_abs_err_median': float(np.median(np.abs(pred_alb - ref_alb))),
+            'ensemble_spread_median': float(np.median(spread)),
+            'seconds': {'data': t_data, 'train': t_train, 'judge_mc': t_ref}}
+    print(json.dumps(line))
+    w.close()
+    return 0
+
+
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
@@ -395,12 +443,16 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep'])
+    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate'])
+    ap.add_argument('--surrogate-configs', type=int, default=4096)
+    ap.add_argument('--surrogate-epochs', type=int, default=300)
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
     if args.workload == 'sweep':
         return run_sweep(args)
+    if args.workload == 'surrogate':
+        return run_surrogate(args)
     return run_ours(args)
 
 

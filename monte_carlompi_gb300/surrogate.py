@@ -332,7 +332,7 @@ def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
     y_mean, y_std = y.mean(0), np.maximum(y.std(0), 1e-3)
     t_all = torch.from_numpy(((y - y_mean) / y_std).astype(np.float32)).cuda()
     x_all = _cast(torch, torch.from_numpy(ds.x).cuda())
-    w_out = torch.ones(DIMS[-1], dtype=torch.float32, device='cuda')
+    w_out = torch.from_numpy(output_weights()).cuda()
     out = []
     n = ds.x.shape[0]
     for k in range(members):
@@ -351,3 +351,57 @@ def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
         out.append(net)
     torch.cuda.synchronize()
     return Ensemble(out)
+
+
+def save(ensemble, path):
+    """FP32 master weights, Adam state and target scaling of every member (torch.save)."""
+    import torch
+    torch.save([{'params': [p.cpu() for p in m.params], 'm': [x.cpu() for x in m.m],
+                 'v': [x.cpu() for x in m.v], 'step': m.step, 'y_mean': m.y_mean.cpu(),
+                 'y_std': m.y_std.cpu()} for m in ensemble.members], path)
+
+
+def load(path):
+    import torch
+    members = []
+    for d in torch.load(path):
+        net = SurrogateMLP()
+        net.params = [p.cuda() for p in d['params']]
+        net.m = [x.cuda() for x in d['m']]
+        net.v = [x.cuda() for x in d['v']]
+        net.w16 = [_cast(torch, w) for w in net.params[0::2]]
+        net.step = d['step']
+        net.y_mean, net.y_std = d['y_mean'].cuda(), d['y_std'].cuda()
+        members.append(net)
+    return Ensemble(members)
+
+
+def make_dataset(walker, n_cfg, n_photon, seed):
+    raw = sample_inputs(n_cfg, seed)
+    brf, alb = mc_brf(walker, raw, n_photon, seed)
+    x = encode(*raw.T)
+    return Dataset(x=x, y=to_target(brf, alb), raw=raw, brf=brf, albedo=alb, photons=n_photon)
+
+
+def output_weights():
+    """Loss weights: BRF bins by their photon share (mean 1), albedo 10."""
+    w = bin_weights()
+    w = w / w.mean()
+    return np.concatenate([w, [10.0]]).astype(np.float32)
+
+
+def inference_rate(ensemble, batch=65536, reps=20):
+    """BRF predictions per second of one member on the tensor-core kernels (CUDA events)."""
+    import torch
+    m = ensemble.members[0]
+    x = torch.rand((batch, 4), device='cuda') * 2 - 1
+    for _ in range(3):
+        m.predict_std(x)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        m.predict_std(x)
+    e1.record()
+    torch.cuda.synchronize()
+    return batch * reps / (e0.elapsed_time(e1) / 1e3)
