@@ -257,8 +257,10 @@ def run_surrogate(args):
     ref_brf, ref_alb = S.mc_brf(w, hold, 1000000, seed=0x5EED0044)
     t_ref = _t.perf_counter() - t0
     ref2_brf, _ = S.mc_brf(w, hold, 1000000, seed=0x5EED0045)
+    ref7_brf, _ = S.mc_brf(w, hold, 10000000, seed=0x5EED0046)
     pred_brf, pred_alb, spread = ens.predict(hold)
     err = S.rel_rms(pred_brf, ref_brf)
+    err7 = S.rel_rms(pred_brf, ref7_brf)
     floor = S.rel_rms(ref2_brf, ref_brf) / np.sqrt(2)
     err_small_mc = S.rel_rms(ds.brf[:n_hold], ref_brf)
     rate_net = S.inference_rate(ens)
@@ -271,7 +273,10 @@ def run_surrogate(args):
             'mc_brf_per_s': rate_mc, 'speedup_vs_mc': rate_net / rate_mc,
             'rms_rel_brf_err_vs_1e6_mc': {'median': float(np.median(err)), 'mean': float(np.mean(err)),
                                           'p90': float(np.percentile(err, 90))},
+            'rms_rel_brf_err_vs_1e7_mc': {'median': float(np.median(err7)), 'mean': float(np.mean(err7)),
+                                          'p90': float(np.percentile(err7, 90))},
             'mc_1e6_noise_floor': float(np.median(floor)),
+            'mc_1e7_noise_floor_est': float(np.median(floor)) / np.sqrt(10),
             'mc_2e5_err_vs_1e6_mc': float(np.median(err_small_mc)),
             'albedo_abs_err_median': float(np.median(np.abs(pred_alb - ref_alb))),
             'ensemble_spread_median': float(np.median(spread)),

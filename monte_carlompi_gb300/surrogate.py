@@ -10,7 +10,8 @@ Network: 4 -> 256 -> 256 -> 256 -> 649, SiLU, BF16 weights and activations on
 tensor cores with FP32 accumulation (include/mcw_mlp.h), FP32 master weights and
 Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
 run those kernels; inputs and outputs are torch CUDA tensors, PyTorch is only the
-container.  Targets are standardised log(BRF + 0.02) per bin and log(albedo).
+container.  Targets are standardised log(BRF / albedo + 0.02) per bin and
+log(albedo).
 """
 import ctypes
 import math
@@ -49,14 +50,17 @@ def in_hull(r_eff, wvl, mu0, depth):
 
 
 def to_target(brf, albedo):
-    """Network target space: log(BRF + floor) per bin, log(albedo)."""
-    return np.concatenate([np.log(np.maximum(brf, 0) + BRF_FLOOR),
-                           np.log(np.maximum(albedo, 1e-6))[:, None]], axis=1).astype(np.float32)
+    """Network target space: log(BRF / albedo + floor) per bin (the shape, about 1 on
+    average) and log(albedo), so every bin keeps relative precision."""
+    a = np.maximum(np.asarray(albedo, np.float64), 1e-6)
+    shape = np.maximum(np.asarray(brf, np.float64), 0) / a[:, None]
+    return np.concatenate([np.log(shape + BRF_FLOOR), np.log(a)[:, None]], axis=1).astype(np.float32)
 
 
 def from_target(y):
     y = np.asarray(y, np.float64)
-    return np.exp(y[:, :N_BRF]) - BRF_FLOOR, np.exp(y[:, N_BRF])
+    a = np.exp(y[:, N_BRF])
+    return (np.exp(y[:, :N_BRF]) - BRF_FLOOR) * a[:, None], a
 
 
 # ------------------------------------------------------------------ kernels
@@ -319,10 +323,10 @@ def bin_weights():
 
 
 def rel_rms(pred, ref, weights=None):
-    """RMS relative BRF error per config, bins weighted by their photon share."""
+    """RMS relative BRF error per config: sqrt(sum_b w_b (pred - ref)^2 / sum_b w_b ref^2),
+    bins weighted by their solid-angle share w_b (the photons they receive)."""
     w = bin_weights() if weights is None else weights
-    rel = (pred - ref) / np.maximum(np.abs(ref), 1e-6)
-    return np.sqrt((rel ** 2 * w).sum(axis=-1) / w.sum())
+    return np.sqrt(((pred - ref) ** 2 * w).sum(axis=-1) / np.maximum((ref ** 2 * w).sum(axis=-1), 1e-30))
 
 
 def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
