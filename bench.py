@@ -265,6 +265,7 @@ def run_surrogate(args):
     err_small_mc = S.rel_rms(ds.brf[:n_hold], ref_brf)
     rate_net = S.inference_rate(ens)
     rate_mc = n_hold / t_ref
+    inv = run_inverse(ens, w, args.inverse_configs) if args.inverse_configs > 0 else None
     line = {'metric': METRIC, 'workload': 'surrogate', 'value': rate_net, 'unit': 'BRF/s',
             'higher_is_better': True, 'dtype': 'bf16 (fp32 accumulate)', 'data': 'synthetic',
             'config': {'configs': n_cfg, 'held_out': n_hold, 'train_photons': n_train_photons,
@@ -280,10 +281,46 @@ def run_surrogate(args):
             'mc_2e5_err_vs_1e6_mc': float(np.median(err_small_mc)),
             'albedo_abs_err_median': float(np.median(np.abs(pred_alb - ref_alb))),
             'ensemble_spread_median': float(np.median(spread)),
-            'seconds': {'data': t_data, 'train': t_train, 'judge_mc': t_ref}}
+            'seconds': {'data': t_data, 'train': t_train, 'judge_mc': t_ref},
+            'inverse': inv}
     print(json.dumps(line))
     w.close()
     return 0
+
+
+def run_inverse(ens, walker, n_obs):
+    """BASELINE inverse configuration: observed BRFs from 1e6-photon MC at hidden r_eff
+    (log-uniform 50-1500 um, known lambda, theta0, depth) plus 1% Gaussian noise; Gauss-Newton
+    on log r_eff through the surrogate with MC fallback where the ensemble spread exceeds 2%,
+    against the same Gauss-Newton driven by plain MC on a subset."""
+    import time as _t
+    from monte_carlompi_gb300 import inverse as I
+    from monte_carlompi_gb300 import surrogate as S
+    raw = S.sample_inputs(n_obs, 0x5EED0005)
+    t0 = _t.perf_counter()
+    obs, _ = S.mc_brf(walker, raw, 1000000, seed=0x5EED0050)
+    t_obs = _t.perf_counter() - t0
+    obs = obs * (1 + 0.01 * np.random.default_rng(0x5EED0051).standard_normal(obs.shape))
+    known = raw[:, 1:]
+    res = I.retrieve(ens, walker, obs, known)
+    err = np.abs(res['r_eff'] / raw[:, 0] - 1)
+    # the same retrieval with plain Monte Carlo only, on a subset
+    n_sub = min(128, n_obs)
+    t0 = _t.perf_counter()
+    s_grid = np.full(n_sub, np.mean(I.LOG_R))
+    s_mc, evals = I.mc_gn(walker, obs[:n_sub], known[:n_sub], s_grid, iters=5)
+    t_mc = _t.perf_counter() - t0
+    err_mc = np.abs(np.exp(s_mc) / raw[:n_sub, 0] - 1)
+    t_sur = res['seconds_net'] + res['seconds_mc']
+    return {'observations': n_obs, 'obs_photons': 1000000, 'noise': 0.01,
+            'flagged_for_mc': float(res['flagged'].mean()),
+            'r_eff_rel_err': {'median': float(np.median(err)), 'p90': float(np.percentile(err, 90))},
+            'r_eff_rel_err_unflagged_median': float(np.median(err[~res['flagged']])) if np.any(~res['flagged']) else None,
+            'seconds_surrogate_path': t_sur, 'seconds_per_retrieval': t_sur / n_obs,
+            'mc_only': {'subset': n_sub, 'r_eff_rel_err_median': float(np.median(err_mc)),
+                        'seconds_per_retrieval': t_mc / n_sub, 'brf_evals': evals},
+            'speedup_per_retrieval_vs_mc': (t_mc / n_sub) / (t_sur / n_obs),
+            'seconds_obs_generation': t_obs}
 
 
 def run_reference(args):
@@ -451,6 +488,7 @@ def main():
     ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate'])
     ap.add_argument('--surrogate-configs', type=int, default=4096)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
+    ap.add_argument('--inverse-configs', type=int, default=4096)
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)

@@ -1,0 +1,112 @@
+"""Grain-size retrieval: batched Gauss-Newton on log r_eff through the BRF surrogate.
+
+Given observed 648-bin BRFs with known wavelength, incident zenith and depth,
+find r_eff.  Each iteration evaluates the ensemble and the exact Jacobian
+d BRF / d log r_eff by reverse-mode autograd through the surrogate's
+torch.autograd.Function (one backward pass per output bin, batched by
+replicating each config once per bin).  Retrievals whose ensemble spread at the
+solution exceeds ``spread_tol`` fall back to plain Monte Carlo: the same
+Gauss-Newton iteration with BRFs and central-difference Jacobians from the GPU
+walk.  The reference has no inverse; this consumes the same BRF definition
+(post_processing.py:73-81, 2-D form).
+"""
+import math
+import time
+
+import numpy as np
+
+from . import surrogate as S
+
+LOG_R = (math.log(S.R_RANGE[0]), math.log(S.R_RANGE[1]))
+
+
+def _brf_and_jacobian(ens, s, known, chunk=96):
+    """Ensemble-mean BRF [n, 648] and d BRF / d log r [n, 648] at log r = s."""
+    import torch
+    n = s.shape[0]
+    f_out = np.zeros((n, S.N_BRF))
+    j_out = np.zeros((n, S.N_BRF))
+    dxds = 2.0 / (LOG_R[1] - LOG_R[0])
+    eye = torch.eye(S.N_BRF, device='cuda', dtype=torch.float64)
+    for lo in range(0, n, chunk):
+        hi = min(n, lo + chunk)
+        rows = hi - lo
+        x = torch.from_numpy(S.encode(np.exp(s[lo:hi]), known[lo:hi, 0], known[lo:hi, 1],
+                                      known[lo:hi, 2])).cuda()
+        # each config once per output bin: row (c, b) back-propagates bin b of config c
+        xr = x.repeat_interleave(S.N_BRF, dim=0).requires_grad_(True)
+        f_acc = torch.zeros((rows, S.N_BRF), dtype=torch.float64, device='cuda')
+        j_acc = torch.zeros((rows, S.N_BRF), dtype=torch.float64, device='cuda')
+        for m in ens.members:
+            y = S.mlp_apply(xr, m.params).double() * m.y_std + m.y_mean
+            alb = torch.exp(y[:, S.N_BRF])
+            brf = (torch.exp(y[:, :S.N_BRF]) - S.BRF_FLOOR) * alb[:, None]
+            sel = (brf.view(rows, S.N_BRF, S.N_BRF) * eye).sum(-1)        # [rows, bins]
+            g, = torch.autograd.grad(sel.sum(), xr)
+            f_acc += sel.detach()
+            j_acc += g[:, 0].view(rows, S.N_BRF).double() * dxds
+        f_out[lo:hi] = (f_acc / len(ens.members)).cpu().numpy()
+        j_out[lo:hi] = (j_acc / len(ens.members)).cpu().numpy()
+    return f_out, j_out
+
+
+def _gn_update(f, jac, obs, s, w, damping=1e-3, max_step=0.7):
+    r = f - obs
+    jtr = (w * jac * r).sum(1)
+    jtj = (w * jac * jac).sum(1)
+    step = -jtr / (jtj * (1 + damping) + 1e-30)
+    step = np.clip(step, -max_step, max_step)
+    return np.clip(s + step, LOG_R[0], LOG_R[1])
+
+
+def surrogate_gn(ens, obs, known, iters=6):
+    """Gauss-Newton on s = log r_eff through the surrogate; starts from the best of a
+    16-point grid.  Returns (s, brf at s, ensemble spread at s)."""
+    n = obs.shape[0]
+    w = S.bin_weights()[None, :]
+    grid = np.linspace(LOG_R[0], LOG_R[1], 16)
+    best = np.full(n, np.inf)
+    s = np.zeros(n)
+    for g in grid:
+        pred, _, _ = ens.predict(np.column_stack([np.full(n, math.exp(g)), known]))
+        cost = (w * (pred - obs) ** 2).sum(1)
+        better = cost < best
+        best[better] = cost[better]
+        s[better] = g
+    for _ in range(iters):
+        f, jac = _brf_and_jacobian(ens, s, known)
+        s = _gn_update(f, jac, obs, s, w)
+    pred, _, spread = ens.predict(np.column_stack([np.exp(s), known]))
+    return s, pred, spread
+
+
+def mc_gn(walker, obs, known, s0, n_photon=1000000, iters=3, h=0.05, seed=0x5EED0055):
+    """Gauss-Newton on log r_eff with BRFs and central-difference Jacobians from the walk."""
+    w = S.bin_weights()[None, :]
+    s = np.array(s0, dtype=np.float64)
+    evals = 0
+    for it in range(iters):
+        rows = np.concatenate([np.column_stack([np.exp(s + d), known]) for d in (0.0, h, -h)])
+        brf, _ = S.mc_brf(walker, rows, n_photon, seed + 1000 * it)
+        evals += rows.shape[0]
+        n = s.shape[0]
+        f, fp, fm = brf[:n], brf[n:2 * n], brf[2 * n:]
+        s = _gn_update(f, (fp - fm) / (2 * h), obs, s, w)
+    return s, evals
+
+
+def retrieve(ens, walker, obs, known, spread_tol=0.02, mc_photons=1000000):
+    """Surrogate retrieval with Monte Carlo fallback.  Returns dict of results and timings."""
+    t0 = time.perf_counter()
+    s, _, spread = surrogate_gn(ens, obs, known)
+    t_net = time.perf_counter() - t0
+    flagged = spread > spread_tol
+    t0 = time.perf_counter()
+    mc_evals = 0
+    if np.any(flagged):
+        s_mc, mc_evals = mc_gn(walker, obs[flagged], known[flagged], s[flagged], n_photon=mc_photons)
+        s = s.copy()
+        s[flagged] = s_mc
+    t_mc = time.perf_counter() - t0
+    return dict(r_eff=np.exp(s), flagged=flagged, spread=spread, seconds_net=t_net, seconds_mc=t_mc,
+                mc_brf_evals=mc_evals)

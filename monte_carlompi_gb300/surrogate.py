@@ -310,8 +310,8 @@ class Ensemble:
         brfs, albs = np.stack(brfs), np.stack(albs)
         mean_brf = brfs.mean(0)
         w = bin_weights()
-        spread = np.sqrt((brfs.std(0) ** 2 * w).sum(1) / w.sum()) / np.maximum(
-            (mean_brf * w).sum(1) / w.sum(), 1e-6)
+        # member spread in the units of rel_rms: weighted RMS std over weighted RMS BRF
+        spread = np.sqrt((brfs.std(0) ** 2 * w).sum(1) / np.maximum((mean_brf ** 2 * w).sum(1), 1e-30))
         return mean_brf, albs.mean(0), spread
 
 
