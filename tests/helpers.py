@@ -89,3 +89,20 @@ def chi2_two_sample(a, b):
     x2 = float(np.sum((ka * a - kb * b) ** 2 / (a + b)))
     dof = int(m.sum()) - 1
     return x2, dof, float(chi2.sf(x2, dof))
+
+
+def reference_mlp(x, params):
+    """float64 CPU copy of the surrogate network with the kernels' bf16 roundings of
+    weights, input and activations (rounded in the forward pass, identity in the
+    backward pass, as the kernels differentiate)."""
+    import torch
+
+    def st(v):
+        return v + (v.to(torch.bfloat16).double() - v).detach()
+
+    h = st(x)
+    ws, bs = params[0::2], params[1::2]
+    for layer in range(4):
+        z = h @ st(ws[layer]).T + bs[layer]
+        h = st(z * torch.sigmoid(z)) if layer < 3 else z
+    return h

@@ -36,20 +36,38 @@ def test_network_beats_the_monte_carlo_it_learned_from(walker, trained):
     assert surrogate.inference_rate(ens, batch=16384, reps=5) > 1e6
 
 
-def test_jacobian_matches_finite_differences(trained):
+def test_jacobian_matches_cpu_autograd(trained):
+    """d BRF / d log r_eff from the batched autograd pass through the kernels equals
+    float64 CPU autograd of the same network (bf16 roundings included)."""
+    from tests.helpers import reference_mlp
     ens, ds, _ = trained
-    known = ds.raw[:16, 1:]
-    s = np.log(ds.raw[:16, 0])
-    f, jac = inverse._brf_and_jacobian(ens, s, known)
-    h = 1e-2
-    fp, _, _ = ens.predict(np.column_stack([np.exp(s + h), known]))
-    fm, _, _ = ens.predict(np.column_stack([np.exp(s - h), known]))
-    fd = (fp - fm) / (2 * h)
-    f0, _, _ = ens.predict(np.column_stack([np.exp(s), known]))
-    assert np.max(np.abs(f - f0)) < 1e-3 * np.max(np.abs(f0))
+    one = surrogate.Ensemble(ens.members[:1])
+    m = ens.members[0]
+    known = ds.raw[:8, 1:]
+    s = np.log(ds.raw[:8, 0])
+    f, jac = inverse._brf_and_jacobian(one, s, known)
+    params = [p.detach().cpu().double() for p in m.params]
+    y_mean, y_std = m.y_mean.cpu().double(), m.y_std.cpu().double()
+    lo, hi = inverse.LOG_R
+
+    def brf_of(sv):
+        r = torch.exp(sv)
+        x = torch.stack([2 * (torch.log(r) - lo) / (hi - lo) - 1,
+                         *[torch.from_numpy(surrogate.encode(np.exp(s), known[:, 0], known[:, 1],
+                                                             known[:, 2])[:, k]).double()
+                           for k in (1, 2, 3)]], dim=1)
+        y = reference_mlp(x, params) * y_std + y_mean
+        alb = torch.exp(y[:, surrogate.N_BRF])
+        return (torch.exp(y[:, :surrogate.N_BRF]) - surrogate.BRF_FLOOR) * alb[:, None]
+
+    sv = torch.from_numpy(s).double().requires_grad_(True)
+    ref_f = brf_of(sv)
+    ref_j = torch.stack([torch.autograd.grad(ref_f[:, b].sum(), sv, retain_graph=True)[0]
+                         for b in range(surrogate.N_BRF)], dim=1).numpy()
     w = surrogate.bin_weights()
-    rel = np.sqrt(((jac - fd) ** 2 * w).sum(1) / ((fd ** 2 * w).sum(1) + 1e-30))
-    assert np.median(rel) < 0.05, np.median(rel)
+    assert np.max(np.abs(f - ref_f.detach().numpy())) < 2e-2 * np.max(np.abs(f))
+    rel = np.sqrt(((jac - ref_j) ** 2 * w).sum(1) / ((ref_j ** 2 * w).sum(1) + 1e-30))
+    assert np.median(rel) < 0.03, np.median(rel)
 
 
 def test_gauss_newton_recovers_r_eff_on_network_brfs(trained):
