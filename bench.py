@@ -288,6 +288,36 @@ def run_surrogate(args):
     return 0
 
 
+def run_mlp(args):
+    """Surrogate network forward (inference) on the BF16 tensor-core kernels: BRF/s and
+    TFLOP/s of the GEMMs against the measured bf16 peak."""
+    import torch
+    from monte_carlompi_gb300 import surrogate as S
+    batch = 65536
+    net = S.SurrogateMLP(seed=0)
+    x = torch.rand((batch, 4), device='cuda') * 2 - 1
+    for _ in range(args.warmup):
+        net.predict_std(x)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        net.predict_std(x)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flop = 2.0 * batch * sum(a * b for a, b in zip(S.DIMS[:-1], S.DIMS[1:]))
+    peaks, src = measured_peaks()
+    tflops = flop / (ms / 1e3) / 1e12
+    peak = float(peaks.get('bf16_tflops') or 1900.0)
+    print(json.dumps({'metric': METRIC, 'workload': 'mlp', 'value': batch / (ms / 1e3), 'unit': 'BRF/s',
+                      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms, 'dtype': 'bf16',
+                      'config': {'batch': batch, 'net': '4-256-256-256-649 SiLU', 'kernels': 'mma.sync m16n8k16'},
+                      'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s',
+                                   'frac': tflops / peak, 'peak_source': src}}))
+    return 0
+
+
 def run_inverse(ens, walker, n_obs):
     """BASELINE inverse configuration: observed BRFs from 1e6-photon MC at hidden r_eff
     (log-uniform 50-1500 um, known lambda, theta0, depth) plus 1% Gaussian noise; Gauss-Newton
@@ -485,7 +515,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate'])
+    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp'])
     ap.add_argument('--surrogate-configs', type=int, default=4096)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
@@ -496,6 +526,8 @@ def main():
         return run_sweep(args)
     if args.workload == 'surrogate':
         return run_surrogate(args)
+    if args.workload == 'mlp':
+        return run_mlp(args)
     return run_ours(args)
 
 
