@@ -51,6 +51,8 @@ constexpr int kFinishCap = 64;                         // finish queue entries p
 // scatter events per loop round: their Philox blocks are computed together so
 // the ten dependent Philox rounds of one overlap those of the others
 constexpr int kStepsPerRound = MCW_STEPS_PER_ROUND;
+// a warp with at most this many active lanes shares the Philox work of a round
+constexpr int kSparseWarp = 32 / kStepsPerRound;
 
 // Per-config values the FP32 walk reads at photon birth.
 struct CfgF32 {
@@ -110,6 +112,8 @@ struct __align__(16) FinishSlot {
 struct WarpQueues {
     BirthSlot birth[32];
     FinishSlot fin[kFinishCap];
+    uint4 rmeta[32];                          // (stream id lo, hi, step) by active rank
+    uint4 rbuf[32][kStepsPerRound + 1];       // step blocks by active rank (padded row)
     WarpTally tally;
 };
 
@@ -429,13 +433,41 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
 
         // ---- kStepsPerRound scatter events per active lane; their Philox blocks
         // are independent of the walk, so they are computed together first
-        int cond = 0;
-        if (P.cfg >= 0) {
-            uint4 rb[kStepsPerRound];
-            const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
+        // The round's step blocks.  A well-filled warp computes them lane by lane,
+        // each lane the four its photon needs.  A sparse warp (the end of a
+        // launch, when the last walks run almost alone) shares the work: active
+        // lanes publish (stream id, step) by rank, every lane computes some of
+        // the n_act * kStepsPerRound blocks, and the chains run side by side
+        // instead of one after another.
+        const unsigned act = ~idle;
+        const bool me_active = P.cfg >= 0;
+        const int n_act = __popc(act);
+        uint4 rb[kStepsPerRound];
+        if (n_act > kSparseWarp) {
+            if (me_active) {
+                const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
 #pragma unroll
-            for (int k = 0; k < kStepsPerRound; ++k)
-                rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
+                for (int k = 0; k < kStepsPerRound; ++k)
+                    rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
+            }
+        } else {
+            const int rank = __popc(act & lt_mask);
+            if (me_active) q.rmeta[rank] = make_uint4((uint32_t)P.rid, (uint32_t)(P.rid >> 32), (uint32_t)P.i, 0u);
+            __syncwarp();
+            const int t = lane;  // n_act * kStepsPerRound <= 32: one block per lane at most
+            if (t < n_act * kStepsPerRound) {
+                const int j = t / kStepsPerRound, k = t % kStepsPerRound;
+                const uint4 m = q.rmeta[j];
+                q.rbuf[j][k] = philox10(make_uint4(m.z + 1u + k, kTagStep, m.x, m.y), a.keys);
+            }
+            __syncwarp();
+            if (me_active) {
+#pragma unroll
+                for (int k = 0; k < kStepsPerRound; ++k) rb[k] = q.rbuf[rank][k];
+            }
+        }
+        int cond = 0;
+        if (me_active) {
 #pragma unroll
             for (int k = 0; k < kStepsPerRound; ++k) {
                 // a lane whose photon ended earlier in the round keeps its final state
