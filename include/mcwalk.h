@@ -222,6 +222,28 @@ int mcw_write_csv(const char *path, const void *records, int32_t mode, int64_t n
 int mcw_format_csv(const void *records, int32_t mode, int64_t n, int32_t header, char *buf,
                    size_t cap, size_t *used);
 
+/* Per-config sums over records for the reference's post-processing. */
+typedef struct {
+    uint64_t q_cond_fx[6];     /* wvn sum per end condition, fixed point 2^-32 */
+    uint64_t n_cond[6];        /* photons per end condition */
+    uint64_t sum_n_scat;
+    double sum_path_length;    /* [m] */
+    double sum_wavelength;     /* sum of 1 / wvn [um] */
+} mcw_post_stats;
+
+/* Post-processing of records on the device (records: host or device pointer, see
+ * records_where; mode selects mcw_record32 / mcw_record64; photons are grouped by
+ * their config field, which must be < n_cfg): the wvn-weighted condition-1 exit
+ * zenith histogram with np.histogram's binning of [0, pi/2] into n_bins bins
+ * (post_processing.py:73-77 brf, :132-134 polar BRFs), and per-config sums for
+ * albedo, the albedo with transmitted photons, mean wavelength, mean n_scat and
+ * mean path length (post_processing.py:250-312, :380-430; monte_carlo3D.py:
+ * 1659-1671).  Outputs are host arrays: bin_wvn_fx and bin_count [n_cfg * n_bins]
+ * (may be NULL when n_bins is 0), stats [n_cfg]. */
+int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t mode, int64_t n,
+             int32_t n_cfg, int32_t n_bins, uint64_t *bin_wvn_fx, uint32_t *bin_count,
+             mcw_post_stats *stats);
+
 /* Largest wavelength lookup table mcw_walk_noalloc holds: grid points of
  * lambda = k / 100 um over wvl0 +- 6.5 sigma, so FWHM up to about 3.6 um. */
 #define MCW_NOALLOC_MAX_LUT 2048

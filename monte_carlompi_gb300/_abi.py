@@ -25,7 +25,7 @@ EXPORTS = ['mcw_abi_version', 'mcw_version', 'mcw_create', 'mcw_destroy', 'mcw_l
            'mcw_set_tables', 'mcw_set_launch', 'mcw_get_launch', 'mcw_set_budget', 'mcw_walk',
            'mcw_brf', 'mcw_autotune', 'mcw_graph_create', 'mcw_graph_launch',
            'mcw_graph_destroy', 'mcw_host_alloc', 'mcw_host_free', 'mcw_write_csv',
-           'mcw_format_csv', 'mcw_walk_noalloc']
+           'mcw_format_csv', 'mcw_walk_noalloc', 'mcw_post']
 
 
 class McwError(RuntimeError):
@@ -103,6 +103,8 @@ RECORD64 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.f
 TALLY = np.dtype([('n_cond', np.uint64, 6), ('q_cond_fx', np.uint64, 6), ('n_events', np.uint64),
                   ('max_n_scat', np.uint32), ('reserved', np.uint32),
                   ('bin_wvn_fx', np.uint64, HIST_BINS), ('bin_count', np.uint32, HIST_BINS)])
+POST_STATS = np.dtype([('q_cond_fx', np.uint64, 6), ('n_cond', np.uint64, 6), ('sum_n_scat', np.uint64),
+                       ('sum_path_length', np.float64), ('sum_wavelength', np.float64)])
 assert RECORD32.itemsize == 32 and RECORD64.itemsize == 56
 assert ctypes.sizeof(ConfigC) == 136 and ctypes.sizeof(StatsC) == 80
 
@@ -145,6 +147,7 @@ def load(path=None):
                             ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
         'mcw_walk_noalloc': ([ctypes.POINTER(ConfigC), ctypes.POINTER(SSPTableC),
                               ctypes.POINTER(SSPTableC), u64, vp, vp, vp], ctypes.c_int),
+        'mcw_post': ([vp, vp, i32, i32, i64, i32, i32, vp, vp, vp], ctypes.c_int),
         'mcw_mlp_gemm': ([ctypes.POINTER(GemmC), vp], ctypes.c_int),
         'mcw_mlp_colsum': ([vp, i32, i32, i32, vp, vp], ctypes.c_int),
         'mcw_mlp_loss': ([vp, i32, vp, i32, vp, i32, i32, vp, i32, vp, i32, vp, vp], ctypes.c_int),

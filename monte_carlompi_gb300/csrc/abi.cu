@@ -95,7 +95,7 @@ struct mcw_ctx {
     int32_t n_ice = 0;
     bool have_tables = false;
     // workspace
-    DevBuf cfgs, lut, tallies, counters, records;
+    DevBuf cfgs, lut, tallies, counters, records, post;
     HostBuf h_stage, h_tallies, h_counters;
     int32_t max_ice_n = 0;
     mcw_launch launch{256, 0, 8, 0};
@@ -353,7 +353,7 @@ int mcw_destroy(mcw_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->tabdata, &ctx->ice_tables, &ctx->cfgs, &ctx->lut, &ctx->tallies, &ctx->counters,
-                      &ctx->records})
+                      &ctx->records, &ctx->post})
         b->release();
     ctx->h_stage.release();
     ctx->h_tallies.release();
@@ -572,6 +572,43 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         return set_err(ctx, MCW_ERR_BUDGET, "walk stopped by the %.3g s time budget; results are partial", ctx->budget_s);
     if (hc->status & kStatusStream)
         return set_err(ctx, MCW_ERR_STREAM, "a replay photon exhausted its 2^33-uniform stream");
+    return MCW_OK;
+}
+
+int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t mode, int64_t n, int32_t n_cfg,
+             int32_t n_bins, uint64_t *bin_wvn_fx, uint32_t *bin_count, mcw_post_stats *stats) {
+    if (!ctx) return MCW_ERR_ARG;
+    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
+    if (records_where != MCW_RECORDS_HOST && records_where != MCW_RECORDS_DEVICE)
+        return set_err(ctx, MCW_ERR_ARG, "records must be on the host or the device");
+    if (n < 0 || (n > 0 && !records) || n_cfg <= 0 || n_bins < 0 || n_bins > (1 << 20) || !stats ||
+        (n_bins > 0 && (!bin_wvn_fx || !bin_count)))
+        return set_err(ctx, MCW_ERR_ARG, "invalid post-processing arguments");
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
+    const size_t b_bins = (size_t)n_cfg * n_bins * sizeof(unsigned long long);
+    const size_t b_cnt = (size_t)n_cfg * n_bins * sizeof(unsigned int);
+    const size_t b_cnt_pad = (b_cnt + 255) & ~size_t(255);
+    const size_t b_stats = (size_t)n_cfg * sizeof(mcw_post_stats);
+    CUDA_TRY(ctx, ctx->post.ensure(b_bins + b_cnt_pad + b_stats));
+    char *dev = (char *)ctx->post.p;
+    const void *drec = records;
+    if (records_where == MCW_RECORDS_HOST && n > 0) {
+        CUDA_TRY(ctx, ctx->records.ensure((size_t)n * rec_size));
+        CUDA_TRY(ctx, cudaMemcpyAsync(ctx->records.p, records, (size_t)n * rec_size, cudaMemcpyHostToDevice, st));
+        drec = ctx->records.p;
+    }
+    CUDA_TRY(ctx, cudaMemsetAsync(dev, 0, b_bins + b_cnt_pad + b_stats, st));
+    CUDA_TRY(ctx, launch_post(drec, mode == MCW_MODE_REPLAY64, n, n_cfg, n_bins, (unsigned long long *)dev,
+                              (unsigned int *)(dev + b_bins), (mcw_post_stats *)(dev + b_bins + b_cnt_pad),
+                              ctx->sm_count, st));
+    if (n_bins > 0) {
+        CUDA_TRY(ctx, cudaMemcpyAsync(bin_wvn_fx, dev, b_bins, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(ctx, cudaMemcpyAsync(bin_count, dev + b_bins, b_cnt, cudaMemcpyDeviceToHost, st));
+    }
+    CUDA_TRY(ctx, cudaMemcpyAsync(stats, dev + b_bins + b_cnt_pad, b_stats, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(ctx, cudaStreamSynchronize(st));
     return MCW_OK;
 }
 

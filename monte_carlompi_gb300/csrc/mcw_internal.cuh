@@ -126,6 +126,8 @@ struct LutArgs {
 const char *config_problem(const mcw_config &c, int32_t n_ice);
 
 // Kernel launchers (defined in the .cu files).
+cudaError_t launch_post(const void *recs, bool f64, int64_t n, int n_cfg, int n_bins, unsigned long long *bins_fx,
+                        unsigned int *bins_cnt, mcw_post_stats *stats, int sms, cudaStream_t s);
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
 // impurity: some config has imp_cnc > 0 (the kernel instance with the species draw)
 cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, cudaStream_t s);
