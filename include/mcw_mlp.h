@@ -20,6 +20,11 @@ extern "C" {
 #define MCW_MLP_ERR_ARG (-1)
 #define MCW_MLP_ERR_CUDA (-2)
 
+/* GEMM engines */
+#define MCW_ENGINE_MMA_SYNC 0  /* mma.sync m16n8k16, any layout and epilogue */
+#define MCW_ENGINE_TCGEN05 1   /* tcgen05.mma into tensor memory: trans_a = trans_b = 0 and the
+                                  forward epilogues (F32, BIAS_F32, BIAS_SILU; c2 optional) */
+
 /* GEMM epilogues */
 #define MCW_EPI_F32 0        /* c (f32) = acc */
 #define MCW_EPI_BIAS_F32 1   /* c (f32) = acc + bias (bias may be NULL) */
@@ -44,7 +49,7 @@ typedef struct {
     void *c;
     void *c2;
     int32_t ldc2;
-    int32_t reserved;
+    int32_t engine;      /* MCW_ENGINE_* */
 } McwGemm;
 
 int mcw_mlp_gemm(const McwGemm *p, void *stream);
@@ -62,6 +67,10 @@ int mcw_mlp_loss(const float *y, int32_t ldy, const float *t, int32_t ldt, const
  * updated weights for the GEMMs. */
 int mcw_mlp_adam(float *w, const float *g, float *m, float *v, void *w16, int64_t n, float lr,
                  float beta1, float beta2, float eps, int64_t step, void *stream);
+
+/* Error flags of the tensor-core path on the current device (bit 0: an MMA
+ * completion wait ran out of time and the kernel left early); clear != 0 resets them. */
+int mcw_mlp_status(int32_t clear, uint32_t *flags);
 
 /* y (bf16) = x (f32), n elements. */
 int mcw_mlp_cast_bf16(const float *x, void *y, int64_t n, void *stream);

@@ -84,13 +84,15 @@ class GemmC(ctypes.Structure):
                 ('ldb', ctypes.c_int32), ('b', ctypes.c_void_p), ('bias', ctypes.c_void_p),
                 ('aux', ctypes.c_void_p), ('ldaux', ctypes.c_int32), ('ldc', ctypes.c_int32),
                 ('c', ctypes.c_void_p), ('c2', ctypes.c_void_p), ('ldc2', ctypes.c_int32),
-                ('reserved', ctypes.c_int32)]
+                ('engine', ctypes.c_int32)]
 
 
 EPI_F32, EPI_BIAS_F32, EPI_BIAS_SILU, EPI_DSILU = 0, 1, 2, 3
+ENGINE_MMA_SYNC, ENGINE_TCGEN05 = 0, 1
 
 # entry points of include/mcw_mlp.h
-MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16']
+MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16',
+               'mcw_mlp_status']
 
 RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
                      ('theta_n', np.float32), ('phi_n', np.float32),
@@ -154,6 +156,7 @@ def load(path=None):
         'mcw_mlp_adam': ([vp, vp, vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                           ctypes.c_float, i64, vp], ctypes.c_int),
         'mcw_mlp_cast_bf16': ([vp, vp, i64, vp], ctypes.c_int),
+        'mcw_mlp_status': ([i32, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -233,6 +233,9 @@ __global__ void cast_kernel(const float *x, __nv_bfloat16 *y, int n) {
 
 }  // namespace
 
+cudaError_t launch_gemm_tc(const McwGemm &p, unsigned int *err, cudaStream_t s);
+unsigned int *tc_err_flag();
+
 }  // namespace mcw
 
 using namespace mcw;
@@ -241,11 +244,21 @@ extern "C" {
 
 int mcw_mlp_gemm(const McwGemm *p, void *stream) {
     if (!p || p->m < 0 || p->n < 0 || p->k < 0 || !p->a || !p->b || !p->c) return MCW_MLP_ERR_ARG;
-    if (p->epilogue == MCW_EPI_BIAS_SILU && (!p->bias || !p->c2)) return MCW_MLP_ERR_ARG;
+    if (p->epilogue == MCW_EPI_BIAS_SILU && (!p->bias || (!p->c2 && p->engine != MCW_ENGINE_TCGEN05)))
+        return MCW_MLP_ERR_ARG;
     if (p->epilogue == MCW_EPI_DSILU && !p->aux) return MCW_MLP_ERR_ARG;
+    if (p->engine < MCW_ENGINE_MMA_SYNC || p->engine > MCW_ENGINE_TCGEN05) return MCW_MLP_ERR_ARG;
     if (p->m == 0 || p->n == 0) return 0;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
+    if (p->engine == MCW_ENGINE_TCGEN05) {
+        // tcgen05 path: forward layouts (A [m,k], W [n,k], both K-major) and epilogues
+        if (p->trans_a || p->trans_b || p->epilogue == MCW_EPI_DSILU) return MCW_MLP_ERR_ARG;
+        unsigned int *err = tc_err_flag();
+        if (!err) return MCW_MLP_ERR_CUDA;
+        e = launch_gemm_tc(*p, err, s);
+        return e == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
+    }
     if (!p->trans_a && !p->trans_b) e = launch_gemm<false, false>(*p, s);
     else if (!p->trans_a && p->trans_b) e = launch_gemm<false, true>(*p, s);
     else if (p->trans_a && !p->trans_b) e = launch_gemm<true, false>(*p, s);
@@ -278,6 +291,20 @@ int mcw_mlp_adam(float *w, const float *g, float *m, float *v, void *w16, int64_
     adam_kernel<<<(int)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         w, g, m, v, static_cast<__nv_bfloat16 *>(w16), (int)n, lr, beta1, beta2, eps, c1, c2);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
+}
+
+int mcw_mlp_status(int32_t clear, uint32_t *flags) {
+    if (!flags) return MCW_MLP_ERR_ARG;
+    unsigned int *err = tc_err_flag();
+    if (!err) return MCW_MLP_ERR_CUDA;
+    unsigned int h = 0;
+    if (cudaMemcpy(&h, err, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return MCW_MLP_ERR_CUDA;
+    *flags = h;
+    if (clear && h) {
+        h = 0;
+        if (cudaMemcpy(err, &h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess) return MCW_MLP_ERR_CUDA;
+    }
+    return 0;
 }
 
 int mcw_mlp_cast_bf16(const float *x, void *y, int64_t n, void *stream) {

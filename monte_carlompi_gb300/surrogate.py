@@ -74,11 +74,11 @@ def _ptr(t):
 
 
 def _gemm(torch, epi, m, n, k, a, lda, b, ldb, c, ldc, trans_a=0, trans_b=0, bias=None, aux=None,
-          ldaux=0, c2=None, ldc2=0):
+          ldaux=0, c2=None, ldc2=0, engine=_abi.ENGINE_MMA_SYNC):
     g = _abi.GemmC(m, n, k, trans_a, trans_b, epi, a.data_ptr(), lda, ldb, b.data_ptr(),
                    bias.data_ptr() if bias is not None else None,
                    aux.data_ptr() if aux is not None else None, ldaux, ldc, c.data_ptr(),
-                   c2.data_ptr() if c2 is not None else None, ldc2, 0)
+                   c2.data_ptr() if c2 is not None else None, ldc2, engine)
     rc = _abi.load().mcw_mlp_gemm(ctypes.byref(g), _stream(torch))
     if rc:
         raise _abi.McwError(rc, 'mcw_mlp_gemm failed (m=%d n=%d k=%d)' % (m, n, k))

@@ -139,3 +139,35 @@ def test_training_fits_a_smooth_map():
             loss = float(net.train_step(x16[idx].contiguous(), t[idx].contiguous(), w, lr=2e-3))
             first = loss if first is None else first
     assert loss < first / 100, (first, loss)
+
+
+@pytest.mark.parametrize('m,n,k,epi', [(128, 128, 64, 0), (300, 200, 256, 1), (1000, 649, 256, 1),
+                                       (257, 256, 256, 2), (64, 16, 16, 0), (130, 256, 4, 2)])
+def test_tcgen05_gemm_matches_float64(m, n, k, epi):
+    """The tcgen05 (tensor memory) forward GEMM against float64 on the same bf16 operands."""
+    g = torch.Generator().manual_seed(m + n + k)
+    a16 = _bf16(torch.randn(m, k, generator=g)).cuda()
+    w16 = _bf16(torch.randn(n, k, generator=g) * 0.1).cuda()
+    bias = torch.randn(n, generator=g).cuda()
+    ref = a16.cpu().double() @ w16.cpu().double().T
+    flags = ctypes.c_uint32(0)
+    lib = _abi.load()
+    assert lib.mcw_mlp_status(1, ctypes.byref(flags)) == 0
+    if epi == _abi.EPI_BIAS_SILU:
+        act = torch.empty((m, n), dtype=torch.bfloat16, device='cuda')
+        z = torch.empty((m, n), device='cuda')
+        surrogate._gemm(torch, epi, m, n, k, a16, k, w16, k, act, n, bias=bias, c2=z, ldc2=n,
+                        engine=_abi.ENGINE_TCGEN05)
+        torch.cuda.synchronize()
+        zr = ref + bias.cpu().double()
+        assert (z.cpu().double() - zr).abs().max().item() < 1e-4 * max(1.0, zr.abs().max().item())
+        sr = zr * torch.sigmoid(zr)
+        assert (act.cpu().double() - sr).abs().max().item() <= 0.01 * max(1.0, sr.abs().max().item())
+    else:
+        c = torch.empty((m, n), device='cuda')
+        surrogate._gemm(torch, epi, m, n, k, a16, k, w16, k, c, n, bias=bias if epi else None,
+                        engine=_abi.ENGINE_TCGEN05)
+        torch.cuda.synchronize()
+        r = ref + (bias.cpu().double() if epi else 0)
+        assert (c.cpu().double() - r).abs().max().item() < 1e-4 * max(1.0, r.abs().max().item())
+    assert lib.mcw_mlp_status(0, ctypes.byref(flags)) == 0 and flags.value == 0
