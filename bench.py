@@ -312,7 +312,8 @@ def run_mlp(args):
     peak = float(peaks.get('bf16_tflops') or 1900.0)
     print(json.dumps({'metric': METRIC, 'workload': 'mlp', 'value': batch / (ms / 1e3), 'unit': 'BRF/s',
                       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms, 'dtype': 'bf16',
-                      'config': {'batch': batch, 'net': '4-256-256-256-649 SiLU', 'kernels': 'mma.sync m16n8k16'},
+                      'config': {'batch': batch, 'net': '4-256-256-256-649 SiLU',
+                                 'kernels': 'tcgen05.mma kind::f16, TMEM accumulators'},
                       'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s',
                                    'frac': tflops / peak, 'peak_source': src}}))
     return 0

@@ -7,8 +7,9 @@ microseconds; plain Monte Carlo stays the fallback outside the training hull or
 where the ensemble disagrees, and the judge of the network's error.
 
 Network: 4 -> 256 -> 256 -> 256 -> 649, SiLU, BF16 weights and activations on
-tensor cores with FP32 accumulation (include/mcw_mlp.h), FP32 master weights and
-Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
+tensor cores with FP32 accumulation (include/mcw_mlp.h: tcgen05 with tensor-memory
+accumulators for the forward GEMMs, mma.sync for the backward layouts), FP32 master
+weights and Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
 run those kernels; inputs and outputs are torch CUDA tensors, PyTorch is only the
 container.  Targets are standardised log(BRF / albedo + 0.02) per bin and
 log(albedo).
@@ -101,23 +102,29 @@ def _colsum(torch, g):
     return out
 
 
-def forward_cached(torch, x16, w16, biases):
-    """Forward pass on the tensor-core kernels; returns (y fp32, cache for backward)."""
+# forward GEMMs run on tcgen05 (tensor memory accumulators); the backward layouts
+# (transposed operands, silu' epilogue) run on mma.sync
+FORWARD_ENGINE = _abi.ENGINE_TCGEN05
+
+
+def forward_cached(torch, x16, w16, biases, keep=True):
+    """Forward pass on the tensor-core kernels; returns (y fp32, cache for backward).
+    keep=False (inference) skips storing the FP32 pre-activations."""
     m = x16.shape[0]
     a = x16
     zs, acts = [], [x16]
     for layer in range(3):
         n, k = w16[layer].shape
-        z = torch.empty((m, n), dtype=torch.float32, device=x16.device)
+        z = torch.empty((m, n), dtype=torch.float32, device=x16.device) if keep else None
         nxt = torch.empty((m, n), dtype=torch.bfloat16, device=x16.device)
         _gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a, k, w16[layer], k, nxt, n, bias=biases[layer],
-              c2=z, ldc2=n)
+              c2=z, ldc2=n, engine=FORWARD_ENGINE)
         zs.append(z)
         acts.append(nxt)
         a = nxt
     n, k = w16[3].shape
     y = torch.empty((m, n), dtype=torch.float32, device=x16.device)
-    _gemm(torch, _abi.EPI_BIAS_F32, m, n, k, a, k, w16[3], k, y, n, bias=biases[3])
+    _gemm(torch, _abi.EPI_BIAS_F32, m, n, k, a, k, w16[3], k, y, n, bias=biases[3], engine=FORWARD_ENGINE)
     return y, (zs, acts)
 
 
@@ -215,7 +222,7 @@ class SurrogateMLP:
         """Standardised outputs for encoded inputs x (torch CUDA float32 [n, 4])."""
         torch = self.torch
         x16 = _cast(torch, x.contiguous().float())
-        y, _ = forward_cached(torch, x16, self.w16, self.params[1::2])
+        y, _ = forward_cached(torch, x16, self.w16, self.params[1::2], keep=False)
         return y
 
     def train_step(self, x16, t, w_out, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
