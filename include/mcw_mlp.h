@@ -23,12 +23,12 @@ extern "C" {
 /* GEMM engines */
 #define MCW_ENGINE_MMA_SYNC 0  /* mma.sync m16n8k16, any layout and epilogue */
 #define MCW_ENGINE_TCGEN05 1   /* tcgen05.mma into tensor memory: trans_a = trans_b = 0 and the
-                                  forward epilogues (F32, BIAS_F32, BIAS_SILU; c2 optional) */
+                                  forward epilogues (F32, BIAS_F32, BIAS_SILU) */
 
 /* GEMM epilogues */
 #define MCW_EPI_F32 0        /* c (f32) = acc */
 #define MCW_EPI_BIAS_F32 1   /* c (f32) = acc + bias (bias may be NULL) */
-#define MCW_EPI_BIAS_SILU 2  /* c2 (f32) = z = acc + bias; c (bf16) = silu(z) */
+#define MCW_EPI_BIAS_SILU 2  /* c2 (f32, optional) = z = acc + bias; c (bf16) = silu(z) */
 #define MCW_EPI_DSILU 3      /* g = acc * silu'(aux); c (bf16) = g; c2 (f32, optional) = g */
 
 /* C[m, n] = sum_k A(m, k) B(n, k) on BF16 tensor cores with FP32 accumulation.
@@ -68,12 +68,32 @@ int mcw_mlp_loss(const float *y, int32_t ldy, const float *t, int32_t ldt, const
 int mcw_mlp_adam(float *w, const float *g, float *m, float *v, void *w16, int64_t n, float lr,
                  float beta1, float beta2, float eps, int64_t step, void *stream);
 
-/* Error flags of the tensor-core path on the current device (bit 0: an MMA
- * completion wait ran out of time and the kernel left early); clear != 0 resets them. */
+/* Error flags of the tensor-core path on the current device (bit 0: an MMA completion
+ * wait of the tcgen05 GEMM ran out of time and the kernel left early; bit 1: the same in
+ * mcw_mlp_forward); clear != 0 resets them. */
 int mcw_mlp_status(int32_t clear, uint32_t *flags);
 
 /* y (bf16) = x (f32), n elements. */
 int mcw_mlp_cast_bf16(const float *x, void *y, int64_t n, void *stream);
+
+/* Fused inference of the whole network MCW_MLP_IN -> 3 x MCW_MLP_HIDDEN (SiLU) -> MCW_MLP_OUT. */
+#define MCW_MLP_IN 4
+#define MCW_MLP_HIDDEN 256
+#define MCW_MLP_OUT 649
+/* five 256 x 256 bf16 blocks (W2, W3, three 256-row blocks of W4) and the 256 x 16 W1 tile */
+#define MCW_MLP_PACK_BYTES (5 * MCW_MLP_HIDDEN * MCW_MLP_HIDDEN * 2 + MCW_MLP_HIDDEN * 16 * 2)
+
+/* Repack the bf16 weights w1 [256, 4], w2, w3 [256, 256] and w4 [649, 256] (row-major
+ * [out, in]) into blob (MCW_MLP_PACK_BYTES, 16-byte aligned), the tensor-core operand
+ * layout read by mcw_mlp_forward.  Call again whenever the weights change. */
+int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4, void *blob, void *stream);
+
+/* y [m, 649] (f32, leading dimension ldy >= 649) = network(x [m, 4] f32) from the packed
+ * weights and the f32 biases (16-byte aligned): one kernel, the hidden activations never
+ * leave shared memory.  Inputs and activations are rounded to bf16 as the layer-by-layer
+ * mcw_mlp_gemm path rounds them.  A wait that runs out sets bit 1 of mcw_mlp_status. */
+int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
+                    const float *b4, const void *blob, float *y, int32_t ldy, void *stream);
 
 #ifdef __cplusplus
 }

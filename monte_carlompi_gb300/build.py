@@ -36,7 +36,7 @@ def nvcc():
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, '*.cuh')) + [os.path.join(ROOT, 'include', 'mcwalk.h')]
+    return glob.glob(os.path.join(CSRC, '*.cuh')) + glob.glob(os.path.join(ROOT, 'include', '*.h'))
 
 
 def _stale(obj, src):

@@ -23,7 +23,7 @@ namespace {
 
 constexpr int BM = 64, BN = 64, BK = 32, LDS = BK + 8;
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
     const float s = 1.f / (1.f + __expf(-z));
     return s * (1.f + z * (1.f - s));
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(128) gemm_kernel(const McwGemm p) {
                 float v = acc[i][j][e];
                 if (kEpi == MCW_EPI_BIAS_SILU) {
                     v += p.bias[n];
-                    static_cast<float *>(p.c2)[(size_t)m * p.ldc2 + n] = v;  // pre-activation
+                    if (p.c2) static_cast<float *>(p.c2)[(size_t)m * p.ldc2 + n] = v;  // pre-activation
                     static_cast<__nv_bfloat16 *>(p.c)[(size_t)m * p.ldc + n] = __float2bfloat16(silu(v));
                 } else if (kEpi == MCW_EPI_BIAS_F32) {
                     if (p.bias) v += p.bias[n];
@@ -244,8 +244,7 @@ extern "C" {
 
 int mcw_mlp_gemm(const McwGemm *p, void *stream) {
     if (!p || p->m < 0 || p->n < 0 || p->k < 0 || !p->a || !p->b || !p->c) return MCW_MLP_ERR_ARG;
-    if (p->epilogue == MCW_EPI_BIAS_SILU && (!p->bias || (!p->c2 && p->engine != MCW_ENGINE_TCGEN05)))
-        return MCW_MLP_ERR_ARG;
+    if (p->epilogue == MCW_EPI_BIAS_SILU && !p->bias) return MCW_MLP_ERR_ARG;
     if (p->epilogue == MCW_EPI_DSILU && !p->aux) return MCW_MLP_ERR_ARG;
     if (p->engine < MCW_ENGINE_MMA_SYNC || p->engine > MCW_ENGINE_TCGEN05) return MCW_MLP_ERR_ARG;
     if (p->m == 0 || p->n == 0) return 0;

@@ -47,7 +47,7 @@ __device__ __forceinline__ unsigned long long now_ns() {
     return t;
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 
 // Stage a 128-row x 64-k chunk of a K-major bf16 matrix (rows of length ld) into
 // the core-matrix layout; rows >= rows_valid and k >= K read as zero.

@@ -7,9 +7,10 @@ microseconds; plain Monte Carlo stays the fallback outside the training hull or
 where the ensemble disagrees, and the judge of the network's error.
 
 Network: 4 -> 256 -> 256 -> 256 -> 649, SiLU, BF16 weights and activations on
-tensor cores with FP32 accumulation (include/mcw_mlp.h: tcgen05 with tensor-memory
-accumulators for the forward GEMMs, mma.sync for the backward layouts), FP32 master
-weights and Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
+tensor cores with FP32 accumulation (include/mcw_mlp.h: inference is one fused
+tcgen05 kernel with tensor-memory accumulators whose hidden activations never leave
+shared memory; training runs layer-by-layer GEMMs that keep the pre-activations for
+the backward pass), FP32 master weights and Adam.  ``MLPFunction`` is the torch.autograd.Function whose forward and backward
 run those kernels; inputs and outputs are torch CUDA tensors, PyTorch is only the
 container.  Targets are standardised log(BRF / albedo + 0.02) per bin and
 log(albedo).
@@ -102,9 +103,33 @@ def _colsum(torch, g):
     return out
 
 
-# forward GEMMs run on tcgen05 (tensor memory accumulators); the backward layouts
-# (transposed operands, silu' epilogue) run on mma.sync
-FORWARD_ENGINE = _abi.ENGINE_TCGEN05
+# engine of the layer-by-layer forward GEMMs of training (the backward layouts --
+# transposed operands, silu' epilogue -- always run on mma.sync); inference runs the
+# fused tcgen05 kernel (forward_fused)
+FORWARD_ENGINE = _abi.ENGINE_MMA_SYNC
+
+
+def pack_weights(torch, w16):
+    """All four weight matrices in the tensor-core operand layout of mcw_mlp_forward."""
+    blob = torch.empty(_abi.MLP_PACK_BYTES, dtype=torch.uint8, device=w16[0].device)
+    rc = _abi.load().mcw_mlp_pack(_ptr(w16[0]), _ptr(w16[1]), _ptr(w16[2]), _ptr(w16[3]), _ptr(blob),
+                                  _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_pack failed')
+    return blob
+
+
+def forward_fused(torch, x, w16, biases, blob):
+    """Inference of the whole network in one kernel (mcw_mlp_forward); x float32 [m, 4]."""
+    x = x.contiguous().float()
+    m = x.shape[0]
+    y = torch.empty((m, DIMS[-1]), dtype=torch.float32, device=x.device)
+    b = [t.contiguous() for t in biases]
+    rc = _abi.load().mcw_mlp_forward(_ptr(x), m, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), _ptr(b[3]), _ptr(blob),
+                                     _ptr(y), DIMS[-1], _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_forward failed (m=%d)' % m)
+    return y
 
 
 def forward_cached(torch, x16, w16, biases, keep=True):
@@ -217,13 +242,21 @@ class SurrogateMLP:
         self.step = 0
         self.y_mean = None
         self.y_std = None
+        self._blob = None
+        self._blob_key = None
+
+    def packed(self):
+        """Packed weights for the fused inference kernel, rebuilt when the weights change."""
+        key = (self.step, tuple(w.data_ptr() for w in self.w16))
+        if self._blob is None or self._blob_key != key:
+            self._blob = pack_weights(self.torch, self.w16)
+            self._blob_key = key
+        return self._blob
 
     def predict_std(self, x):
-        """Standardised outputs for encoded inputs x (torch CUDA float32 [n, 4])."""
-        torch = self.torch
-        x16 = _cast(torch, x.contiguous().float())
-        y, _ = forward_cached(torch, x16, self.w16, self.params[1::2], keep=False)
-        return y
+        """Standardised outputs for encoded inputs x (torch CUDA float32 [n, 4]) from the
+        fused inference kernel."""
+        return forward_fused(self.torch, x, self.w16, self.params[1::2], self.packed())
 
     def train_step(self, x16, t, w_out, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         """One Adam step on a batch (x16 bf16 [b, 4], t fp32 standardised targets)."""

@@ -171,3 +171,63 @@ def test_tcgen05_gemm_matches_float64(m, n, k, epi):
         r = ref + (bias.cpu().double() if epi else 0)
         assert (c.cpu().double() - r).abs().max().item() < 1e-4 * max(1.0, r.abs().max().item())
     assert lib.mcw_mlp_status(0, ctypes.byref(flags)) == 0 and flags.value == 0
+
+
+def _random_net(seed):
+    net = surrogate.SurrogateMLP(seed=seed)
+    g = torch.Generator().manual_seed(seed + 1)
+    for i in range(1, 8, 2):                       # non-zero biases
+        net.params[i].copy_((torch.randn(net.params[i].shape, generator=g) * 0.3).cuda())
+    return net
+
+
+@pytest.mark.parametrize('m', [1, 127, 128, 129, 1000, 4097])
+def test_fused_forward_matches_layerwise_and_float64(m):
+    """mcw_mlp_forward (one tcgen05 kernel, activations in shared memory) against float64
+    with the same bf16 roundings, and against the layer-by-layer GEMM forward."""
+    net = _random_net(40 + m)
+    g = torch.Generator().manual_seed(m)
+    x = (torch.rand(m, 4, generator=g) * 2 - 1).cuda()
+    flags = ctypes.c_uint32(0)
+    lib = _abi.load()
+    assert lib.mcw_mlp_status(1, ctypes.byref(flags)) == 0
+    y = net.predict_std(x)
+    y_layer, _ = surrogate.forward_cached(torch, surrogate._cast(torch, x), net.w16, net.params[1::2], keep=False)
+    torch.cuda.synchronize()
+    assert lib.mcw_mlp_status(0, ctypes.byref(flags)) == 0 and flags.value == 0
+    ref = _reference_mlp(x.cpu().double(), [p.cpu().double() for p in net.params])
+    scale = ref.abs().max().item()
+    assert y.shape == (m, 649) and torch.isfinite(y).all()
+    assert (y.cpu().double() - ref).abs().max().item() < 2e-2 * scale
+    assert (y - y_layer).abs().max().item() < 5e-3 * scale
+
+
+def test_fused_forward_leading_dimension_and_repack():
+    """Rows land at stride ldy without touching the padding; after an Adam step the
+    packed weights are rebuilt so inference follows the new weights."""
+    net = _random_net(7)
+    m, ldy = 300, 700
+    x = (torch.rand(m, 4, generator=torch.Generator().manual_seed(2)) * 2 - 1).cuda()
+    out = torch.full((m, ldy), 12345.0, device='cuda')
+    b = [t.contiguous() for t in net.params[1::2]]
+    rc = _abi.load().mcw_mlp_forward(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
+                                     surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
+                                     surrogate._ptr(out), ldy, surrogate._stream(torch))
+    assert rc == 0
+    y = net.predict_std(x)
+    torch.cuda.synchronize()
+    assert torch.equal(out[:, :649], y)
+    assert (out[:, 649:] == 12345.0).all()
+    bad = _abi.load().mcw_mlp_forward(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
+                                      surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
+                                      surrogate._ptr(out), 600, surrogate._stream(torch))
+    assert bad == -1
+    before = net.predict_std(x).clone()
+    t = torch.randn(64, 649, device='cuda')
+    w_out = torch.from_numpy(surrogate.output_weights()).cuda()
+    net.train_step(surrogate._cast(torch, x[:64].contiguous()), t, w_out, lr=1e-2)
+    after = net.predict_std(x)
+    y_layer, _ = surrogate.forward_cached(torch, surrogate._cast(torch, x), net.w16, net.params[1::2], keep=False)
+    torch.cuda.synchronize()
+    assert not torch.equal(before, after)
+    assert (after - y_layer).abs().max().item() < 5e-3 * y_layer.abs().max().item()
