@@ -88,7 +88,8 @@ int mcw_mlp_cast_bf16(const float *x, void *y, int64_t n, void *stream);
  * layout read by mcw_mlp_forward.  Call again whenever the weights change. */
 int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4, void *blob, void *stream);
 
-/* y [m, 649] (f32, leading dimension ldy >= 649) = network(x [m, 4] f32) from the packed
+/* y [m, 649] (f32; y 16-byte aligned, leading dimension ldy >= 652 and a multiple of 4;
+ * columns 649 .. ldy - 1 are left untouched) = network(x [m, 4] f32) from the packed
  * weights and the f32 biases (16-byte aligned): one kernel, the hidden activations never
  * leave shared memory.  Inputs and activations are rounded to bf16 as the layer-by-layer
  * mcw_mlp_gemm path rounds them.  A wait that runs out sets bit 1 of mcw_mlp_status. */

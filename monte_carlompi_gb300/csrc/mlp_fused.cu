@@ -1,29 +1,34 @@
 // Fused forward (inference) of the surrogate network 4 -> 256 -> 256 -> 256 -> 649
 // on the 5th-generation tensor cores.
 //
-// One CTA (16 warps, one CTA per SM) carries 128 input rows through all four
-// layers.  Every layer is a tcgen05.mma (M = 128, N = 256) from shared memory into a
-// tensor-memory accumulator:
-//  * operands are K-major core matrices (8 rows x 16 bytes; 128 B apart along K,
-//    kdim * 16 B apart along M/N), no swizzle;
-//  * the input rows (K = 4, zero-padded to 16) are written by the threads; the
-//    weights come pre-packed in that layout (mcw_mlp_pack) and arrive by
-//    cp.async.bulk, one 128 KB block of 256 output rows at a time, signalled through
-//    an mbarrier's transaction count;
-//  * the hidden epilogue (bias, SiLU, bf16) writes the next layer's A operand back
-//    into the same 64 KB activation tile, so activations never leave shared memory;
-//  * the output layer runs as three 256-column blocks ping-ponging between the two
-//    halves of a 512-column accumulator, so the MMAs of block j + 1 overlap the
-//    epilogue of block j; that epilogue transposes 32 x 16 pieces through a swizzled
-//    shared-memory stage so each output row is written as a contiguous run.
-// Warp w reads accumulator lanes 32 (w % 4) .. +31 (its rows) and columns
-// 64 (w / 4) .. +63 of each 256-column half.  Every wait is bounded by %globaltimer
-// (2 s); a timeout sets bit 1 of the error flag read by mcw_mlp_status, waits
-// (bounded) for copies and MMAs still in flight, frees the tensor memory and leaves.
+// One CTA carries 128 input rows through all four layers; two CTAs share an SM
+// (112 KB of shared memory and 256 tensor-memory columns each), so one CTA's
+// epilogue runs while the other's MMAs occupy the tensor core.  Warps are
+// specialised:
+//  * warp 8 (producer) streams the pre-packed weights (mcw_mlp_pack) as 41 chunks of
+//    at most 16 KB through a two-slot shared-memory ring with cp.async.bulk, each
+//    chunk signalled through its slot's mbarrier transaction count;
+//  * warp 9 (MMA) owns the tensor memory and issues tcgen05.mma (M = 128, K-major
+//    core-matrix operands, no swizzle) from shared memory into it: layer 1 (K = 4
+//    zero-padded to 16) and layers 2 and 3 with N = 256, the output layer as six
+//    N = 128 blocks ping-ponging between the two halves of the accumulator;
+//  * warps 0-7 write the input tile and run the epilogues: hidden layers (bias,
+//    SiLU, bf16) write the next layer's A operand back into the 64 KB activation
+//    tile, so activations never leave shared memory; output blocks leave through a
+//    double-buffered 32-row x 8-column stage per warp as 2-D TMA tensor stores
+//    (cp.async.bulk.tensor), which clip rows >= m and columns >= 649 themselves.
+//    Epilogue warp w reads accumulator lanes 32 (w % 4) .. +31 (its rows).
+// Hand-offs are mbarriers: ring full/empty, accumulator full (tcgen05.commit) and
+// empty, activation tile ready.  Every wait is bounded by %globaltimer (2 s) and
+// checks a CTA-wide abort flag; a timeout sets bit 1 of the error flag read by
+// mcw_mlp_status, lets copies and MMAs in flight finish (bounded), frees the tensor
+// memory and leaves.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/mcw_mlp.h"
 
@@ -38,23 +43,41 @@ constexpr int FH = MCW_MLP_HIDDEN;      // 256
 constexpr int FO = MCW_MLP_OUT;         // 649
 constexpr int FIN = MCW_MLP_IN;         // 4
 constexpr int FK1 = 16;                 // layer-1 K, zero-padded
-constexpr int kThreads = 512;
-constexpr int kOutBlocks = (FO + FH - 1) / FH;       // 3 blocks of 256 output rows
-constexpr int kBlockBytes = FH * FH * 2;             // 128 KB: 256 rows x 256 k bf16
-constexpr int kW1Bytes = FH * FK1 * 2;               // 8 KB
-constexpr int kXBytes = FM * FK1 * 2;                // 4 KB
-constexpr int kActBytes = FM * FH * 2;               // 64 KB
-constexpr int kStageBytes = 16 * 32 * 16 * 4;        // 32 KB: per warp 32 rows x 16 floats
-constexpr size_t kSmemBytes = (size_t)kActBytes + kBlockBytes + kStageBytes;
-constexpr size_t kW1Offset = (size_t)(2 + kOutBlocks) * kBlockBytes;   // W1 tile after the five blocks
-constexpr uint32_t kTmemCols = 512;
+constexpr int kEpiWarps = 8;
+constexpr int kProducerWarp = 8, kMmaWarp = 9;
+constexpr int kThreads = 32 * (kEpiWarps + 2);
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kOutN = 128;                            // output block width
+constexpr int kOutBlocks = (FO + kOutN - 1) / kOutN;  // 6
+// weight chunks, in the order the MMA warp consumes them
+constexpr int kHidK = 32;                             // k per hidden-layer chunk (256 rows)
+constexpr int kOutK = 64;                             // k per output chunk (128 rows)
+constexpr int kHidChunks = FH / kHidK;                // 8 per hidden layer
+constexpr int kOutChunks = FH / kOutK;                // 4 per output block
+constexpr int kChunkBytes = 16384;
+constexpr int kW1Bytes = FH * FK1 * 2;                // 8 KB, chunk 0
+constexpr int kNumChunks = 1 + 2 * kHidChunks + kOutBlocks * kOutChunks;   // 41
+constexpr int kXBytes = FM * FK1 * 2;                 // 4 KB
+constexpr int kActBytes = FM * FH * 2;                // 64 KB
+constexpr int kRingBytes = 2 * kChunkBytes;           // 32 KB
+constexpr int kStageCols = 8;                         // output columns per TMA store box
+constexpr int kStageBuf = 32 * kStageCols * 4;        // 1 KB: one box
+constexpr int kStageBytes = kEpiWarps * 2 * kStageBuf;  // 16 KB: two boxes per warp
+constexpr size_t kSmemBytes = (size_t)kActBytes + kRingBytes + kStageBytes;
+constexpr uint32_t kTmemCols = 256;
 constexpr unsigned long long kWaitNs = 2000000000ull;
-// F32 += BF16 x BF16, both K-major, N = 256 (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4)
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(FH >> 3) << 17) |
-                            ((uint32_t)(FM >> 4) << 24);
+constexpr uint32_t kSuspendNs = 1000000;              // a waiting thread sleeps until the phase completes or 1 ms
+// F32 += BF16 x BF16, both K-major; N >> 3 in bits 17-22, M >> 4 in bits 24-28
+__host__ __device__ constexpr uint32_t idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(FM >> 4) << 24);
+}
 
-static_assert(kW1Offset + kW1Bytes == MCW_MLP_PACK_BYTES, "packed blob layout");
-static_assert(kXBytes + kW1Bytes <= kStageBytes, "layer-1 operands live in the stage region");
+static_assert(kHidK * FH * 2 == kChunkBytes && kOutK * kOutN * 2 == kChunkBytes, "chunk sizes");
+static_assert(kW1Bytes + (kNumChunks - 1) * kChunkBytes == MCW_MLP_PACK_BYTES, "packed blob layout");
+static_assert(kXBytes <= kStageBytes, "the input tile lives in the stage region");
+
+__host__ __device__ constexpr size_t chunk_offset(int i) { return i == 0 ? 0 : kW1Bytes + (size_t)(i - 1) * kChunkBytes; }
+__host__ __device__ constexpr uint32_t chunk_bytes(int i) { return i == 0 ? kW1Bytes : kChunkBytes; }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -79,53 +102,65 @@ __host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int kdim) 
     return (uint32_t)((row >> 3) * (kdim / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ __forceinline__ bool try_wait(uint64_t *bar, uint32_t phase) {
+__device__ __forceinline__ bool try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done) : "r"(smem_u32(bar)), "r"(phase));
+        : "=r"(done) : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs));
     return done != 0;
 }
 
-// Bounded wait on an mbarrier phase; false on timeout.
-__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t phase) {
+// Bounded wait on the phase of the given parity.  With an abort flag the wait also
+// gives up as soon as another role has given up, and a timeout raises the flag.
+__device__ __forceinline__ bool wait_bar(uint64_t *bar, uint32_t parity, volatile int *abort) {
     const unsigned long long t0 = now_ns();
-    while (!try_wait(bar, phase))
-        if (now_ns() - t0 > kWaitNs) return false;
+    while (!try_wait(bar, parity)) {
+        if (abort && *abort) return false;
+        if (now_ns() - t0 > kWaitNs) {
+            if (abort) *abort = 1;
+            return false;
+        }
+    }
     return true;
 }
 
-__device__ __forceinline__ void expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(smem_u32(bar)), "r"(bytes));
+__device__ __forceinline__ void arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" :: "r"(smem_u32(bar)) : "memory");
 }
 
-__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+__device__ __forceinline__ void bar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" :: "r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void load_chunk(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" :: "r"(smem_u32(bar)), "r"(bytes));
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
                  :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
 
-// acc (+)= A [128 x 16 ksteps] * B [256 x 16 ksteps]^T, K-major core matrices with rows of kdim.
-__device__ __forceinline__ void issue_mma(uint32_t tmem, const unsigned char *a, const unsigned char *b, int kdim,
-                                          uint64_t *bar) {
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    const uint32_t a0 = smem_u32(a), b0 = smem_u32(b);
-    const uint32_t sbo = (uint32_t)(kdim / 8) * 128;
+__device__ __forceinline__ void commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
+                 :: "r"(smem_u32(bar)));
+}
+
+// `steps` MMAs of K = 16: A k-steps a_step0 .. from a tile with rows of a_kdim,
+// B k-steps 0 .. from a tile with rows of b_kdim.
+__device__ __forceinline__ void mma_steps(uint32_t tmem, uint32_t a_base, int a_kdim, int a_step0, uint32_t b_base,
+                                          int b_kdim, int steps, uint32_t id, bool accumulate_first) {
 #pragma unroll 1
-    for (int s = 0; s < kdim / 16; ++s) {
-        const uint64_t da = smem_desc(a0 + s * 256, 128, sbo);
-        const uint64_t db = smem_desc(b0 + s * 256, 128, sbo);
-        const uint32_t accumulate = s > 0 ? 1u : 0u;
+    for (int t = 0; t < steps; ++t) {
+        const uint64_t da = smem_desc(a_base + (uint32_t)(a_step0 + t) * 256, 128, (uint32_t)(a_kdim / 8) * 128);
+        const uint64_t db = smem_desc(b_base + (uint32_t)t * 256, 128, (uint32_t)(b_kdim / 8) * 128);
+        const uint32_t acc = (accumulate_first || t > 0) ? 1u : 0u;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
             "setp.ne.b32 p, %4, 0;\n\t"
             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
-            :: "r"(tmem), "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
+            :: "r"(tmem), "l"(da), "l"(db), "r"(id), "r"(acc));
     }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
-                 :: "r"(smem_u32(bar)));
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
@@ -145,16 +180,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Hidden epilogue: this warp's 32 rows x 64 columns of the accumulator half at tcol
-// -> SiLU(z + b) as bf16 into the activation tile.
-__device__ __forceinline__ void epilogue_hidden(uint32_t tmem, uint32_t tcol, const float *bias,
-                                                unsigned char *act, int quarter, int group, int lane) {
+// Hidden epilogue: this warp's 32 rows x 128 columns (64 group .. ) of the 256-column
+// accumulator -> SiLU(z + b) as bf16 into the activation tile.
+__device__ __forceinline__ void epilogue_hidden(uint32_t tlane, const float *bias, unsigned char *act, int quarter,
+                                                int group, int lane) {
     const int row = quarter * 32 + lane;
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const int c0 = group * 64 + h * 32;
+    for (int h = 0; h < 4; ++h) {
+        const int c0 = group * 128 + h * 32;
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + tcol + (uint32_t)c0, v);
+        tmem_ld32(tlane + (uint32_t)c0, v);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const float4 ba = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8));
@@ -173,195 +208,253 @@ __device__ __forceinline__ void epilogue_hidden(uint32_t tmem, uint32_t tcol, co
     }
 }
 
-// Output epilogue of block `blk` (output columns 256 blk ..): z + b4 through the
-// warp's 32 x 16 stage (element (r, c) at r * 16 + (c ^ ((r >> 1) & 15)), free of bank
-// conflicts both ways) into rows of y, 16 consecutive columns per half-warp.
-__device__ __forceinline__ void epilogue_out(uint32_t tmem, uint32_t tcol, int blk, const float *b4, float *stage,
-                                             float *y, int ldy, int row0, int rows, int quarter, int group,
-                                             int lane) {
+// Output epilogue of block blk (output columns 128 blk ..): this warp's 32 rows x 64
+// columns, z + b4, leave in 32 x 8 boxes: registers -> stage buffer (row r at
+// 32 r bytes) -> one TMA tensor store by lane 0.  Two buffers alternate; a buffer is
+// rewritten once the store issued from it two boxes earlier has read it.
+__device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
+                                             const CUtensorMap *ymap, float *y, int ldy, int m, int row0,
+                                             int group, int lane, int &box) {
 #pragma unroll 1
     for (int h = 0; h < 2; ++h) {
         const int c0 = group * 64 + h * 32;
-        const int nb = blk * FH + c0;
+        const int nb = blk * kOutN + c0;
         if (nb >= FO) break;
+        float bv[32];
+        static_assert(FO % kStageCols == 1, "one ragged column at the end");
+        if (nb + 32 <= FO) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(b4 + nb + 4 * q));
+                bv[4 * q] = b.x, bv[4 * q + 1] = b.y, bv[4 * q + 2] = b.z, bv[4 * q + 3] = b.w;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) bv[c] = nb + c < FO ? __ldg(b4 + nb + c) : 0.f;
+        }
         float v[32];
-        tmem_ld32(tmem + ((uint32_t)(quarter * 32) << 16) + tcol + (uint32_t)c0, v);
+        tmem_ld32(tlane + (uint32_t)c0, v);
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int ch = nb + half * 16;
-            if (ch >= FO) break;
-            const int sw = (lane >> 1) & 15;
-            if (ch + 16 <= FO) {
+        for (int p = 0; p < 32 / kStageCols; ++p) {
+            const int col = nb + p * kStageCols;
+            if (col >= FO) break;
+            const int e = p * kStageCols;
+            if (col + kStageCols > FO) {
+                // ragged last box: tensor stores clip columns only to 16-byte granules, so the
+                // columns past 648 that share one with a valid column are written here directly
+                if (row0 + lane < m) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float4 b = __ldg(reinterpret_cast<const float4 *>(b4 + ch + q * 4));
-                    stage[lane * 16 + ((q * 4 + 0) ^ sw)] = v[half * 16 + q * 4 + 0] + b.x;
-                    stage[lane * 16 + ((q * 4 + 1) ^ sw)] = v[half * 16 + q * 4 + 1] + b.y;
-                    stage[lane * 16 + ((q * 4 + 2) ^ sw)] = v[half * 16 + q * 4 + 2] + b.z;
-                    stage[lane * 16 + ((q * 4 + 3) ^ sw)] = v[half * 16 + q * 4 + 3] + b.w;
+                    for (int c = 0; c < kStageCols; ++c)
+                        if (c < FO - col) y[(size_t)(row0 + lane) * ldy + col + c] = v[e + c] + bv[e + c];
                 }
-            } else {
-#pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    stage[lane * 16 + (c ^ sw)] = v[half * 16 + c] + (ch + c < FO ? __ldg(b4 + ch + c) : 0.f);
+                continue;
             }
+            unsigned char *buf = stage + (box & 1) * kStageBuf;
+            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
             __syncwarp();
-            const int c = lane & 15;
-            if (ch + c < FO) {
-#pragma unroll 4
-                for (int i = 0; i < 16; ++i) {
-                    const int r = 2 * i + (lane >> 4);
-                    if (r < rows) y[(size_t)(row0 + r) * ldy + ch + c] = stage[r * 16 + (c ^ (i & 15))];
-                }
+            float4 *dst = reinterpret_cast<float4 *>(buf + lane * (kStageCols * 4));
+            dst[0] = make_float4(v[e] + bv[e], v[e + 1] + bv[e + 1], v[e + 2] + bv[e + 2], v[e + 3] + bv[e + 3]);
+            dst[1] = make_float4(v[e + 4] + bv[e + 4], v[e + 5] + bv[e + 5], v[e + 6] + bv[e + 6],
+                                 v[e + 7] + bv[e + 7]);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0 && row0 < m) {
+                asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n"
+                             :: "l"(reinterpret_cast<uint64_t>(ymap)), "r"(col), "r"(row0), "r"(smem_u32(buf))
+                             : "memory");
+                asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
             }
-            __syncwarp();
+            ++box;
         }
     }
 }
 
-__global__ void __launch_bounds__(kThreads, 1) mlp_fused_kernel(const float *x, int m, const float *b1,
-                                                                const float *b2, const float *b3, const float *b4,
-                                                                const unsigned char *blob, float *y, int ldy,
-                                                                unsigned int *err) {
-    extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *act = smem;                                   // 64 KB activation tile
-    unsigned char *wbuf = smem + kActBytes;                      // 128 KB weight block
-    unsigned char *stage_all = smem + kActBytes + kBlockBytes;   // 32 KB: output stage
-    unsigned char *xt = stage_all;                               // layer 1: 4 KB input tile ...
-    unsigned char *w1t = stage_all + kXBytes;                    // ... and 8 KB W1 tile
-    __shared__ __align__(8) uint64_t wbar, mbar;
-    __shared__ uint32_t tmem_slot;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int quarter = warp & 3, group = warp >> 2;
-    const int m0 = blockIdx.x * FM;
-    const int row0 = m0 + quarter * 32;
-    const int rows = min(32, max(0, m - row0));
-    float *stage = reinterpret_cast<float *>(stage_all) + warp * 32 * 16;
+struct Bars {
+    uint64_t full[2], empty[2];   // weight ring
+    uint64_t accf[2], acce[2];    // accumulator halves: full (MMA -> epilogue), empty (epilogue -> MMA)
+    uint64_t act;                 // input / activation tile written (epilogue -> MMA)
+    uint64_t fin;                 // every MMA of the CTA complete
+};
 
-    if (warp == 0) {
+__global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, int m, const float *b1,
+                                                                const float *b2, const float *b3, const float *b4,
+                                                                const unsigned char *blob,
+                                                                const __grid_constant__ CUtensorMap ymap, float *y,
+                                                                int ldy, unsigned int *err) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char *act = smem;                                   // 64 KB activation tile
+    unsigned char *ring = smem + kActBytes;                      // 2 x 16 KB weight chunks
+    unsigned char *stage_all = smem + kActBytes + kRingBytes;    // 16 KB output stage ...
+    unsigned char *xt = stage_all;                               // ... and, for layer 1, the input tile
+    __shared__ __align__(8) Bars bars;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+    volatile int *abort = &abort_flag;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * FM;
+
+    if (warp == kMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
                      :: "r"(smem_u32(&tmem_slot)), "r"(kTmemCols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&wbar)));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mbar)));
+        // tensor stores read their boxes from 128-byte aligned shared memory
+        abort_flag = (smem_u32(stage_all) & 127u) != 0;
+        for (int i = 0; i < 2; ++i) {
+            bar_init(&bars.full[i], 1);
+            bar_init(&bars.empty[i], 1);
+            bar_init(&bars.accf[i], 1);
+            bar_init(&bars.acce[i], kEpiThreads);
+        }
+        bar_init(&bars.act, kEpiThreads);
+        bar_init(&bars.fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     const uint32_t tmem = tmem_slot;
-    uint32_t wphase = 0, mphase = 0;
-    bool w_pending = false, m_pending = false, ok = true;
-    const bool leader = threadIdx.x == 0;
 
-    // W1 and W2 start arriving while the input tile is written
-    if (leader) {
-        expect_tx(&wbar, kW1Bytes + kBlockBytes);
-        bulk_copy(w1t, blob + kW1Offset, kW1Bytes, &wbar);
-        bulk_copy(wbuf, blob, kBlockBytes, &wbar);
-    }
-    w_pending = true;
-    if (threadIdx.x < FM) {
-        const int r = threadIdx.x, gm = m0 + r;
-        float xin[FIN];
-#pragma unroll
-        for (int k = 0; k < FIN; ++k) xin[k] = gm < m ? x[(size_t)gm * FIN + k] : 0.f;
-        const __nv_bfloat162 p0 = __floats2bfloat162_rn(xin[0], xin[1]);
-        const __nv_bfloat162 p1 = __floats2bfloat162_rn(xin[2], xin[3]);
-        *reinterpret_cast<uint4 *>(xt + core_off(r, 0, FK1)) =
-            make_uint4(*reinterpret_cast<const uint32_t *>(&p0), *reinterpret_cast<const uint32_t *>(&p1), 0u, 0u);
-        *reinterpret_cast<uint4 *>(xt + core_off(r, 8, FK1)) = make_uint4(0u, 0u, 0u, 0u);
-    }
-    asm volatile("fence.proxy.async.shared::cta;\n");
-
-    // Waits below are made uniform across the CTA; a timeout ends the sequence.
-#define MCW_WAIT(bar, phase, pending)                                  \
-    do {                                                               \
-        ok = __syncthreads_and(wait_phase(&(bar), (phase))) != 0;      \
-        if (!ok) goto done;                                            \
-        (phase) ^= 1u;                                                 \
-        (pending) = false;                                             \
-    } while (0)
-
-    MCW_WAIT(wbar, wphase, w_pending);                       // W1, W2 landed; input tile written
-    if (leader) issue_mma(tmem, xt, w1t, FK1, &mbar);        // layer 1
-    m_pending = true;
-    MCW_WAIT(mbar, mphase, m_pending);
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    epilogue_hidden(tmem, 0, b1, act, quarter, group, lane);
-    asm volatile("fence.proxy.async.shared::cta;\n");
-    asm volatile("tcgen05.fence::before_thread_sync;\n");
-    __syncthreads();
-
-    // layers 2 and 3: the weights of the next block arrive during the epilogue
-    for (int layer = 0; layer < 2; ++layer) {
-        if (layer > 0) MCW_WAIT(wbar, wphase, w_pending);
-        if (leader) issue_mma(tmem, act, wbuf, FH, &mbar);
-        m_pending = true;
-        MCW_WAIT(mbar, mphase, m_pending);
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-        if (leader) {
-            expect_tx(&wbar, kBlockBytes);
-            bulk_copy(wbuf, blob + (size_t)(layer + 1) * kBlockBytes, kBlockBytes, &wbar);
+    if (warp == kProducerWarp) {
+        if (lane == 0) {
+            int issued = 0;
+            for (int i = 0; i < kNumChunks; ++i) {
+                const int slot = i & 1;
+                if (i >= 2 && !wait_bar(&bars.empty[slot], (uint32_t)((i >> 1) - 1) & 1u, abort)) break;
+                load_chunk(ring + slot * kChunkBytes, blob + chunk_offset(i), chunk_bytes(i), &bars.full[slot]);
+                issued = i + 1;
+            }
+            // the last copy into each slot has landed before the CTA can leave
+            for (int i = issued - 2 < 0 ? 0 : issued - 2; i < issued; ++i)
+                wait_bar(&bars.full[i & 1], (uint32_t)(i >> 1) & 1u, nullptr);
         }
-        w_pending = true;
-        epilogue_hidden(tmem, 0, layer == 0 ? b2 : b3, act, quarter, group, lane);
+    } else if (warp == kMmaWarp) {
+        if (lane == 0) {
+            const uint32_t act_a = smem_u32(act), ring_a = smem_u32(ring), x_a = smem_u32(xt);
+            int chunk = 0;
+            uint32_t act_phase = 0;
+            bool ok = true;
+            auto take = [&](void) -> uint32_t {      // wait for the next chunk; its shared address
+                const int slot = chunk & 1;
+                ok = ok && wait_bar(&bars.full[slot], (uint32_t)(chunk >> 1) & 1u, abort);
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                return ring_a + (uint32_t)slot * kChunkBytes;
+            };
+            auto release = [&](void) {               // chunk's MMAs issued: free its slot when they finish
+                commit(&bars.empty[chunk & 1]);
+                ++chunk;
+            };
+            // layer 1: input tile x W1
+            ok = wait_bar(&bars.act, act_phase, abort);
+            act_phase ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            if (ok) {
+                const uint32_t w = take();
+                if (ok) {
+                    mma_steps(tmem, x_a, FK1, 0, w, FK1, 1, idesc(FH), false);
+                    release();
+                    commit(&bars.accf[0]);
+                }
+            }
+            // layers 2 and 3: eight chunks of 32 k each
+            for (int layer = 0; layer < 2 && ok; ++layer) {
+                ok = wait_bar(&bars.act, act_phase, abort);
+                act_phase ^= 1u;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                for (int c = 0; c < kHidChunks && ok; ++c) {
+                    const uint32_t w = take();
+                    if (!ok) break;
+                    mma_steps(tmem, act_a, FH, c * (kHidK / 16), w, kHidK, kHidK / 16, idesc(FH), c > 0);
+                    release();
+                }
+                if (ok) commit(&bars.accf[0]);
+            }
+            // output layer: six 128-column blocks alternating between accumulator halves
+            if (ok) {
+                ok = wait_bar(&bars.act, act_phase, abort);
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+            }
+            for (int j = 0; j < kOutBlocks && ok; ++j) {
+                const int h = j & 1;
+                if (j >= 2) {
+                    ok = wait_bar(&bars.acce[h], (uint32_t)((j >> 1) - 1) & 1u, abort);
+                    asm volatile("tcgen05.fence::after_thread_sync;\n");
+                    if (!ok) break;
+                }
+                for (int c = 0; c < kOutChunks && ok; ++c) {
+                    const uint32_t w = take();
+                    if (!ok) break;
+                    mma_steps(tmem + (uint32_t)(h * kOutN), act_a, FH, c * (kOutK / 16), w, kOutK, kOutK / 16,
+                              idesc(kOutN), c > 0);
+                    release();
+                }
+                if (ok) commit(&bars.accf[h]);
+            }
+            // every MMA issued by this thread has completed before the memory is freed
+            commit(&bars.fin);
+            wait_bar(&bars.fin, 0, nullptr);
+        }
+    } else {
+        // epilogue warps
+        const int quarter = warp & 3, group = warp >> 2;
+        const int row0 = m0 + quarter * 32;
+        const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
+        unsigned char *stage = stage_all + warp * 2 * kStageBuf;
+        int box = 0;
+        uint32_t accf_phase[2] = {0u, 0u};
+        if (threadIdx.x < FM) {
+            const int r = threadIdx.x, gm = m0 + r;
+            float xin[FIN];
+#pragma unroll
+            for (int k = 0; k < FIN; ++k) xin[k] = gm < m ? x[(size_t)gm * FIN + k] : 0.f;
+            const __nv_bfloat162 p0 = __floats2bfloat162_rn(xin[0], xin[1]);
+            const __nv_bfloat162 p1 = __floats2bfloat162_rn(xin[2], xin[3]);
+            *reinterpret_cast<uint4 *>(xt + core_off(r, 0, FK1)) = make_uint4(
+                *reinterpret_cast<const uint32_t *>(&p0), *reinterpret_cast<const uint32_t *>(&p1), 0u, 0u);
+            *reinterpret_cast<uint4 *>(xt + core_off(r, 8, FK1)) = make_uint4(0u, 0u, 0u, 0u);
+        }
         asm volatile("fence.proxy.async.shared::cta;\n");
-        asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();
+        arrive(&bars.act);
+        const float *hb[3] = {b1, b2, b3};
+        bool ok = true;
+        for (int layer = 0; layer < 3 && ok; ++layer) {
+            ok = wait_bar(&bars.accf[0], accf_phase[0], abort);
+            accf_phase[0] ^= 1u;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            epilogue_hidden(tlane, hb[layer], act, quarter, group, lane);
+            asm volatile("fence.proxy.async.shared::cta;\n");
+            asm volatile("tcgen05.fence::before_thread_sync;\n");
+            arrive(&bars.act);
+        }
+        for (int j = 0; j < kOutBlocks && ok; ++j) {
+            const int h = j & 1;
+            ok = wait_bar(&bars.accf[h], accf_phase[h], abort);
+            accf_phase[h] ^= 1u;
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            epilogue_out(tlane + (uint32_t)(h * kOutN), j, b4, stage, &ymap, y, ldy, m, row0, group, lane, box);
+            asm volatile("tcgen05.fence::before_thread_sync;\n");
+            arrive(&bars.acce[h]);
+        }
+        // the stores have finished reading shared memory and writing y
+        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
     }
 
-    // output layer: block 0 -> columns 0-255 of tensor memory, block 1 -> 256-511, block 2 -> 0-255
-    MCW_WAIT(wbar, wphase, w_pending);
-    if (leader) issue_mma(tmem, act, wbuf, FH, &mbar);
-    m_pending = true;
-    MCW_WAIT(mbar, mphase, m_pending);
-    if (leader) {
-        expect_tx(&wbar, kBlockBytes);
-        bulk_copy(wbuf, blob + 3 * (size_t)kBlockBytes, kBlockBytes, &wbar);
-    }
-    w_pending = true;
-    MCW_WAIT(wbar, wphase, w_pending);
-    if (leader) issue_mma(tmem + FH, act, wbuf, FH, &mbar);      // block 1 runs during block 0's epilogue
-    m_pending = true;
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    epilogue_out(tmem, 0, 0, b4, stage, y, ldy, row0, rows, quarter, group, lane);
-    asm volatile("tcgen05.fence::before_thread_sync;\n");
-    MCW_WAIT(mbar, mphase, m_pending);                       // block 1 done: wbuf free, columns 0-255 read
-    if (leader) {
-        expect_tx(&wbar, kBlockBytes);
-        bulk_copy(wbuf, blob + 4 * (size_t)kBlockBytes, kBlockBytes, &wbar);
-    }
-    w_pending = true;
-    MCW_WAIT(wbar, wphase, w_pending);
-    if (leader) issue_mma(tmem, act, wbuf, FH, &mbar);           // block 2 runs during block 1's epilogue
-    m_pending = true;
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    epilogue_out(tmem, FH, 1, b4, stage, y, ldy, row0, rows, quarter, group, lane);
-    MCW_WAIT(mbar, mphase, m_pending);
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    epilogue_out(tmem, 0, 2, b4, stage, y, ldy, row0, rows, quarter, group, lane);
-#undef MCW_WAIT
-
-done:
-    if (!ok) {
-        if (leader) atomicOr(err, 2u);
-        // copies and MMAs still in flight finish (bounded) before the CTA leaves
-        if (w_pending) wait_phase(&wbar, wphase);
-        if (m_pending) wait_phase(&mbar, mphase);
-    }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
-    if (warp == 0) {
+    if (threadIdx.x == 0 && abort_flag) atomicOr(err, 2u);
+    if (warp == kMmaWarp) {
+        __syncwarp();
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(kTmemCols));
     }
 }
 
-// Repack rows [row0, row0 + rows_out) of W [n, k] (row-major bf16) into a K-major
-// core-matrix tile with rows of kdim; rows >= n and k >= k_in are zero.
-__global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, int rows_out, int kdim,
+// Rows [row0, row0 + rows_out) and k [k0, k0 + kdim) of W [n, k_in] (row-major bf16) as a
+// K-major core-matrix tile with rows of kdim; entries outside W are zero.
+__global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, int rows_out, int k0, int kdim,
                             unsigned char *tile) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;   // one 16-byte chunk: row, k8
     const int per_row = kdim / 8;
@@ -370,7 +463,7 @@ __global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, i
     __align__(16) __nv_bfloat16 h[8];
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
-        const int gr = row0 + r, gk = k8 * 8 + e;
+        const int gr = row0 + r, gk = k0 + k8 * 8 + e;
         h[e] = (gr < n && gk < k_in) ? w[(size_t)gr * k_in + gk] : __float2bfloat16(0.f);
     }
     *reinterpret_cast<uint4 *>(tile + core_off(r, k8 * 8, kdim)) = *reinterpret_cast<const uint4 *>(h);
@@ -382,6 +475,29 @@ __global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, i
 
 using namespace mcw;
 
+namespace {
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver through the runtime (no link against libcuda).
+EncodeTiled encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiled fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    });
+    return fn;
+}
+
+}  // namespace
+
 extern "C" {
 
 int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4, void *blob, void *stream) {
@@ -390,31 +506,46 @@ int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4,
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     unsigned char *b = static_cast<unsigned char *>(blob);
     const int threads = 256;
-    const int grid = (FH * (FH / 8) + threads - 1) / threads;
-    const __nv_bfloat16 *w[3] = {static_cast<const __nv_bfloat16 *>(w2), static_cast<const __nv_bfloat16 *>(w3),
-                                 static_cast<const __nv_bfloat16 *>(w4)};
-    pack_kernel<<<grid, threads, 0, s>>>(w[0], FH, FH, 0, FH, FH, b);
-    pack_kernel<<<grid, threads, 0, s>>>(w[1], FH, FH, 0, FH, FH, b + kBlockBytes);
+    auto pack = [&](const void *w, int n, int k_in, int row0, int rows_out, int k0, int kdim, int chunk) {
+        const int units = rows_out * (kdim / 8);
+        pack_kernel<<<(units + threads - 1) / threads, threads, 0, s>>>(
+            static_cast<const __nv_bfloat16 *>(w), n, k_in, row0, rows_out, k0, kdim, b + chunk_offset(chunk));
+    };
+    int chunk = 0;
+    pack(w1, FH, FIN, 0, FH, 0, FK1, chunk++);
+    for (const void *w : {w2, w3})
+        for (int c = 0; c < kHidChunks; ++c) pack(w, FH, FH, 0, FH, c * kHidK, kHidK, chunk++);
     for (int j = 0; j < kOutBlocks; ++j)
-        pack_kernel<<<grid, threads, 0, s>>>(w[2], FO, FH, j * FH, FH, FH, b + (size_t)(2 + j) * kBlockBytes);
-    pack_kernel<<<(FH * (FK1 / 8) + threads - 1) / threads, threads, 0, s>>>(
-        static_cast<const __nv_bfloat16 *>(w1), FH, FIN, 0, FH, FK1, b + kW1Offset);
+        for (int c = 0; c < kOutChunks; ++c) pack(w4, FO, FH, j * kOutN, kOutN, c * kOutK, kOutK, chunk++);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
 }
 
 int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3, const float *b4,
                     const void *blob, float *y, int32_t ldy, void *stream) {
-    if (!x || !b1 || !b2 || !b3 || !b4 || !blob || !y || m < 0 || ldy < FO) return MCW_MLP_ERR_ARG;
-    if ((((uintptr_t)blob | (uintptr_t)b1 | (uintptr_t)b2 | (uintptr_t)b3 | (uintptr_t)b4) & 15) != 0)
+    if (!x || !b1 || !b2 || !b3 || !b4 || !blob || !y || m < 0 || ldy < FO || (ldy & 3) != 0)
+        return MCW_MLP_ERR_ARG;
+    if ((((uintptr_t)blob | (uintptr_t)b1 | (uintptr_t)b2 | (uintptr_t)b3 | (uintptr_t)b4 | (uintptr_t)y) & 15) != 0)
         return MCW_MLP_ERR_ARG;
     if (m == 0) return 0;
     unsigned int *err = tc_err_flag();
     if (!err) return MCW_MLP_ERR_CUDA;
+    EncodeTiled encode = encode_tiled();
+    if (!encode) return MCW_MLP_ERR_CUDA;
+    // y as a 2-D f32 tensor [m rows][649 columns], row pitch 4 ldy bytes, stored in 8 x 32 boxes
+    CUtensorMap ymap;
+    const cuuint64_t dims[2] = {(cuuint64_t)FO, (cuuint64_t)m};
+    const cuuint64_t strides[1] = {(cuuint64_t)ldy * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kStageCols, 32u};
+    const cuuint32_t estr[2] = {1u, 1u};
+    if (encode(&ymap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return MCW_MLP_ERR_ARG;
     cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSmemBytes);
     if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
     mlp_fused_kernel<<<(m + FM - 1) / FM, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(
-        x, m, b1, b2, b3, b4, static_cast<const unsigned char *>(blob), y, ldy, err);
+        x, m, b1, b2, b3, b4, static_cast<const unsigned char *>(blob), ymap, y, ldy, err);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
 }
 

@@ -119,17 +119,21 @@ def pack_weights(torch, w16):
     return blob
 
 
+# row pitch of the fused kernel's output: 649 rounded up to 16 bytes (tensor-store rule)
+Y_PITCH = 652
+
+
 def forward_fused(torch, x, w16, biases, blob):
     """Inference of the whole network in one kernel (mcw_mlp_forward); x float32 [m, 4]."""
     x = x.contiguous().float()
     m = x.shape[0]
-    y = torch.empty((m, DIMS[-1]), dtype=torch.float32, device=x.device)
+    y = torch.empty((m, Y_PITCH), dtype=torch.float32, device=x.device)
     b = [t.contiguous() for t in biases]
     rc = _abi.load().mcw_mlp_forward(_ptr(x), m, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), _ptr(b[3]), _ptr(blob),
-                                     _ptr(y), DIMS[-1], _stream(torch))
+                                     _ptr(y), Y_PITCH, _stream(torch))
     if rc:
         raise _abi.McwError(rc, 'mcw_mlp_forward failed (m=%d)' % m)
-    return y
+    return y[:, :DIMS[-1]]
 
 
 def forward_cached(torch, x16, w16, biases, keep=True):

@@ -203,12 +203,13 @@ def test_fused_forward_matches_layerwise_and_float64(m):
 
 
 def test_fused_forward_leading_dimension_and_repack():
-    """Rows land at stride ldy without touching the padding; after an Adam step the
-    packed weights are rebuilt so inference follows the new weights."""
+    """Rows land at stride ldy without touching the padding columns or the rows past m;
+    after an Adam step the packed weights are rebuilt so inference follows the new weights."""
     net = _random_net(7)
     m, ldy = 300, 700
     x = (torch.rand(m, 4, generator=torch.Generator().manual_seed(2)) * 2 - 1).cuda()
-    out = torch.full((m, ldy), 12345.0, device='cuda')
+    full = torch.full((m + 40, ldy), 12345.0, device='cuda')
+    out = full[:m]
     b = [t.contiguous() for t in net.params[1::2]]
     rc = _abi.load().mcw_mlp_forward(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
                                      surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
@@ -218,10 +219,15 @@ def test_fused_forward_leading_dimension_and_repack():
     torch.cuda.synchronize()
     assert torch.equal(out[:, :649], y)
     assert (out[:, 649:] == 12345.0).all()
+    assert (full[m:] == 12345.0).all()
     bad = _abi.load().mcw_mlp_forward(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
                                       surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
                                       surrogate._ptr(out), 600, surrogate._stream(torch))
     assert bad == -1
+    bad = _abi.load().mcw_mlp_forward(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
+                                      surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
+                                      surrogate._ptr(out), 650, surrogate._stream(torch))
+    assert bad == -1                               # row pitch not a multiple of 16 bytes
     before = net.predict_std(x).clone()
     t = torch.randn(64, 649, device='cuda')
     w_out = torch.from_numpy(surrogate.output_weights()).cuda()
