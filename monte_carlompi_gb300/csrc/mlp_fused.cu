@@ -14,21 +14,19 @@
 //    N = 128 blocks ping-ponging between the two halves of the accumulator;
 //  * warps 0-7 write the input tile and run the epilogues: hidden layers (bias,
 //    SiLU, bf16) write the next layer's A operand back into the 64 KB activation
-//    tile, so activations never leave shared memory; output blocks leave through a
-//    double-buffered 32-row x 8-column stage per warp as 2-D TMA tensor stores
-//    (cp.async.bulk.tensor), which clip rows >= m and columns >= 649 themselves.
+//    tile, so activations never leave shared memory; output blocks are transposed
+//    8 rows at a time through a small per-warp stage so that every output row is
+//    written as whole 128-byte runs (a warp's 16-byte stores cover 4 rows x 128 B).
 //    Epilogue warp w reads accumulator lanes 32 (w % 4) .. +31 (its rows).
 // Hand-offs are mbarriers: ring full/empty, accumulator full (tcgen05.commit) and
 // empty, activation tile ready.  Every wait is bounded by %globaltimer (2 s) and
 // checks a CTA-wide abort flag; a timeout sets bit 1 of the error flag read by
 // mcw_mlp_status, lets copies and MMAs in flight finish (bounded), frees the tensor
 // memory and leaves.
-#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 
 #include "../../include/mcw_mlp.h"
 
@@ -43,8 +41,20 @@ constexpr int FH = MCW_MLP_HIDDEN;      // 256
 constexpr int FO = MCW_MLP_OUT;         // 649
 constexpr int FIN = MCW_MLP_IN;         // 4
 constexpr int FK1 = 16;                 // layer-1 K, zero-padded
-constexpr int kEpiWarps = 8;
-constexpr int kProducerWarp = 8, kMmaWarp = 9;
+#ifndef MCW_FUSED_SLOTS
+#define MCW_FUSED_SLOTS 2
+#endif
+#ifndef MCW_FUSED_EPI_WARPS
+#define MCW_FUSED_EPI_WARPS 8
+#endif
+#ifndef MCW_FUSED_CTAS_PER_SM
+#define MCW_FUSED_CTAS_PER_SM 2
+#endif
+constexpr int kSlots = MCW_FUSED_SLOTS;              // weight ring depth
+constexpr int kEpiWarps = MCW_FUSED_EPI_WARPS;       // 8 or 16
+constexpr int kCtasPerSm = MCW_FUSED_CTAS_PER_SM;
+constexpr int kGroups = kEpiWarps / 4;               // column groups per accumulator lane quarter
+constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
 constexpr int kEpiThreads = 32 * kEpiWarps;
 constexpr int kOutN = 128;                            // output block width
@@ -59,10 +69,14 @@ constexpr int kW1Bytes = FH * FK1 * 2;                // 8 KB, chunk 0
 constexpr int kNumChunks = 1 + 2 * kHidChunks + kOutBlocks * kOutChunks;   // 41
 constexpr int kXBytes = FM * FK1 * 2;                 // 4 KB
 constexpr int kActBytes = FM * FH * 2;                // 64 KB
-constexpr int kRingBytes = 2 * kChunkBytes;           // 32 KB
-constexpr int kStageCols = 8;                         // output columns per TMA store box
-constexpr int kStageBuf = 32 * kStageCols * 4;        // 1 KB: one box
-constexpr int kStageBytes = kEpiWarps * 2 * kStageBuf;  // 16 KB: two boxes per warp
+constexpr int kRingBytes = kSlots * kChunkBytes;
+constexpr int kStagePitch = 36 * 4;                   // stage row: 32 floats + 16 B pad (no bank conflicts)
+constexpr int kStageWarp = 8 * kStagePitch;           // 8 rows per warp
+constexpr int kStageBytes = kEpiWarps * kStageWarp < 4096 ? 4096 : kEpiWarps * kStageWarp;
+constexpr int kHidCols = FH / kGroups;                // hidden columns per epilogue warp
+constexpr int kOutCols = kOutN / kGroups;             // output-block columns per epilogue warp
+static_assert(kEpiWarps % 4 == 0 && kHidCols % 32 == 0 && kOutCols % 32 == 0, "epilogue split");
+static_assert(kActBytes + kRingBytes + kStageBytes <= 227 * 1024, "shared memory");
 constexpr size_t kSmemBytes = (size_t)kActBytes + kRingBytes + kStageBytes;
 constexpr uint32_t kTmemCols = 256;
 constexpr unsigned long long kWaitNs = 2000000000ull;
@@ -163,8 +177,9 @@ __device__ __forceinline__ void mma_steps(uint32_t tmem, uint32_t a_base, int a_
     }
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-    uint32_t r[32];
+// 32 consecutive accumulator columns of this warp's 32 lanes: issue, then wait.  The
+// wait names the destination registers so no use of them is scheduled before it.
+__device__ __forceinline__ void tmem_ld32_issue(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -175,112 +190,140 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
           "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
           "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+}
+
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+                   "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                   "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]),
+                   "+r"(r[21]), "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]),
+                   "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31]));
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    tmem_ld32_issue(taddr, r);
+    tmem_ld_wait(r);
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
 }
 
-// Hidden epilogue: this warp's 32 rows x 128 columns (64 group .. ) of the 256-column
-// accumulator -> SiLU(z + b) as bf16 into the activation tile.
+// SiLU(z + b) of 32 accumulator columns -> bf16 at (row, c0 ..) of the activation tile.
+__device__ __forceinline__ void silu_store32(const uint32_t (&r)[32], const float *bias, unsigned char *act, int row,
+                                             int c0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float4 ba = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8));
+        const float4 bb = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8 + 4));
+        const float bv[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
+        uint32_t packed[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const __nv_bfloat162 two =
+                __floats2bfloat162_rn(silu(__uint_as_float(r[q * 8 + 2 * e]) + bv[2 * e]),
+                                      silu(__uint_as_float(r[q * 8 + 2 * e + 1]) + bv[2 * e + 1]));
+            packed[e] = *reinterpret_cast<const uint32_t *>(&two);
+        }
+        *reinterpret_cast<uint4 *>(act + core_off(row, c0 + q * 8, FH)) =
+            make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    }
+}
+
+// Hidden epilogue: this warp's 32 rows x kHidCols columns of the 256-column
+// accumulator -> SiLU(z + b) as bf16 into the activation tile.  The load of the next
+// 32 columns is in flight while the current ones are computed.
 __device__ __forceinline__ void epilogue_hidden(uint32_t tlane, const float *bias, unsigned char *act, int quarter,
                                                 int group, int lane) {
     const int row = quarter * 32 + lane;
-#pragma unroll 1
-    for (int h = 0; h < 4; ++h) {
-        const int c0 = group * 128 + h * 32;
-        float v[32];
-        tmem_ld32(tlane + (uint32_t)c0, v);
+    const int cbase = group * kHidCols;
+    uint32_t ra[32], rb[32];
+    tmem_ld32_issue(tlane + (uint32_t)cbase, ra);
+    tmem_ld_wait(ra);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float4 ba = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8));
-            const float4 bb = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8 + 4));
-            const float bv[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
-            uint32_t packed[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const __nv_bfloat162 two = __floats2bfloat162_rn(silu(v[q * 8 + 2 * e] + bv[2 * e]),
-                                                                 silu(v[q * 8 + 2 * e + 1] + bv[2 * e + 1]));
-                packed[e] = *reinterpret_cast<const uint32_t *>(&two);
-            }
-            *reinterpret_cast<uint4 *>(act + core_off(row, c0 + q * 8, FH)) =
-                make_uint4(packed[0], packed[1], packed[2], packed[3]);
+    for (int h = 0; h < kHidCols / 32; h += 2) {
+        if (h + 1 < kHidCols / 32) tmem_ld32_issue(tlane + (uint32_t)(cbase + (h + 1) * 32), rb);
+        silu_store32(ra, bias, act, row, cbase + h * 32);
+        if (h + 1 < kHidCols / 32) {
+            tmem_ld_wait(rb);
+            if (h + 2 < kHidCols / 32) tmem_ld32_issue(tlane + (uint32_t)(cbase + (h + 2) * 32), ra);
+            silu_store32(rb, bias, act, row, cbase + (h + 1) * 32);
+            if (h + 2 < kHidCols / 32) tmem_ld_wait(ra);
         }
     }
 }
 
-// Output epilogue of block blk (output columns 128 blk ..): this warp's 32 rows x 64
-// columns, z + b4, leave in 32 x 8 boxes: registers -> stage buffer (row r at
-// 32 r bytes) -> one TMA tensor store by lane 0.  Two buffers alternate; a buffer is
-// rewritten once the store issued from it two boxes earlier has read it.
-__device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
-                                             const CUtensorMap *ymap, float *y, int ldy, int m, int row0,
-                                             int group, int lane, int &box) {
+// Output epilogue of block blk (output columns 128 blk ..): this warp's 32 rows x
+// kOutCols columns, z + b4.  Per 32 columns the warp's rows go through its stage 8 at
+// a time (lanes 8p .. 8p + 7 write their rows, then every lane reads 16 bytes), and
+// each 16-byte store instruction writes 4 rows x 128 contiguous bytes of y.  The
+// ragged last 32 columns (640 .. 648 valid) are written one float per lane.
+__device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const float *b4, unsigned char *stage, float *y,
+                                             int ldy, int m, int row0, int group, int lane) {
 #pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const int c0 = group * 64 + h * 32;
+    for (int h = 0; h < kOutCols / 32; ++h) {
+        const int c0 = group * kOutCols + h * 32;
         const int nb = blk * kOutN + c0;
         if (nb >= FO) break;
-        float bv[32];
-        static_assert(FO % kStageCols == 1, "one ragged column at the end");
-        if (nb + 32 <= FO) {
+        const bool full = nb + 32 <= FO;
+        float z[32];
+        if (full) {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 const float4 b = __ldg(reinterpret_cast<const float4 *>(b4 + nb + 4 * q));
-                bv[4 * q] = b.x, bv[4 * q + 1] = b.y, bv[4 * q + 2] = b.z, bv[4 * q + 3] = b.w;
+                z[4 * q] = b.x, z[4 * q + 1] = b.y, z[4 * q + 2] = b.z, z[4 * q + 3] = b.w;
             }
         } else {
 #pragma unroll
-            for (int c = 0; c < 32; ++c) bv[c] = nb + c < FO ? __ldg(b4 + nb + c) : 0.f;
+            for (int c = 0; c < 32; ++c) z[c] = nb + c < FO ? __ldg(b4 + nb + c) : 0.f;
         }
-        float v[32];
-        tmem_ld32(tlane + (uint32_t)c0, v);
+        {
+            float v[32];
+            tmem_ld32(tlane + (uint32_t)c0, v);
 #pragma unroll
-        for (int p = 0; p < 32 / kStageCols; ++p) {
-            const int col = nb + p * kStageCols;
-            if (col >= FO) break;
-            const int e = p * kStageCols;
-            if (col + kStageCols > FO) {
-                // ragged last box: tensor stores clip columns only to 16-byte granules, so the
-                // columns past 648 that share one with a valid column are written here directly
-                if (row0 + lane < m) {
+            for (int c = 0; c < 32; ++c) z[c] += v[c];
+        }
 #pragma unroll
-                    for (int c = 0; c < kStageCols; ++c)
-                        if (c < FO - col) y[(size_t)(row0 + lane) * ldy + col + c] = v[e + c] + bv[e + c];
+        for (int p = 0; p < 4; ++p) {
+            __syncwarp();
+            if ((lane >> 3) == p) {
+                float4 *dst = reinterpret_cast<float4 *>(stage + (lane & 7) * kStagePitch);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) dst[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+            }
+            __syncwarp();
+            const int rbase = row0 + 8 * p;      // first of the 8 rows in the stage
+            if (full) {
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int r = (lane >> 3) + 4 * k;
+                    const float4 val = *reinterpret_cast<const float4 *>(stage + r * kStagePitch + (lane & 7) * 16);
+                    if (rbase + r < m)
+                        *reinterpret_cast<float4 *>(y + (size_t)(rbase + r) * ldy + nb + (lane & 7) * 4) = val;
                 }
-                continue;
+            } else if (nb + lane < FO) {
+#pragma unroll
+                for (int r = 0; r < 8; ++r)
+                    if (rbase + r < m)
+                        y[(size_t)(rbase + r) * ldy + nb + lane] =
+                            *reinterpret_cast<const float *>(stage + r * kStagePitch + lane * 4);
             }
-            unsigned char *buf = stage + (box & 1) * kStageBuf;
-            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;\n" ::: "memory");
-            __syncwarp();
-            float4 *dst = reinterpret_cast<float4 *>(buf + lane * (kStageCols * 4));
-            dst[0] = make_float4(v[e] + bv[e], v[e + 1] + bv[e + 1], v[e + 2] + bv[e + 2], v[e + 3] + bv[e + 3]);
-            dst[1] = make_float4(v[e + 4] + bv[e + 4], v[e + 5] + bv[e + 5], v[e + 6] + bv[e + 6],
-                                 v[e + 7] + bv[e + 7]);
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            __syncwarp();
-            if (lane == 0 && row0 < m) {
-                asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];\n"
-                             :: "l"(reinterpret_cast<uint64_t>(ymap)), "r"(col), "r"(row0), "r"(smem_u32(buf))
-                             : "memory");
-                asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
-            }
-            ++box;
         }
+        __syncwarp();
     }
 }
 
 struct Bars {
-    uint64_t full[2], empty[2];   // weight ring
+    uint64_t full[kSlots], empty[kSlots];   // weight ring
     uint64_t accf[2], acce[2];    // accumulator halves: full (MMA -> epilogue), empty (epilogue -> MMA)
     uint64_t act;                 // input / activation tile written (epilogue -> MMA)
     uint64_t fin;                 // every MMA of the CTA complete
 };
 
-__global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, int m, const float *b1,
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const float *x, int m, const float *b1,
                                                                 const float *b2, const float *b3, const float *b4,
-                                                                const unsigned char *blob,
-                                                                const __grid_constant__ CUtensorMap ymap, float *y,
-                                                                int ldy, unsigned int *err) {
+                                                                const unsigned char *blob, float *y, int ldy,
+                                                                unsigned int *err) {
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *act = smem;                                   // 64 KB activation tile
     unsigned char *ring = smem + kActBytes;                      // 2 x 16 KB weight chunks
@@ -299,11 +342,12 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        // tensor stores read their boxes from 128-byte aligned shared memory
-        abort_flag = (smem_u32(stage_all) & 127u) != 0;
-        for (int i = 0; i < 2; ++i) {
+        abort_flag = 0;
+        for (int i = 0; i < kSlots; ++i) {
             bar_init(&bars.full[i], 1);
             bar_init(&bars.empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
             bar_init(&bars.accf[i], 1);
             bar_init(&bars.acce[i], kEpiThreads);
         }
@@ -320,14 +364,14 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, 
         if (lane == 0) {
             int issued = 0;
             for (int i = 0; i < kNumChunks; ++i) {
-                const int slot = i & 1;
-                if (i >= 2 && !wait_bar(&bars.empty[slot], (uint32_t)((i >> 1) - 1) & 1u, abort)) break;
+                const int slot = i % kSlots;
+                if (i >= kSlots && !wait_bar(&bars.empty[slot], (uint32_t)(i / kSlots - 1) & 1u, abort)) break;
                 load_chunk(ring + slot * kChunkBytes, blob + chunk_offset(i), chunk_bytes(i), &bars.full[slot]);
                 issued = i + 1;
             }
             // the last copy into each slot has landed before the CTA can leave
-            for (int i = issued - 2 < 0 ? 0 : issued - 2; i < issued; ++i)
-                wait_bar(&bars.full[i & 1], (uint32_t)(i >> 1) & 1u, nullptr);
+            for (int i = issued - kSlots < 0 ? 0 : issued - kSlots; i < issued; ++i)
+                wait_bar(&bars.full[i % kSlots], (uint32_t)(i / kSlots) & 1u, nullptr);
         }
     } else if (warp == kMmaWarp) {
         if (lane == 0) {
@@ -336,13 +380,13 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, 
             uint32_t act_phase = 0;
             bool ok = true;
             auto take = [&](void) -> uint32_t {      // wait for the next chunk; its shared address
-                const int slot = chunk & 1;
-                ok = ok && wait_bar(&bars.full[slot], (uint32_t)(chunk >> 1) & 1u, abort);
+                const int slot = chunk % kSlots;
+                ok = ok && wait_bar(&bars.full[slot], (uint32_t)(chunk / kSlots) & 1u, abort);
                 asm volatile("tcgen05.fence::after_thread_sync;\n");
                 return ring_a + (uint32_t)slot * kChunkBytes;
             };
             auto release = [&](void) {               // chunk's MMAs issued: free its slot when they finish
-                commit(&bars.empty[chunk & 1]);
+                commit(&bars.empty[chunk % kSlots]);
                 ++chunk;
             };
             // layer 1: input tile x W1
@@ -397,11 +441,10 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, 
         }
     } else {
         // epilogue warps
-        const int quarter = warp & 3, group = warp >> 2;
-        const int row0 = m0 + quarter * 32;
+        const int quarter = warp & 3, group = warp >> 2;   // lane quarter, column group
         const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
-        unsigned char *stage = stage_all + warp * 2 * kStageBuf;
-        int box = 0;
+        unsigned char *stage = stage_all + warp * kStageWarp;
+        const int row0 = m0 + quarter * 32;
         uint32_t accf_phase[2] = {0u, 0u};
         if (threadIdx.x < FM) {
             const int r = threadIdx.x, gm = m0 + r;
@@ -434,12 +477,10 @@ __global__ void __launch_bounds__(kThreads, 2) mlp_fused_kernel(const float *x, 
             accf_phase[h] ^= 1u;
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n");
-            epilogue_out(tlane + (uint32_t)(h * kOutN), j, b4, stage, &ymap, y, ldy, m, row0, group, lane, box);
+            epilogue_out(tlane + (uint32_t)(h * kOutN), j, b4, stage, y, ldy, m, row0, group, lane);
             asm volatile("tcgen05.fence::before_thread_sync;\n");
             arrive(&bars.acce[h]);
         }
-        // the stores have finished reading shared memory and writing y
-        if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
     }
 
     asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -475,29 +516,6 @@ __global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, i
 
 using namespace mcw;
 
-namespace {
-
-using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// cuTensorMapEncodeTiled from the driver through the runtime (no link against libcuda).
-EncodeTiled encode_tiled() {
-    static std::once_flag once;
-    static EncodeTiled fn = nullptr;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(p);
-    });
-    return fn;
-}
-
-}  // namespace
-
 extern "C" {
 
 int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4, void *blob, void *stream) {
@@ -529,23 +547,11 @@ int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2,
     if (m == 0) return 0;
     unsigned int *err = tc_err_flag();
     if (!err) return MCW_MLP_ERR_CUDA;
-    EncodeTiled encode = encode_tiled();
-    if (!encode) return MCW_MLP_ERR_CUDA;
-    // y as a 2-D f32 tensor [m rows][649 columns], row pitch 4 ldy bytes, stored in 8 x 32 boxes
-    CUtensorMap ymap;
-    const cuuint64_t dims[2] = {(cuuint64_t)FO, (cuuint64_t)m};
-    const cuuint64_t strides[1] = {(cuuint64_t)ldy * 4};
-    const cuuint32_t box[2] = {(cuuint32_t)kStageCols, 32u};
-    const cuuint32_t estr[2] = {1u, 1u};
-    if (encode(&ymap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
-               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return MCW_MLP_ERR_ARG;
     cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSmemBytes);
     if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
     mlp_fused_kernel<<<(m + FM - 1) / FM, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(
-        x, m, b1, b2, b3, b4, static_cast<const unsigned char *>(blob), ymap, y, ldy, err);
+        x, m, b1, b2, b3, b4, static_cast<const unsigned char *>(blob), y, ldy, err);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
 }
 

@@ -119,7 +119,7 @@ def pack_weights(torch, w16):
     return blob
 
 
-# row pitch of the fused kernel's output: 649 rounded up to 16 bytes (tensor-store rule)
+# row pitch of the fused kernel's output: 649 floats rounded up to 16 bytes (its 16-byte stores)
 Y_PITCH = 652
 
 
