@@ -289,8 +289,9 @@ def run_surrogate(args):
 
 
 def run_mlp(args):
-    """Surrogate network forward (inference) on the BF16 tensor-core kernels: BRF/s and
-    TFLOP/s of the GEMMs against the measured bf16 peak."""
+    """Surrogate network inference on the fused tcgen05 kernel (mcw_mlp_forward): BRF/s,
+    TFLOP/s of the four layers against the measured bf16 peak, and the output stream
+    (f32 rows of 652) against the measured HBM copy bandwidth."""
     import torch
     from monte_carlompi_gb300 import surrogate as S
     batch = 65536
@@ -307,15 +308,23 @@ def run_mlp(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     flop = 2.0 * batch * sum(a * b for a, b in zip(S.DIMS[:-1], S.DIMS[1:]))
+    out_bytes = batch * S.Y_PITCH * 4 + batch * 4 * 4
     peaks, src = measured_peaks()
     tflops = flop / (ms / 1e3) / 1e12
+    gbs = out_bytes / (ms / 1e3) / 1e9
     peak = float(peaks.get('bf16_tflops') or 1900.0)
+    hbm = float(peaks.get('hbm_gbs') or 6800.0)
     print(json.dumps({'metric': METRIC, 'workload': 'mlp', 'value': batch / (ms / 1e3), 'unit': 'BRF/s',
                       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms, 'dtype': 'bf16',
+                      'gpu_launches': args.steps,
                       'config': {'batch': batch, 'net': '4-256-256-256-649 SiLU',
-                                 'kernels': 'tcgen05.mma kind::f16, TMEM accumulators'},
+                                 'kernels': 'one fused kernel: tcgen05.mma kind::f16 into tensor memory, '
+                                            'cp.async.bulk weight ring, activations in shared memory',
+                                 'l2': 'output (171 MB) larger than L2'},
                       'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s',
-                                   'frac': tflops / peak, 'peak_source': src}}))
+                                   'frac': tflops / peak, 'peak_source': src,
+                                   'hbm': {'achieved': gbs, 'peak': hbm, 'unit': 'GB/s', 'frac': gbs / hbm,
+                                           'bytes': 'x in + y out (f32, row pitch 652)'}}}))
     return 0
 
 
@@ -377,7 +386,8 @@ def run_reference(args):
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': 1e3 * tot / args.steps, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-        'config': dict(CONFIG_DESC, sample_photons_per_step=n),
+        'config': dict(CONFIG_DESC, sample_photons_per_step=n,
+                       mode='FP64 replay stream of the reference algorithm (C oracle on the host cores)'),
         'scatter_events_per_s': events / tot,
         'cpu_baseline': {'value': value, 'unit': 'photons/s', 'cores': cores, 'kind': 'port',
                          'sample': '%d photons per step of the workload (FP64 C oracle, '
