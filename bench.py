@@ -167,7 +167,7 @@ def committed_traffic():
 
 
 def sweep_workload():
-    """BASELINE config 3: 64 configs from r_eff x lambda0 x theta0 x depth, photon counts
+    """Sweep workload: 64 configs from r_eff x lambda0 x theta0 x depth, photon counts
     log-uniform over 1e4-1e6, seeded (0x5EED0003)."""
     from monte_carlompi_gb300 import ssp
     from monte_carlompi_gb300.config import WalkConfig
@@ -234,9 +234,10 @@ def run_sweep(args):
 
 
 def run_surrogate(args):
-    """BASELINE surrogate configuration: 4,096 configs x 2e5 photons walked on the GPU,
-    5-member ensemble trained on the tensor-core kernels, 512 held-out configs judged by
-    1e6-photon Monte Carlo; BRF/s of the network against plain Monte Carlo."""
+    """Surrogate workload: --surrogate-configs configs (16,384 by default) x 2e5 photons walked
+    on the GPU, 5-member ensemble trained on the tensor-core kernels, 512 held-out configs
+    judged by 1e6- and 1e7-photon Monte Carlo; BRF/s of the network against plain Monte
+    Carlo; then the inverse workload."""
     import time as _t
     import torch
     from monte_carlompi_gb300 import surrogate as S
@@ -329,10 +330,10 @@ def run_mlp(args):
 
 
 def run_inverse(ens, walker, n_obs):
-    """BASELINE inverse configuration: observed BRFs from 1e6-photon MC at hidden r_eff
+    """Inverse configuration: observed BRFs from 1e6-photon MC at hidden r_eff
     (log-uniform 50-1500 um, known lambda, theta0, depth) plus 1% Gaussian noise; Gauss-Newton
     on log r_eff through the surrogate with MC fallback where the ensemble spread exceeds 2%,
-    against the same Gauss-Newton driven by plain MC on a subset."""
+    against the same retrieval (grid + Gauss-Newton) driven by plain MC on a subset."""
     import time as _t
     from monte_carlompi_gb300 import inverse as I
     from monte_carlompi_gb300 import surrogate as S
@@ -345,19 +346,25 @@ def run_inverse(ens, walker, n_obs):
     res = I.retrieve(ens, walker, obs, known)
     err = np.abs(res['r_eff'] / raw[:, 0] - 1)
     # the same retrieval with plain Monte Carlo only, on a subset
-    n_sub = min(128, n_obs)
+    n_sub = min(64, n_obs)
     t0 = _t.perf_counter()
-    s_grid = np.full(n_sub, np.mean(I.LOG_R))
-    s_mc, evals = I.mc_gn(walker, obs[:n_sub], known[:n_sub], s_grid, iters=5)
+    s_mc, evals = I.mc_retrieve(walker, obs[:n_sub], known[:n_sub])
     t_mc = _t.perf_counter() - t0
     err_mc = np.abs(np.exp(s_mc) / raw[:n_sub, 0] - 1)
     t_sur = res['seconds_net'] + res['seconds_mc']
+    net_evals = n_obs * (16 + 6 + 1)
     return {'observations': n_obs, 'obs_photons': 1000000, 'noise': 0.01,
             'flagged_for_mc': float(res['flagged'].mean()),
             'r_eff_rel_err': {'median': float(np.median(err)), 'p90': float(np.percentile(err, 90))},
-            'r_eff_rel_err_unflagged_median': float(np.median(err[~res['flagged']])) if np.any(~res['flagged']) else None,
-            'seconds_surrogate_path': t_sur, 'seconds_per_retrieval': t_sur / n_obs,
-            'mc_only': {'subset': n_sub, 'r_eff_rel_err_median': float(np.median(err_mc)),
+            'r_eff_rel_err_unflagged_median':
+                float(np.median(err[~res['flagged']])) if np.any(~res['flagged']) else None,
+            'seconds': {'surrogate_gn': res['seconds_net'], 'mc_fallback': res['seconds_mc']},
+            'seconds_per_retrieval': t_sur / n_obs,
+            'brf_evals': {'surrogate': net_evals, 'mc_fallback': res['mc_brf_evals']},
+            'mc_only': {'subset': n_sub, 'method': '16-point grid + 4 Gauss-Newton iterations, 1e6-photon '
+                                                    'BRFs, central-difference Jacobians',
+                        'r_eff_rel_err_median': float(np.median(err_mc)),
+                        'surrogate_path_err_median_same_subset': float(np.median(err[:n_sub])),
                         'seconds_per_retrieval': t_mc / n_sub, 'brf_evals': evals},
             'speedup_per_retrieval_vs_mc': (t_mc / n_sub) / (t_sur / n_obs),
             'seconds_obs_generation': t_obs}
@@ -527,7 +534,7 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp'])
-    ap.add_argument('--surrogate-configs', type=int, default=4096)
+    ap.add_argument('--surrogate-configs', type=int, default=16384)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
     args = ap.parse_args()

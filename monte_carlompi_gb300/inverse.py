@@ -1,10 +1,10 @@
 """Grain-size retrieval: batched Gauss-Newton on log r_eff through the BRF surrogate.
 
 Given observed 648-bin BRFs with known wavelength, incident zenith and depth,
-find r_eff.  Each iteration evaluates the ensemble and the exact Jacobian
-d BRF / d log r_eff by reverse-mode autograd through the surrogate's
-torch.autograd.Function (one backward pass per output bin, batched by
-replicating each config once per bin).  Retrievals whose ensemble spread at the
+find r_eff.  Each iteration evaluates the ensemble and the Jacobian
+d BRF / d log r_eff in forward mode through the surrogate's tensor-core kernels
+(`surrogate.forward_tangent`: the input is one scalar, so one tangent pass replaces a
+backward pass per output bin).  Retrievals whose ensemble spread at the
 solution exceeds ``spread_tol`` fall back to plain Monte Carlo: the same
 Gauss-Newton iteration with BRFs and central-difference Jacobians from the GPU
 walk.  The reference has no inverse; this consumes the same BRF definition
@@ -20,31 +20,33 @@ from . import surrogate as S
 LOG_R = (math.log(S.R_RANGE[0]), math.log(S.R_RANGE[1]))
 
 
-def _brf_and_jacobian(ens, s, known, chunk=96):
-    """Ensemble-mean BRF [n, 648] and d BRF / d log r [n, 648] at log r = s."""
+def _brf_and_jacobian(ens, s, known, chunk=65536):
+    """Ensemble-mean BRF [n, 648] and d BRF / d log r [n, 648] at log r = s: one
+    forward-mode pass per member through the tensor-core kernels (the tangent of the
+    first input, d x0 / d log r = 2 / (log r_max - log r_min)), then the chain rule
+    through the target standardisation, exp and the albedo factor."""
     import torch
     n = s.shape[0]
     f_out = np.zeros((n, S.N_BRF))
     j_out = np.zeros((n, S.N_BRF))
     dxds = 2.0 / (LOG_R[1] - LOG_R[0])
-    eye = torch.eye(S.N_BRF, device='cuda', dtype=torch.float64)
     for lo in range(0, n, chunk):
         hi = min(n, lo + chunk)
-        rows = hi - lo
         x = torch.from_numpy(S.encode(np.exp(s[lo:hi]), known[lo:hi, 0], known[lo:hi, 1],
                                       known[lo:hi, 2])).cuda()
-        # each config once per output bin: row (c, b) back-propagates bin b of config c
-        xr = x.repeat_interleave(S.N_BRF, dim=0).requires_grad_(True)
-        f_acc = torch.zeros((rows, S.N_BRF), dtype=torch.float64, device='cuda')
-        j_acc = torch.zeros((rows, S.N_BRF), dtype=torch.float64, device='cuda')
+        xdot = torch.zeros_like(x)
+        xdot[:, 0] = dxds
+        x16, xdot16 = S._cast(torch, x), S._cast(torch, xdot)
+        f_acc = torch.zeros((hi - lo, S.N_BRF), dtype=torch.float64, device='cuda')
+        j_acc = torch.zeros_like(f_acc)
         for m in ens.members:
-            y = S.mlp_apply(xr, m.params).double() * m.y_std + m.y_mean
-            alb = torch.exp(y[:, S.N_BRF])
-            brf = (torch.exp(y[:, :S.N_BRF]) - S.BRF_FLOOR) * alb[:, None]
-            sel = (brf.view(rows, S.N_BRF, S.N_BRF) * eye).sum(-1)        # [rows, bins]
-            g, = torch.autograd.grad(sel.sum(), xr)
-            f_acc += sel.detach()
-            j_acc += g[:, 0].view(rows, S.N_BRF).double() * dxds
+            y, ydot = S.forward_tangent(torch, x16, xdot16, m.w16, m.params[1::2])
+            yp = y.double() * m.y_std + m.y_mean                  # log(BRF / albedo + floor), log(albedo)
+            dp = ydot.double() * m.y_std
+            alb = torch.exp(yp[:, S.N_BRF])
+            shape = torch.exp(yp[:, :S.N_BRF])
+            f_acc += (shape - S.BRF_FLOOR) * alb[:, None]
+            j_acc += shape * dp[:, :S.N_BRF] * alb[:, None] + (shape - S.BRF_FLOOR) * (alb * dp[:, S.N_BRF])[:, None]
         f_out[lo:hi] = (f_acc / len(ens.members)).cpu().numpy()
         j_out[lo:hi] = (j_acc / len(ens.members)).cpu().numpy()
     return f_out, j_out
@@ -93,6 +95,20 @@ def mc_gn(walker, obs, known, s0, n_photon=1000000, iters=3, h=0.05, seed=0x5EED
         f, fp, fm = brf[:n], brf[n:2 * n], brf[2 * n:]
         s = _gn_update(f, (fp - fm) / (2 * h), obs, s, w)
     return s, evals
+
+
+def mc_retrieve(walker, obs, known, grid=16, iters=4, n_photon=1000000, seed=0x5EED0077):
+    """The same retrieval with plain Monte Carlo only: the 16-point log r_eff grid and the
+    Gauss-Newton iterations evaluated by the walk.  Returns (s, BRF evaluations)."""
+    n = obs.shape[0]
+    w = S.bin_weights()[None, :]
+    g = np.linspace(LOG_R[0], LOG_R[1], grid)
+    rows = np.concatenate([np.column_stack([np.full(n, math.exp(v)), known]) for v in g])
+    brf, _ = S.mc_brf(walker, rows, n_photon, seed)
+    cost = np.stack([(w * (brf[k * n:(k + 1) * n] - obs) ** 2).sum(1) for k in range(grid)])
+    s0 = g[np.argmin(cost, axis=0)]
+    s, evals = mc_gn(walker, obs, known, s0, n_photon=n_photon, iters=iters, seed=seed + 1)
+    return s, evals + rows.shape[0]
 
 
 def retrieve(ens, walker, obs, known, spread_tol=0.02, mc_photons=1000000):

@@ -26,7 +26,7 @@ from . import _abi
 DIMS = (4, 256, 256, 256, 649)
 N_BRF = 648
 BRF_FLOOR = 0.02
-# training hull (BASELINE surrogate configuration)
+# training hull: the parameter ranges the surrogate is trained and judged on
 R_RANGE = (50.0, 1500.0)      # r_eff [um], log-uniform
 WVL_RANGE = (0.9, 1.8)        # centre wavelength [um]
 MU_RANGE = (0.3, 1.0)         # cos theta0
@@ -184,6 +184,26 @@ def backward_cached(torch, gy, w16, cache, need_dx=True):
         _gemm(torch, _abi.EPI_DSILU, m, k_in, n_out, g16, n_out, w16[layer], k_in, g16_prev, k_in,
               trans_b=1, aux=zs[layer - 1], ldaux=k_in, c2=g32_prev, ldc2=k_in)
         g16, g32 = g16_prev, g32_prev
+
+
+def forward_tangent(torch, x16, xdot16, w16, biases):
+    """Network outputs and their directional derivative along the input tangent xdot,
+    in one forward pass on the tensor-core kernels (forward mode: 4 more GEMMs, not one
+    backward pass per output).  x16, xdot16 bf16 [n, 4]; returns (y, ydot) fp32 [n, 649].
+    Per layer: hdot_l = (hdot_{l-1} W_l^T) * silu'(z_l), the SiLU' epilogue of the backward
+    GEMMs with the pre-activations z_l of the forward pass; ydot = hdot_3 W_4^T."""
+    y, (zs, _) = forward_cached(torch, x16, w16, biases, keep=True)
+    m = x16.shape[0]
+    t = xdot16
+    for layer in range(3):
+        n, k = w16[layer].shape
+        nxt = torch.empty((m, n), dtype=torch.bfloat16, device=x16.device)
+        _gemm(torch, _abi.EPI_DSILU, m, n, k, t, k, w16[layer], k, nxt, n, aux=zs[layer], ldaux=n)
+        t = nxt
+    n, k = w16[3].shape
+    ydot = torch.empty((m, n), dtype=torch.float32, device=x16.device)
+    _gemm(torch, _abi.EPI_F32, m, n, k, t, k, w16[3], k, ydot, n)
+    return y, ydot
 
 
 def _mlp_function():

@@ -237,3 +237,21 @@ def test_fused_forward_leading_dimension_and_repack():
     torch.cuda.synchronize()
     assert not torch.equal(before, after)
     assert (after - y_layer).abs().max().item() < 5e-3 * y_layer.abs().max().item()
+
+
+def test_forward_tangent_matches_cpu_jvp():
+    """surrogate.forward_tangent (forward mode on the kernels: SiLU' epilogue GEMMs) against
+    float64 CPU forward-mode autograd of the same bf16-rounded network."""
+    net = _random_net(21)
+    g = torch.Generator().manual_seed(5)
+    x = torch.rand(300, 4, generator=g) * 2 - 1
+    xdot = torch.zeros_like(x)
+    xdot[:, 0] = 0.57
+    y, ydot = surrogate.forward_tangent(torch, surrogate._cast(torch, x.cuda()), surrogate._cast(torch, xdot.cuda()),
+                                        net.w16, net.params[1::2])
+    params = [p.detach().cpu().double() for p in net.params]
+    _, ref = torch.autograd.functional.jvp(lambda v: _reference_mlp(v, params), x.double(), xdot.double())
+    ydot = ydot.cpu().double()
+    rel = (ydot - ref).norm(dim=1) / ref.norm(dim=1)
+    assert torch.isfinite(ydot).all()
+    assert rel.median().item() < 0.02 and rel.max().item() < 0.08, (rel.median().item(), rel.max().item())
