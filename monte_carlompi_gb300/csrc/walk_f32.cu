@@ -186,8 +186,10 @@ __device__ __forceinline__ void pop(Photon &P, const BirthSlot &b) {
     P.tau = o.tau;
     P.R = o.R;
     P.inv_ext = o.inv_ext;
-    P.coalb_ice = o.coalb_ice;
-    P.coalb_imp = o.coalb_imp;
+    // on a Lambertian surface every step's absorption test uses 1 - R (:1455-1466)
+    const bool lam_surface = (o.flags & kFlagLamSurface) != 0;
+    P.coalb_ice = lam_surface ? 1.f - o.R : o.coalb_ice;
+    P.coalb_imp = lam_surface ? 1.f - o.R : o.coalb_imp;
     P.p_imp = o.p_imp;
     P.hg_a = o.hg_a;
     P.hg_b = o.hg_b;
@@ -218,7 +220,7 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     // Lambertian cos = sqrt(u) after a bottom reflection
     const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
     float ct = (P.hg_d != 0.f) ? P.hg_e * (P.hg_a - t * t) : fmaf(-2.f, u1, 1.f);
-    ct = lamb ? sqrtf(u1) : ct;
+    if (lamb) ct = sqrtf(u1);                                   // rare: a branch, not a select
     const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
     float sp, cp;
     __sincosf(kTwoPiF * (u2 - 0.5f), &sp, &cp);
@@ -237,12 +239,16 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
         const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
         gx *= inv; gy *= inv; gz *= inv;
     }
-    // pole (monte_carlo3D.py:1262-1269), taken for |mu_z| > 0.99999
-    const float sg = copysignf(1.f, mz);
-    const bool pole = fabsf(mz) > 0.99999f;
-    const float nx = first ? mx : (pole ? st * cp : gx);
-    const float ny = first ? my : (pole ? sg * st * sp : gy);
-    const float nz = first ? mz : (pole ? sg * ct : gz);
+    // pole (monte_carlo3D.py:1262-1269), taken for |mu_z| > 0.99999 (rare: a branch)
+    if (fabsf(mz) > 0.99999f) {
+        const float sg = copysignf(1.f, mz);
+        gx = st * cp;
+        gy = sg * st * sp;
+        gz = sg * ct;
+    }
+    const float nx = first ? mx : gx;
+    const float ny = first ? my : gy;
+    const float nz = first ? mz : gz;
 
     const float z0 = P.z;
     float zn = fmaf(dtau, nz, z0);
@@ -262,7 +268,7 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
                                              (uint32_t)(P.rid >> 32)), a.keys);
         imp = ((float)r2.x * kTwo32Inv) < P.p_imp;
     }
-    const float coalb = lam_surface ? 1.f - P.R : (imp ? P.coalb_imp : P.coalb_ice);
+    const float coalb = imp ? P.coalb_imp : P.coalb_ice;       // 1 - R on a Lambertian surface
 
     const bool top = zn > 0.f;                                  // :1390-1397
     const bool bot = zn < -P.tau;                               // :1399-1459
@@ -474,14 +480,16 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
                 const bool alive = cond == 0;
                 Photon Q = P;
                 const int c = step<kImpurity>(Q, a, rb[k], k == kStepsPerRound - 1);
+                // a finished photon's record uses i, the direction and the path only;
+                // its z, flags and path compensation are never read again
                 P.i = alive ? Q.i : P.i;
-                P.flags = alive ? Q.flags : P.flags;
                 P.mux = alive ? Q.mux : P.mux;
                 P.muy = alive ? Q.muy : P.muy;
                 P.muz = alive ? Q.muz : P.muz;
-                P.z = alive ? Q.z : P.z;
                 P.path = alive ? Q.path : P.path;
-                P.pathc = alive ? Q.pathc : P.pathc;
+                P.flags = Q.flags;
+                P.z = Q.z;
+                P.pathc = Q.pathc;
                 cond = alive ? c : cond;
             }
         }

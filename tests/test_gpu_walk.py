@@ -149,6 +149,22 @@ def test_f32_same_records_for_any_launch_shape(walker):
     assert np.array_equal(a.tallies, b.tallies) and np.array_equal(a.tallies, c.tallies)
 
 
+@pytest.mark.parametrize('case', ['cfg2', 'imp', 'lamsurf'])
+def test_f32_records_independent_of_photon_count(walker, case):
+    """Photon p's record depends only on (seed, config, p): a 300-photon launch, whose
+    warps walk mostly with few active lanes (steps precomputed on the idle lanes), gives
+    the first 300 records of a 100,000-photon launch (mostly full warps) bit for bit;
+    with impurities (species draw) and a Lambertian surface too."""
+    if case == 'cfg2':
+        cfg, ice, imp = cfg2_geometry(100000)
+    else:
+        cfg, ice, imp = _golden_case(case, 100000)
+    walker.set_tables([ice], imp)
+    big = walker.walk([cfg], 91, mode='f32')
+    small = walker.walk([dataclasses.replace(cfg, n_photon=300)], 91, mode='f32')
+    assert np.array_equal(small.records, big.records[:300])
+
+
 def test_f32_tallies_agree_with_records(walker):
     cfg, ice, imp = cfg2_geometry(300000, depth=0.02, rds=1500.0)
     walker.set_tables([ice], imp)
