@@ -149,7 +149,9 @@ typedef struct {
     int32_t block_size;    /* threads per block, multiple of 32, 32..1024 */
     int32_t blocks_per_sm; /* resident blocks per SM to launch (0 = occupancy maximum) */
     int32_t regen_chunk;   /* refill a warp once this many lanes are idle (1..32) */
-    int32_t reserved;
+    int32_t drain_below;   /* once every photon has started, a warp with at most this many
+                              walking photons hands them to a queue served by whole warps,
+                              one photon each (0..32; 0 = never; default 4) */
 } mcw_launch;
 
 /* Library identity.  No reference counterpart. */

@@ -78,7 +78,10 @@ struct Plan {
 struct Counters {
     unsigned long long work;
     unsigned int status;
-    unsigned int pad;
+    unsigned int drain_count;   // drain-queue slots reserved
+    unsigned int drain_next;    // next drain ticket
+    unsigned int warps_done;    // walk warps past their photon loop
+    unsigned int pad[3];
 };
 
 }  // namespace
@@ -95,24 +98,25 @@ struct mcw_ctx {
     int32_t n_ice = 0;
     bool have_tables = false;
     // workspace
-    DevBuf cfgs, lut, tallies, counters, records, post;
+    DevBuf cfgs, lut, tallies, counters, records, post, drain;
     HostBuf h_stage, h_tallies, h_counters;
     int32_t max_ice_n = 0;
-    mcw_launch launch{256, 0, 8, 0};
+    mcw_launch launch{256, 0, 8, 4};
     double budget_s = 300.0;
+    uint32_t epoch = 0;   // drain-queue epoch of the last launch
 };
 
 struct mcw_graph {
     mcw_ctx *ctx = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaGraphNode_t walk_node = nullptr;
-    cudaKernelNodeParams walk_params{};
+    std::vector<cudaGraphNode_t> walk_nodes;         // the walk and drain kernels (seeded per launch)
+    std::vector<cudaKernelNodeParams> walk_params;
     WalkArgs args{};
     int32_t n_cfg = 0;
     int64_t total = 0;
     int grid = 0, block = 0;
-    DevBuf cfgs, lut, tallies, counters;
+    DevBuf cfgs, lut, tallies, counters, drain;
     HostBuf h_tallies, h_counters;
 };
 
@@ -293,7 +297,7 @@ LutArgs lut_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut
 
 WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &tallies,
                    DevBuf &counters, mcw_record32 *records, int chunk, uint64_t seed) {
-    WalkArgs wa;
+    WalkArgs wa{};
     wa.cfgs = (const DevConfig *)cfgs.p;
     wa.prefix = (const int64_t *)((const char *)cfgs.p + prefix_offset(plan.cfgs.size()));
     wa.lut = (const LutEntry *)lut.p;
@@ -307,7 +311,32 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &l
     wa.tallies = (mcw_tally *)tallies.p;
     wa.budget_ns = (unsigned long long)(ctx->budget_s * 1e9);
     wa.keys = philox_schedule(seed);
+    wa.drain_count = &cn->drain_count;
+    wa.drain_next = &cn->drain_next;
+    wa.warps_done = &cn->warps_done;
     return wa;
+}
+
+// A fresh epoch for the drain queue of one launch (never 0, the mark of a taken slot).
+uint32_t next_epoch(mcw_ctx *ctx) {
+    if (++ctx->epoch == 0) ++ctx->epoch;
+    return ctx->epoch;
+}
+
+// Attach the drain queue (one slot per thread of the walk grid) when handover is on.
+int attach_drain(mcw_ctx *ctx, WalkArgs &wa, DevBuf &drain, const Shape &shape) {
+    wa.drain = nullptr;
+    wa.drain_below = 0;
+    if (ctx->launch.drain_below <= 0) return MCW_OK;
+    void *old = drain.p;
+    CUDA_TRY(ctx, drain.ensure((size_t)shape.grid * shape.block * kDrainSlot * sizeof(float4)));
+    // slots are recognised by their epoch word: a new buffer starts cleared
+    if (drain.p != old) CUDA_TRY(ctx, cudaMemsetAsync(drain.p, 0, drain.cap, ctx->stream));
+    wa.drain = (float4 *)drain.p;
+    wa.drain_cap = (uint32_t)((size_t)shape.grid * shape.block);
+    wa.drain_below = ctx->launch.drain_below;
+    wa.epoch = next_epoch(ctx);
+    return MCW_OK;
 }
 
 }  // namespace
@@ -353,7 +382,7 @@ int mcw_destroy(mcw_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (DevBuf *b : {&ctx->tabdata, &ctx->ice_tables, &ctx->cfgs, &ctx->lut, &ctx->tallies, &ctx->counters,
-                      &ctx->records, &ctx->post})
+                      &ctx->records, &ctx->post, &ctx->drain})
         b->release();
     ctx->h_stage.release();
     ctx->h_tallies.release();
@@ -460,6 +489,7 @@ int mcw_set_launch(mcw_ctx *ctx, const mcw_launch *l) {
         return set_err(ctx, MCW_ERR_ARG, "block_size must be a multiple of 32 in [32, 256]");
     if (l->blocks_per_sm < 0 || l->blocks_per_sm > 64) return set_err(ctx, MCW_ERR_ARG, "blocks_per_sm must be in [0, 64]");
     if (l->regen_chunk < 1 || l->regen_chunk > 32) return set_err(ctx, MCW_ERR_ARG, "regen_chunk must be in [1, 32]");
+    if (l->drain_below < 0 || l->drain_below > 32) return set_err(ctx, MCW_ERR_ARG, "drain_below must be in [0, 32]");
     ctx->launch = *l;
     return MCW_OK;
 }
@@ -510,8 +540,11 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         shape = pick_shape(ctx, ctx->launch, plan);
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
+        rc = attach_drain(ctx, wa, ctx->drain, shape);
+        if (rc) return rc;
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
-        if (plan.total > 0) CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, st));
+        if (plan.total > 0)
+            CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, ctx->sm_count, st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
     } else {
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->tallies.p, 0, n_cfg * sizeof(mcw_tally), st));
@@ -652,7 +685,7 @@ int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t s
         for (int bi = 0; bi < 2; ++bi) {
             if (bi == 1 && bps_opts[1] == bps_opts[0]) continue;
             for (int ch : chunks) {
-                mcw_launch l{b, bps_opts[bi], ch, 0};
+                mcw_launch l{b, bps_opts[bi], ch, saved.drain_below};
                 ctx->launch = l;
                 mcw_stats s;
                 double t = 0;
@@ -707,11 +740,14 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     g->grid = shape.grid;
     g->block = shape.block;
     g->args = walk_args(ctx, plan, g->cfgs, g->lut, g->tallies, g->counters, device_records, shape.chunk, 0);
+    rc = attach_drain(ctx, g->args, g->drain, shape);
+    if (rc) return fail(rc);
     const LutArgs la = lut_args(ctx, plan, g->cfgs, g->lut, g->tallies, g->counters);
     if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_CUDA, "stream capture failed to start"));
     cudaError_t e = launch_lut(la, st);  // clears counters and tallies too
-    if (e == cudaSuccess && plan.total > 0) e = launch_walk_f32(g->args, plan.impurity, g->grid, g->block, st);
+    if (e == cudaSuccess && plan.total > 0)
+        e = launch_walk_f32(g->args, plan.impurity, g->grid, g->block, ctx->sm_count, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(g->h_tallies.p, g->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->h_counters.p, g->counters.p, sizeof(Counters), cudaMemcpyDeviceToHost, st);
@@ -729,11 +765,11 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
         cudaKernelNodeParams p;
         if (cudaGraphKernelNodeGetParams(nd, &p) != cudaSuccess) continue;
         if (walk_f32_is_kernel(p.func)) {
-            g->walk_node = nd;
-            g->walk_params = p;
+            g->walk_nodes.push_back(nd);
+            g->walk_params.push_back(p);
         }
     }
-    if (plan.total > 0 && !g->walk_node) return fail(set_err(ctx, MCW_ERR_CUDA, "walk node not found in graph"));
+    if (plan.total > 0 && g->walk_nodes.empty()) return fail(set_err(ctx, MCW_ERR_CUDA, "walk node not found in graph"));
     if (cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess)
         return fail(set_err(ctx, MCW_ERR_CUDA, "graph instantiation failed"));
     *out = g;
@@ -746,13 +782,14 @@ int mcw_graph_launch(mcw_graph *g, uint64_t seed, mcw_tally *tallies, mcw_stats 
     const auto t_start = std::chrono::steady_clock::now();
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    if (g->walk_node) {
-        g->args.keys = philox_schedule(seed);
+    g->args.keys = philox_schedule(seed);
+    if (g->args.drain) g->args.epoch = next_epoch(ctx);
+    for (size_t i = 0; i < g->walk_nodes.size(); ++i) {
         void *kp[1] = {&g->args};
-        cudaKernelNodeParams p = g->walk_params;
+        cudaKernelNodeParams p = g->walk_params[i];
         p.kernelParams = kp;
         p.extra = nullptr;
-        CUDA_TRY(ctx, cudaGraphExecKernelNodeSetParams(g->exec, g->walk_node, &p));
+        CUDA_TRY(ctx, cudaGraphExecKernelNodeSetParams(g->exec, g->walk_nodes[i], &p));
     }
     CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
     CUDA_TRY(ctx, cudaGraphLaunch(g->exec, st));
@@ -790,7 +827,7 @@ int mcw_graph_destroy(mcw_graph *g) {
     }
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
-    for (DevBuf *b : {&g->cfgs, &g->lut, &g->tallies, &g->counters}) b->release();
+    for (DevBuf *b : {&g->cfgs, &g->lut, &g->tallies, &g->counters, &g->drain}) b->release();
     g->h_tallies.release();
     g->h_counters.release();
     delete g;

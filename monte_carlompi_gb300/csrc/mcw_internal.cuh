@@ -92,6 +92,19 @@ struct WalkArgs {
     mcw_tally *tallies;          // n_cfg device tallies
     unsigned long long budget_ns;
     PhiloxKeys keys;
+    // drain handover: once the photon supply is exhausted, a warp with at most
+    // drain_below active lanes writes its photons to drain (kDrainSlot float4
+    // each; the last word of a slot is `epoch`, written after the rest) and then
+    // walks handed-over photons with the whole warp; the drain kernel after the
+    // walk takes any left.  drain == null or drain_below == 0: no handover.
+    float4 *drain;
+    unsigned int *drain_count;   // slots reserved
+    unsigned int *drain_next;    // next ticket
+    unsigned int *warps_done;    // warps of the walk grid past their photon loop
+    int32_t drain_below;
+    uint32_t epoch;              // differs between launches, never 0 (0 marks a taken slot)
+    uint32_t drain_cap;          // slots in drain (grid * block)
+    uint32_t drain_pad;
 };
 
 struct ReplayArgs {
@@ -129,10 +142,15 @@ const char *config_problem(const mcw_config &c, int32_t n_ice);
 cudaError_t launch_post(const void *recs, bool f64, int64_t n, int n_cfg, int n_bins, unsigned long long *bins_fx,
                         unsigned int *bins_cnt, mcw_post_stats *stats, int sms, cudaStream_t s);
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
-// impurity: some config has imp_cnc > 0 (the kernel instance with the species draw)
-cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, cudaStream_t s);
+// Photons the walk hands over to its drain queue are packed as this many float4.
+constexpr int kDrainSlot = 6;
+// impurity: some config has imp_cnc > 0 (the kernel instance with the species draw).
+// Launches the walk and, when a.drain_below > 0, the drain kernel after it
+// (sm_count SMs; a.drain must then hold grid * block slots).
+cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s);
 cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);
 int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity);
+// The walk and drain kernels (their one parameter is a WalkArgs).
 bool walk_f32_is_kernel(const void *fn);
 size_t walk_f32_smem_bytes(int block, int n_cfg);
 

@@ -177,7 +177,7 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     la.counters = nullptr;
     if (launch_lut(la, st) != cudaSuccess) return MCW_ERR_CUDA;
     if (c.n_photon > 0) {
-        WalkArgs wa;
+        WalkArgs wa{};   // no drain handover: its queue would need an allocation
         wa.cfgs = &s->cfg;
         wa.prefix = s->prefix;
         wa.lut = s->lut;
@@ -198,7 +198,7 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
         int64_t grid = (int64_t)sms * bps;
         const int64_t needed = (c.n_photon + 255) / 256;
         if (grid > needed) grid = needed;
-        if (launch_walk_f32(wa, impurity, (int)grid, 256, st) != cudaSuccess) return MCW_ERR_CUDA;
+        if (launch_walk_f32(wa, impurity, (int)grid, 256, sms, st) != cudaSuccess) return MCW_ERR_CUDA;
     }
     NoAllocCounters h;
     if (cudaMemcpyAsync(&h, &s->counters, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess) return MCW_ERR_CUDA;

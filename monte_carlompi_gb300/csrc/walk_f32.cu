@@ -12,6 +12,21 @@
 //    finish queue; once 32 are queued the warp computes theta_n / phi_n,
 //    writes the 32 records and folds the tallies with warp reductions.
 //
+// The end of a launch: once the photon supply is exhausted, the warps empty
+// out and the last, longest walks would run with a few lanes of a warp each,
+// bound by the latency of one photon's step chain.  A warp that is down to
+// WalkArgs::drain_below photons hands them over (their state packed into a
+// device queue) and then serves the queue: it walks one handed-over photon at a
+// time with the whole warp.  The 32 lanes compute the direction-independent part
+// of the photon's next 32 steps at once (Philox block, HG and Lambertian angles,
+// azimuth, optical path) and the step chain that remains (rotation, move,
+// boundaries) runs without the per-round work of the main loop.  A warp leaves
+// once every warp is past its photon loop and no slot is left for it, or after
+// kDrainIdleNs without its slot arriving; the drain kernel launched after the
+// walk takes whatever is left, so no warp ever waits on one that may not run.
+// The arithmetic of a step is the same on both paths, so records do not depend
+// on where a photon ends its walk.
+//
 // Per step (monte_carloMPI/monte_carlo3D.py:1212-1466, HG branch) one
 // Philox4x32-10 block keyed by (step, photon) supplies the four uniforms the
 // step needs: HG cosine (:915), azimuth (:921), optical path (:1014) and the
@@ -31,6 +46,8 @@
 //  * phi_n = atan2(mu_y, mu_x) mapped to [0, 2 pi) (the quadrant arctan of
 //    :1472-1485, defined on the axes too).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 
 #include "mcw_internal.cuh"
 #include "tally.cuh"
@@ -91,6 +108,31 @@ struct Photon {
     float hg_a, hg_b, hg_c, hg_d, hg_e;  // 1+g^2, 1-g^2, 1-g, 2g, 1/(2g); hg_d == 0: isotropic
 };
 
+// A photon handed to the drain queue: kDrainSlot = 6 float4 (.w of the last: epoch).
+__device__ __forceinline__ void pack_photon(float4 *d, const Photon &P) {
+    d[0] = make_float4(__uint_as_float((uint32_t)P.rid), __uint_as_float((uint32_t)(P.rid >> 32)),
+                       __int_as_float(P.cfg), __int_as_float(P.lut));
+    d[1] = make_float4(__int_as_float(P.i), __uint_as_float(P.flags), P.mux, P.muy);
+    d[2] = make_float4(P.muz, P.z, P.path, P.pathc);
+    d[3] = make_float4(P.tau, P.R, P.inv_ext, P.coalb_ice);
+    d[4] = make_float4(P.coalb_imp, P.p_imp, P.hg_a, P.hg_b);
+    d[5] = make_float4(P.hg_c, P.hg_d, P.hg_e, 0.f);
+}
+
+__device__ __forceinline__ void unpack_photon(Photon &P, const float4 *d) {
+    const float4 a = d[0], b = d[1], c = d[2], e = d[3], f = d[4], g = d[5];
+    P.rid = ((uint64_t)__float_as_uint(a.y) << 32) | __float_as_uint(a.x);
+    P.cfg = __float_as_int(a.z);
+    P.lut = __float_as_int(a.w);
+    P.i = __float_as_int(b.x);
+    P.flags = __float_as_uint(b.y);
+    P.mux = b.z, P.muy = b.w;
+    P.muz = c.x, P.z = c.y, P.path = c.z, P.pathc = c.w;
+    P.tau = e.x, P.R = e.y, P.inv_ext = e.z, P.coalb_ice = e.w;
+    P.coalb_imp = f.x, P.p_imp = f.y, P.hg_a = f.z, P.hg_b = f.w;
+    P.hg_c = g.x, P.hg_d = g.y, P.hg_e = g.z;
+}
+
 // A born photon waiting in the queue: 20 words = 5 x float4.
 struct __align__(16) BirthSlot {
     uint32_t rid_lo, rid_hi, cfg, lut;
@@ -113,7 +155,10 @@ struct WarpQueues {
     BirthSlot birth[32];
     FinishSlot fin[kFinishCap];
     uint4 rmeta[32];                          // (stream id lo, hi, step) by active rank
-    uint4 rbuf[32][kStepsPerRound + 1];       // step blocks by active rank (padded row)
+    union {
+        uint4 rbuf[32][kStepsPerRound + 1];   // step blocks by active rank (padded row)
+        float4 pbuf[2 * 32];                  // drain: a photon's next 32 steps (StepPre)
+    };
     WarpTally tally;
 };
 
@@ -290,6 +335,95 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     return cond;
 }
 
+// The same scatter event as step(), split for the drain path: the part that does
+// not depend on the photon's direction or position (everything drawn from the
+// step's Philox block and the photon's phase-function constants), computed for 32
+// steps at once on the 32 lanes of a warp, and the chain that does.  Every value is
+// the same function of the same inputs as in step(): st is sqrt(1 - ct^2) of the
+// selected cosine whichever way the selection is made.
+struct StepPre {
+    float ct_hg, st_hg;   // HG scattering cosine (monte_carlo3D.py:915), or 1 - 2u if isotropic
+    float ct_l, st_l;     // Lambertian direction after a reflection, cos = sqrt(u)
+    float sp, cp;         // azimuth (:921), uniform on (-pi, pi)
+    float dtau;           // optical path -ln u (:1014)
+    float u4;             // absorption draw (:1020), or the bottom reflectance draw
+};
+
+__device__ __forceinline__ StepPre step_pre(const uint4 r, const Photon &P) {
+    StepPre o;
+    const float u1 = u01_f32(r.x);
+    const float u2 = u01_f32(r.y);
+    const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
+    o.dtau = -__logf(u3);
+    const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
+    o.ct_hg = (P.hg_d != 0.f) ? P.hg_e * (P.hg_a - t * t) : fmaf(-2.f, u1, 1.f);
+    o.st_hg = sqrtf(fmaxf(0.f, fmaf(-o.ct_hg, o.ct_hg, 1.f)));
+    o.ct_l = sqrtf(u1);
+    o.st_l = sqrtf(fmaxf(0.f, fmaf(-o.ct_l, o.ct_l, 1.f)));
+    __sincosf(kTwoPiF * (u2 - 0.5f), &o.sp, &o.cp);
+    o.u4 = (float)r.w * kTwo32Inv;
+    return o;
+}
+
+// Ice or impurity for step n (monte_carlo3D.py:1023, :1375-1383), as in step().
+__device__ __forceinline__ bool impurity_draw(uint64_t rid, uint32_t n, float p_imp, const WalkArgs &a) {
+    const uint4 r2 = philox10(make_uint4(n, kTagSpecies, (uint32_t)rid, (uint32_t)(rid >> 32)), a.keys);
+    return ((float)r2.x * kTwo32Inv) < p_imp;
+}
+
+__device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool imp, const bool renorm) {
+    P.i += 1;
+    const bool first = (P.i == 1);
+    const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
+    const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
+    const float dtau = (first && lam_surface) ? 0.f : s.dtau;
+    const float ct = lamb ? s.ct_l : s.ct_hg;
+    const float st = lamb ? s.st_l : s.st_hg;
+    const float sp = s.sp, cp = s.cp;
+    const float mx = lamb ? 0.f : P.mux;
+    const float my = lamb ? 0.f : P.muy;
+    const float mz = lamb ? 1.f : P.muz;
+    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
+    const float rs = rsqrtf(s2);
+    const float tq = st * rs;
+    float gx = fmaf(tq, mx * mz * cp - my * sp, mx * ct);
+    float gy = fmaf(tq, my * mz * cp + mx * sp, my * ct);
+    float gz = fmaf(-(s2 * rs) * st, cp, mz * ct);
+    if (renorm) {
+        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
+        gx *= inv; gy *= inv; gz *= inv;
+    }
+    const float sg = copysignf(1.f, mz);
+    const bool pole = fabsf(mz) > 0.99999f;
+    const float nx = first ? mx : (pole ? st * cp : gx);
+    const float ny = first ? my : (pole ? sg * st * sp : gy);
+    const float nz = first ? mz : (pole ? sg * ct : gz);
+    const float z0 = P.z;
+    float zn = fmaf(dtau, nz, z0);
+    const float inc = dtau * P.inv_ext;
+    {
+        const float y = inc - P.pathc;
+        const float tt = P.path + y;
+        P.pathc = (tt - P.path) - y;
+        P.path = tt;
+    }
+    const float coalb = imp ? P.coalb_imp : P.coalb_ice;       // 1 - R on a Lambertian surface
+    const bool top = zn > 0.f;
+    const bool bot = zn < -P.tau;
+    const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
+    if (top || bot) P.path -= frac * inc;
+    zn = bot ? -P.tau : zn;
+    const bool refl = bot && (P.flags & kFlagLamBottom) && s.u4 < P.R;
+    P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
+    const bool absorb = s.u4 < coalb;
+    const int cond = top ? 1 : (bot ? (refl ? 0 : (first ? 3 : 2)) : (absorb ? (imp ? 5 : 4) : 0));
+    P.mux = nx;
+    P.muy = ny;
+    P.muz = nz;
+    P.z = zn;
+    return cond;
+}
+
 // Exact warp sum of 64-bit values below 2^47.
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
     const unsigned lo = __reduce_add_sync(0xffffffffu, (unsigned)(v & 0xffffu));
@@ -301,15 +435,15 @@ __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v)
 // Epilogue of up to 32 finished photons (entries [base, base + n) of the
 // finish queue): records, histogram bins and the warp's running totals.
 // Warp-collective.
-__device__ __noinline__ void finish_batch(WarpQueues &q, int base, int n, const WalkArgs &a,
-                                          const CfgF32 *scfg, const int64_t *prefix, bool staged,
-                                          int lane) {
+__device__ __noinline__ void finish_batch(const FinishSlot *fin, WarpTally &tally, int base, int n,
+                                          const WalkArgs &a, const CfgF32 *scfg, const int64_t *prefix,
+                                          bool staged, int lane) {
     const bool have = lane < n;
     int cfg = -1, cond = 0, nscat = 0;
     unsigned long long wfx = 0;
     if (have) {
         FinishSlot f;
-        copy_f4<3>(&f, &q.fin[base + lane]);
+        copy_f4<3>(&f, &fin[base + lane]);
         cfg = (int)f.cfg;
         cond = f.cond;
         nscat = f.n_step - 1;
@@ -340,9 +474,9 @@ __device__ __noinline__ void finish_batch(WarpQueues &q, int base, int n, const 
         const int c = __shfl_sync(0xffffffffu, cfg, __ffs(pending) - 1);
         const bool mine = have && cfg == c;
         pending &= ~__ballot_sync(0xffffffffu, mine);
-        if (q.tally.cfg != c) {
-            warp_tally_flush(q.tally, a.tallies, lane);
-            if (lane == 0) q.tally.cfg = c;
+        if (tally.cfg != c) {
+            warp_tally_flush(tally, a.tallies, lane);
+            if (lane == 0) tally.cfg = c;
             __syncwarp();
         }
         const unsigned ev = __reduce_add_sync(0xffffffffu, mine ? (unsigned)nscat : 0u);
@@ -356,17 +490,20 @@ __device__ __noinline__ void finish_batch(WarpQueues &q, int base, int n, const 
             qs[k] = cnt[k] ? warp_sum_u64(hit ? wfx : 0ull) : 0ull;
         }
         if (lane == 0) {
-            q.tally.n_events += ev;
-            q.tally.max_n_scat = max(q.tally.max_n_scat, mx);
+            tally.n_events += ev;
+            tally.max_n_scat = max(tally.max_n_scat, mx);
 #pragma unroll
             for (int k = 1; k < 6; ++k) {
-                q.tally.n_cond[k] += cnt[k];
-                q.tally.q_cond_fx[k] += qs[k];
+                tally.n_cond[k] += cnt[k];
+                tally.q_cond_fx[k] += qs[k];
             }
         }
         __syncwarp();
     }
 }
+
+__device__ __noinline__ void drain_serve(FinishSlot *fin, WarpTally &tally, float4 *pbuf, int &n_fin,
+                                         const WalkArgs &a, unsigned long long t0, int lane);
 
 template <bool kImpurity>
 __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
@@ -436,6 +573,27 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
             __syncwarp();
         }
         if (idle == 0xffffffffu && exhausted && n_birth == 0) break;
+
+        // ---- drain handover: the supply is exhausted and the warp is nearly empty
+        if (a.drain_below > 0 && exhausted && n_birth == 0 && __popc(~idle) <= a.drain_below) {
+            const unsigned act = ~idle;
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(a.drain_count, (unsigned)__popc(act));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (P.cfg >= 0) {
+                float4 *slot = a.drain + (size_t)(base + __popc(act & lt_mask)) * kDrainSlot;
+                float4 v[kDrainSlot];
+                pack_photon(v, P);
+#pragma unroll
+                for (int k = 0; k < kDrainSlot - 1; ++k) __stcg(&slot[k], v[k]);
+                __threadfence();
+                v[kDrainSlot - 1].w = __uint_as_float(a.epoch);
+                __stcg(&slot[kDrainSlot - 1], v[kDrainSlot - 1]);
+                P.cfg = -1;
+            }
+            idle = 0xffffffffu;
+            break;
+        }
 
         // ---- kStepsPerRound scatter events per active lane; their Philox blocks
         // are independent of the walk, so they are computed together first
@@ -517,7 +675,7 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
             __syncwarp();
             n_fin += __popc(fin_mask);
             if (n_fin >= 32) {
-                finish_batch(q, n_fin - 32, 32, a, scfg, prefix, staged, lane);
+                finish_batch(q.fin, q.tally, n_fin - 32, 32, a, scfg, prefix, staged, lane);
                 n_fin -= 32;
             }
         }
@@ -538,9 +696,165 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
         }
     }
     __syncwarp();
-    if (n_fin > 0) finish_batch(q, 0, n_fin, a, scfg, prefix, staged, lane);
+    if (a.drain_below > 0) {
+        // this warp is past its photon loop; then it serves the drain queue
+        if (lane == 0) {
+            __threadfence();
+            atomicAdd(a.warps_done, 1u);
+        }
+        __syncwarp();
+        drain_serve(q.fin, q.tally, q.pbuf, n_fin, a, t0, lane);
+        __syncwarp();
+    }
+    if (n_fin > 0) finish_batch(q.fin, q.tally, 0, n_fin, a, scfg, prefix, staged, lane);
     warp_tally_flush(q.tally, a.tallies, lane);
 }
+
+constexpr unsigned long long kDrainIdleNs = 2000000ull;  // a serving warp waits at most 2 ms for its slot
+
+// Walk the photon in drain slot `slot` with the whole warp and push it to the
+// warp's finish queue (n_fin entries).  Returns false if the time budget ran out.
+__device__ __forceinline__ bool drain_walk(const float4 *slot, FinishSlot *fin, WarpTally &tally, float4 *pbuf,
+                                           int &n_fin, const WalkArgs &a, unsigned long long t0, int lane) {
+    float4 v[kDrainSlot];
+#pragma unroll
+    for (int k = 0; k < kDrainSlot; ++k) v[k] = __ldcg(&slot[k]);
+    // every lane holds the same photon; the chain below runs on all of them alike
+    Photon P;
+    unpack_photon(P, v);
+    int cond = 0;
+    while (cond == 0) {
+        // direction-independent part of steps P.i + 1 .. P.i + 32, one per lane
+        const uint32_t n = (uint32_t)P.i + 1u + (uint32_t)lane;
+        const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)P.rid, (uint32_t)(P.rid >> 32)), a.keys);
+        const StepPre t = step_pre(r, P);
+        __syncwarp();
+        pbuf[2 * lane] = make_float4(t.ct_hg, t.st_hg, t.ct_l, t.st_l);
+        pbuf[2 * lane + 1] = make_float4(t.sp, t.cp, t.dtau, t.u4);
+        const bool imp_t = (P.flags & kFlagImpurity) && impurity_draw(P.rid, n, P.p_imp, a);
+        const unsigned impm = __ballot_sync(0xffffffffu, imp_t);
+        __syncwarp();
+        // P.i is a multiple of 4 here (photons leave the main loop between rounds),
+        // so every fourth step renormalises, as in the main loop
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+            const float4 x = pbuf[2 * k], y = pbuf[2 * k + 1];
+            StepPre s;
+            s.ct_hg = x.x, s.st_hg = x.y, s.ct_l = x.z, s.st_l = x.w;
+            s.sp = y.x, s.cp = y.y, s.dtau = y.z, s.u4 = y.w;
+            cond = step_post(P, s, (impm >> k) & 1u, (k & 3) == 3);
+            if (cond != 0) break;
+        }
+        int over = 0;
+        if (lane == 0)
+            over = (global_ns() - t0 > a.budget_ns) || (*(volatile unsigned int *)a.status & kStatusBudget);
+        if (__shfl_sync(0xffffffffu, over, 0)) {
+            if (lane == 0) atomicOr(a.status, kStatusBudget);
+            return false;
+        }
+    }
+    if (lane == 0) {
+        FinishSlot f;
+        f.rid_lo = (uint32_t)P.rid;
+        f.rid_hi = (uint32_t)(P.rid >> 32);
+        f.cfg = (uint32_t)P.cfg;
+        f.lut = (uint32_t)P.lut;
+        f.n_step = P.i;
+        f.cond = cond;
+        f.mux = P.mux;
+        f.muy = P.muy;
+        f.muz = P.muz;
+        f.path = P.path;
+        f.pad0 = f.pad1 = 0.f;
+        copy_f4<3>(&fin[n_fin], &f);
+    }
+    __syncwarp();
+    if (++n_fin >= 32) {
+        finish_batch(fin, tally, n_fin - 32, 32, a, nullptr, a.prefix, false, lane);
+        n_fin -= 32;
+    }
+    return true;
+}
+
+// Serve the drain queue from a warp of the walk grid: take a ticket (the next
+// slot), wait for that slot to be written (polling the slot itself, with growing
+// pauses), mark it taken and walk it; repeat.  Leave when every warp of the grid is
+// past its photon loop and no slot is left for the ticket, or after kDrainIdleNs
+// without the slot arriving (the drain kernel then walks it).  Warp-collective.
+__device__ __noinline__ void drain_serve(FinishSlot *fin, WarpTally &tally, float4 *pbuf, int &n_fin,
+                                         const WalkArgs &a, unsigned long long t0, int lane) {
+    const unsigned total_warps = gridDim.x * (blockDim.x >> 5);
+    for (;;) {
+        unsigned j = 0;
+        int go = 0;
+        if (lane == 0) j = atomicAdd(a.drain_next, 1u);
+        // a ticket past the buffer can never be filled: leave without touching memory
+        if (__shfl_sync(0xffffffffu, j, 0) >= a.drain_cap) break;
+        if (lane == 0) {
+            float4 *slot = a.drain + (size_t)j * kDrainSlot;
+            const unsigned long long w0 = global_ns();
+            unsigned pause = 32;
+            for (uint32_t it = 0;; ++it) {
+                if (__float_as_uint(__ldcg(&slot[kDrainSlot - 1]).w) == a.epoch) {
+                    // taken (0 is never an epoch): the drain kernel must not walk it again
+                    float4 last = __ldcg(&slot[kDrainSlot - 1]);
+                    last.w = __uint_as_float(0u);
+                    __stcg(&slot[kDrainSlot - 1], last);
+                    go = 1;
+                    break;
+                }
+                if ((it & 15u) == 0u) {
+                    const unsigned done = *(volatile unsigned int *)a.warps_done;
+                    __threadfence();
+                    if (done >= total_warps && j >= *(volatile unsigned int *)a.drain_count) break;
+                }
+                const unsigned long long now = global_ns();
+                if (now - w0 > kDrainIdleNs) break;
+                if (now - t0 > a.budget_ns || (*(volatile unsigned int *)a.status & kStatusBudget)) {
+                    atomicOr(a.status, kStatusBudget);
+                    break;
+                }
+                __nanosleep(pause);
+                pause = min(pause * 2u, 2048u);
+            }
+        }
+        if (!__shfl_sync(0xffffffffu, go, 0)) break;
+        __threadfence();
+        j = __shfl_sync(0xffffffffu, j, 0);
+        if (!drain_walk(a.drain + (size_t)j * kDrainSlot, fin, tally, pbuf, n_fin, a, t0, lane)) break;
+    }
+}
+
+// Shared memory of one drain-kernel warp.
+struct DrainWarp {
+    FinishSlot fin[32];
+    float4 pbuf[2 * 32];
+    WarpTally tally;
+};
+
+// After the walk: slots written but never taken (normally none; the walk's own
+// warps serve the queue) are walked here.
+__global__ void __launch_bounds__(256) drain_kernel(const WalkArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    DrainWarp &d = reinterpret_cast<DrainWarp *>(smem)[threadIdx.x >> 5];
+    warp_tally_reset(d.tally, lane);
+    __syncwarp();
+    const unsigned cnt = *a.drain_count;
+    const unsigned long long t0 = global_ns();
+    int n_fin = 0;
+    const unsigned nw = gridDim.x * (blockDim.x >> 5);
+    for (unsigned j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < cnt; j += nw) {
+        const float4 *slot = a.drain + (size_t)j * kDrainSlot;
+        if (__float_as_uint(__ldcg(&slot[kDrainSlot - 1]).w) != a.epoch) continue;   // taken, or never written
+        if (!drain_walk(slot, d.fin, d.tally, d.pbuf, n_fin, a, t0, lane)) break;
+    }
+    __syncwarp();
+    if (n_fin > 0) finish_batch(d.fin, d.tally, 0, n_fin, a, nullptr, a.prefix, false, lane);
+    warp_tally_flush(d.tally, a.tallies, lane);
+}
+
+constexpr int kDrainBlock = 256;
 
 size_t smem_bytes(int block, int n_cfg) {
     const size_t cfg = n_cfg <= kSmemCfgMax ? (size_t)n_cfg * (sizeof(CfgF32) + sizeof(int64_t)) : 0;
@@ -569,14 +883,19 @@ int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity) {
 
 bool walk_f32_is_kernel(const void *fn) {
     return fn == reinterpret_cast<const void *>(walk_f32_kernel<false>) ||
-           fn == reinterpret_cast<const void *>(walk_f32_kernel<true>);
+           fn == reinterpret_cast<const void *>(walk_f32_kernel<true>) ||
+           fn == reinterpret_cast<const void *>(drain_kernel);
 }
 
-cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, cudaStream_t s) {
+cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s) {
     cudaError_t e = allow_smem();
     if (e != cudaSuccess) return e;
     if (impurity) walk_f32_kernel<true><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
     else walk_f32_kernel<false><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || a.drain_below <= 0 || !a.drain) return e;
+    // the drain kernel for slots still unwalked (normally none): one block per SM
+    drain_kernel<<<std::max(1, sm_count), kDrainBlock, sizeof(DrainWarp) * (kDrainBlock / 32), s>>>(a);
     return cudaGetLastError();
 }
 

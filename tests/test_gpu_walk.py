@@ -133,15 +133,17 @@ def test_f32_known_answer_slab(walker):
 # ---------------------------------------------------------------- FP32 invariants
 
 def test_f32_same_records_for_any_launch_shape(walker):
+    """Records and tallies do not depend on the launch shape, nor on which photons end
+    their walk in the drain queue (drain_below 0: none; 32: whole warps)."""
     cfg, ice, imp = cfg2_geometry(100000)
     walker.set_tables([ice], imp)
     saved = walker.get_launch()
     try:
-        walker.set_launch(256, 0, 8)
+        walker.set_launch(256, 0, 8, 8)
         a = walker.walk([cfg], 77, mode='f32')
-        walker.set_launch(128, 2, 1)
+        walker.set_launch(128, 2, 1, 0)
         b = walker.walk([cfg], 77, mode='f32')
-        walker.set_launch(64, 1, 32)
+        walker.set_launch(64, 1, 32, 32)
         c = walker.walk([cfg], 77, mode='f32')
     finally:
         walker.set_launch(**saved)
