@@ -90,11 +90,17 @@ int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4,
 
 /* y [m, 649] (f32; y 16-byte aligned, leading dimension ldy >= 652 and a multiple of 4;
  * columns 649 .. ldy - 1 are left untouched) = network(x [m, 4] f32) from the packed
- * weights and the f32 biases (16-byte aligned): one kernel, the hidden activations never
- * leave shared memory.  Inputs and activations are rounded to bf16 as the layer-by-layer
+ * weights and the f32 biases: one kernel, the hidden activations never leave shared
+ * memory.  Inputs and activations are rounded to bf16 as the layer-by-layer
  * mcw_mlp_gemm path rounds them.  A wait that runs out sets bit 1 of mcw_mlp_status. */
 int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
                     const float *b4, const void *blob, float *y, int32_t ldy, void *stream);
+
+/* The same with y rounded to fp16 (11-bit significand, below the bf16 rounding of the
+ * activations): y 16-byte aligned, ldy >= 656 halves and a multiple of 8.  Half the
+ * bytes of the output stream. */
+int mcw_mlp_forward_f16(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
+                        const float *b4, const void *blob, void *y, int32_t ldy, void *stream);
 
 #ifdef __cplusplus
 }

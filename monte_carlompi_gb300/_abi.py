@@ -92,7 +92,7 @@ ENGINE_MMA_SYNC, ENGINE_TCGEN05 = 0, 1
 
 # entry points of include/mcw_mlp.h
 MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16',
-               'mcw_mlp_status', 'mcw_mlp_pack', 'mcw_mlp_forward']
+               'mcw_mlp_status', 'mcw_mlp_pack', 'mcw_mlp_forward', 'mcw_mlp_forward_f16']
 MLP_PACK_BYTES = 5 * 256 * 256 * 2 + 256 * 16 * 2
 
 RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
@@ -160,6 +160,7 @@ def load(path=None):
         'mcw_mlp_status': ([i32, ctypes.POINTER(ctypes.c_uint32)], ctypes.c_int),
         'mcw_mlp_pack': ([vp, vp, vp, vp, vp, vp], ctypes.c_int),
         'mcw_mlp_forward': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
+        'mcw_mlp_forward_f16': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -24,6 +24,7 @@
 // mcw_mlp_status, lets copies and MMAs in flight finish (bounded), frees the tensor
 // memory and leaves.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -73,11 +74,15 @@ constexpr int kRingBytes = kSlots * kChunkBytes;
 constexpr int kStagePitch = 36 * 4;                   // stage row: 32 floats + 16 B pad (no bank conflicts)
 constexpr int kStageWarp = 8 * kStagePitch;           // 8 rows per warp
 constexpr int kStageBytes = kEpiWarps * kStageWarp < 4096 ? 4096 : kEpiWarps * kStageWarp;
+// biases in shared memory: b1, b2, b3 (256 each), b4 zero-padded to the six 128-column blocks
+constexpr int kB4Pad = 6 * 128;
+constexpr int kBiasFloats = 3 * 256 + kB4Pad;
+constexpr int kBiasBytes = kBiasFloats * 4;
 constexpr int kHidCols = FH / kGroups;                // hidden columns per epilogue warp
 constexpr int kOutCols = kOutN / kGroups;             // output-block columns per epilogue warp
 static_assert(kEpiWarps % 4 == 0 && kHidCols % 32 == 0 && kOutCols % 32 == 0, "epilogue split");
-static_assert(kActBytes + kRingBytes + kStageBytes <= 227 * 1024, "shared memory");
-constexpr size_t kSmemBytes = (size_t)kActBytes + kRingBytes + kStageBytes;
+static_assert(kActBytes + kRingBytes + kStageBytes + kBiasBytes <= 227 * 1024, "shared memory");
+constexpr size_t kSmemBytes = (size_t)kActBytes + kRingBytes + kStageBytes + kBiasBytes;
 constexpr uint32_t kTmemCols = 256;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 constexpr uint32_t kSuspendNs = 1000000;              // a waiting thread sleeps until the phase completes or 1 ms
@@ -214,8 +219,8 @@ __device__ __forceinline__ void silu_store32(const uint32_t (&r)[32], const floa
                                              int c0) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        const float4 ba = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8));
-        const float4 bb = __ldg(reinterpret_cast<const float4 *>(bias + c0 + q * 8 + 4));
+        const float4 ba = *reinterpret_cast<const float4 *>(bias + c0 + q * 8);       // shared memory
+        const float4 bb = *reinterpret_cast<const float4 *>(bias + c0 + q * 8 + 4);
         const float bv[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
         uint32_t packed[4];
 #pragma unroll
@@ -267,15 +272,10 @@ __device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const floa
         if (nb >= FO) break;
         const bool full = nb + 32 <= FO;
         float z[32];
-        if (full) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const float4 b = __ldg(reinterpret_cast<const float4 *>(b4 + nb + 4 * q));
-                z[4 * q] = b.x, z[4 * q + 1] = b.y, z[4 * q + 2] = b.z, z[4 * q + 3] = b.w;
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < 32; ++c) z[c] = nb + c < FO ? __ldg(b4 + nb + c) : 0.f;
+        for (int q = 0; q < 8; ++q) {      // b4 in shared memory, zero past column 648
+            const float4 b = *reinterpret_cast<const float4 *>(b4 + nb + 4 * q);
+            z[4 * q] = b.x, z[4 * q + 1] = b.y, z[4 * q + 2] = b.z, z[4 * q + 3] = b.w;
         }
         {
             float v[32];
@@ -313,6 +313,59 @@ __device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const floa
     }
 }
 
+// The same in fp16: this warp's 64 columns (both 32-column halves of its share) are
+// packed into half2 first, so a stage row again holds 128 bytes and each output row
+// leaves as 128-byte runs.  Row pitch ldy (halves) is a multiple of 8.
+__device__ __forceinline__ void epilogue_out_half(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
+                                                  __half *y, int ldy, int m, int row0, int group, int lane) {
+    static_assert(kOutCols == 64, "fp16 output: 64 columns per warp");
+    const int c0 = group * kOutCols;
+    const int nb = blk * kOutN + c0;
+    if (nb >= FO) return;
+    uint32_t hp[32];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(tlane + (uint32_t)(c0 + 32 * h), v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float4 b = *reinterpret_cast<const float4 *>(b4 + nb + 32 * h + 4 * q);
+            const __half2 lo = __floats2half2_rn(v[4 * q] + b.x, v[4 * q + 1] + b.y);
+            const __half2 hi = __floats2half2_rn(v[4 * q + 2] + b.z, v[4 * q + 3] + b.w);
+            hp[16 * h + 2 * q] = *reinterpret_cast<const uint32_t *>(&lo);
+            hp[16 * h + 2 * q + 1] = *reinterpret_cast<const uint32_t *>(&hi);
+        }
+    }
+    const bool full = nb + 64 <= FO;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        __syncwarp();
+        if ((lane >> 3) == p) {
+            uint4 *dst = reinterpret_cast<uint4 *>(stage + (lane & 7) * kStagePitch);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+        }
+        __syncwarp();
+        const int rbase = row0 + 8 * p;
+        if (full) {
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int r = (lane >> 3) + 4 * k;
+                const uint4 val = *reinterpret_cast<const uint4 *>(stage + r * kStagePitch + (lane & 7) * 16);
+                if (rbase + r < m)
+                    *reinterpret_cast<uint4 *>(y + (size_t)(rbase + r) * ldy + nb + (lane & 7) * 8) = val;
+            }
+        } else if (nb + lane < FO) {       // the ragged block: columns 640 .. 648
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+                if (rbase + r < m)
+                    y[(size_t)(rbase + r) * ldy + nb + lane] =
+                        *reinterpret_cast<const __half *>(stage + r * kStagePitch + lane * 2);
+        }
+    }
+    __syncwarp();
+}
+
 struct Bars {
     uint64_t full[kSlots], empty[kSlots];   // weight ring
     uint64_t accf[2], acce[2];    // accumulator halves: full (MMA -> epilogue), empty (epilogue -> MMA)
@@ -320,15 +373,17 @@ struct Bars {
     uint64_t fin;                 // every MMA of the CTA complete
 };
 
+template <bool kHalf>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const float *x, int m, const float *b1,
                                                                 const float *b2, const float *b3, const float *b4,
-                                                                const unsigned char *blob, float *y, int ldy,
+                                                                const unsigned char *blob, void *y, int ldy,
                                                                 unsigned int *err) {
     extern __shared__ __align__(128) unsigned char smem[];
     unsigned char *act = smem;                                   // 64 KB activation tile
     unsigned char *ring = smem + kActBytes;                      // 2 x 16 KB weight chunks
     unsigned char *stage_all = smem + kActBytes + kRingBytes;    // 16 KB output stage ...
     unsigned char *xt = stage_all;                               // ... and, for layer 1, the input tile
+    float *sbias = reinterpret_cast<float *>(stage_all + kStageBytes);   // b1 | b2 | b3 | b4 (padded)
     __shared__ __align__(8) Bars bars;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
@@ -446,6 +501,16 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
         unsigned char *stage = stage_all + warp * kStageWarp;
         const int row0 = m0 + quarter * 32;
         uint32_t accf_phase[2] = {0u, 0u};
+        // biases into shared memory (b4 zero past column 648), then the epilogue warps meet
+        for (int i = threadIdx.x; i < kBiasFloats; i += kEpiThreads) {
+            float v;
+            if (i < 256) v = b1[i];
+            else if (i < 512) v = b2[i - 256];
+            else if (i < 768) v = b3[i - 512];
+            else v = i - 768 < FO ? b4[i - 768] : 0.f;
+            sbias[i] = v;
+        }
+        asm volatile("bar.sync 1, %0;\n" :: "n"(kEpiThreads) : "memory");
         if (threadIdx.x < FM) {
             const int r = threadIdx.x, gm = m0 + r;
             float xin[FIN];
@@ -459,7 +524,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
         }
         asm volatile("fence.proxy.async.shared::cta;\n");
         arrive(&bars.act);
-        const float *hb[3] = {b1, b2, b3};
+        const float *hb[3] = {sbias, sbias + 256, sbias + 512};
         bool ok = true;
         for (int layer = 0; layer < 3 && ok; ++layer) {
             ok = wait_bar(&bars.accf[0], accf_phase[0], abort);
@@ -477,7 +542,12 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
             accf_phase[h] ^= 1u;
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;\n");
-            epilogue_out(tlane + (uint32_t)(h * kOutN), j, b4, stage, y, ldy, m, row0, group, lane);
+            if (kHalf)
+                epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<__half *>(y), ldy,
+                                  m, row0, group, lane);
+            else
+                epilogue_out(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<float *>(y), ldy, m,
+                             row0, group, lane);
             asm volatile("tcgen05.fence::before_thread_sync;\n");
             arrive(&bars.acce[h]);
         }
@@ -516,6 +586,31 @@ __global__ void pack_kernel(const __nv_bfloat16 *w, int n, int k_in, int row0, i
 
 using namespace mcw;
 
+namespace {
+
+int forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3, const float *b4,
+            const void *blob, void *y, int32_t ldy, bool half, void *stream) {
+    const int align = half ? 8 : 4;   // 16-byte row starts
+    if (!x || !b1 || !b2 || !b3 || !b4 || !blob || !y || m < 0 || ldy < FO || (ldy % align) != 0)
+        return MCW_MLP_ERR_ARG;
+    if ((((uintptr_t)blob | (uintptr_t)y) & 15) != 0) return MCW_MLP_ERR_ARG;
+    if (m == 0) return 0;
+    unsigned int *err = tc_err_flag();
+    if (!err) return MCW_MLP_ERR_CUDA;
+    const void *fn = half ? reinterpret_cast<const void *>(mlp_fused_kernel<true>)
+                          : reinterpret_cast<const void *>(mlp_fused_kernel<false>);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
+    if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
+    const unsigned grid = (unsigned)((m + FM - 1) / FM);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const unsigned char *wb = static_cast<const unsigned char *>(blob);
+    if (half) mlp_fused_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err);
+    else mlp_fused_kernel<false><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err);
+    return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
+}
+
+}  // namespace
+
 extern "C" {
 
 int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4, void *blob, void *stream) {
@@ -540,19 +635,12 @@ int mcw_mlp_pack(const void *w1, const void *w2, const void *w3, const void *w4,
 
 int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3, const float *b4,
                     const void *blob, float *y, int32_t ldy, void *stream) {
-    if (!x || !b1 || !b2 || !b3 || !b4 || !blob || !y || m < 0 || ldy < FO || (ldy & 3) != 0)
-        return MCW_MLP_ERR_ARG;
-    if ((((uintptr_t)blob | (uintptr_t)b1 | (uintptr_t)b2 | (uintptr_t)b3 | (uintptr_t)b4 | (uintptr_t)y) & 15) != 0)
-        return MCW_MLP_ERR_ARG;
-    if (m == 0) return 0;
-    unsigned int *err = tc_err_flag();
-    if (!err) return MCW_MLP_ERR_CUDA;
-    cudaError_t e = cudaFuncSetAttribute(mlp_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kSmemBytes);
-    if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
-    mlp_fused_kernel<<<(m + FM - 1) / FM, kThreads, kSmemBytes, static_cast<cudaStream_t>(stream)>>>(
-        x, m, b1, b2, b3, b4, static_cast<const unsigned char *>(blob), y, ldy, err);
-    return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
+    return forward(x, m, b1, b2, b3, b4, blob, y, ldy, false, stream);
+}
+
+int mcw_mlp_forward_f16(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
+                        const float *b4, const void *blob, void *y, int32_t ldy, void *stream) {
+    return forward(x, m, b1, b2, b3, b4, blob, y, ldy, true, stream);
 }
 
 }  // extern "C"

@@ -119,18 +119,23 @@ def pack_weights(torch, w16):
     return blob
 
 
-# row pitch of the fused kernel's output: 649 floats rounded up to 16 bytes (its 16-byte stores)
+# row pitch of the fused kernel's output: 649 values rounded up to 16 bytes (its
+# 16-byte stores): 652 floats or 656 halves
 Y_PITCH = 652
+Y_PITCH_F16 = 656
 
 
-def forward_fused(torch, x, w16, biases, blob):
-    """Inference of the whole network in one kernel (mcw_mlp_forward); x float32 [m, 4]."""
+def forward_fused(torch, x, w16, biases, blob, half=False):
+    """Inference of the whole network in one kernel (mcw_mlp_forward, or
+    mcw_mlp_forward_f16 with half=True: outputs rounded to fp16, half the bytes);
+    x float32 [m, 4]; returns a [m, 649] view of the output rows."""
     x = x.contiguous().float()
     m = x.shape[0]
-    y = torch.empty((m, Y_PITCH), dtype=torch.float32, device=x.device)
+    pitch = Y_PITCH_F16 if half else Y_PITCH
+    y = torch.empty((m, pitch), dtype=torch.float16 if half else torch.float32, device=x.device)
     b = [t.contiguous() for t in biases]
-    rc = _abi.load().mcw_mlp_forward(_ptr(x), m, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), _ptr(b[3]), _ptr(blob),
-                                     _ptr(y), Y_PITCH, _stream(torch))
+    fn = _abi.load().mcw_mlp_forward_f16 if half else _abi.load().mcw_mlp_forward
+    rc = fn(_ptr(x), m, _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), _ptr(b[3]), _ptr(blob), _ptr(y), pitch, _stream(torch))
     if rc:
         raise _abi.McwError(rc, 'mcw_mlp_forward failed (m=%d)' % m)
     return y[:, :DIMS[-1]]
@@ -277,10 +282,11 @@ class SurrogateMLP:
             self._blob_key = key
         return self._blob
 
-    def predict_std(self, x):
+    def predict_std(self, x, half=True):
         """Standardised outputs for encoded inputs x (torch CUDA float32 [n, 4]) from the
-        fused inference kernel."""
-        return forward_fused(self.torch, x, self.w16, self.params[1::2], self.packed())
+        fused inference kernel; fp16 by default (its rounding, 2^-11 relative, is below the
+        network's bf16 activations), float32 with half=False."""
+        return forward_fused(self.torch, x, self.w16, self.params[1::2], self.packed(), half=half)
 
     def train_step(self, x16, t, w_out, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         """One Adam step on a batch (x16 bf16 [b, 4], t fp32 standardised targets)."""

@@ -191,10 +191,13 @@ def test_fused_forward_matches_layerwise_and_float64(m):
     flags = ctypes.c_uint32(0)
     lib = _abi.load()
     assert lib.mcw_mlp_status(1, ctypes.byref(flags)) == 0
-    y = net.predict_std(x)
+    y = net.predict_std(x, half=False)
+    y16 = net.predict_std(x).float()
     y_layer, _ = surrogate.forward_cached(torch, surrogate._cast(torch, x), net.w16, net.params[1::2], keep=False)
     torch.cuda.synchronize()
     assert lib.mcw_mlp_status(0, ctypes.byref(flags)) == 0 and flags.value == 0
+    # fp16 output: y rounded to 11 significant bits
+    assert (y16 - y).abs().max().item() <= 2.0 ** -10 * y.abs().max().item()
     ref = _reference_mlp(x.cpu().double(), [p.cpu().double() for p in net.params])
     scale = ref.abs().max().item()
     assert y.shape == (m, 649) and torch.isfinite(y).all()
@@ -215,7 +218,7 @@ def test_fused_forward_leading_dimension_and_repack():
                                      surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
                                      surrogate._ptr(out), ldy, surrogate._stream(torch))
     assert rc == 0
-    y = net.predict_std(x)
+    y = net.predict_std(x, half=False)
     torch.cuda.synchronize()
     assert torch.equal(out[:, :649], y)
     assert (out[:, 649:] == 12345.0).all()
@@ -228,6 +231,18 @@ def test_fused_forward_leading_dimension_and_repack():
                                       surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
                                       surrogate._ptr(out), 650, surrogate._stream(torch))
     assert bad == -1                               # row pitch not a multiple of 16 bytes
+    # fp16 rows at pitch 664: padding and rows past m untouched; odd pitches refused
+    full16 = torch.full((m + 40, 664), 7.0, dtype=torch.float16, device='cuda')
+    rc = _abi.load().mcw_mlp_forward_f16(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
+                                         surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
+                                         surrogate._ptr(full16), 664, surrogate._stream(torch))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert torch.equal(full16[:m, :649], net.predict_std(x))
+    assert (full16[:m, 649:] == 7.0).all() and (full16[m:] == 7.0).all()
+    assert _abi.load().mcw_mlp_forward_f16(surrogate._ptr(x), m, surrogate._ptr(b[0]), surrogate._ptr(b[1]),
+                                           surrogate._ptr(b[2]), surrogate._ptr(b[3]), surrogate._ptr(net.packed()),
+                                           surrogate._ptr(full16), 660, surrogate._stream(torch)) == -1
     before = net.predict_std(x).clone()
     t = torch.randn(64, 649, device='cuda')
     w_out = torch.from_numpy(surrogate.output_weights()).cuda()
