@@ -21,9 +21,9 @@ extern "C" {
 #define MCW_MLP_ERR_CUDA (-2)
 
 /* GEMM engines */
-#define MCW_ENGINE_MMA_SYNC 0  /* mma.sync m16n8k16, any layout and epilogue */
-#define MCW_ENGINE_TCGEN05 1   /* tcgen05.mma into tensor memory: trans_a = trans_b = 0 and the
-                                  forward epilogues (F32, BIAS_F32, BIAS_SILU) */
+#define MCW_ENGINE_MMA_SYNC 0  /* mma.sync m16n8k16 */
+#define MCW_ENGINE_TCGEN05 1   /* tcgen05.mma into tensor memory, double-buffered K chunks */
+/* Both engines take any operand layout and every epilogue. */
 
 /* GEMM epilogues */
 #define MCW_EPI_F32 0        /* c (f32) = acc */

@@ -251,8 +251,6 @@ int mcw_mlp_gemm(const McwGemm *p, void *stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     if (p->engine == MCW_ENGINE_TCGEN05) {
-        // tcgen05 path: forward layouts (A [m,k], W [n,k], both K-major) and epilogues
-        if (p->trans_a || p->trans_b || p->epilogue == MCW_EPI_DSILU) return MCW_MLP_ERR_ARG;
         unsigned int *err = tc_err_flag();
         if (!err) return MCW_MLP_ERR_CUDA;
         e = launch_gemm_tc(*p, err, s);

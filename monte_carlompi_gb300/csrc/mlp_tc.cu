@@ -1,15 +1,18 @@
-// Forward GEMM of the surrogate network on the 5th-generation tensor cores:
-// C[m, n] = sum_k A[m, k] W[n, k] with A (activations) and W (weights) both
-// K-major bf16, FP32 accumulation in tensor memory, fused bias (+ SiLU) epilogue.
+// GEMM of the surrogate network on the 5th-generation tensor cores:
+// C[m, n] = sum_k A(m, k) B(n, k), bf16 operands stored K-major ([m, k], [n, k]) or
+// transposed ([k, m], [k, n]), FP32 accumulation in tensor memory, fused epilogues
+// (bias, bias + SiLU, SiLU' product of the backward pass).  Used for the forward and
+// the backward GEMMs of training.
 //
-// One CTA of four warps computes a 128 x 128 tile.  K is walked in chunks of 64:
-// all threads stage the A and W chunks in shared memory as 8 x 16-byte core
-// matrices (no swizzle; core matrices 128 B apart along K, 1024 B apart along
-// M / N), one elected thread issues four tcgen05.mma (K = 16 each) into a
-// 128-column TMEM accumulator and commits them to an mbarrier, and the CTA waits
-// on that barrier (with a bounded number of polls) before reusing the buffers.
-// The epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM lanes
-// 32w..32w+31, i.e. tile rows) and stores 32 consecutive columns per thread.
+// One CTA of four warps computes a 128 x 128 tile.  K is walked in chunks of 64
+// through two shared-memory buffers: all threads stage chunk k + 1 as 8 x 16-byte
+// core matrices (no swizzle; 128 B apart along K, 1024 B apart along M / N) while
+// the tensor core runs chunk k's four tcgen05.mma (K = 16 each), issued by one
+// thread into a 128-column TMEM accumulator and committed to the buffer's mbarrier;
+// a buffer is restaged only after that barrier reports its MMAs complete (bounded
+// wait).  Transposed operands are staged with rows fastest across the threads, so a
+// warp's loads of one k cover 32 consecutive rows.  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31, i.e. tile rows).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -23,8 +26,9 @@ namespace {
 
 constexpr int TM = 128, TN = 128, TK = 64;
 constexpr int kChunkBytes = TM * TK * 2;          // 16 KB per operand chunk
+constexpr int kBufBytes = 2 * kChunkBytes;        // A and B chunks of one buffer
 constexpr uint32_t kTmemCols = 128;
-constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded wait on the MMA barrier (2 s)
+constexpr unsigned long long kWaitNs = 2000000000ull;  // bounded wait on an MMA barrier (2 s)
 
 // Instruction descriptor of tcgen05.mma kind::f16: F32 accumulate, BF16 A and B,
 // both K-major, N = 128 (bits 17-22: N >> 3), M = 128 (bits 24-28: M >> 4).
@@ -48,37 +52,95 @@ __device__ __forceinline__ unsigned long long now_ns() {
 }
 
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+__device__ __forceinline__ float dsilu(float z) {
+    const float s = 1.f / (1.f + __expf(-z));
+    return s * (1.f + z * (1.f - s));
+}
 
-// Stage a 128-row x 64-k chunk of a K-major bf16 matrix (rows of length ld) into
-// the core-matrix layout; rows >= rows_valid and k >= K read as zero.
+// Stage a 128-row x 64-k chunk into the core-matrix layout; rows >= rows_valid and
+// k >= K read as zero.  Stored K-major (g[row * ld + k]): 16-byte loads along k.  All
+// eight loads of a thread are issued before any store, so their latencies overlap.
 __device__ __forceinline__ void stage_chunk(unsigned char *dst, const __nv_bfloat16 *g, int ld, int row0,
                                             int rows_valid, int k0, int K, bool vec) {
+    const bool full = vec && row0 + 128 <= rows_valid && k0 + 64 <= K;
+    uint4 v[8];
+    if (full) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int c = threadIdx.x + 128 * q;  // 1024 chunks of 16 B
+            const int r = c >> 3, k8 = c & 7;
+            v[q] = __ldg(reinterpret_cast<const uint4 *>(g + (size_t)(row0 + r) * ld + k0 + k8 * 8));
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int c = threadIdx.x + 128 * q;
+            const int r = c >> 3, k8 = c & 7;
+            const int gr = row0 + r, gk = k0 + k8 * 8;
+            __align__(16) __nv_bfloat16 tmp[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                tmp[e] = (gr < rows_valid && gk + e < K) ? g[(size_t)gr * ld + gk + e] : __float2bfloat16(0.f);
+            v[q] = *reinterpret_cast<const uint4 *>(tmp);
+        }
+    }
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const int c = threadIdx.x + 128 * q;  // 1024 chunks of 16 B
+        const int c = threadIdx.x + 128 * q;
         const int r = c >> 3, k8 = c & 7;
-        const int gr = row0 + r, gk = k0 + k8 * 8;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (gr < rows_valid) {
-            if (vec && gk + 8 <= K) {
-                v = *reinterpret_cast<const uint4 *>(g + (size_t)gr * ld + gk);
-            } else {
-                __align__(16) __nv_bfloat16 tmp[8];
+        *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + k8 * 128 + (r & 7) * 16) = v[q];
+    }
+}
+
+// The same from a transposed operand (g[k * ld + row]): thread c takes row c % 128,
+// so for each k a warp reads 32 consecutive rows; four 16-byte chunks' loads at a time.
+__device__ __forceinline__ void stage_chunk_t(unsigned char *dst, const __nv_bfloat16 *g, int ld, int row0,
+                                              int rows_valid, int k0, int K) {
+    const bool full = row0 + 128 <= rows_valid && k0 + 64 <= K;
 #pragma unroll
-                for (int e = 0; e < 8; ++e) tmp[e] = (gk + e < K) ? g[(size_t)gr * ld + gk + e] : __float2bfloat16(0.f);
-                v = *reinterpret_cast<const uint4 *>(tmp);
-            }
+    for (int half = 0; half < 2; ++half) {
+        __nv_bfloat16 tv[4][8];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int c = threadIdx.x + 128 * (4 * half + q);
+            const int r = c & 127, k8 = c >> 7;
+            const int gr = row0 + r, gk = k0 + k8 * 8;
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                tv[q][e] = (full || (gr < rows_valid && gk + e < K)) ? g[(size_t)(gk + e) * ld + gr]
+                                                                     : __float2bfloat16(0.f);
         }
-        *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + k8 * 128 + (r & 7) * 16) = v;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int c = threadIdx.x + 128 * (4 * half + q);
+            const int r = c & 127, k8 = c >> 7;
+            __align__(16) __nv_bfloat16 tmp[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) tmp[e] = tv[q][e];
+            *reinterpret_cast<uint4 *>(dst + (r >> 3) * 1024 + k8 * 128 + (r & 7) * 16) =
+                *reinterpret_cast<const uint4 *>(tmp);
+        }
+    }
+}
+
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity) {
+    const unsigned long long t0 = now_ns();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done) : "r"(smem_u32(bar)), "r"(parity));
+        if (done) return true;
+        if (now_ns() - t0 > kWaitNs) return false;
     }
 }
 
 template <int kEpi>
 __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned int *err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sa = smem;
-    unsigned char *sb = smem + kChunkBytes;
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base_slot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * TM, n0 = blockIdx.y * TN;
@@ -93,7 +155,8 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -102,12 +165,25 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned 
     const uint32_t tmem = tmem_base_slot;
 
     bool ok = true;
-    uint32_t phase = 0;
+    uint32_t phase[2] = {0u, 0u};
+    bool pending[2] = {false, false};
     const int n_chunks = (p.k + TK - 1) / TK;
     for (int kc = 0; kc < n_chunks && ok; ++kc) {
+        const int b = kc & 1;
+        unsigned char *sa = smem + b * kBufBytes;
+        unsigned char *sb = sa + kChunkBytes;
+        // the buffer's previous MMAs (chunk kc - 2) must be done before it is restaged
+        if (pending[b]) {
+            ok = __syncthreads_and(bar_wait(&mbar[b], phase[b])) != 0;
+            if (!ok) break;
+            phase[b] ^= 1u;
+            pending[b] = false;
+        }
         const int k0 = kc * TK;
-        stage_chunk(sa, A, p.lda, m0, p.m, k0, p.k, vec_a);
-        stage_chunk(sb, W, p.ldb, n0, p.n, k0, p.k, vec_b);
+        if (p.trans_a) stage_chunk_t(sa, A, p.lda, m0, p.m, k0, p.k);
+        else stage_chunk(sa, A, p.lda, m0, p.m, k0, p.k, vec_a);
+        if (p.trans_b) stage_chunk_t(sb, W, p.ldb, n0, p.n, k0, p.k);
+        else stage_chunk(sb, W, p.ldb, n0, p.n, k0, p.k, vec_b);
         // make the generic-proxy stores visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;\n");
         __syncthreads();
@@ -126,24 +202,23 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned 
                     :: "r"(tmem), "l"(da), "l"(db), "r"(kIdesc), "r"(accumulate));
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
-                         :: "r"(smem_u32(&mbar)));
+                         :: "r"(smem_u32(&mbar[b])));
         }
-        // wait for the MMAs of this chunk, bounded in time (a working kernel never
-        // comes near the limit); the outcome is made uniform across the CTA
-        uint32_t done = 0;
-        const unsigned long long t0 = now_ns();
-        while (!done) {
-            asm volatile(
-                "{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                "selp.u32 %0, 1, 0, p;\n\t}\n"
-                : "=r"(done) : "r"(smem_u32(&mbar)), "r"(phase));
-            if (!done && now_ns() - t0 > kWaitNs) break;
+        pending[b] = true;
+    }
+    // the last MMAs (and with them all earlier ones) complete before the epilogue
+    for (int b = 0; b < 2 && ok; ++b) {
+        if (pending[b]) {
+            ok = __syncthreads_and(bar_wait(&mbar[b], phase[b])) != 0;
+            if (ok) pending[b] = false;
         }
-        phase ^= 1u;
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-        ok = __syncthreads_and(done) != 0;
-        if (!ok && threadIdx.x == 0) atomicOr(err, 1u);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (!ok) {
+        if (threadIdx.x == 0) atomicOr(err, 1u);
+        // MMAs still in flight finish (bounded) before the memory is freed
+        for (int b = 0; b < 2; ++b)
+            if (pending[b]) bar_wait(&mbar[b], phase[b]);
     }
 
     if (ok) {
@@ -164,21 +239,57 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned 
                   "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-            if (m < p.m) {
+            const int nb = n0 + c0;
+            if (m < p.m && nb < p.n) {
+                const int cnt = min(32, p.n - nb);
+                // the inputs of the 32 columns first (their loads overlap), then the stores
+                float add[32];
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
-                    const int n = n0 + c0 + j;
-                    if (n >= p.n) break;
-                    float z = __uint_as_float(v[j]);
-                    if (kEpi == MCW_EPI_BIAS_SILU) {
-                        z += p.bias[n];
-                        if (p.c2) static_cast<float *>(p.c2)[(size_t)m * p.ldc2 + n] = z;
-                        static_cast<__nv_bfloat16 *>(p.c)[(size_t)m * p.ldc + n] = __float2bfloat16(silu(z));
-                    } else if (kEpi == MCW_EPI_BIAS_F32) {
-                        if (p.bias) z += p.bias[n];
-                        static_cast<float *>(p.c)[(size_t)m * p.ldc + n] = z;
+                    add[j] = 0.f;
+                    if (j < cnt) {
+                        if (kEpi == MCW_EPI_DSILU) add[j] = __ldg(p.aux + (size_t)m * p.ldaux + nb + j);
+                        else if (kEpi != MCW_EPI_F32 && p.bias) add[j] = __ldg(p.bias + nb + j);
+                    }
+                }
+                float z[32];
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    z[j] = __uint_as_float(v[j]);
+                    if (kEpi == MCW_EPI_DSILU) z[j] *= dsilu(add[j]);
+                    else z[j] += add[j];
+                }
+                float *c32 = nullptr;
+                if (kEpi == MCW_EPI_F32 || kEpi == MCW_EPI_BIAS_F32) c32 = static_cast<float *>(p.c) + (size_t)m * p.ldc + nb;
+                else if (p.c2) c32 = static_cast<float *>(p.c2) + (size_t)m * p.ldc2 + nb;
+                __nv_bfloat16 *c16 = nullptr;
+                if (kEpi == MCW_EPI_BIAS_SILU || kEpi == MCW_EPI_DSILU)
+                    c16 = static_cast<__nv_bfloat16 *>(p.c) + (size_t)m * p.ldc + nb;
+                if (c32) {
+                    if (cnt == 32 && (reinterpret_cast<uintptr_t>(c32) & 15) == 0) {
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            reinterpret_cast<float4 *>(c32)[q] =
+                                make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
                     } else {
-                        static_cast<float *>(p.c)[(size_t)m * p.ldc + n] = z;
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (j < cnt) c32[j] = z[j];
+                    }
+                }
+                if (c16) {
+                    __align__(16) __nv_bfloat16 h[32];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j)
+                        h[j] = __float2bfloat16(kEpi == MCW_EPI_BIAS_SILU ? silu(z[j]) : z[j]);
+                    if (cnt == 32 && (reinterpret_cast<uintptr_t>(c16) & 15) == 0) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            reinterpret_cast<uint4 *>(c16)[q] = reinterpret_cast<const uint4 *>(h)[q];
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j)
+                            if (j < cnt) c16[j] = h[j];
                     }
                 }
             }
@@ -203,9 +314,9 @@ unsigned int *tc_err_flag() {
     return static_cast<unsigned int *>(p);
 }
 
-// Dynamic shared memory: two 16 KB chunks, padded so that at most four CTAs share
-// an SM (4 x 128 TMEM columns = the SM's 512).
-constexpr size_t kTcSmem = 48 * 1024;
+// Dynamic shared memory: two buffers of two 16 KB chunks (at most three CTAs per SM,
+// 3 x 128 TMEM columns of the SM's 512).
+constexpr size_t kTcSmem = 2 * kBufBytes;
 
 cudaError_t launch_gemm_tc(const McwGemm &p, unsigned int *err, cudaStream_t s) {
     dim3 grid((p.m + TM - 1) / TM, (p.n + TN - 1) / TN);
@@ -225,6 +336,11 @@ cudaError_t launch_gemm_tc(const McwGemm &p, unsigned int *err, cudaStream_t s) 
             e = cudaFuncSetAttribute(gemm_tc_kernel<MCW_EPI_F32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
             if (e != cudaSuccess) return e;
             gemm_tc_kernel<MCW_EPI_F32><<<grid, 128, kTcSmem, s>>>(p, err);
+            break;
+        case MCW_EPI_DSILU:
+            e = cudaFuncSetAttribute(gemm_tc_kernel<MCW_EPI_DSILU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+            if (e != cudaSuccess) return e;
+            gemm_tc_kernel<MCW_EPI_DSILU><<<grid, 128, kTcSmem, s>>>(p, err);
             break;
         default:
             return cudaErrorInvalidValue;

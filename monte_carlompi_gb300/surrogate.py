@@ -103,10 +103,10 @@ def _colsum(torch, g):
     return out
 
 
-# engine of the layer-by-layer forward GEMMs of training (the backward layouts --
-# transposed operands, silu' epilogue -- always run on mma.sync); inference runs the
-# fused tcgen05 kernel (forward_fused)
-FORWARD_ENGINE = _abi.ENGINE_MMA_SYNC
+# engine of training's GEMMs (forward with kept pre-activations, and the backward
+# layouts: transposed operands, silu' epilogue); inference runs the fused tcgen05
+# kernel (forward_fused)
+TRAIN_ENGINE = _abi.ENGINE_TCGEN05
 
 
 def pack_weights(torch, w16):
@@ -152,13 +152,13 @@ def forward_cached(torch, x16, w16, biases, keep=True):
         z = torch.empty((m, n), dtype=torch.float32, device=x16.device) if keep else None
         nxt = torch.empty((m, n), dtype=torch.bfloat16, device=x16.device)
         _gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a, k, w16[layer], k, nxt, n, bias=biases[layer],
-              c2=z, ldc2=n, engine=FORWARD_ENGINE)
+              c2=z, ldc2=n, engine=TRAIN_ENGINE)
         zs.append(z)
         acts.append(nxt)
         a = nxt
     n, k = w16[3].shape
     y = torch.empty((m, n), dtype=torch.float32, device=x16.device)
-    _gemm(torch, _abi.EPI_BIAS_F32, m, n, k, a, k, w16[3], k, y, n, bias=biases[3], engine=FORWARD_ENGINE)
+    _gemm(torch, _abi.EPI_BIAS_F32, m, n, k, a, k, w16[3], k, y, n, bias=biases[3], engine=TRAIN_ENGINE)
     return y, (zs, acts)
 
 
@@ -174,20 +174,22 @@ def backward_cached(torch, gy, w16, cache, need_dx=True):
         a_in = acts[layer]
         dw = torch.empty((n_out, k_in), dtype=torch.float32, device=gy.device)
         # dW[o, i] = sum_b G[b, o] A[b, i]
-        _gemm(torch, _abi.EPI_F32, n_out, k_in, m, g16, n_out, a_in, k_in, dw, k_in, trans_a=1, trans_b=1)
+        _gemm(torch, _abi.EPI_F32, n_out, k_in, m, g16, n_out, a_in, k_in, dw, k_in, trans_a=1, trans_b=1,
+              engine=TRAIN_ENGINE)
         dws[layer] = dw
         dbs[layer] = _colsum(torch, g32)
         if layer == 0:
             if not need_dx:
                 return None, dws, dbs
             dx = torch.empty((m, k_in), dtype=torch.float32, device=gy.device)
-            _gemm(torch, _abi.EPI_F32, m, k_in, n_out, g16, n_out, w16[layer], k_in, dx, k_in, trans_b=1)
+            _gemm(torch, _abi.EPI_F32, m, k_in, n_out, g16, n_out, w16[layer], k_in, dx, k_in, trans_b=1,
+                  engine=TRAIN_ENGINE)
             return dx, dws, dbs
         # G_prev[b, i] = (sum_o G[b, o] W[o, i]) * silu'(Z_prev[b, i])
         g16_prev = torch.empty((m, k_in), dtype=torch.bfloat16, device=gy.device)
         g32_prev = torch.empty((m, k_in), dtype=torch.float32, device=gy.device)
         _gemm(torch, _abi.EPI_DSILU, m, k_in, n_out, g16, n_out, w16[layer], k_in, g16_prev, k_in,
-              trans_b=1, aux=zs[layer - 1], ldaux=k_in, c2=g32_prev, ldc2=k_in)
+              trans_b=1, aux=zs[layer - 1], ldaux=k_in, c2=g32_prev, ldc2=k_in, engine=TRAIN_ENGINE)
         g16, g32 = g16_prev, g32_prev
 
 

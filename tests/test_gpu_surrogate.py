@@ -18,16 +18,20 @@ def _bf16(t):
     return t.to(torch.bfloat16)
 
 
+ENGINES = [_abi.ENGINE_MMA_SYNC, _abi.ENGINE_TCGEN05]
+
+
+@pytest.mark.parametrize('engine', ENGINES)
 @pytest.mark.parametrize('trans_a,trans_b', [(0, 0), (0, 1), (1, 0), (1, 1)])
-@pytest.mark.parametrize('m,n,k', [(100, 70, 37), (256, 649, 256), (64, 64, 4), (1, 5, 300)])
-def test_gemm_layouts_match_float64(trans_a, trans_b, m, n, k):
+@pytest.mark.parametrize('m,n,k', [(100, 70, 37), (256, 649, 256), (64, 64, 4), (1, 5, 300), (300, 130, 200)])
+def test_gemm_layouts_match_float64(trans_a, trans_b, m, n, k, engine):
     g = torch.Generator().manual_seed(m * 7 + n * 3 + k)
     a = torch.randn((k, m) if trans_a else (m, k), generator=g)
     b = torch.randn((k, n) if trans_b else (n, k), generator=g)
     a16, b16 = _bf16(a).cuda(), _bf16(b).cuda()
     c = torch.empty((m, n), dtype=torch.float32, device='cuda')
     surrogate._gemm(torch, _abi.EPI_F32, m, n, k, a16, a16.shape[1], b16, b16.shape[1], c, n,
-                    trans_a=trans_a, trans_b=trans_b)
+                    trans_a=trans_a, trans_b=trans_b, engine=engine)
     A = a16.cpu().double()
     B = b16.cpu().double()
     ref = (A.T if trans_a else A) @ (B if trans_b else B.T)
@@ -35,7 +39,8 @@ def test_gemm_layouts_match_float64(trans_a, trans_b, m, n, k):
     assert err <= 1e-4 * max(1.0, ref.abs().max().item()) + 1e-5 * math.sqrt(k), err
 
 
-def test_gemm_epilogues():
+@pytest.mark.parametrize('engine', ENGINES)
+def test_gemm_epilogues(engine):
     g = torch.Generator().manual_seed(5)
     m, n, k = 96, 200, 64
     a16 = _bf16(torch.randn(m, k, generator=g)).cuda()
@@ -43,7 +48,8 @@ def test_gemm_epilogues():
     bias = torch.randn(n, generator=g).cuda()
     z = torch.empty((m, n), device='cuda')
     act = torch.empty((m, n), dtype=torch.bfloat16, device='cuda')
-    surrogate._gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a16, k, w16, k, act, n, bias=bias, c2=z, ldc2=n)
+    surrogate._gemm(torch, _abi.EPI_BIAS_SILU, m, n, k, a16, k, w16, k, act, n, bias=bias, c2=z, ldc2=n,
+                    engine=engine)
     zr = a16.cpu().double() @ w16.cpu().double().T + bias.cpu().double()
     assert (z.cpu().double() - zr).abs().max().item() < 1e-4
     ar = zr * torch.sigmoid(zr)
@@ -52,7 +58,7 @@ def test_gemm_epilogues():
     gout16 = torch.empty((m, n), dtype=torch.bfloat16, device='cuda')
     gout32 = torch.empty((m, n), device='cuda')
     surrogate._gemm(torch, _abi.EPI_DSILU, m, n, k, a16, k, w16, k, gout16, n, aux=z, ldaux=n,
-                    c2=gout32, ldc2=n)
+                    c2=gout32, ldc2=n, engine=engine)
     s = torch.sigmoid(z.cpu().double())
     ds = s * (1 + z.cpu().double() * (1 - s))
     gr = (a16.cpu().double() @ w16.cpu().double().T) * ds
