@@ -62,6 +62,7 @@ constexpr float kTwo33Inv = 1.16415321826934814e-10f; // 2^-33
 constexpr uint32_t kFlagReflect = 8u;                  // bottom reflection pending
 constexpr int kSmemCfgMax = 256;                       // configs staged in shared memory
 constexpr int kFinishCap = 64;                         // finish queue entries per warp
+constexpr int kLongWalk = 1024;                        // steps after which a walk leaves for the drain queue
 #ifndef MCW_STEPS_PER_ROUND
 #define MCW_STEPS_PER_ROUND 4
 #endif
@@ -574,25 +575,31 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
         }
         if (idle == 0xffffffffu && exhausted && n_birth == 0) break;
 
-        // ---- drain handover: the supply is exhausted and the warp is nearly empty
-        if (a.drain_below > 0 && exhausted && n_birth == 0 && __popc(~idle) <= a.drain_below) {
-            const unsigned act = ~idle;
-            unsigned base = 0;
-            if (lane == 0) base = atomicAdd(a.drain_count, (unsigned)__popc(act));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (P.cfg >= 0) {
-                float4 *slot = a.drain + (size_t)(base + __popc(act & lt_mask)) * kDrainSlot;
-                float4 v[kDrainSlot];
-                pack_photon(v, P);
+        // ---- drain handover, once the supply is exhausted: the photons of a nearly
+        // empty warp, and any photon already kLongWalk steps long (likely to walk much
+        // longer), go to the queue to be walked with a whole warp each
+        if (a.drain_below > 0 && exhausted && n_birth == 0) {
+            const bool whole = __popc(~idle) <= a.drain_below;
+            const bool leave = P.cfg >= 0 && (whole || P.i >= kLongWalk);
+            const unsigned lm = __ballot_sync(0xffffffffu, leave);
+            if (lm) {
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(a.drain_count, (unsigned)__popc(lm));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (leave) {
+                    float4 *slot = a.drain + (size_t)(base + __popc(lm & lt_mask)) * kDrainSlot;
+                    float4 v[kDrainSlot];
+                    pack_photon(v, P);
 #pragma unroll
-                for (int k = 0; k < kDrainSlot - 1; ++k) __stcg(&slot[k], v[k]);
-                __threadfence();
-                v[kDrainSlot - 1].w = __uint_as_float(a.epoch);
-                __stcg(&slot[kDrainSlot - 1], v[kDrainSlot - 1]);
-                P.cfg = -1;
+                    for (int k = 0; k < kDrainSlot - 1; ++k) __stcg(&slot[k], v[k]);
+                    __threadfence();
+                    v[kDrainSlot - 1].w = __uint_as_float(a.epoch);
+                    __stcg(&slot[kDrainSlot - 1], v[kDrainSlot - 1]);
+                    P.cfg = -1;
+                }
+                idle |= lm;
             }
-            idle = 0xffffffffu;
-            break;
+            if (whole) break;
         }
 
         // ---- kStepsPerRound scatter events per active lane; their Philox blocks

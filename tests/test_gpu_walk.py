@@ -167,6 +167,29 @@ def test_f32_records_independent_of_photon_count(walker, case):
     assert np.array_equal(small.records, big.records[:300])
 
 
+def test_f32_long_walks_same_records_with_and_without_drain(walker):
+    """Weakly absorbing, deep snow (lambda 1.0 um, r_eff 50 um, tau ~1000: walks of
+    thousands of steps): the walks that leave for the drain queue end exactly as they
+    would in the main loop."""
+    lo, hi = ssp.grid_for(1.0, 0.085)
+    ice = ssp.synthetic_ice_table(50.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = 0.1 * ssp.ext_cff_mss_sphere(50.0) * 300.0
+    cfg = WalkConfig(n_photon=3000, wvl0=1.0, half_width=0.085, theta0_deg=30.0, tau_tot=tau,
+                     lambertian_reflectance=0.5)
+    walker.set_tables([ice], imp)
+    saved = walker.get_launch()
+    try:
+        walker.set_launch(256, 0, 8, 0)
+        a = walker.walk([cfg], 5, mode='f32')
+        walker.set_launch(256, 0, 8, 4)
+        b = walker.walk([cfg], 5, mode='f32')
+    finally:
+        walker.set_launch(**saved)
+    assert int(a.records['n_scat'].max()) > 4096
+    assert np.array_equal(a.records, b.records) and np.array_equal(a.tallies, b.tallies)
+
+
 def test_f32_tallies_agree_with_records(walker):
     cfg, ice, imp = cfg2_geometry(300000, depth=0.02, rds=1500.0)
     walker.set_tables([ice], imp)
