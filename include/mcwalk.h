@@ -37,7 +37,9 @@ extern "C" {
 
 /* where mcw_walk writes per-photon records */
 #define MCW_RECORDS_NONE 0
-#define MCW_RECORDS_HOST 1   /* host pointer; the library copies device -> host */
+#define MCW_RECORDS_HOST 1   /* host pointer; pinned host memory (mcw_host_alloc, cudaHostAlloc,
+                                cudaHostRegister) is written by the walk directly, other host
+                                memory receives a device -> host copy after it */
 #define MCW_RECORDS_DEVICE 2 /* device pointer owned by the caller */
 
 /* exit-direction histogram: 18 zenith bins of 5 deg x 36 azimuth bins of 10 deg */

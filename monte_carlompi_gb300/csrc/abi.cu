@@ -529,9 +529,21 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
     void *dev_records = nullptr;
     if (records_where == MCW_RECORDS_DEVICE) dev_records = records;
+    bool direct = false;   // host records written by the kernels themselves
     if (records_where == MCW_RECORDS_HOST && plan.total > 0) {
-        CUDA_TRY(ctx, ctx->records.ensure((size_t)plan.total * rec_size));
-        dev_records = ctx->records.p;
+        // pinned host memory the device can address (mcw_host_alloc, cudaHostAlloc,
+        // cudaHostRegister): the walk writes the records straight into it over the
+        // host link, so no copy follows the kernel.  Otherwise a device buffer and a copy.
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, records) == cudaSuccess && at.type == cudaMemoryTypeHost &&
+            at.devicePointer && ((uintptr_t)at.devicePointer % 16) == 0) {
+            dev_records = at.devicePointer;
+            direct = true;
+        } else {
+            (void)cudaGetLastError();
+            CUDA_TRY(ctx, ctx->records.ensure((size_t)plan.total * rec_size));
+            dev_records = ctx->records.p;
+        }
     }
     Shape shape{0, 0, 0, 0};
     if (mode == MCW_MODE_F32) {
@@ -569,7 +581,7 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         shape.block = 128;
         shape.grid = (int)((plan.total + 127) / 128);
     }
-    if (records_where == MCW_RECORDS_HOST && plan.total > 0)
+    if (records_where == MCW_RECORDS_HOST && plan.total > 0 && !direct)
         CUDA_TRY(ctx, cudaMemcpyAsync(records, dev_records, (size_t)plan.total * rec_size, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(ctx, ctx->h_tallies.ensure(n_cfg * sizeof(mcw_tally)));
     CUDA_TRY(ctx, cudaMemcpyAsync(ctx->h_tallies.p, ctx->tallies.p, n_cfg * sizeof(mcw_tally), cudaMemcpyDeviceToHost, st));

@@ -190,6 +190,30 @@ def test_f32_long_walks_same_records_with_and_without_drain(walker):
     assert np.array_equal(a.records, b.records) and np.array_equal(a.tallies, b.tallies)
 
 
+def test_records_into_pinned_host_memory(walker):
+    """Pinned host buffers are written by the walk directly (no copy after the kernel);
+    their records equal those copied into pageable memory, in both modes."""
+    import ctypes
+    cfg, ice, imp = cfg2_geometry(10000)
+    walker.set_tables([ice], imp)
+    lib = _abi.load()
+    for mode, dtype in (('f32', _abi.RECORD32), ('replay64', _abi.RECORD64)):
+        n = cfg.n_photon
+        nbytes = n * dtype.itemsize
+        ptr = ctypes.c_void_p()
+        _abi.check(lib.mcw_host_alloc(nbytes, ctypes.byref(ptr)), what='host alloc')
+        try:
+            pinned = np.frombuffer((ctypes.c_char * nbytes).from_address(ptr.value), dtype=dtype, count=n)
+            pinned[:] = np.zeros(1, dtype)
+            a = walker.walk([cfg], 3, mode=mode, records='host', out=pinned)
+            b = walker.walk([cfg], 3, mode=mode)
+            assert np.array_equal(pinned, b.records)
+            assert np.array_equal(a.tallies, b.tallies)
+            assert a.stats['d2h_bytes'] == b.stats['d2h_bytes']
+        finally:
+            lib.mcw_host_free(ptr)
+
+
 def test_f32_tallies_agree_with_records(walker):
     cfg, ice, imp = cfg2_geometry(300000, depth=0.02, rds=1500.0)
     walker.set_tables([ice], imp)
