@@ -153,7 +153,7 @@ typedef struct {
     int32_t regen_chunk;   /* refill a warp once this many lanes are idle (1..32) */
     int32_t drain_below;   /* once every photon has started, a warp with at most this many
                               walking photons hands them to a queue served by whole warps,
-                              one photon each (0..32; 0 = never; default 4) */
+                              one photon each (0..32; 0 = never, the default) */
 } mcw_launch;
 
 /* Library identity.  No reference counterpart. */

@@ -101,7 +101,7 @@ struct mcw_ctx {
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
     HostBuf h_stage, h_tallies, h_counters;
     int32_t max_ice_n = 0;
-    mcw_launch launch{256, 0, 8, 4};
+    mcw_launch launch{256, 0, 8, 0};
     double budget_s = 300.0;
     uint32_t epoch = 0;   // drain-queue epoch of the last launch
 };

@@ -13,19 +13,22 @@
 //    writes the 32 records and folds the tallies with warp reductions.
 //
 // The end of a launch: once the photon supply is exhausted, the warps empty
-// out and the last, longest walks would run with a few lanes of a warp each,
-// bound by the latency of one photon's step chain.  A warp that is down to
-// WalkArgs::drain_below photons hands them over (their state packed into a
-// device queue) and then serves the queue: it walks one handed-over photon at a
-// time with the whole warp.  The 32 lanes compute the direction-independent part
-// of the photon's next 32 steps at once (Philox block, HG and Lambertian angles,
-// azimuth, optical path) and the step chain that remains (rotation, move,
-// boundaries) runs without the per-round work of the main loop.  A warp leaves
-// once every warp is past its photon loop and no slot is left for it, or after
-// kDrainIdleNs without its slot arriving; the drain kernel launched after the
-// walk takes whatever is left, so no warp ever waits on one that may not run.
-// The arithmetic of a step is the same on both paths, so records do not depend
-// on where a photon ends its walk.
+// out and the last, longest walks (a few hundred to ~1,500 events) would run
+// with a few lanes of a warp each, bound by the latency of one photon's step
+// chain.  A warp with at most kSparseWarp photons runs sparse rounds: its 32
+// lanes compute the direction-independent part of the photons' next steps at
+// once (Philox block, HG and Lambertian angles, azimuth, optical path; up to 32
+// steps of a lone photon) and each photon's lane then runs only the chain that
+// remains (rotation, move, boundaries).
+//
+// Optionally (WalkArgs::drain_below > 0) a warp that is down to drain_below
+// photons hands them over (their state packed into a device queue) and then
+// serves the queue, walking one handed-over photon at a time with the whole warp.
+// A warp leaves once every warp is past its photon loop and no slot is left for
+// it, or after kDrainIdleNs without its slot arriving; the drain kernel launched
+// after the walk takes whatever is left, so no warp ever waits on one that may not
+// run.  The arithmetic of a step is the same on every path, so records do not
+// depend on where or how a photon ends its walk.
 //
 // Per step (monte_carloMPI/monte_carlo3D.py:1212-1466, HG branch) one
 // Philox4x32-10 block keyed by (step, photon) supplies the four uniforms the
@@ -62,15 +65,28 @@ constexpr float kTwo33Inv = 1.16415321826934814e-10f; // 2^-33
 constexpr uint32_t kFlagReflect = 8u;                  // bottom reflection pending
 constexpr int kSmemCfgMax = 256;                       // configs staged in shared memory
 constexpr int kFinishCap = 64;                         // finish queue entries per warp
-constexpr int kLongWalk = 1024;                        // steps after which a walk leaves for the drain queue
+#ifndef MCW_LONG_WALK
+#define MCW_LONG_WALK 1024
+#endif
+// steps after which a walk still going once the supply is exhausted leaves for the drain queue
+constexpr int kLongWalk = MCW_LONG_WALK;
 #ifndef MCW_STEPS_PER_ROUND
 #define MCW_STEPS_PER_ROUND 4
 #endif
 // scatter events per loop round: their Philox blocks are computed together so
 // the ten dependent Philox rounds of one overlap those of the others
 constexpr int kStepsPerRound = MCW_STEPS_PER_ROUND;
-// a warp with at most this many active lanes shares the Philox work of a round
-constexpr int kSparseWarp = 32 / kStepsPerRound;
+static_assert(kStepsPerRound >= 1 && kStepsPerRound <= 32 && (kStepsPerRound & (kStepsPerRound - 1)) == 0,
+              "steps per round: a power of two");
+constexpr int kLogStepsPerRound = __builtin_ctz(kStepsPerRound);
+#ifndef MCW_SPARSE_WARP
+#define MCW_SPARSE_WARP (32 / kStepsPerRound)
+#endif
+// a warp with at most this many active lanes runs sparse rounds; each lane
+// precomputes one or two steps of them
+constexpr int kSparseWarp = MCW_SPARSE_WARP;
+constexpr int kSparseSlots = kSparseWarp * kStepsPerRound > 32 ? 64 : 32;
+static_assert(kSparseWarp >= 1 && kSparseWarp * kStepsPerRound <= 64, "sparse rounds: at most 64 steps");
 
 // Per-config values the FP32 walk reads at photon birth.
 struct CfgF32 {
@@ -155,11 +171,8 @@ struct __align__(16) FinishSlot {
 struct WarpQueues {
     BirthSlot birth[32];
     FinishSlot fin[kFinishCap];
-    uint4 rmeta[32];                          // (stream id lo, hi, step) by active rank
-    union {
-        uint4 rbuf[32][kStepsPerRound + 1];   // step blocks by active rank (padded row)
-        float4 pbuf[2 * 32];                  // drain: a photon's next 32 steps (StepPre)
-    };
+    uint4 rmeta[3 * kSparseWarp];             // sparse round: each photon's stream, step and constants
+    float4 pbuf[2 * kSparseSlots];            // sparse round and drain: StepPre of up to 64 steps
     WarpTally tally;
 };
 
@@ -350,14 +363,15 @@ struct StepPre {
     float u4;             // absorption draw (:1020), or the bottom reflectance draw
 };
 
-__device__ __forceinline__ StepPre step_pre(const uint4 r, const Photon &P) {
+// hg = (hg_a, hg_b, hg_c, hg_d) and hg_e of the photon (Photon::hg_*).
+__device__ __forceinline__ StepPre step_pre(const uint4 r, const float4 hg, const float hg_e) {
     StepPre o;
     const float u1 = u01_f32(r.x);
     const float u2 = u01_f32(r.y);
     const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
     o.dtau = -__logf(u3);
-    const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
-    o.ct_hg = (P.hg_d != 0.f) ? P.hg_e * (P.hg_a - t * t) : fmaf(-2.f, u1, 1.f);
+    const float t = __fdividef(hg.y, fmaf(hg.w, u1, hg.z));
+    o.ct_hg = (hg.w != 0.f) ? hg_e * (hg.x - t * t) : fmaf(-2.f, u1, 1.f);
     o.st_hg = sqrtf(fmaxf(0.f, fmaf(-o.ct_hg, o.ct_hg, 1.f)));
     o.ct_l = sqrtf(u1);
     o.st_l = sqrtf(fmaxf(0.f, fmaf(-o.ct_l, o.ct_l, 1.f)));
@@ -422,6 +436,72 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     P.muy = ny;
     P.muz = nz;
     P.z = zn;
+    return cond;
+}
+
+// One round of a sparse warp (at most kSparseWarp photons; the end of a launch,
+// when the last and longest walks would otherwise advance one step per lane per
+// round with most lanes idle).  The photons publish their stream, step and
+// phase-function constants; entry t (lane t, and lane t - 32 for a second pass)
+// is the direction-independent part of step k = t % S of photon t / S, where
+// S = 32 / n_act rounded down to a power of two, at least kStepsPerRound; then
+// each photon's lane runs the chain of its S steps (step_post), leaving at its end
+// condition.  S is a multiple of kStepsPerRound and rounds start at a multiple of
+// it, so renormalisation falls on the same steps as in the dense rounds and the
+// records are bit-identical.
+template <bool kImpurity>
+__device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsigned act, const int n_act,
+                                            const int lane, const unsigned lt_mask, const WalkArgs &a) {
+    // 1 <= n_act <= kSparseWarp; S = 2^ls
+    const int ls = max(kLogStepsPerRound, 5 - (32 - __clz(n_act - 1)));
+    const int S = 1 << ls;
+    const bool me = P.cfg >= 0;
+    const int rank = __popc(act & lt_mask);
+    if (me) {
+        q.rmeta[3 * rank] = make_uint4((uint32_t)P.rid, (uint32_t)(P.rid >> 32), (uint32_t)P.i, P.flags);
+        q.rmeta[3 * rank + 1] = make_uint4(__float_as_uint(P.hg_a), __float_as_uint(P.hg_b),
+                                           __float_as_uint(P.hg_c), __float_as_uint(P.hg_d));
+        q.rmeta[3 * rank + 2] = make_uint4(__float_as_uint(P.hg_e), __float_as_uint(P.p_imp), 0u, 0u);
+    }
+    __syncwarp();
+    uint64_t impm = 0;
+#pragma unroll
+    for (int pass = 0; pass < kSparseSlots / 32; ++pass) {
+        if (pass > 0 && (n_act << ls) <= 32) break;            // warp-uniform
+        const int e = lane + 32 * pass;
+        const int j = e >> ls, k = e & (S - 1);
+        bool imp_t = false;
+        if (j < n_act) {
+            const uint4 m0 = q.rmeta[3 * j], m1 = q.rmeta[3 * j + 1], m2 = q.rmeta[3 * j + 2];
+            const uint32_t n = m0.z + 1u + (uint32_t)k;
+            const uint4 r = philox10(make_uint4(n, kTagStep, m0.x, m0.y), a.keys);
+            const StepPre t = step_pre(r, make_float4(__uint_as_float(m1.x), __uint_as_float(m1.y),
+                                                      __uint_as_float(m1.z), __uint_as_float(m1.w)),
+                                       __uint_as_float(m2.x));
+            q.pbuf[2 * e] = make_float4(t.ct_hg, t.st_hg, t.ct_l, t.st_l);
+            q.pbuf[2 * e + 1] = make_float4(t.sp, t.cp, t.dtau, t.u4);
+            if (kImpurity && (m0.w & kFlagImpurity))
+                imp_t = impurity_draw(((uint64_t)m0.y << 32) | m0.x, n, __uint_as_float(m2.y), a);
+        }
+        impm |= (uint64_t)__ballot_sync(0xffffffffu, imp_t) << (32 * pass);
+    }
+    __syncwarp();
+    int cond = 0;
+    if (me) {
+        for (int k0 = 0; k0 < S && cond == 0; k0 += kStepsPerRound) {
+#pragma unroll
+            for (int u = 0; u < kStepsPerRound; ++u) {
+                const int t = (rank << ls) + k0 + u;
+                const float4 x = q.pbuf[2 * t], y = q.pbuf[2 * t + 1];
+                StepPre st;
+                st.ct_hg = x.x, st.st_hg = x.y, st.ct_l = x.z, st.st_l = x.w;
+                st.sp = y.x, st.cp = y.y, st.dtau = y.z, st.u4 = y.w;
+                cond = step_post(P, st, (impm >> t) & 1u, u == kStepsPerRound - 1);
+                if (cond != 0) break;
+            }
+        }
+    }
+    __syncwarp();
     return cond;
 }
 
@@ -602,43 +682,21 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
             if (whole) break;
         }
 
-        // ---- kStepsPerRound scatter events per active lane; their Philox blocks
-        // are independent of the walk, so they are computed together first
-        // The round's step blocks.  A well-filled warp computes them lane by lane,
-        // each lane the four its photon needs.  A sparse warp (the end of a
-        // launch, when the last walks run almost alone) shares the work: active
-        // lanes publish (stream id, step) by rank, every lane computes some of
-        // the n_act * kStepsPerRound blocks, and the chains run side by side
-        // instead of one after another.
+        // ---- kStepsPerRound scatter events per active lane of a well-filled warp;
+        // their Philox blocks are independent of the walk, so they are computed
+        // together first.  A sparse warp runs sparse_round instead.
         const unsigned act = ~idle;
         const bool me_active = P.cfg >= 0;
         const int n_act = __popc(act);
-        uint4 rb[kStepsPerRound];
-        if (n_act > kSparseWarp) {
-            if (me_active) {
-                const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
-#pragma unroll
-                for (int k = 0; k < kStepsPerRound; ++k)
-                    rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
-            }
-        } else {
-            const int rank = __popc(act & lt_mask);
-            if (me_active) q.rmeta[rank] = make_uint4((uint32_t)P.rid, (uint32_t)(P.rid >> 32), (uint32_t)P.i, 0u);
-            __syncwarp();
-            const int t = lane;  // n_act * kStepsPerRound <= 32: one block per lane at most
-            if (t < n_act * kStepsPerRound) {
-                const int j = t / kStepsPerRound, k = t % kStepsPerRound;
-                const uint4 m = q.rmeta[j];
-                q.rbuf[j][k] = philox10(make_uint4(m.z + 1u + k, kTagStep, m.x, m.y), a.keys);
-            }
-            __syncwarp();
-            if (me_active) {
-#pragma unroll
-                for (int k = 0; k < kStepsPerRound; ++k) rb[k] = q.rbuf[rank][k];
-            }
-        }
         int cond = 0;
-        if (me_active) {
+        if (n_act <= kSparseWarp) {
+            if (n_act > 0) cond = sparse_round<kImpurity>(P, q, act, n_act, lane, lt_mask, a);
+        } else if (me_active) {
+            uint4 rb[kStepsPerRound];
+            const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
+#pragma unroll
+            for (int k = 0; k < kStepsPerRound; ++k)
+                rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
 #pragma unroll
             for (int k = 0; k < kStepsPerRound; ++k) {
                 // a lane whose photon ended earlier in the round keeps its final state
@@ -734,7 +792,7 @@ __device__ __forceinline__ bool drain_walk(const float4 *slot, FinishSlot *fin, 
         // direction-independent part of steps P.i + 1 .. P.i + 32, one per lane
         const uint32_t n = (uint32_t)P.i + 1u + (uint32_t)lane;
         const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)P.rid, (uint32_t)(P.rid >> 32)), a.keys);
-        const StepPre t = step_pre(r, P);
+        const StepPre t = step_pre(r, make_float4(P.hg_a, P.hg_b, P.hg_c, P.hg_d), P.hg_e);
         __syncwarp();
         pbuf[2 * lane] = make_float4(t.ct_hg, t.st_hg, t.ct_l, t.st_l);
         pbuf[2 * lane + 1] = make_float4(t.sp, t.cp, t.dtau, t.u4);

@@ -167,6 +167,23 @@ def test_f32_records_independent_of_photon_count(walker, case):
     assert np.array_equal(small.records, big.records[:300])
 
 
+@pytest.mark.parametrize('n', [1, 2, 3, 5, 8, 12])
+def test_f32_sparse_rounds_same_records(walker, n):
+    """A launch of n photons walks them in sparse rounds (32 / n steps of each photon
+    per round, drawn across the warp's lanes; n = 12 starts in full rounds): their
+    records equal the first n of a 20,000-photon launch bit for bit, with impurities
+    (the species draw) too."""
+    for case in ('cfg2', 'imp'):
+        if case == 'cfg2':
+            cfg, ice, imp = cfg2_geometry(20000)
+        else:
+            cfg, ice, imp = _golden_case(case, 20000)
+        walker.set_tables([ice], imp)
+        big = walker.walk([cfg], 4242, mode='f32')
+        small = walker.walk([dataclasses.replace(cfg, n_photon=n)], 4242, mode='f32')
+        assert np.array_equal(small.records, big.records[:n]), case
+
+
 def test_f32_long_walks_same_records_with_and_without_drain(walker):
     """Weakly absorbing, deep snow (lambda 1.0 um, r_eff 50 um, tau ~1000: walks of
     thousands of steps): the walks that leave for the drain queue end exactly as they
