@@ -257,6 +257,45 @@ __device__ __forceinline__ void pop(Photon &P, const BirthSlot &b) {
     P.hg_e = o.hg_e;
 }
 
+// The arithmetic shared by step() and step_post().  Every product and sum is
+// rounded as written (explicit fmaf / __fmul_rn, no contraction left to the
+// compiler), so the two paths give the same bits for the same draws.
+
+// Henyey-Greenstein scattering cosine by inversion (monte_carlo3D.py:915), or
+// 1 - 2u when isotropic (hg_d == 0).
+__device__ __forceinline__ float hg_cos(const float u1, const float hg_a, const float hg_b, const float hg_c,
+                                        const float hg_d, const float hg_e) {
+    const float t = __fdividef(hg_b, fmaf(hg_d, u1, hg_c));
+    return (hg_d != 0.f) ? __fmul_rn(hg_e, fmaf(-t, t, hg_a)) : fmaf(-2.f, u1, 1.f);
+}
+
+__device__ __forceinline__ float sin_of(const float ct) { return sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f))); }
+
+// General rotation of direction m by polar cosine/sine (ct, st) and azimuth
+// (cp, sp) (monte_carlo3D.py:1270-1281), renormalised when `renorm`.
+__device__ __forceinline__ float3 rotate(const float mx, const float my, const float mz, const float ct,
+                                         const float st, const float cp, const float sp, const bool renorm) {
+    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
+    const float rs = rsqrtf(s2);
+    const float tq = __fmul_rn(st, rs);
+    float gx = fmaf(tq, fmaf(__fmul_rn(mx, mz), cp, -__fmul_rn(my, sp)), __fmul_rn(mx, ct));
+    float gy = fmaf(tq, fmaf(__fmul_rn(my, mz), cp, __fmul_rn(mx, sp)), __fmul_rn(my, ct));
+    float gz = fmaf(-__fmul_rn(__fmul_rn(s2, rs), st), cp, __fmul_rn(mz, ct));
+    if (renorm) {
+        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, __fmul_rn(gz, gz))));
+        gx = __fmul_rn(gx, inv);
+        gy = __fmul_rn(gy, inv);
+        gz = __fmul_rn(gz, inv);
+    }
+    return make_float3(gx, gy, gz);
+}
+
+// The pole case (monte_carlo3D.py:1262-1269): sg = sign of mu_z.
+__device__ __forceinline__ float3 pole_dir(const float sg, const float ct, const float st, const float cp,
+                                           const float sp) {
+    return make_float3(__fmul_rn(st, cp), __fmul_rn(__fmul_rn(sg, st), sp), __fmul_rn(sg, ct));
+}
+
 // One scatter event (monte_carlo3D.py:1213-1466) with its step block r =
 // Philox(step P.i + 1, photon) already computed.  Returns the end condition
 // (0 = still walking).  The alternatives of the reference's branches (first
@@ -277,42 +316,28 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
 
     // scattering cosine: HG inversion (isotropic when hg_d == 0), or the
     // Lambertian cos = sqrt(u) after a bottom reflection
-    const float t = __fdividef(P.hg_b, fmaf(P.hg_d, u1, P.hg_c));
-    float ct = (P.hg_d != 0.f) ? P.hg_e * (P.hg_a - t * t) : fmaf(-2.f, u1, 1.f);
+    float ct = hg_cos(u1, P.hg_a, P.hg_b, P.hg_c, P.hg_d, P.hg_e);
     if (lamb) ct = sqrtf(u1);                                   // rare: a branch, not a select
-    const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
+    const float st = sin_of(ct);
     float sp, cp;
     __sincosf(kTwoPiF * (u2 - 0.5f), &sp, &cp);
 
+    // after a bottom reflection the direction is drawn about the vertical: the
+    // pole case of mu = (0, 0, 1)
     const float mx = lamb ? 0.f : P.mux;
     const float my = lamb ? 0.f : P.muy;
     const float mz = lamb ? 1.f : P.muz;
-    // general rotation (monte_carlo3D.py:1270-1281)
-    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
-    const float rs = rsqrtf(s2);
-    const float tq = st * rs;
-    float gx = fmaf(tq, mx * mz * cp - my * sp, mx * ct);
-    float gy = fmaf(tq, my * mz * cp + mx * sp, my * ct);
-    float gz = fmaf(-(s2 * rs) * st, cp, mz * ct);
-    if (renorm) {
-        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
-        gx *= inv; gy *= inv; gz *= inv;
-    }
-    // pole (monte_carlo3D.py:1262-1269), taken for |mu_z| > 0.99999 (rare: a branch)
-    if (fabsf(mz) > 0.99999f) {
-        const float sg = copysignf(1.f, mz);
-        gx = st * cp;
-        gy = sg * st * sp;
-        gz = sg * ct;
-    }
-    const float nx = first ? mx : gx;
-    const float ny = first ? my : gy;
-    const float nz = first ? mz : gz;
+    float3 g = rotate(mx, my, mz, ct, st, cp, sp, renorm);
+    // pole, taken for |mu_z| > 0.99999 (rare: a branch)
+    if (fabsf(mz) > 0.99999f) g = pole_dir(copysignf(1.f, mz), ct, st, cp, sp);
+    const float nx = first ? mx : g.x;
+    const float ny = first ? my : g.y;
+    const float nz = first ? mz : g.z;
 
     const float z0 = P.z;
     float zn = fmaf(dtau, nz, z0);
     // path length, compensated sum
-    const float inc = dtau * P.inv_ext;
+    const float inc = __fmul_rn(dtau, P.inv_ext);
     {
         const float y = inc - P.pathc;
         const float tt = P.path + y;
@@ -332,7 +357,7 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     const bool top = zn > 0.f;                                  // :1390-1397
     const bool bot = zn < -P.tau;                               // :1399-1459
     const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
-    if (top || bot) P.path -= frac * inc;
+    if (top || bot) P.path = fmaf(-frac, inc, P.path);
     zn = bot ? -P.tau : zn;
     // r.w is the absorption draw; a step that reaches the bottom is never tested
     // for absorption (the reference's elif chain), so there it is the
@@ -370,11 +395,10 @@ __device__ __forceinline__ StepPre step_pre(const uint4 r, const float4 hg, cons
     const float u2 = u01_f32(r.y);
     const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
     o.dtau = -__logf(u3);
-    const float t = __fdividef(hg.y, fmaf(hg.w, u1, hg.z));
-    o.ct_hg = (hg.w != 0.f) ? hg_e * (hg.x - t * t) : fmaf(-2.f, u1, 1.f);
-    o.st_hg = sqrtf(fmaxf(0.f, fmaf(-o.ct_hg, o.ct_hg, 1.f)));
+    o.ct_hg = hg_cos(u1, hg.x, hg.y, hg.z, hg.w, hg_e);
+    o.st_hg = sin_of(o.ct_hg);
     o.ct_l = sqrtf(u1);
-    o.st_l = sqrtf(fmaxf(0.f, fmaf(-o.ct_l, o.ct_l, 1.f)));
+    o.st_l = sin_of(o.ct_l);
     __sincosf(kTwoPiF * (u2 - 0.5f), &o.sp, &o.cp);
     o.u4 = (float)r.w * kTwo32Inv;
     return o;
@@ -392,30 +416,20 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
     const float dtau = (first && lam_surface) ? 0.f : s.dtau;
-    const float ct = lamb ? s.ct_l : s.ct_hg;
-    const float st = lamb ? s.st_l : s.st_hg;
-    const float sp = s.sp, cp = s.cp;
-    const float mx = lamb ? 0.f : P.mux;
-    const float my = lamb ? 0.f : P.muy;
-    const float mz = lamb ? 1.f : P.muz;
-    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
-    const float rs = rsqrtf(s2);
-    const float tq = st * rs;
-    float gx = fmaf(tq, mx * mz * cp - my * sp, mx * ct);
-    float gy = fmaf(tq, my * mz * cp + mx * sp, my * ct);
-    float gz = fmaf(-(s2 * rs) * st, cp, mz * ct);
-    if (renorm) {
-        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, gz * gz)));
-        gx *= inv; gy *= inv; gz *= inv;
-    }
-    const float sg = copysignf(1.f, mz);
-    const bool pole = fabsf(mz) > 0.99999f;
-    const float nx = first ? mx : (pole ? st * cp : gx);
-    const float ny = first ? my : (pole ? sg * st * sp : gy);
-    const float nz = first ? mz : (pole ? sg * ct : gz);
+    // The HG rotation of the current direction does not wait for `lamb` (which
+    // depends on the previous step's bottom test): a Lambertian direction is the
+    // pole case of mu = (0, 0, 1) and is selected afterwards, so only that select
+    // sits on the chain between steps.  Same values as step().
+    const float3 g = rotate(P.mux, P.muy, P.muz, s.ct_hg, s.st_hg, s.cp, s.sp, renorm);
+    const float3 pd = pole_dir(copysignf(1.f, P.muz), s.ct_hg, s.st_hg, s.cp, s.sp);
+    const float3 ld = pole_dir(1.f, s.ct_l, s.st_l, s.cp, s.sp);
+    const bool pole = fabsf(P.muz) > 0.99999f;
+    const float nx = first ? P.mux : (lamb ? ld.x : (pole ? pd.x : g.x));
+    const float ny = first ? P.muy : (lamb ? ld.y : (pole ? pd.y : g.y));
+    const float nz = first ? P.muz : (lamb ? ld.z : (pole ? pd.z : g.z));
     const float z0 = P.z;
     float zn = fmaf(dtau, nz, z0);
-    const float inc = dtau * P.inv_ext;
+    const float inc = __fmul_rn(dtau, P.inv_ext);
     {
         const float y = inc - P.pathc;
         const float tt = P.path + y;
@@ -426,7 +440,7 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     const bool top = zn > 0.f;
     const bool bot = zn < -P.tau;
     const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
-    if (top || bot) P.path -= frac * inc;
+    if (top || bot) P.path = fmaf(-frac, inc, P.path);
     zn = bot ? -P.tau : zn;
     const bool refl = bot && (P.flags & kFlagLamBottom) && s.u4 < P.R;
     P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
@@ -488,17 +502,36 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
     __syncwarp();
     int cond = 0;
     if (me) {
-        for (int k0 = 0; k0 < S && cond == 0; k0 += kStepsPerRound) {
+        // groups of kStepsPerRound steps, branch-free inside a group as in the dense
+        // rounds (a lane whose photon ended keeps its final state), so one step's
+        // rotation overlaps the previous step's boundary tests
+        for (int k0 = 0; k0 < S; k0 += kStepsPerRound) {
+            const int t0 = (rank << ls) + k0;
+            float4 xs[kStepsPerRound], ys[kStepsPerRound];
 #pragma unroll
             for (int u = 0; u < kStepsPerRound; ++u) {
-                const int t = (rank << ls) + k0 + u;
-                const float4 x = q.pbuf[2 * t], y = q.pbuf[2 * t + 1];
-                StepPre st;
-                st.ct_hg = x.x, st.st_hg = x.y, st.ct_l = x.z, st.st_l = x.w;
-                st.sp = y.x, st.cp = y.y, st.dtau = y.z, st.u4 = y.w;
-                cond = step_post(P, st, (impm >> t) & 1u, u == kStepsPerRound - 1);
-                if (cond != 0) break;
+                xs[u] = q.pbuf[2 * (t0 + u)];
+                ys[u] = q.pbuf[2 * (t0 + u) + 1];
             }
+#pragma unroll
+            for (int u = 0; u < kStepsPerRound; ++u) {
+                StepPre st;
+                st.ct_hg = xs[u].x, st.st_hg = xs[u].y, st.ct_l = xs[u].z, st.st_l = xs[u].w;
+                st.sp = ys[u].x, st.cp = ys[u].y, st.dtau = ys[u].z, st.u4 = ys[u].w;
+                const bool alive = cond == 0;
+                Photon Q = P;
+                const int c = step_post(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1);
+                P.i = alive ? Q.i : P.i;
+                P.mux = alive ? Q.mux : P.mux;
+                P.muy = alive ? Q.muy : P.muy;
+                P.muz = alive ? Q.muz : P.muz;
+                P.path = alive ? Q.path : P.path;
+                P.flags = Q.flags;
+                P.z = Q.z;
+                P.pathc = Q.pathc;
+                cond = alive ? c : cond;
+            }
+            if (cond != 0) break;
         }
     }
     __syncwarp();
