@@ -261,12 +261,28 @@ __device__ __forceinline__ void pop(Photon &P, const BirthSlot &b) {
 // rounded as written (explicit fmaf / __fmul_rn, no contraction left to the
 // compiler), so the two paths give the same bits for the same draws.
 
+// Independent pairs of operations go through the packed FP32 forms
+// (__fadd2_rn, __fmul2_rn, __ffma2_rn): each lane of a pair is rounded as the
+// scalar operation would be, in one issue slot instead of two.
+
+// The step's four uniforms from its Philox block: (u1, u2) in [2^-24, 1 - 2^-24]
+// from the top 23 bits (u01_f32), u3 = (z + 1/2) 2^-32 in (0, 1), u4 = w 2^-32.
+__device__ __forceinline__ float4 step_uniforms(const uint4 r) {
+    const float2 a = __fadd2_rn(make_float2(__uint_as_float(0x3F800000u | (r.x >> 9)),
+                                            __uint_as_float(0x3F800000u | (r.y >> 9))),
+                                make_float2(-0.99999994f, -0.99999994f));
+    const float2 b = __ffma2_rn(make_float2((float)r.z, (float)r.w), make_float2(kTwo32Inv, kTwo32Inv),
+                                make_float2(kTwo33Inv, 0.f));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
 // Henyey-Greenstein scattering cosine by inversion (monte_carlo3D.py:915), or
 // 1 - 2u when isotropic (hg_d == 0).
 __device__ __forceinline__ float hg_cos(const float u1, const float hg_a, const float hg_b, const float hg_c,
                                         const float hg_d, const float hg_e) {
-    const float t = __fdividef(hg_b, fmaf(hg_d, u1, hg_c));
-    return (hg_d != 0.f) ? __fmul_rn(hg_e, fmaf(-t, t, hg_a)) : fmaf(-2.f, u1, 1.f);
+    const float2 d = __ffma2_rn(make_float2(hg_d, -2.f), make_float2(u1, u1), make_float2(hg_c, 1.f));
+    const float t = __fdividef(hg_b, d.x);
+    return (hg_d != 0.f) ? __fmul_rn(hg_e, fmaf(-t, t, hg_a)) : d.y;
 }
 
 __device__ __forceinline__ float sin_of(const float ct) { return sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f))); }
@@ -278,16 +294,19 @@ __device__ __forceinline__ float3 rotate(const float mx, const float my, const f
     const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
     const float rs = rsqrtf(s2);
     const float tq = __fmul_rn(st, rs);
-    float gx = fmaf(tq, fmaf(__fmul_rn(mx, mz), cp, -__fmul_rn(my, sp)), __fmul_rn(mx, ct));
-    float gy = fmaf(tq, fmaf(__fmul_rn(my, mz), cp, __fmul_rn(mx, sp)), __fmul_rn(my, ct));
+    // x and y as pairs: (mx mz cp - my sp, my mz cp + mx sp), then tq * that + (mx ct, my ct)
+    const float2 m = make_float2(mx, my);
+    const float2 mzp = __fmul2_rn(m, make_float2(mz, mz));
+    const float2 spp = __fmul2_rn(make_float2(-my, mx), make_float2(sp, sp));
+    const float2 in = __ffma2_rn(mzp, make_float2(cp, cp), spp);
+    float2 gxy = __ffma2_rn(make_float2(tq, tq), in, __fmul2_rn(m, make_float2(ct, ct)));
     float gz = fmaf(-__fmul_rn(__fmul_rn(s2, rs), st), cp, __fmul_rn(mz, ct));
     if (renorm) {
-        const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, __fmul_rn(gz, gz))));
-        gx = __fmul_rn(gx, inv);
-        gy = __fmul_rn(gy, inv);
+        const float inv = rsqrtf(fmaf(gxy.x, gxy.x, fmaf(gxy.y, gxy.y, __fmul_rn(gz, gz))));
+        gxy = __fmul2_rn(gxy, make_float2(inv, inv));
         gz = __fmul_rn(gz, inv);
     }
-    return make_float3(gx, gy, gz);
+    return make_float3(gxy.x, gxy.y, gz);
 }
 
 // The pole case (monte_carlo3D.py:1262-1269): sg = sign of mu_z.
@@ -305,9 +324,8 @@ __device__ __forceinline__ float3 pole_dir(const float sg, const float ct, const
 template <bool kImpurity>
 __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm) {
     P.i += 1;
-    const float u1 = u01_f32(r.x);
-    const float u2 = u01_f32(r.y);
-    const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
+    const float4 uu = step_uniforms(r);
+    const float u1 = uu.x, u2 = uu.y, u3 = uu.z;
     const bool first = (P.i == 1);
     const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
@@ -335,9 +353,11 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     const float nz = first ? mz : g.z;
 
     const float z0 = P.z;
-    float zn = fmaf(dtau, nz, z0);
+    // zn = dtau nz + z0 and the path increment dtau / (ext rho) as one pair
+    const float2 zi = __ffma2_rn(make_float2(dtau, dtau), make_float2(nz, P.inv_ext), make_float2(z0, 0.f));
+    float zn = zi.x;
     // path length, compensated sum
-    const float inc = __fmul_rn(dtau, P.inv_ext);
+    const float inc = zi.y;
     {
         const float y = inc - P.pathc;
         const float tt = P.path + y;
@@ -356,13 +376,14 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
 
     const bool top = zn > 0.f;                                  // :1390-1397
     const bool bot = zn < -P.tau;                               // :1399-1459
-    const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
+    const float2 fd = __fadd2_rn(make_float2(zn, zn), make_float2(P.tau, -z0));
+    const float frac = __fdividef(top ? zn : fd.x, fd.y);
     if (top || bot) P.path = fmaf(-frac, inc, P.path);
     zn = bot ? -P.tau : zn;
     // r.w is the absorption draw; a step that reaches the bottom is never tested
     // for absorption (the reference's elif chain), so there it is the
     // Lambertian-bottom reflectance draw (:1422, :1453)
-    const float u4 = (float)r.w * kTwo32Inv;
+    const float u4 = uu.w;
     const bool refl = bot && (P.flags & kFlagLamBottom) && u4 < P.R;
     P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
     const bool absorb = u4 < coalb;                             // :1461-1466
@@ -391,16 +412,15 @@ struct StepPre {
 // hg = (hg_a, hg_b, hg_c, hg_d) and hg_e of the photon (Photon::hg_*).
 __device__ __forceinline__ StepPre step_pre(const uint4 r, const float4 hg, const float hg_e) {
     StepPre o;
-    const float u1 = u01_f32(r.x);
-    const float u2 = u01_f32(r.y);
-    const float u3 = fmaf((float)r.z, kTwo32Inv, kTwo33Inv);
+    const float4 uu = step_uniforms(r);
+    const float u1 = uu.x, u2 = uu.y, u3 = uu.z;
     o.dtau = -__logf(u3);
     o.ct_hg = hg_cos(u1, hg.x, hg.y, hg.z, hg.w, hg_e);
     o.st_hg = sin_of(o.ct_hg);
     o.ct_l = sqrtf(u1);
     o.st_l = sin_of(o.ct_l);
     __sincosf(kTwoPiF * (u2 - 0.5f), &o.sp, &o.cp);
-    o.u4 = (float)r.w * kTwo32Inv;
+    o.u4 = uu.w;
     return o;
 }
 
@@ -428,8 +448,9 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     const float ny = first ? P.muy : (lamb ? ld.y : (pole ? pd.y : g.y));
     const float nz = first ? P.muz : (lamb ? ld.z : (pole ? pd.z : g.z));
     const float z0 = P.z;
-    float zn = fmaf(dtau, nz, z0);
-    const float inc = __fmul_rn(dtau, P.inv_ext);
+    const float2 zi = __ffma2_rn(make_float2(dtau, dtau), make_float2(nz, P.inv_ext), make_float2(z0, 0.f));
+    float zn = zi.x;
+    const float inc = zi.y;
     {
         const float y = inc - P.pathc;
         const float tt = P.path + y;
@@ -439,7 +460,8 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     const float coalb = imp ? P.coalb_imp : P.coalb_ice;       // 1 - R on a Lambertian surface
     const bool top = zn > 0.f;
     const bool bot = zn < -P.tau;
-    const float frac = __fdividef(top ? zn : zn + P.tau, zn - z0);
+    const float2 fd = __fadd2_rn(make_float2(zn, zn), make_float2(P.tau, -z0));
+    const float frac = __fdividef(top ? zn : fd.x, fd.y);
     if (top || bot) P.path = fmaf(-frac, inc, P.path);
     zn = bot ? -P.tau : zn;
     const bool refl = bot && (P.flags & kFlagLamBottom) && s.u4 < P.R;
