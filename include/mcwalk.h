@@ -52,8 +52,12 @@ extern "C" {
 typedef struct mcw_ctx mcw_ctx;
 typedef struct mcw_graph mcw_graph;
 
+/* Units of mcw_ssp_table.wvl. */
+#define MCW_WVL_METRES 0  /* the netCDF tables (monte_carlo3D.py:511-514, :666-671) */
+#define MCW_WVL_MICRONS 1 /* the aspherical isca.dat rows (monte_carlo3D.py:215-236) */
+
 /* One SSP table in the reference's netCDF layout (monte_carlo3D.py:511-514):
- * wvl in metres (ascending), ss_alb, ext_cff_mss [m^2/kg], asm_prm (NULL for
+ * wvl (distinct; any order), ss_alb, ext_cff_mss [m^2/kg], asm_prm (NULL for
  * an impurity table).  Copied into device memory by mcw_set_tables. */
 typedef struct {
     const double *wvl;
@@ -61,7 +65,8 @@ typedef struct {
     const double *ext_cff_mss;
     const double *asm_prm;
     int32_t n;
-    int32_t reserved;
+    int32_t wvl_unit;      /* MCW_WVL_METRES or MCW_WVL_MICRONS; wavelengths are compared
+                              in this unit, as the reference compares them */
 } mcw_ssp_table;
 
 /* One run of MonteCarlo.run (monte_carlo3D.py:1492-1496) plus the model
@@ -80,7 +85,11 @@ typedef struct {
     int32_t lambertian_surface;
     int32_t lambertian_bottom;
     int32_t ice_table;             /* index into the ice tables of mcw_set_tables */
-    int32_t reserved;
+    int32_t ssp_nearest;           /* 0: the two nearest ice-table points, interpolated
+                                      (spheres, monte_carlo3D.py:594-616); 1: the nearest
+                                      point, and the photon's wavelength becomes that
+                                      point's (HG-forced aspherical particles,
+                                      :323-415, :1528-1545) */
     /* run(test=True) overrides (monte_carlo3D.py:1553-1573); NaN = use table */
     double ssa_ice_override;
     double g_override;

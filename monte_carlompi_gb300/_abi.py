@@ -41,7 +41,7 @@ class BudgetExceeded(McwError):
 class SSPTableC(ctypes.Structure):
     _fields_ = [('wvl', ctypes.c_void_p), ('ss_alb', ctypes.c_void_p),
                 ('ext_cff_mss', ctypes.c_void_p), ('asm_prm', ctypes.c_void_p),
-                ('n', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+                ('n', ctypes.c_int32), ('wvl_unit', ctypes.c_int32)]
 
 
 class ConfigC(ctypes.Structure):
@@ -52,7 +52,7 @@ class ConfigC(ctypes.Structure):
                 ('rho_snw', ctypes.c_double), ('rho_ice', ctypes.c_double),
                 ('lambertian_reflectance', ctypes.c_double),
                 ('lambertian_surface', ctypes.c_int32), ('lambertian_bottom', ctypes.c_int32),
-                ('ice_table', ctypes.c_int32), ('reserved', ctypes.c_int32),
+                ('ice_table', ctypes.c_int32), ('ssp_nearest', ctypes.c_int32),
                 ('ssa_ice_override', ctypes.c_double), ('g_override', ctypes.c_double),
                 ('ext_ice_override', ctypes.c_double), ('ssa_imp_override', ctypes.c_double),
                 ('ext_imp_override', ctypes.c_double)]

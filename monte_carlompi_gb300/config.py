@@ -60,6 +60,7 @@ class WalkConfig:
     ssa_imp_override: float = math.nan
     ext_imp_override: float = math.nan
     first_photon: int = 0            # first photon index (a shard of a larger run)
+    ssp_nearest: bool = False        # HG-forced aspherical lookup: nearest table point, wavelength replaced
     rds_snw: float = field(default=math.nan)  # grain size [um], bookkeeping (selects the table)
 
     def to_c(self):
@@ -67,7 +68,8 @@ class WalkConfig:
                             float(self.theta0_deg), float(self.tau_tot), float(self.imp_cnc),
                             float(self.rho_snw), float(self.rho_ice),
                             float(self.lambertian_reflectance), int(bool(self.lambertian_surface)),
-                            int(bool(self.lambertian_bottom)), int(self.ice_table), 0,
+                            int(bool(self.lambertian_bottom)), int(self.ice_table),
+                            int(bool(self.ssp_nearest)),
                             float(self.ssa_ice_override), float(self.g_override),
                             float(self.ext_ice_override), float(self.ssa_imp_override),
                             float(self.ext_imp_override))

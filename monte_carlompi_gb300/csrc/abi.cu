@@ -157,6 +157,7 @@ const char *check_config(const mcw_config &c, int32_t n_ice) {
     if (!std::isfinite(c.lambertian_reflectance) || c.lambertian_reflectance < 0 || c.lambertian_reflectance > 1)
         return "lambertian_reflectance must be in [0, 1]";
     if (c.ice_table < 0 || c.ice_table >= n_ice) return "ice_table out of range";
+    if (c.ssp_nearest != 0 && c.ssp_nearest != 1) return "ssp_nearest must be 0 or 1";
     if (!std::isnan(c.ssa_ice_override) && !(c.ssa_ice_override >= 0 && c.ssa_ice_override <= 1)) return "ssa_ice_override must be in [0, 1]";
     if (!std::isnan(c.ssa_imp_override) && !(c.ssa_imp_override >= 0 && c.ssa_imp_override <= 1)) return "ssa_imp_override must be in [0, 1]";
     if (!std::isnan(c.g_override) && !(c.g_override > -1 && c.g_override < 1)) return "g_override must be in (-1, 1)";
@@ -201,7 +202,7 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
         d.lut_off = lut_off;
         lut_off += d.lut_n;
         d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
-                  (c.imp_cnc > 0 ? kFlagImpurity : 0u);
+                  (c.imp_cnc > 0 ? kFlagImpurity : 0u) | (c.ssp_nearest ? kFlagNearest : 0u);
         d.ice_table = c.ice_table;
         if (c.imp_cnc > 0) plan.impurity = true;
         const double theta0 = (kPi * c.theta0_deg) / 180.;  // monte_carlo3D.py:1508
@@ -405,6 +406,8 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     if (!ice || n_ice <= 0 || !imp) return set_err(ctx, MCW_ERR_ARG, "need >= 1 ice table and an impurity table");
     auto check = [](const mcw_ssp_table &t, bool need_asm) -> const char * {
         if (t.n < 2) return "a table needs at least 2 wavelengths";
+        if (t.wvl_unit != MCW_WVL_METRES && t.wvl_unit != MCW_WVL_MICRONS)
+            return "wvl_unit must be MCW_WVL_METRES or MCW_WVL_MICRONS";
         if (!t.wvl || !t.ss_alb || !t.ext_cff_mss || (need_asm && !t.asm_prm)) return "missing table column";
         for (int32_t i = 0; i < t.n; ++i) {
             if (!std::isfinite(t.wvl[i]) || !std::isfinite(t.ss_alb[i]) || !std::isfinite(t.ext_cff_mss[i]))
@@ -467,7 +470,7 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
         d.ext = dbase + o + 2 * n;
         d.asm_ = dbase + o + 3 * n;
         d.n = n;
-        d.pad = 0;
+        d.unit = t.wvl_unit;
         o += 4 * (size_t)n;
     };
     for (int32_t i = 0; i < n_ice; ++i) put(ice[i], tabs[i]);

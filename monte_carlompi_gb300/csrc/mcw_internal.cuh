@@ -22,6 +22,7 @@ constexpr uint32_t kStatusStream = 2u;
 constexpr uint32_t kFlagLamSurface = 1u;
 constexpr uint32_t kFlagLamBottom = 2u;
 constexpr uint32_t kFlagImpurity = 4u;  // imp_cnc > 0: the species draw matters
+constexpr uint32_t kFlagNearest = 16u;  // ssp_nearest: nearest ice-table point, wavelength replaced
 
 constexpr double kPi = 3.141592653589793;
 constexpr double kTwoPi = 6.283185307179586;  // 2*np.pi (monte_carlo3D.py:26)
@@ -30,7 +31,7 @@ constexpr double kTwoPi = 6.283185307179586;  // 2*np.pi (monte_carlo3D.py:26)
 struct DevTable {
     const double *wvl, *ssa, *ext, *asm_;
     int32_t n;
-    int32_t pad;
+    int32_t unit;        // MCW_WVL_METRES or MCW_WVL_MICRONS
 };
 
 // Per-config launch data computed on the host from mcw_config.

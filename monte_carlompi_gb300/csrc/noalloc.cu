@@ -90,7 +90,8 @@ int scratch_for_device(int dev, NoAllocScratch **out) {
 }
 
 bool table_ok(const mcw_ssp_table *t, bool need_asm) {
-    return t && t->n >= 2 && t->wvl && t->ss_alb && t->ext_cff_mss && (!need_asm || t->asm_prm);
+    return t && t->n >= 2 && t->wvl && t->ss_alb && t->ext_cff_mss && (!need_asm || t->asm_prm) &&
+           (t->wvl_unit == MCW_WVL_METRES || t->wvl_unit == MCW_WVL_MICRONS);
 }
 
 }  // namespace
@@ -129,7 +130,7 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     d.lut_n = (int32_t)(khi - klo + 1);
     d.k_lo = (int32_t)klo;
     d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
-              (c.imp_cnc > 0 ? kFlagImpurity : 0u);
+              (c.imp_cnc > 0 ? kFlagImpurity : 0u) | (c.ssp_nearest ? kFlagNearest : 0u);
     d.ice_table = 0;
     const double theta0 = (kPi * c.theta0_deg) / 180.;
     d.wvl0_100 = (float)(c.wvl0 * 100.0);
@@ -152,8 +153,8 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     d.ov_ext_ice = c.ext_ice_override;
     d.ov_ssa_imp = c.ssa_imp_override;
     d.ov_ext_imp = c.ext_imp_override;
-    DevTable ice{ice_dev->wvl, ice_dev->ss_alb, ice_dev->ext_cff_mss, ice_dev->asm_prm, ice_dev->n, 0};
-    DevTable imp{imp_dev->wvl, imp_dev->ss_alb, imp_dev->ext_cff_mss, imp_dev->asm_prm, imp_dev->n, 0};
+    DevTable ice{ice_dev->wvl, ice_dev->ss_alb, ice_dev->ext_cff_mss, ice_dev->asm_prm, ice_dev->n, ice_dev->wvl_unit};
+    DevTable imp{imp_dev->wvl, imp_dev->ss_alb, imp_dev->ext_cff_mss, imp_dev->asm_prm, imp_dev->n, imp_dev->wvl_unit};
 
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCW_ERR_CUDA;

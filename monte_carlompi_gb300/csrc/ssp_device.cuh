@@ -6,7 +6,7 @@
 
 namespace mcw {
 
-// The two table points nearest to w (metres); ties keep the lower index.
+// The two table points nearest to w (in the table's unit); ties keep the lower index.
 // monte_carlo3D.py:594-597 (argsort of |wvl - wvl_in|, first two).  Tables are
 // strictly increasing (mcw_set_tables sorts and checks them), so the two
 // nearest points are among the two on either side of w: a binary search finds
@@ -44,18 +44,37 @@ __device__ inline double ssp_interp_two(const DevTable &t, const double *y, int 
 }
 
 struct Optics {
+    double wvl_um;   // the photon's wavelength: its drawn one, or the nearest table point's (ssp_nearest)
     double ssa_ice, ssa_imp, g, ext_cff_mss, p_imp, snow_depth;
 };
 
-// Per-photon optics at wavelength wvl_um: monte_carlo3D.py:1524-1612.
+// A wavelength in um in the table's unit: wvl * 1e-6 for the netCDF tables
+// (monte_carlo3D.py:518, :673), as is for the aspherical rows (:323-334).
+__device__ inline double in_table_unit(const DevTable &t, double wvl_um) {
+    return t.unit == MCW_WVL_MICRONS ? wvl_um : wvl_um * 1e-6;
+}
+
+// Per-photon optics at wavelength wvl_um: monte_carlo3D.py:1524-1612.  With
+// ssp_nearest (HG-forced aspherical particles) the ice properties are those of
+// the nearest table point and the photon carries that point's wavelength from
+// then on: the impurity lookup and wvn use it (:323-334, :396-415, :1534-1549).
 __device__ inline Optics photon_optics(const DevConfig &c, const DevTable &ice, const DevTable &imp,
                                        double wvl_um) {
-    double w = wvl_um * 1e-6;
+    double w = in_table_unit(ice, wvl_um);
     int i0, i1;
     ssp_nearest_two(ice, w, i0, i1);
-    double ssa_ice = ssp_interp_two(ice, ice.ssa, i0, i1, w);
-    double ext_ice = ssp_interp_two(ice, ice.ext, i0, i1, w);
-    double g = ssp_interp_two(ice, ice.asm_, i0, i1, w);
+    double ssa_ice, ext_ice, g;
+    if (c.flags & kFlagNearest) {
+        ssa_ice = ice.ssa[i0];
+        ext_ice = ice.ext[i0];
+        g = ice.asm_[i0];
+        wvl_um = ice.unit == MCW_WVL_MICRONS ? ice.wvl[i0] : ice.wvl[i0] * 1e6;
+    } else {
+        ssa_ice = ssp_interp_two(ice, ice.ssa, i0, i1, w);
+        ext_ice = ssp_interp_two(ice, ice.ext, i0, i1, w);
+        g = ssp_interp_two(ice, ice.asm_, i0, i1, w);
+    }
+    w = in_table_unit(imp, wvl_um);
     ssp_nearest_two(imp, w, i0, i1);
     double ssa_imp = ssp_interp_two(imp, imp.ssa, i0, i1, w);
     double ext_imp = ssp_interp_two(imp, imp.ext, i0, i1, w);
@@ -66,6 +85,7 @@ __device__ inline Optics photon_optics(const DevConfig &c, const DevTable &ice, 
     if (!isnan(c.ov_ext_imp)) ext_imp = c.ov_ext_imp;
     double cnc = c.imp_cnc;
     Optics o;
+    o.wvl_um = wvl_um;
     o.ssa_ice = ssa_ice;
     o.ssa_imp = ssa_imp;
     o.g = g;

@@ -42,7 +42,7 @@ __global__ void lut_kernel(const LutArgs a) {
         const int k = c.k_lo + j;
         const double wvl = (double)k / 100.0;
         const Optics o = photon_optics(c, ice, imp, wvl);
-        const double wvn = 1.0 / wvl;
+        const double wvn = 1.0 / o.wvl_um;
         LutEntry L;
         L.wvn = (float)wvn;
         L.coalb_ice = (float)(1.0 - o.ssa_ice);

@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(128) walk_replay_kernel(const ReplayArgs a) {
     mcw_record64 r;
     r.condition = condition;
     r.n_scat = (int32_t)(i - 1);                                      // :1487
-    r.wvn = 1. / wvl;                                                 // :1468
+    r.wvn = 1. / o.wvl_um;                                            // :1468
     r.theta_n = acos(muz_0);                                          // :1469
     r.flags = 0;
     if (i == 1) r.phi_n = 0.;                                         // :1472-1485

@@ -17,9 +17,12 @@ HEADER = 'condition wvn[um^-1] theta_n phi_n n_scat path_length[m], snow_depth[m
 COLUMNS = ['condition', 'wvn', 'theta_n', 'phi_n', 'n_scat', 'path_length', 'snow_depth']
 
 
-def output_path(output_dir, wvl0, half_width, rds_snw, n_photon, theta0_deg, make_dirs=True):
-    """Free output file name, as setup_output builds it."""
-    save_dir = os.path.join(output_dir, 'sphere')
+def output_path(output_dir, wvl0, half_width, rds_snw, n_photon, theta0_deg, make_dirs=True,
+                subdir=('sphere',)):
+    """Free output file name, as setup_output builds it (monte_carlo3D.py:96-143):
+    under output_dir/sphere, or output_dir/<shape dir>/<roughness dir> for an
+    aspherical run, with rds_snw the effective radius of the particles walked."""
+    save_dir = os.path.join(output_dir, *subdir)
     if make_dirs:
         os.makedirs(save_dir, exist_ok=True)
     stem = '%s_%s_%s_%s_%s_%s' % (wvl0, half_width, rds_snw, n_photon, theta0_deg, 'HG')

@@ -20,9 +20,16 @@ Extra keyword arguments (not in the reference): ``device`` (CUDA device),
 they are missing, 'file' requires them, 'synthetic' never reads them) and
 ``write_csv`` (False skips the file).
 
-Not available (raise): non-sphere shapes and polarised Stokes input (the
-Yang et al. 2013 data are not part of the reference archive), ``debug`` and
-``phase_functions`` (matplotlib figures).
+Non-spherical shapes run on the Henyey-Greenstein path when ``HG=True``
+(get_aspherical_SSPs, monte_carlo3D.py:173-256, :313-415): the particle size
+of ``<optics_dir>/ice_optics/<band>/<shape>/<roughness>/isca.dat`` whose
+effective radius is nearest to ``rds_snw``, each photon's wavelength moved to the
+nearest tabulated one, no interpolation; the CSV goes under
+``output_dir/<shape>/<roughness>/`` named with that effective radius.
+
+Not available (raise): non-sphere shapes without HG and polarised Stokes input
+(they need the Yang et al. 2013 phase matrices, which are not part of the
+reference archive), ``debug`` and ``phase_functions`` (matplotlib figures).
 """
 import math
 import os
@@ -60,6 +67,13 @@ class MonteCarlo(object):
         self.output_file = None
 
     # -- SSP tables (get_optical_properties :498-514, get_impurity_optics :661-671)
+    def _imp_table(self, wvl0, half_width):
+        imp_path = os.path.join(self.optics_dir, 'mie', 'snicar', self.fi_imp)
+        if self.ssp_source == 'file' or (self.ssp_source == 'auto' and os.path.exists(imp_path)):
+            return ssp.read_netcdf(imp_path)
+        lo, hi = ssp.grid_for(wvl0, half_width)
+        return ssp.synthetic_impurity_table(lo, hi)
+
     def _tables(self, wvl0, half_width, rds_snw):
         base = os.path.join(self.optics_dir, 'mie', 'snicar')
         ice_path = os.path.join(base, ssp.ice_file_name(rds_snw))
@@ -98,9 +112,8 @@ class MonteCarlo(object):
         """Walk n_photon photons and write the per-photon CSV.  ALL VALUES IN MICRONS."""
         if shape != 'sphere' and not self.HG:
             raise NotImplementedError('only the Henyey-Greenstein path is built: shape=%r needs '
-                                      'the Yang et al. (2013) phase matrices' % shape)
-        if shape != 'sphere':
-            raise NotImplementedError('aspherical SSP tables are not available')
+                                      'the Yang et al. (2013) phase matrices (pass HG=True for '
+                                      'the HG-forced aspherical path)' % shape)
         if not np.array_equal(np.asarray(stokes_params), [1, 0, 0, 0]):
             raise NotImplementedError('HG mode carries the Stokes vector [1, 0, 0, 0] only')
         if debug:
@@ -116,7 +129,16 @@ class MonteCarlo(object):
         self.wvl0 = wvl0
         self.snow_effective_radius = rds_snw
 
-        ice, imp = self._tables(wvl0, half_width, rds_snw)
+        if shape == 'sphere':
+            ice, imp = self._tables(wvl0, half_width, rds_snw)
+            subdir = ('sphere',)
+        else:
+            path = ssp.isca_path(self.optics_dir, shape, roughness, wvl0)
+            ice, self.snow_effective_radius = ssp.aspherical_table(path, wvl0, rds_snw, self.rho_ice)
+            imp = self._imp_table(wvl0, half_width)
+            self.shape_dir = ssp.SHAPE_DIRS[shape]
+            self.roughness_dir = ssp.ROUGHNESS_DIRS[roughness]
+            subdir = (self.shape_dir, self.roughness_dir)
         w = self.walker()
         w.set_tables([ice], imp)
         cfg = WalkConfig(n_photon=int(n_photon), wvl0=float(wvl0), half_width=float(half_width),
@@ -125,7 +147,8 @@ class MonteCarlo(object):
                          rho_ice=float(self.rho_ice),
                          lambertian_reflectance=float(Lambertian_reflectance),
                          lambertian_surface=bool(Lambertian_surface),
-                         lambertian_bottom=bool(Lambertian_bottom), rds_snw=float(rds_snw),
+                         lambertian_bottom=bool(Lambertian_bottom),
+                         rds_snw=float(self.snow_effective_radius), ssp_nearest=shape != 'sphere',
                          **self._overrides(test))
         seed = self.seed
         if seed is None:
@@ -134,8 +157,8 @@ class MonteCarlo(object):
         res = w.walk([cfg], seed, mode=self.mode, records='host')
         self.records, self.tallies, self.stats = res.records, res.tallies, res.stats
         if self.write_csv:
-            path = csv_io.output_path(self.output_dir, wvl0, half_width, rds_snw, n_photon,
-                                      csv_io.theta0_label(theta_0))
+            path = csv_io.output_path(self.output_dir, wvl0, half_width, self.snow_effective_radius,
+                                      n_photon, csv_io.theta0_label(theta_0), subdir=subdir)
             csv_io.write_csv(path, res.records)
             self.output_file = path
             print('%s' % path)

@@ -32,13 +32,18 @@ IMP_SSA = 0.30
 IMP_EXT = 12000.0
 
 
+WVL_METRES = 0    # netCDF tables
+WVL_MICRONS = 1   # aspherical isca.dat rows
+
+
 @dataclass
 class SSPTable:
     """One SSP table, as the reference's netCDF variables hold it."""
-    wvl: np.ndarray          # metres, ascending
+    wvl: np.ndarray          # metres (wvl_unit WVL_METRES) or um (WVL_MICRONS), ascending
     ss_alb: np.ndarray
     ext_cff_mss: np.ndarray  # m^2/kg
     asm_prm: np.ndarray      # zeros for an impurity table
+    wvl_unit: int = WVL_METRES
 
     def __post_init__(self):
         self.wvl = np.ascontiguousarray(self.wvl, dtype=np.float64)
@@ -149,3 +154,103 @@ def load_tables(optics_dir, rds_snw, fi_imp):
     ice = read_netcdf(os.path.join(base, ice_file_name(rds_snw)))
     imp = read_netcdf(os.path.join(base, fi_imp))
     return ice, imp
+
+
+# ---------------------------------------------------------------- aspherical particles
+# The Yang et al. (2013) database the reference reads for non-spherical grains
+# (get_aspherical_SSPs, monte_carlo3D.py:173-256): one text file per shape and
+# roughness, <optics_dir>/ice_optics/<band>/<shape>/<roughness>/isca.dat.  The
+# data are not part of the reference archive; the HG-forced path (run(shape=...)
+# with HG=True) needs only isca.dat, so tests write synthetic ones.
+
+SHAPE_DIRS = {  # monte_carlo3D.py:185-202
+    'solid hexagonal column': 'solid_column',
+    'hexagonal plate': 'plate',
+    'hollow hexagonal column': 'hollow_column',
+    'droxtal': 'droxtal',
+    'hollow bullet rosette': 'hollow_bullet_rosette',
+    'solid bullet rosette': 'solid_bullet_rosette',
+    '8-element column aggregate': 'column_8elements',
+    '5-element plate aggregate': 'plate_5elements',
+    '10-element plate aggregate': 'plate_10elements',
+}
+ROUGHNESS_DIRS = {'smooth': 'Rough000', 'moderately rough': 'Rough003',  # :206-211
+                  'severely rough': 'Rough050'}
+
+
+def isca_path(optics_dir, shape, roughness, wvl0):
+    """Path of the isca.dat the reference opens for this shape, roughness and
+    centre wavelength (the 0.2-15.25 um or 16.4-99.0 um band, :180-183, :1528-1545)."""
+    if shape not in SHAPE_DIRS:
+        raise ValueError('unknown shape %r' % (shape,))
+    if roughness not in ROUGHNESS_DIRS:
+        raise ValueError('unknown roughness %r' % (roughness,))
+    if 0.2 <= wvl0 <= 15.25:
+        band = '0.2-15.25'
+    elif 16.4 <= wvl0 <= 99.0:
+        band = '16.4-99.0'
+    else:
+        raise ValueError('wvl0 = %r um lies in neither band of the aspherical database' % (wvl0,))
+    return os.path.join(optics_dir, 'ice_optics', band, SHAPE_DIRS[shape], ROUGHNESS_DIRS[roughness],
+                        'isca.dat')
+
+
+def read_isca(path):
+    """Columns of isca.dat as float64 (monte_carlo3D.py:220-245): wavelength [um],
+    maximum dimension [um], particle volume [um^3], projected area G [um^2], Q_ext,
+    single-scattering albedo, asymmetry factor.  Parsed field by field with float(),
+    as the reference does."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            v = line.split()
+            rows.append([float(v[k]) for k in range(7)])
+    return np.array(rows, dtype=np.float64).reshape(-1, 7)
+
+
+def aspherical_table(path, wvl0, rds_snw, rho_ice=917.0):
+    """The HG-forced aspherical lookup table of get_aspherical_SSPs (monte_carlo3D.py:
+    248-264, :396-415): the rows of the particle size whose effective radius
+    RE = 3/4 V / G at wvl0 is nearest to rds_snw (wvl0 must be one of the file's
+    wavelengths, as the reference requires), with ext_cff_mss = 1e6 G Q_ext /
+    (rho_ice V) [m^2/kg], sorted by wavelength, in micrometres.  Walk it with
+    WalkConfig(ssp_nearest=True).  Returns (table, RE)."""
+    a = read_isca(path)
+    wvl, vol, G, qext, ssa, asm = a[:, 0], a[:, 2], a[:, 3], a[:, 4], a[:, 5], a[:, 6]
+    at0 = np.where(wvl == wvl0)[0]
+    if at0.size == 0:
+        raise ValueError('wvl0 = %r um is not a wavelength of %s' % (wvl0, path))
+    re = (3. / 4.) * (vol / G)
+    re_sel = re[at0][np.argsort(np.absolute(rds_snw - re[at0]))[0]]
+    rows = np.where(re == re_sel)[0]
+    ext = (1e6 * G[rows] * qext[rows]) / (rho_ice * vol[rows])
+    order = np.argsort(wvl[rows], kind='stable')
+    w = wvl[rows][order]
+    if np.any(np.diff(w) <= 0):
+        raise ValueError('%s: repeated wavelength for RE = %r um' % (path, re_sel))
+    return SSPTable(w, ssa[rows][order], ext[order], asm[rows][order], wvl_unit=WVL_MICRONS), float(re_sel)
+
+
+def synthetic_isca_rows(wvls_um, re_um):
+    """Synthetic isca.dat rows (for tests and fixtures): for every effective radius RE
+    and wavelength, a particle with G = pi (1.25 RE)^2 and V = 4/3 RE G (so
+    3/4 V / G = RE), Q_ext = 2 + 0.05 sin(lambda), the sphere co-albedo formula and
+    g = 0.78 + 0.02 (lambda - 1)."""
+    out = []
+    for r in re_um:
+        dmax = 2.5 * r
+        G = math.pi * (1.25 * r) ** 2
+        V = (4. / 3.) * r * G
+        for w in wvls_um:
+            q = 2.0 + 0.05 * math.sin(w)
+            co = min(1e-4 * 100.0 ** ((w - 1.2) / 0.4) * (r / 100.0), CO_ALBEDO_CAP)
+            out.append((w, dmax, V, G, q, 1.0 - co, 0.78 + 0.02 * (w - 1.0)))
+    return out
+
+
+def write_isca(path, rows):
+    """Write isca.dat rows (wavelength printed with 4 decimals, the rest as repr)."""
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, 'w') as f:
+        for r in rows:
+            f.write('%.4f %r %r %r %r %r %r\n' % tuple(float(x) for x in r))

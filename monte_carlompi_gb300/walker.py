@@ -19,7 +19,7 @@ def _table_c(t, keep):
             np.ascontiguousarray(t.ext_cff_mss, np.float64), np.ascontiguousarray(t.asm_prm, np.float64)]
     keep.extend(cols)
     return _abi.SSPTableC(cols[0].ctypes.data, cols[1].ctypes.data, cols[2].ctypes.data,
-                          cols[3].ctypes.data, cols[0].size, 0)
+                          cols[3].ctypes.data, cols[0].size, int(getattr(t, 'wvl_unit', 0)))
 
 
 @dataclass

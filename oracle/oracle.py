@@ -21,7 +21,7 @@ RECORD_DTYPE = np.dtype([
 
 class Table(ctypes.Structure):
     _fields_ = [('wvl', ctypes.c_void_p), ('ssa', ctypes.c_void_p), ('ext', ctypes.c_void_p),
-                ('asm_', ctypes.c_void_p), ('n', ctypes.c_int32)]
+                ('asm_', ctypes.c_void_p), ('n', ctypes.c_int32), ('unit', ctypes.c_int32)]
 
 
 class Config(ctypes.Structure):
@@ -32,7 +32,8 @@ class Config(ctypes.Structure):
                 ('lam_surface', ctypes.c_int32), ('lam_bottom', ctypes.c_int32),
                 ('R', ctypes.c_double), ('ssa_ice_override', ctypes.c_double),
                 ('g_override', ctypes.c_double), ('ext_ice_override', ctypes.c_double),
-                ('ssa_imp_override', ctypes.c_double), ('ext_imp_override', ctypes.c_double)]
+                ('ssa_imp_override', ctypes.c_double), ('ext_imp_override', ctypes.c_double),
+                ('nearest', ctypes.c_int32), ('pad', ctypes.c_int32)]
 
 
 def build():
@@ -86,7 +87,7 @@ class _Tables:
                     np.ascontiguousarray(t.asm_prm, dtype=np.float64)]
             self.arrays.extend(cols)
             return Table(cols[0].ctypes.data, cols[1].ctypes.data, cols[2].ctypes.data,
-                         cols[3].ctypes.data, cols[0].size)
+                         cols[3].ctypes.data, cols[0].size, int(getattr(t, 'wvl_unit', 0)))
         self.ice = mk(ice)
         self.imp = mk(imp)
 
@@ -94,10 +95,11 @@ class _Tables:
 def make_config(n_photon, wvl0, half_width, theta0_deg, tau_tot, imp_cnc=0.0, rho_snw=300.0,
                 rho_ice=917.0, lam_surface=False, lam_bottom=True, R=1.0,
                 ssa_ice_override=np.nan, g_override=np.nan, ext_ice_override=np.nan,
-                ssa_imp_override=np.nan, ext_imp_override=np.nan):
+                ssa_imp_override=np.nan, ext_imp_override=np.nan, nearest=False):
     return Config(int(n_photon), wvl0, half_width, theta0_deg, tau_tot, imp_cnc, rho_snw, rho_ice,
                   int(bool(lam_surface)), int(bool(lam_bottom)), R, ssa_ice_override,
-                  g_override, ext_ice_override, ssa_imp_override, ext_imp_override)
+                  g_override, ext_ice_override, ssa_imp_override, ext_imp_override,
+                  int(bool(nearest)), 0)
 
 
 def walk(cfg, ice, imp, seed, p0=0, p1=None, threads=1):
@@ -123,11 +125,13 @@ def config_from_golden(g):
     return make_config(p('n_photon'), p('wvl0'), p('half_width'), p('theta0'), p('tau_tot'),
                        p('imp_cnc'), p('rho_snw'), p('rho_ice'), p('lam_surface'),
                        p('lam_bottom'), p('R'), ssa_ice_override=p('ssa_ice_override'),
-                       g_override=p('g_override'))
+                       g_override=p('g_override'),
+                       nearest=bool(g['param_ssp_nearest'].item()) if 'param_ssp_nearest' in g else False)
 
 
 def tables_from_golden(g):
     from monte_carlompi_gb300.ssp import SSPTable
-    ice = SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'])
+    unit = int(g['ice_unit'].item()) if 'ice_unit' in g else 0
+    ice = SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'], wvl_unit=unit)
     imp = SSPTable(g['imp_wvl'], g['imp_ssa'], g['imp_ext'], None)
     return ice, imp

@@ -81,11 +81,12 @@ static double stream_next(orc_stream *s)
 
 /* ---------------------------------------------------------------- types */
 typedef struct {
-    const double *wvl;   /* metres */
+    const double *wvl;   /* metres (netCDF tables) or micrometres (aspherical isca.dat rows) */
     const double *ssa;
     const double *ext;
     const double *asm_;  /* may be NULL (impurity) */
     int32_t n;
+    int32_t unit;        /* 0: wvl in metres, 1: in micrometres */
 } orc_table;
 
 typedef struct {
@@ -95,6 +96,11 @@ typedef struct {
     double R;
     /* run(test=True) overrides (monte_carlo3D.py:1553-1573); NaN = from table */
     double ssa_ice_override, g_override, ext_ice_override, ssa_imp_override, ext_imp_override;
+    /* 1: the HG-forced aspherical lookup (monte_carlo3D.py:323-334, :396-415,
+     * :1528-1549): the nearest ice-table point, no interpolation, and the photon
+     * takes that point's wavelength for the impurity lookup and wvn */
+    int32_t nearest;
+    int32_t pad;
 } orc_config;
 
 typedef struct {
@@ -148,15 +154,34 @@ double orc_wavelength(uint64_t seed, uint64_t photon, double wvl0, double half_w
 /* Per-photon optics: monte_carlo3D.py:1524-1612. */
 typedef struct { double wvl, ssa_ice, ssa_imp, g, ext_cff_mss, P_ext_imp, snow_depth; } orc_optics;
 
+/* A wavelength in um in a table's unit: the netCDF lookups compare wvl * 1e-6
+ * with metres (monte_carlo3D.py:518, :673); the aspherical one compares um
+ * with um (:323-334). */
+static double in_unit(const orc_table *t, double wvl_um)
+{
+    return t->unit ? wvl_um : wvl_um * 1e-6;
+}
+
 static orc_optics photon_optics(const orc_config *c, const orc_table *ice, const orc_table *imp, double wvl_um)
 {
     orc_optics o;
-    double w = wvl_um * 1e-6;
+    double w = in_unit(ice, wvl_um);
     int32_t i0, i1;
+    double ssa_ice, ext_ice, g;
     nearest_two(ice, w, &i0, &i1);
-    double ssa_ice = interp_two(ice, ice->ssa, i0, i1, w);
-    double ext_ice = interp_two(ice, ice->ext, i0, i1, w);
-    double g = interp_two(ice, ice->asm_, i0, i1, w);
+    if (c->nearest) {
+        /* argsort(|wvl - wvl_in|)[0]: ssa_in, Q_ext-derived ext_cff_mss and asm_in of that
+         * row (:396-415); the photon's wavelength becomes wvl_in of that row (:399, :1536) */
+        ssa_ice = ice->ssa[i0];
+        ext_ice = ice->ext[i0];
+        g = ice->asm_[i0];
+        wvl_um = ice->unit ? ice->wvl[i0] : ice->wvl[i0] * 1e6;
+    } else {
+        ssa_ice = interp_two(ice, ice->ssa, i0, i1, w);
+        ext_ice = interp_two(ice, ice->ext, i0, i1, w);
+        g = interp_two(ice, ice->asm_, i0, i1, w);
+    }
+    w = in_unit(imp, wvl_um);
     nearest_two(imp, w, &i0, &i1);
     double ssa_imp = interp_two(imp, imp->ssa, i0, i1, w);
     double ext_imp = interp_two(imp, imp->ext, i0, i1, w);
@@ -297,7 +322,7 @@ void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table 
     }
 
     out->condition = condition;
-    out->wvn = 1. / wvl;                                                       /* :1468 */
+    out->wvn = 1. / o.wvl;                                                     /* :1468 */
     out->theta_n = acos(muz_0);                                                /* :1469 */
     out->phi_undefined = 0;
     if (i == 1) out->phi_n = 0.;                                               /* :1472-1485 */

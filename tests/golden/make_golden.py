@@ -79,7 +79,17 @@ CASES = {
     # one photon: the scalar branch of the SSP lookup (monte_carlo3D.py:518-583)
     'single': dict(n_photon=1, wvl0=1.3, half_width=0.085, rds=100.0, theta0=15.0,
                    depth_m=0.5, lam_bottom=True, R=0.5, seed=0x5EED0015, csv=False),
+    # HG-forced aspherical grains (run(shape=...), HG=True): a synthetic isca.dat with
+    # three particle sizes on a 25 nm grid; nearest size and nearest wavelength, the
+    # photon's wavelength replaced; an impurity table whose extinction varies with
+    # wavelength, so the impurity lookup at the replaced wavelength shows in snow_depth
+    'asph': dict(n_photon=600, wvl0=1.3, half_width=0.085, rds=100.0, theta0=30.0,
+                 tau_tot=40.0, imp_cnc=1e-4, lam_bottom=True, R=0.5, seed=0x5EED0016,
+                 shape='solid hexagonal column', roughness='smooth', csv=True),
 }
+
+ASPH_WVLS = [round(1.0 + 0.025 * i, 4) for i in range(41)]   # 1.0 .. 2.0 um
+ASPH_RE = [60.0, 120.0, 250.0]
 
 
 def _install_stubs():
@@ -173,6 +183,9 @@ def run_case(name, spec, outdir):
     lo, hi = spec.get('table_nm') or ssp.grid_for(spec['wvl0'], spec['half_width'])
     ice = ssp.synthetic_ice_table(spec['rds'], lo, hi, rho_ice)
     imp = ssp.synthetic_impurity_table(lo, hi)
+    shape = spec.get('shape', 'sphere')
+    if shape != 'sphere':
+        imp.ext_cff_mss = imp.ext_cff_mss * (1.0 + 2.0 * (imp.wvl * 1e6 - spec['wvl0']))
     if 'tau_tot' in spec:
         tau_tot = float(spec['tau_tot'])
     else:
@@ -190,10 +203,18 @@ def run_case(name, spec, outdir):
         optics = os.path.join(work, 'optics')
         ssp.write_netcdf(os.path.join(optics, 'mie', 'snicar', ssp.ice_file_name(spec['rds'])), ice)
         ssp.write_netcdf(os.path.join(optics, 'mie', 'snicar', 'imp.nc'), imp, with_asm=False)
+        isca_rows = None
+        if shape != 'sphere':
+            isca_rows = np.array(ssp.synthetic_isca_rows(ASPH_WVLS, ASPH_RE), dtype=np.float64)
+            isca = ssp.isca_path(optics, shape, spec['roughness'], spec['wvl0'])
+            ssp.write_isca(isca, isca_rows)
+            # what the library walks: this package's reader of the same file
+            ice, re_sel = ssp.aspherical_table(isca, spec['wvl0'], spec['rds'], rho_ice)
+            isca_rows = ssp.read_isca(isca)
         model = ref.MonteCarlo(tau_tot=tau_tot, imp_cnc=spec.get('imp_cnc', 0.0),
                                rho_snw=rho_snw, rho_ice=rho_ice,
                                output_dir=os.path.join(work, 'out'), optics_dir=optics,
-                               fi_imp='imp.nc')
+                               fi_imp='imp.nc', HG=shape != 'sphere')
         for k, v in spec.get('test', {}).items():
             setattr(model, k, v)
 
@@ -222,6 +243,7 @@ def run_case(name, spec, outdir):
         try:
             model.run(spec['n_photon'], spec['wvl0'], spec['half_width'], spec['rds'],
                       theta_0=spec['theta0'], test=bool(spec.get('test')),
+                      shape=shape, roughness=spec.get('roughness', 'smooth'),
                       Lambertian_surface=spec.get('lam_surface', False),
                       Lambertian_bottom=spec['lam_bottom'],
                       Lambertian_reflectance=spec['R'])
@@ -230,10 +252,13 @@ def run_case(name, spec, outdir):
             ref.MonteCarlo.initial_pdfs = orig_init
             np.random.rand, np.random.uniform, np.random.normal = saved
             np.set_printoptions(legacy=False)
-        outs = os.listdir(os.path.join(work, 'out', 'sphere'))
+        out_dir = os.path.join(work, 'out', 'sphere')
+        if shape != 'sphere':
+            out_dir = os.path.join(work, 'out', ssp.SHAPE_DIRS[shape], ssp.ROUGHNESS_DIRS[spec['roughness']])
+        outs = os.listdir(out_dir)
         assert len(outs) == 1, outs
         csv_name = outs[0]
-        with open(os.path.join(work, 'out', 'sphere', csv_name), 'rb') as f:
+        with open(os.path.join(out_dir, csv_name), 'rb') as f:
             csv_bytes = f.read()
     finally:
         os.chdir(old_cwd)
@@ -253,12 +278,17 @@ def run_case(name, spec, outdir):
                   lam_bottom=int(spec['lam_bottom']), R=spec['R'], seed=spec['seed'],
                   ssa_ice_override=spec.get('test', {}).get('ssa_ice', np.nan),
                   g_override=spec.get('test', {}).get('g', np.nan))
+    extra = {}
+    if shape != 'sphere':
+        params.update(ssp_nearest=1, rds_selected=re_sel)
+        extra = dict(ice_unit=np.asarray(ice.wvl_unit), isca_rows=isca_rows,
+                     shape=np.asarray(shape), roughness=np.asarray(spec['roughness']))
     np.savez_compressed(
         os.path.join(outdir, name + '.npz'),
         **rec, **{'param_' + k: np.asarray(v) for k, v in params.items()},
         ice_wvl=ice.wvl, ice_ssa=ice.ss_alb, ice_ext=ice.ext_cff_mss, ice_asm=ice.asm_prm,
         imp_wvl=imp.wvl, imp_ssa=imp.ss_alb, imp_ext=imp.ext_cff_mss,
-        csv_name=np.asarray(csv_name))
+        csv_name=np.asarray(csv_name), **extra)
     if spec.get('csv'):
         with open(os.path.join(outdir, name + '.csv'), 'wb') as f:
             f.write(csv_bytes)

@@ -47,11 +47,13 @@ def golden_config(g):
                       rho_snw=p('rho_snw'), rho_ice=p('rho_ice'),
                       lambertian_reflectance=p('R'), lambertian_surface=bool(p('lam_surface')),
                       lambertian_bottom=bool(p('lam_bottom')),
-                      ssa_ice_override=p('ssa_ice_override'), g_override=p('g_override'))
+                      ssa_ice_override=p('ssa_ice_override'), g_override=p('g_override'),
+                      ssp_nearest=bool(p('ssp_nearest')) if 'param_ssp_nearest' in g else False)
 
 
 def golden_tables(g):
-    ice = ssp.SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'])
+    unit = int(g['ice_unit'].item()) if 'ice_unit' in g else ssp.WVL_METRES
+    ice = ssp.SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'], wvl_unit=unit)
     imp = ssp.SSPTable(g['imp_wvl'], g['imp_ssa'], g['imp_ext'], None)
     return ice, imp
 

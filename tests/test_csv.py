@@ -15,7 +15,7 @@ def _records64(g):
     return r
 
 
-@pytest.mark.parametrize('name', ['cfg1', 'cfg2'])
+@pytest.mark.parametrize('name', ['cfg1', 'cfg2', 'asph'])
 def test_reference_csv_bytes(name, tmp_path):
     g = load_golden(name)
     ref = open(os.path.join(GOLDEN, name + '.csv'), 'rb').read()

@@ -8,7 +8,7 @@ import pytest
 from monte_carlompi_gb300 import csv_io, ssp
 from monte_carlompi_gb300.monte_carlo import MonteCarlo
 from tests.conftest import GOLDEN, load_golden
-from tests.helpers import compare_replay
+from tests.helpers import compare_replay, golden_tables
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +19,33 @@ def _write_tables(optics, g, rds):
     base = os.path.join(optics, 'mie', 'snicar')
     ssp.write_netcdf(os.path.join(base, ssp.ice_file_name(rds)), ice)
     ssp.write_netcdf(os.path.join(base, 'imp.nc'), imp, with_asm=False)
+
+
+def test_run_aspherical_hg_reproduces_reference_csv(tmp_path, monkeypatch, capsys):
+    """run(shape=..., HG=True) on the same isca.dat rows and impurity table: the file
+    lands where the reference writes it (shape and roughness directories, named with
+    the selected effective radius) and holds the reference's photons."""
+    g = load_golden('asph')
+    p = lambda k: g['param_' + k].item()  # noqa: E731
+    monkeypatch.chdir(tmp_path)
+    optics = str(tmp_path / 'optics')
+    shape, rough = str(g['shape']), str(g['roughness'])
+    ssp.write_isca(ssp.isca_path(optics, shape, rough, p('wvl0')), g['isca_rows'])
+    _, imp = golden_tables(g)
+    ssp.write_netcdf(os.path.join(optics, 'mie', 'snicar', 'imp.nc'), imp, with_asm=False)
+    mc = MonteCarlo(tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'), rho_snw=p('rho_snw'),
+                    rho_ice=p('rho_ice'), output_dir=str(tmp_path / 'out'), optics_dir=optics,
+                    fi_imp='imp.nc', ssp='file', mode='replay64', seed=int(p('seed')), HG=True)
+    mc.run(int(p('n_photon')), p('wvl0'), p('half_width'), p('rds'), theta_0=p('theta0'),
+           shape=shape, roughness=rough, Lambertian_bottom=bool(p('lam_bottom')),
+           Lambertian_reflectance=p('R'))
+    printed = capsys.readouterr().out.strip()
+    assert printed.endswith(os.path.join(ssp.SHAPE_DIRS[shape], ssp.ROUGHNESS_DIRS[rough],
+                                         str(g['csv_name'])))
+    assert mc.snow_effective_radius == p('rds_selected')
+    got = csv_io.read_csv(printed)
+    compare_replay(got, g)
+    compare_replay(got, csv_io.read_csv(os.path.join(GOLDEN, 'asph.csv')))
 
 
 @pytest.mark.parametrize('name', ['cfg1', 'cfg2'])

@@ -35,7 +35,8 @@ def oracle_run(cfg, ice, imp, seed, threads=16):
     c = oracle.make_config(cfg.n_photon, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot,
                            cfg.imp_cnc, cfg.rho_snw, cfg.rho_ice, cfg.lambertian_surface,
                            cfg.lambertian_bottom, cfg.lambertian_reflectance,
-                           ssa_ice_override=cfg.ssa_ice_override, g_override=cfg.g_override)
+                           ssa_ice_override=cfg.ssa_ice_override, g_override=cfg.g_override,
+                           nearest=cfg.ssp_nearest)
     return oracle.walk(c, ice, imp, seed, p0=cfg.first_photon,
                        p1=cfg.first_photon + cfg.n_photon, threads=threads if cfg.first_photon == 0 else 1)
 
@@ -88,7 +89,7 @@ def _golden_case(name, n):
 
 @pytest.mark.parametrize('case,n', [('cfg2', 200000), ('thin', 200000), ('kat', 200000),
                                     ('imp', 100000), ('lamsurf', 50000), ('edge', 50000),
-                                    ('cfg1', 20000)])
+                                    ('cfg1', 20000), ('asph', 100000)])
 def test_f32_statistics_match_oracle(walker, case, n):
     if case in STAT_CASES:
         cfg, ice, imp = STAT_CASES[case][0]()

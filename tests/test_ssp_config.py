@@ -67,3 +67,47 @@ def test_walk_config_c_layout():
     c = WalkConfig(n_photon=5, wvl0=1.3, half_width=0.085, first_photon=7).to_c()
     assert c.n_photon == 5 and c.first_photon == 7 and abs(c.wvl0 - 1.3) < 1e-15
     assert np.isnan(c.g_override)
+
+
+def test_aspherical_table_selects_like_the_reference():
+    """get_aspherical_SSPs (HG-forced): the reference's own run on these isca.dat rows
+    (tests/golden/asph.npz) selected RE = 120 um and gave each photon the nearest
+    tabulated wavelength; the reader picks the same rows, k_ext = 1e6 G Q / (rho_ice V)."""
+    from tests.conftest import load_golden
+    g = load_golden('asph')
+    rows = g['isca_rows']
+    t = ssp.SSPTable(g['ice_wvl'], g['ice_ssa'], g['ice_ext'], g['ice_asm'], wvl_unit=ssp.WVL_MICRONS)
+    assert g['param_rds_selected'].item() == 120.0
+    assert '_120.0_' in str(g['csv_name'])
+    # every photon's wavelength is a row of the selected size (wvn = 1 / that wavelength)
+    assert np.all(np.isin(np.round(1.0 / g['wvn'], 12), np.round(t.wvl, 12)))
+    sel = rows[np.isclose(0.75 * rows[:, 2] / rows[:, 3], 120.0)]
+    assert np.array_equal(t.wvl, np.sort(sel[:, 0]))
+    ext = (1e6 * sel[:, 3] * sel[:, 4]) / (917.0 * sel[:, 2])
+    assert np.array_equal(t.ext_cff_mss, ext[np.argsort(sel[:, 0])])
+
+
+def test_aspherical_reader_round_trip_and_errors(tmp_path):
+    rows = ssp.synthetic_isca_rows([1.0, 1.05, 1.1, 1.3, 1.7], [50.0, 200.0])
+    p = ssp.isca_path(str(tmp_path), 'droxtal', 'severely rough', 1.3)
+    assert p.endswith('ice_optics/0.2-15.25/droxtal/Rough050/isca.dat')
+    assert ssp.isca_path('o', 'hexagonal plate', 'smooth', 20.0).endswith(
+        '16.4-99.0/plate/Rough000/isca.dat')
+    ssp.write_isca(p, rows)
+    assert np.array_equal(ssp.read_isca(p), np.array(rows))
+    t, re = ssp.aspherical_table(p, 1.3, 150.0)
+    assert abs(re - 200.0) < 1e-9 and t.wvl_unit == ssp.WVL_MICRONS and t.wvl.size == 5
+    t, re = ssp.aspherical_table(p, 1.3, 110.0)   # nearer to 50 than to 200
+    assert abs(re - 50.0) < 1e-9
+    import pytest
+    with pytest.raises(ValueError):
+        ssp.aspherical_table(p, 1.31, 150.0)      # wvl0 must be a tabulated wavelength
+    with pytest.raises(ValueError):
+        ssp.isca_path('o', 'sphere', 'smooth', 1.3)
+    with pytest.raises(ValueError):
+        ssp.isca_path('o', 'droxtal', 'smooth', 15.8)
+
+
+def test_walk_config_nearest_flag_in_c_layout():
+    c = WalkConfig(n_photon=5, wvl0=1.3, half_width=0.085, ssp_nearest=True).to_c()
+    assert c.ssp_nearest == 1 and c.ice_table == 0
