@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCW_ABI_VERSION 1
+#define MCW_ABI_VERSION 2
 
 /* status codes */
 #define MCW_OK 0
@@ -34,6 +34,8 @@ extern "C" {
 /* walk modes */
 #define MCW_MODE_F32 0       /* production: FP32 walk, Philox4x32-10 per (photon, step) */
 #define MCW_MODE_REPLAY64 1  /* FP64 walk on the photon-indexed replay stream, reference order */
+#define MCW_MODE_POL64 2     /* the polarised walk of aspherical grains (HG off): FP64, replay
+                                stream, reference order; records mcw_record64p */
 
 /* where mcw_walk writes per-photon records */
 #define MCW_RECORDS_NONE 0
@@ -96,6 +98,13 @@ typedef struct {
     double ext_ice_override;
     double ssa_imp_override;
     double ext_imp_override;
+    /* 1: the polarised walk of aspherical grains (run(shape=...) with HG off): scattering
+     * angles by rejection from the phase matrices of the ice table (mcw_set_phase_matrices)
+     * and the photon's Stokes vector carried through every scattering (monte_carlo3D.py:
+     * 905-1004, :1282-1342).  Needs ssp_nearest = 1 and MCW_MODE_POL64. */
+    int32_t polarised;
+    int32_t pad;
+    double stokes0[4];             /* incident Stokes vector (I, Q, U, V), run(stokes_params=...) */
 } mcw_config;
 
 /* Per-photon answer of MCW_MODE_F32: the 7 CSV columns of
@@ -125,6 +134,43 @@ typedef struct {
     uint32_t config;
     uint32_t flags;
 } mcw_record64;
+
+/* Per-photon answer of MCW_MODE_POL64: mcw_record64's fields and the final
+ * Stokes vector's Q, U, V divided by I (the CSV's Q_n, U_n, V_n,
+ * monte_carlo3D.py:1637-1646).  80 bytes. */
+typedef struct {
+    int32_t condition;
+    int32_t n_scat;
+    double wvn;
+    double theta_n;
+    double phi_n;
+    double path_length;
+    double snow_depth;
+    uint32_t config;
+    uint32_t flags;
+    double stokes_q;
+    double stokes_u;
+    double stokes_v;
+} mcw_record64p;
+
+/* Phase matrices of the polarised walk for one ice table (one row per table
+ * row, in the order the table was given to mcw_set_tables), as
+ * interpolate_phase_matrix (monte_carlo3D.py:819-883) prepares them: element e
+ * (P11, P12, P22, P33, P43, P44) tabulated at cos_asc[e] (cos of the file's
+ * scattering angles, strictly ascending, n_angle[e] points) with values
+ * p_asc[e][row * n_angle[e] + j] (P12 ... P44 multiplied by P11; P11 > 0).
+ * The rejection sampler's two areas meet at cos_cutoff in [cos_min, cos_max];
+ * a1 / a2 hold each row's largest |P11| over the first (cos >= cos_cutoff) and
+ * second area, b1 / b2 the same for |P12| (:929-947).  Host pointers, copied. */
+typedef struct {
+    int32_t n_rows;
+    int32_t n_angle[6];
+    int32_t pad;
+    const double *cos_asc[6];
+    const double *p_asc[6];
+    const double *a1, *a2, *b1, *b2;
+    double cos_max, cos_min, cos_cutoff;
+} mcw_phase_table;
 
 /* Per-config totals and the condition-1 exit histogram; the inputs of the
  * BRF and albedo of post_processing.py:73-81,125-128 and monte_carlo3D.py:
@@ -186,6 +232,11 @@ int mcw_last_error(const mcw_ctx *ctx, char *buf, size_t len);
 int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice,
                    const mcw_ssp_table *imp);
 
+/* Attach phase matrices to the ice tables of the last mcw_set_tables: tabs[i]
+ * belongs to ice table i (n = n_ice; n_rows 0 = none).  Replaces the P11.dat ...
+ * P44.dat reads of get_aspherical_SSPs (monte_carlo3D.py:145-171, :267-475). */
+int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n);
+
 /* Launch shape and time budget of later walks. */
 int mcw_set_launch(mcw_ctx *ctx, const mcw_launch *launch);
 int mcw_get_launch(const mcw_ctx *ctx, mcw_launch *launch);
@@ -197,8 +248,10 @@ int mcw_set_budget(mcw_ctx *ctx, double seconds);
  * (p = 0 .. n_photon-1) is record sum(n_photon[:c]) + p; its random streams
  * are keyed by (seed, c << 40 | (first_photon + p)), so a run split into
  * shards by first_photon gives the same photons as the whole run.
- * records: mcw_record32 (F32) or mcw_record64 (REPLAY64), or NULL with
- * MCW_RECORDS_NONE.  tallies: n_cfg host structs or NULL.  stats: or NULL. */
+ * records: mcw_record32 (F32), mcw_record64 (REPLAY64) or mcw_record64p
+ * (POL64), or NULL with MCW_RECORDS_NONE.  Polarised configs walk in
+ * MCW_MODE_POL64 only, and POL64 walks polarised configs only.  tallies: n_cfg
+ * host structs or NULL.  stats: or NULL. */
 int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed, int32_t mode,
              void *records, int32_t records_where, mcw_tally *tallies, mcw_stats *stats);
 
@@ -228,7 +281,9 @@ int mcw_host_free(void *p);
 
 /* Per-photon CSV in the reference's format (monte_carlo3D.py:1627-1636):
  * header line, then "%d %r %r %r %d %r %r" rows with Python's shortest
- * round-trip float repr.  mode selects mcw_record32 / mcw_record64.
+ * round-trip float repr.  mode selects mcw_record32 / mcw_record64, or
+ * mcw_record64p with the polarised walk's header and three more columns
+ * (Q_n, U_n, V_n, :1637-1646).
  * mcw_format_csv writes into buf (cap bytes; *used = bytes needed). */
 int mcw_write_csv(const char *path, const void *records, int32_t mode, int64_t n,
                   int32_t n_threads);

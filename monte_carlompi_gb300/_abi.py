@@ -16,6 +16,7 @@ ERRORS = {-1: 'MCW_ERR_ARG', -2: 'MCW_ERR_CUDA', -3: 'MCW_ERR_BUDGET', -4: 'MCW_
           -5: 'MCW_ERR_OOM', -6: 'MCW_ERR_STATE'}
 MODE_F32 = 0
 MODE_REPLAY64 = 1
+MODE_POL64 = 2
 RECORDS_NONE, RECORDS_HOST, RECORDS_DEVICE = 0, 1, 2
 HIST_NTHETA, HIST_NPHI, HIST_BINS = 18, 36, 648
 WVN_FX_SCALE = 4294967296.0
@@ -25,7 +26,7 @@ EXPORTS = ['mcw_abi_version', 'mcw_version', 'mcw_create', 'mcw_destroy', 'mcw_l
            'mcw_set_tables', 'mcw_set_launch', 'mcw_get_launch', 'mcw_set_budget', 'mcw_walk',
            'mcw_brf', 'mcw_autotune', 'mcw_graph_create', 'mcw_graph_launch',
            'mcw_graph_destroy', 'mcw_host_alloc', 'mcw_host_free', 'mcw_write_csv',
-           'mcw_format_csv', 'mcw_walk_noalloc', 'mcw_post']
+           'mcw_format_csv', 'mcw_walk_noalloc', 'mcw_post', 'mcw_set_phase_matrices']
 
 
 class McwError(RuntimeError):
@@ -55,7 +56,17 @@ class ConfigC(ctypes.Structure):
                 ('ice_table', ctypes.c_int32), ('ssp_nearest', ctypes.c_int32),
                 ('ssa_ice_override', ctypes.c_double), ('g_override', ctypes.c_double),
                 ('ext_ice_override', ctypes.c_double), ('ssa_imp_override', ctypes.c_double),
-                ('ext_imp_override', ctypes.c_double)]
+                ('ext_imp_override', ctypes.c_double),
+                ('polarised', ctypes.c_int32), ('pad', ctypes.c_int32),
+                ('stokes0', ctypes.c_double * 4)]
+
+
+class PhaseTableC(ctypes.Structure):
+    _fields_ = [('n_rows', ctypes.c_int32), ('n_angle', ctypes.c_int32 * 6), ('pad', ctypes.c_int32),
+                ('cos_asc', ctypes.c_void_p * 6), ('p_asc', ctypes.c_void_p * 6),
+                ('a1', ctypes.c_void_p), ('a2', ctypes.c_void_p), ('b1', ctypes.c_void_p),
+                ('b2', ctypes.c_void_p), ('cos_max', ctypes.c_double), ('cos_min', ctypes.c_double),
+                ('cos_cutoff', ctypes.c_double)]
 
 
 class StatsC(ctypes.Structure):
@@ -103,13 +114,18 @@ RECORD64 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.f
                      ('theta_n', np.float64), ('phi_n', np.float64),
                      ('path_length', np.float64), ('snow_depth', np.float64),
                      ('config', np.uint32), ('flags', np.uint32)])
+RECORD64P = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float64),
+                      ('theta_n', np.float64), ('phi_n', np.float64),
+                      ('path_length', np.float64), ('snow_depth', np.float64),
+                      ('config', np.uint32), ('flags', np.uint32),
+                      ('stokes_q', np.float64), ('stokes_u', np.float64), ('stokes_v', np.float64)])
 TALLY = np.dtype([('n_cond', np.uint64, 6), ('q_cond_fx', np.uint64, 6), ('n_events', np.uint64),
                   ('max_n_scat', np.uint32), ('reserved', np.uint32),
                   ('bin_wvn_fx', np.uint64, HIST_BINS), ('bin_count', np.uint32, HIST_BINS)])
 POST_STATS = np.dtype([('q_cond_fx', np.uint64, 6), ('n_cond', np.uint64, 6), ('sum_n_scat', np.uint64),
                        ('sum_path_length', np.float64), ('sum_wavelength', np.float64)])
-assert RECORD32.itemsize == 32 and RECORD64.itemsize == 56
-assert ctypes.sizeof(ConfigC) == 136 and ctypes.sizeof(StatsC) == 80
+assert RECORD32.itemsize == 32 and RECORD64.itemsize == 56 and RECORD64P.itemsize == 80
+assert ctypes.sizeof(ConfigC) == 176 and ctypes.sizeof(StatsC) == 80
 
 _lib = None
 
@@ -132,6 +148,7 @@ def load(path=None):
         'mcw_destroy': ([vp], ctypes.c_int),
         'mcw_last_error': ([vp, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
         'mcw_set_tables': ([vp, ctypes.POINTER(SSPTableC), i32, ctypes.POINTER(SSPTableC)], ctypes.c_int),
+        'mcw_set_phase_matrices': ([vp, ctypes.POINTER(PhaseTableC), i32], ctypes.c_int),
         'mcw_set_launch': ([vp, ctypes.POINTER(LaunchC)], ctypes.c_int),
         'mcw_get_launch': ([vp, ctypes.POINTER(LaunchC)], ctypes.c_int),
         'mcw_set_budget': ([vp, dbl], ctypes.c_int),

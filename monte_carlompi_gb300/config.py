@@ -7,6 +7,7 @@ reference's ``config.ini`` keys (monte_carloMPI/config.ini; parsed at
 monte_carlo3D.py:1778-1806).
 """
 import configparser
+import ctypes
 import math
 import os
 from dataclasses import dataclass, field, asdict
@@ -61,6 +62,8 @@ class WalkConfig:
     ext_imp_override: float = math.nan
     first_photon: int = 0            # first photon index (a shard of a larger run)
     ssp_nearest: bool = False        # HG-forced aspherical lookup: nearest table point, wavelength replaced
+    polarised: bool = False          # polarised walk of aspherical grains (phase matrices, mode 'pol64')
+    stokes0: tuple = (1.0, 0.0, 0.0, 0.0)  # incident Stokes vector of the polarised walk
     rds_snw: float = field(default=math.nan)  # grain size [um], bookkeeping (selects the table)
 
     def to_c(self):
@@ -72,7 +75,8 @@ class WalkConfig:
                             int(bool(self.ssp_nearest)),
                             float(self.ssa_ice_override), float(self.g_override),
                             float(self.ext_ice_override), float(self.ssa_imp_override),
-                            float(self.ext_imp_override))
+                            float(self.ext_imp_override), int(bool(self.polarised)), 0,
+                            (ctypes.c_double * 4)(*[float(x) for x in self.stokes0]))
 
     def as_dict(self):
         return asdict(self)

@@ -16,7 +16,8 @@
 
 using namespace mcw;
 
-static_assert(sizeof(mcw_config) == 136, "mcw_config layout");
+static_assert(sizeof(mcw_config) == 176, "mcw_config layout");
+static_assert(sizeof(mcw_record64p) == 80, "mcw_record64p layout");
 static_assert(sizeof(mcw_record32) == 32, "mcw_record32 layout");
 static_assert(sizeof(mcw_record64) == 56, "mcw_record64 layout");
 static_assert(sizeof(mcw_stats) == 80, "mcw_stats layout");
@@ -97,6 +98,10 @@ struct mcw_ctx {
     DevTable imp{};
     int32_t n_ice = 0;
     bool have_tables = false;
+    std::vector<std::vector<int32_t>> ice_order;   // row permutation of each ice table (stored ascending)
+    // phase matrices of the polarised walk, one per ice table (n_rows 0 = none)
+    DevBuf phasedata, phase_tables;
+    std::vector<int32_t> phase_rows;
     // workspace
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
     HostBuf h_stage, h_tallies, h_counters;
@@ -158,6 +163,13 @@ const char *check_config(const mcw_config &c, int32_t n_ice) {
         return "lambertian_reflectance must be in [0, 1]";
     if (c.ice_table < 0 || c.ice_table >= n_ice) return "ice_table out of range";
     if (c.ssp_nearest != 0 && c.ssp_nearest != 1) return "ssp_nearest must be 0 or 1";
+    if (c.polarised != 0 && c.polarised != 1) return "polarised must be 0 or 1";
+    if (c.polarised) {
+        if (!c.ssp_nearest) return "the polarised walk needs ssp_nearest = 1 (aspherical tables)";
+        for (int k = 0; k < 4; ++k)
+            if (!std::isfinite(c.stokes0[k])) return "stokes0 must be finite";
+        if (c.stokes0[0] == 0) return "stokes0[0] (I) must not be 0";
+    }
     if (!std::isnan(c.ssa_ice_override) && !(c.ssa_ice_override >= 0 && c.ssa_ice_override <= 1)) return "ssa_ice_override must be in [0, 1]";
     if (!std::isnan(c.ssa_imp_override) && !(c.ssa_imp_override >= 0 && c.ssa_imp_override <= 1)) return "ssa_imp_override must be in [0, 1]";
     if (!std::isnan(c.g_override) && !(c.g_override > -1 && c.g_override < 1)) return "g_override must be in (-1, 1)";
@@ -168,9 +180,19 @@ const char *check_config(const mcw_config &c, int32_t n_ice) {
 
 constexpr int32_t kMaxLutPerConfig = 1 << 16;
 
-int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
+int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, int32_t mode, Plan &plan) {
     if (!cfgs || n_cfg <= 0) return set_err(ctx, MCW_ERR_ARG, "need at least one config");
     if (n_cfg > (1 << 23)) return set_err(ctx, MCW_ERR_ARG, "at most 2^23 configs per call");
+    for (int32_t i = 0; i < n_cfg; ++i) {
+        if (cfgs[i].polarised && mode != MCW_MODE_POL64)
+            return set_err(ctx, MCW_ERR_ARG, "config %d: the polarised walk runs in MCW_MODE_POL64", i);
+        if (!cfgs[i].polarised && mode == MCW_MODE_POL64)
+            return set_err(ctx, MCW_ERR_ARG, "config %d: MCW_MODE_POL64 walks polarised configs only", i);
+        if (cfgs[i].polarised && cfgs[i].ice_table >= 0 && cfgs[i].ice_table < ctx->n_ice &&
+            ((int32_t)ctx->phase_rows.size() <= cfgs[i].ice_table || ctx->phase_rows[cfgs[i].ice_table] == 0))
+            return set_err(ctx, MCW_ERR_STATE, "config %d: ice table %d has no phase matrices", i,
+                           cfgs[i].ice_table);
+    }
     plan.cfgs.resize(n_cfg);
     plan.prefix.resize(n_cfg + 1);
     int64_t off = 0;
@@ -202,7 +224,9 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, Plan &plan) {
         d.lut_off = lut_off;
         lut_off += d.lut_n;
         d.flags = (c.lambertian_surface ? kFlagLamSurface : 0u) | (c.lambertian_bottom ? kFlagLamBottom : 0u) |
-                  (c.imp_cnc > 0 ? kFlagImpurity : 0u) | (c.ssp_nearest ? kFlagNearest : 0u);
+                  (c.imp_cnc > 0 ? kFlagImpurity : 0u) | (c.ssp_nearest ? kFlagNearest : 0u) |
+                  (c.polarised ? kFlagPolarised : 0u);
+        for (int k = 0; k < 4; ++k) d.stokes0[k] = c.polarised ? c.stokes0[k] : (k == 0 ? 1.0 : 0.0);
         d.ice_table = c.ice_table;
         if (c.imp_cnc > 0) plan.impurity = true;
         const double theta0 = (kPi * c.theta0_deg) / 180.;  // monte_carlo3D.py:1508
@@ -482,7 +506,86 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     ctx->n_ice = n_ice;
     ctx->max_ice_n = 0;
     for (int32_t i = 0; i < n_ice; ++i) ctx->max_ice_n = std::max(ctx->max_ice_n, ice[i].n);
+    ctx->ice_order.assign(n_ice, {});
+    for (int32_t i = 0; i < n_ice; ++i) order_of(ice[i], ctx->ice_order[i]);
+    ctx->phase_rows.assign(n_ice, 0);   // phase matrices belong to the previous tables
     ctx->have_tables = true;
+    return MCW_OK;
+}
+
+int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n) {
+    if (!ctx) return MCW_ERR_ARG;
+    if (!ctx->have_tables) return set_err(ctx, MCW_ERR_STATE, "call mcw_set_tables first");
+    if (!tabs || n != ctx->n_ice) return set_err(ctx, MCW_ERR_ARG, "need one phase table per ice table (%d)", ctx->n_ice);
+    size_t total = 0;
+    for (int32_t t = 0; t < n; ++t) {
+        const mcw_phase_table &p = tabs[t];
+        if (p.n_rows == 0) continue;
+        if (p.n_rows != (int32_t)ctx->ice_order[t].size())
+            return set_err(ctx, MCW_ERR_ARG, "phase table %d: n_rows must equal the ice table's rows", t);
+        if (!p.a1 || !p.a2 || !p.b1 || !p.b2) return set_err(ctx, MCW_ERR_ARG, "phase table %d: missing maxima", t);
+        if (!(p.cos_min <= p.cos_cutoff && p.cos_cutoff <= p.cos_max))
+            return set_err(ctx, MCW_ERR_ARG, "phase table %d: cos_cutoff outside [cos_min, cos_max]", t);
+        for (int e = 0; e < 6; ++e) {
+            const int32_t m = p.n_angle[e];
+            if (m < 2 || !p.cos_asc[e] || !p.p_asc[e]) return set_err(ctx, MCW_ERR_ARG, "phase table %d: element %d", t, e);
+            for (int32_t j = 0; j < m; ++j) {
+                if (!std::isfinite(p.cos_asc[e][j]) || (j > 0 && !(p.cos_asc[e][j] > p.cos_asc[e][j - 1])))
+                    return set_err(ctx, MCW_ERR_ARG, "phase table %d: cos_asc[%d] must rise strictly", t, e);
+            }
+            if (p.cos_asc[e][0] > p.cos_min || p.cos_asc[e][m - 1] < p.cos_max)
+                return set_err(ctx, MCW_ERR_ARG, "phase table %d: cos_asc[%d] must cover [cos_min, cos_max]", t, e);
+            for (size_t k = 0; k < (size_t)p.n_rows * m; ++k) {
+                const double v = p.p_asc[e][k];
+                if (!std::isfinite(v) || (e == 0 && !(v > 0)))
+                    return set_err(ctx, MCW_ERR_ARG, "phase table %d: element %d must be finite (P11 > 0)", t, e);
+            }
+            total += (size_t)m * (1 + p.n_rows);
+        }
+        total += 4 * (size_t)p.n_rows;
+    }
+    CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<double> host(std::max<size_t>(total, 1));
+    std::vector<DevPhase> dev(n);
+    CUDA_TRY(ctx, ctx->phasedata.ensure(host.size() * sizeof(double)));
+    CUDA_TRY(ctx, ctx->phase_tables.ensure(n * sizeof(DevPhase)));
+    const double *dbase = (const double *)ctx->phasedata.p;
+    size_t o = 0;
+    for (int32_t t = 0; t < n; ++t) {
+        const mcw_phase_table &p = tabs[t];
+        DevPhase d{};
+        d.n_rows = p.n_rows;
+        if (p.n_rows > 0) {
+            // rows follow the device table, which mcw_set_tables stored in ascending wavelength
+            const std::vector<int32_t> &ord = ctx->ice_order[t];
+            for (int e = 0; e < 6; ++e) {
+                const int32_t m = p.n_angle[e];
+                d.n_angle[e] = m;
+                memcpy(&host[o], p.cos_asc[e], m * sizeof(double));
+                d.cos_asc[e] = dbase + o;
+                o += m;
+                for (int32_t r = 0; r < p.n_rows; ++r)
+                    memcpy(&host[o + (size_t)r * m], p.p_asc[e] + (size_t)ord[r] * m, m * sizeof(double));
+                d.p_asc[e] = dbase + o;
+                o += (size_t)m * p.n_rows;
+            }
+            const double *src[4] = {p.a1, p.a2, p.b1, p.b2};
+            const double **dst[4] = {&d.a1, &d.a2, &d.b1, &d.b2};
+            for (int k = 0; k < 4; ++k) {
+                for (int32_t r = 0; r < p.n_rows; ++r) host[o + r] = src[k][ord[r]];
+                *dst[k] = dbase + o;
+                o += p.n_rows;
+            }
+            d.cos_max = p.cos_max;
+            d.cos_min = p.cos_min;
+            d.cos_cutoff = p.cos_cutoff;
+        }
+        dev[t] = d;
+    }
+    CUDA_TRY(ctx, cudaMemcpy(ctx->phasedata.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(ctx->phase_tables.p, dev.data(), n * sizeof(DevPhase), cudaMemcpyHostToDevice));
+    for (int32_t t = 0; t < n; ++t) ctx->phase_rows[t] = tabs[t].n_rows;
     return MCW_OK;
 }
 
@@ -515,21 +618,24 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     if (!ctx) return MCW_ERR_ARG;
     const auto t_start = std::chrono::steady_clock::now();
     if (!ctx->have_tables) return set_err(ctx, MCW_ERR_STATE, "mcw_set_tables has not been called");
-    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
+    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64 && mode != MCW_MODE_POL64)
+        return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
     if (records_where < MCW_RECORDS_NONE || records_where > MCW_RECORDS_DEVICE)
         return set_err(ctx, MCW_ERR_ARG, "unknown records_where %d", records_where);
     if (records_where != MCW_RECORDS_NONE && !records) return set_err(ctx, MCW_ERR_ARG, "records is NULL");
     if (records_where == MCW_RECORDS_DEVICE && ((uintptr_t)records % 16) != 0)
         return set_err(ctx, MCW_ERR_ARG, "device records must be 16-byte aligned");
     Plan plan;
-    int rc = make_plan(ctx, cfgs, n_cfg, plan);
+    int rc = make_plan(ctx, cfgs, n_cfg, mode, plan);
     if (rc) return rc;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     uint64_t h2d = 0;
     rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
     if (rc) return rc;
-    const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
+    const size_t rec_size = (mode == MCW_MODE_F32)     ? sizeof(mcw_record32)
+                            : (mode == MCW_MODE_POL64) ? sizeof(mcw_record64p)
+                                                       : sizeof(mcw_record64);
     void *dev_records = nullptr;
     if (records_where == MCW_RECORDS_DEVICE) dev_records = records;
     bool direct = false;   // host records written by the kernels themselves
@@ -568,13 +674,14 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         ra.cfgs = (const DevConfig *)ctx->cfgs.p;
         ra.prefix = (const int64_t *)((const char *)ctx->cfgs.p + prefix_offset(plan.cfgs.size()));
         ra.n_cfg = n_cfg;
-        ra.pad = 0;
+        ra.pol = (mode == MCW_MODE_POL64) ? 1 : 0;
+        ra.phase = (const DevPhase *)ctx->phase_tables.p;
         ra.total = plan.total;
         ra.imp = ctx->imp;
         ra.ice = (const DevTable *)ctx->ice_tables.p;
         Counters *cn = (Counters *)ctx->counters.p;
         ra.status = &cn->status;
-        ra.records = (mcw_record64 *)dev_records;
+        ra.records = dev_records;
         ra.tallies = (mcw_tally *)ctx->tallies.p;
         ra.budget_ns = (unsigned long long)(ctx->budget_s * 1e9);
         ra.seed = seed;
@@ -733,7 +840,7 @@ int mcw_graph_create(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, mcw_re
     if (device_records && ((uintptr_t)device_records % 16) != 0)
         return set_err(ctx, MCW_ERR_ARG, "device records must be 16-byte aligned");
     Plan plan;
-    int rc = make_plan(ctx, cfgs, n_cfg, plan);
+    int rc = make_plan(ctx, cfgs, n_cfg, MCW_MODE_F32, plan);
     if (rc) return rc;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     mcw_graph *g = new (std::nothrow) mcw_graph();

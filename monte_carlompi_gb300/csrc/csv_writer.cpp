@@ -17,6 +17,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mcwalk.h"
@@ -24,6 +25,9 @@
 namespace {
 
 const char kHeader[] = "condition wvn[um^-1] theta_n phi_n n_scat path_length[m], snow_depth[m]\n";
+// the polarised walk's file (monte_carlo3D.py:1637-1646)
+const char kHeaderPol[] =
+    "condition wvn[um^-1] theta_n phi_n n_scat path_length[m], snow_depth[m], Q_n, U_n, V_n\n";
 
 // Lay out shortest digits the way Python's float repr does.
 template <class T>
@@ -100,7 +104,9 @@ char *put_int(char *p, int64_t v) {
     return r.ptr;
 }
 
-constexpr size_t kMaxRow = 7 * 32 + 16;
+constexpr size_t kMaxRow = 10 * 32 + 16;
+
+bool mode_ok(int32_t mode) { return mode == MCW_MODE_F32 || mode == MCW_MODE_REPLAY64 || mode == MCW_MODE_POL64; }
 
 template <class R>
 size_t format_rows(const R *rec, int64_t n, char *out) {
@@ -120,6 +126,14 @@ size_t format_rows(const R *rec, int64_t n, char *out) {
         p = put_repr(p, r.path_length);
         *p++ = ' ';
         p = put_repr(p, r.snow_depth);
+        if constexpr (std::is_same<R, mcw_record64p>::value) {
+            *p++ = ' ';
+            p = put_repr(p, r.stokes_q);
+            *p++ = ' ';
+            p = put_repr(p, r.stokes_u);
+            *p++ = ' ';
+            p = put_repr(p, r.stokes_v);
+        }
         *p++ = '\n';
     }
     return (size_t)(p - out);
@@ -127,8 +141,11 @@ size_t format_rows(const R *rec, int64_t n, char *out) {
 
 size_t format_any(const void *rec, int32_t mode, int64_t off, int64_t n, char *out) {
     if (mode == MCW_MODE_F32) return format_rows(static_cast<const mcw_record32 *>(rec) + off, n, out);
+    if (mode == MCW_MODE_POL64) return format_rows(static_cast<const mcw_record64p *>(rec) + off, n, out);
     return format_rows(static_cast<const mcw_record64 *>(rec) + off, n, out);
 }
+
+const char *header_of(int32_t mode) { return mode == MCW_MODE_POL64 ? kHeaderPol : kHeader; }
 
 }  // namespace
 
@@ -137,13 +154,15 @@ extern "C" {
 int mcw_format_csv(const void *records, int32_t mode, int64_t n, int32_t header, char *buf, size_t cap,
                    size_t *used) {
     if ((!records && n > 0) || n < 0 || !used) return MCW_ERR_ARG;
-    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return MCW_ERR_ARG;
+    if (!mode_ok(mode)) return MCW_ERR_ARG;
+    const char *hdr = header_of(mode);
+    const size_t hlen = strlen(hdr);
     std::string tmp;
-    tmp.resize((size_t)n * kMaxRow + sizeof(kHeader));
+    tmp.resize((size_t)n * kMaxRow + hlen + 1);
     size_t len = 0;
     if (header) {
-        memcpy(&tmp[0], kHeader, sizeof(kHeader) - 1);
-        len = sizeof(kHeader) - 1;
+        memcpy(&tmp[0], hdr, hlen);
+        len = hlen;
     }
     len += format_any(records, mode, 0, n, &tmp[len]);
     *used = len;
@@ -153,12 +172,14 @@ int mcw_format_csv(const void *records, int32_t mode, int64_t n, int32_t header,
 
 int mcw_write_csv(const char *path, const void *records, int32_t mode, int64_t n, int32_t n_threads) {
     if (!path || (!records && n > 0) || n < 0) return MCW_ERR_ARG;
-    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return MCW_ERR_ARG;
+    if (!mode_ok(mode)) return MCW_ERR_ARG;
     if (n_threads <= 0) n_threads = (int32_t)std::max(1u, std::thread::hardware_concurrency());
     FILE *f = fopen(path, "wb");
     if (!f) return MCW_ERR_ARG;
     int rc = MCW_OK;
-    if (fwrite(kHeader, 1, sizeof(kHeader) - 1, f) != sizeof(kHeader) - 1) rc = MCW_ERR_ARG;
+    const char *hdr = header_of(mode);
+    const size_t hlen = strlen(hdr);
+    if (fwrite(hdr, 1, hlen, f) != hlen) rc = MCW_ERR_ARG;
     // chunks of rows formatted by n_threads workers, written in order
     const int64_t chunk = 1 << 16;
     std::vector<std::string> bufs(n_threads);

@@ -23,6 +23,7 @@ constexpr uint32_t kFlagLamSurface = 1u;
 constexpr uint32_t kFlagLamBottom = 2u;
 constexpr uint32_t kFlagImpurity = 4u;  // imp_cnc > 0: the species draw matters
 constexpr uint32_t kFlagNearest = 16u;  // ssp_nearest: nearest ice-table point, wavelength replaced
+constexpr uint32_t kFlagPolarised = 32u;  // polarised walk (phase matrices, Stokes vector)
 
 constexpr double kPi = 3.141592653589793;
 constexpr double kTwoPi = 6.283185307179586;  // 2*np.pi (monte_carlo3D.py:26)
@@ -54,6 +55,19 @@ struct DevConfig {
     double wvl0, scale, theta0, tau_tot_d, R_d, imp_cnc, rho_snw;
     double mux0_d, muz0_d;  // sin(theta0), -cos(theta0), evaluated on the host
     double ov_ssa_ice, ov_g, ov_ext_ice, ov_ssa_imp, ov_ext_imp;  // NaN = table
+    double stokes0[4];    // polarised walk: incident Stokes vector
+};
+
+// Phase matrices of one ice table on the device (mcw_phase_table, rows in the
+// device table's order).
+struct DevPhase {
+    const double *cos_asc[6];
+    const double *p_asc[6];
+    const double *a1, *a2, *b1, *b2;
+    int32_t n_angle[6];
+    int32_t n_rows;
+    int32_t pad;
+    double cos_max, cos_min, cos_cutoff;
 };
 
 // Optics of one wavelength grid point, FP32 walk.  32 bytes + fixed-point wvn.
@@ -112,12 +126,13 @@ struct ReplayArgs {
     const DevConfig *cfgs;
     const int64_t *prefix;
     int32_t n_cfg;
-    int32_t pad;
+    int32_t pol;                 // 1: the polarised walk, records mcw_record64p
+    const DevPhase *phase;       // per ice table (pol)
     int64_t total;
     DevTable imp;
     const DevTable *ice;         // device array of ice tables
     unsigned int *status;
-    mcw_record64 *records;
+    void *records;               // mcw_record64, or mcw_record64p (pol)
     mcw_tally *tallies;
     unsigned long long budget_ns;
     uint64_t seed;

@@ -103,7 +103,7 @@ using namespace mcw;
 extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_dev, const mcw_ssp_table *imp_dev,
                                 uint64_t seed, mcw_record32 *records_dev, mcw_tally *tally_dev, void *stream) {
     if (!cfg || !table_ok(ice_dev, true) || !table_ok(imp_dev, false)) return MCW_ERR_ARG;
-    if (cfg->ice_table != 0 || config_problem(*cfg, 1)) return MCW_ERR_ARG;
+    if (cfg->ice_table != 0 || cfg->polarised || config_problem(*cfg, 1)) return MCW_ERR_ARG;
     if (records_dev && ((uintptr_t)records_dev % 16) != 0) return MCW_ERR_ARG;
     if (tally_dev && ((uintptr_t)tally_dev % 8) != 0) return MCW_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);

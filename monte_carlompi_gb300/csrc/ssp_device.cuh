@@ -44,6 +44,7 @@ __device__ inline double ssp_interp_two(const DevTable &t, const double *y, int 
 }
 
 struct Optics {
+    int row;         // the nearest ice-table row
     double wvl_um;   // the photon's wavelength: its drawn one, or the nearest table point's (ssp_nearest)
     double ssa_ice, ssa_imp, g, ext_cff_mss, p_imp, snow_depth;
 };
@@ -63,6 +64,7 @@ __device__ inline Optics photon_optics(const DevConfig &c, const DevTable &ice, 
     double w = in_table_unit(ice, wvl_um);
     int i0, i1;
     ssp_nearest_two(ice, w, i0, i1);
+    const int i_row = i0;
     double ssa_ice, ext_ice, g;
     if (c.flags & kFlagNearest) {
         ssa_ice = ice.ssa[i0];
@@ -85,6 +87,7 @@ __device__ inline Optics photon_optics(const DevConfig &c, const DevTable &ice, 
     if (!isnan(c.ov_ext_imp)) ext_imp = c.ov_ext_imp;
     double cnc = c.imp_cnc;
     Optics o;
+    o.row = i_row;
     o.wvl_um = wvl_um;
     o.ssa_ice = ssa_ice;
     o.ssa_imp = ssa_imp;

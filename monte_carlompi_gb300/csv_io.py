@@ -18,14 +18,16 @@ COLUMNS = ['condition', 'wvn', 'theta_n', 'phi_n', 'n_scat', 'path_length', 'sno
 
 
 def output_path(output_dir, wvl0, half_width, rds_snw, n_photon, theta0_deg, make_dirs=True,
-                subdir=('sphere',)):
+                subdir=('sphere',), appendix='HG'):
     """Free output file name, as setup_output builds it (monte_carlo3D.py:96-143):
     under output_dir/sphere, or output_dir/<shape dir>/<roughness dir> for an
-    aspherical run, with rds_snw the effective radius of the particles walked."""
+    aspherical run, with rds_snw the effective radius of the particles walked;
+    appendix 'HG', or 'I%d%d%d%d' of the incident Stokes vector for the polarised
+    walk (:125-130)."""
     save_dir = os.path.join(output_dir, *subdir)
     if make_dirs:
         os.makedirs(save_dir, exist_ok=True)
-    stem = '%s_%s_%s_%s_%s_%s' % (wvl0, half_width, rds_snw, n_photon, theta0_deg, 'HG')
+    stem = '%s_%s_%s_%s_%s_%s' % (wvl0, half_width, rds_snw, n_photon, theta0_deg, appendix)
     path = os.path.join(save_dir, stem + '.txt')
     i = 0
     while os.path.isfile(path):
@@ -44,7 +46,9 @@ def _mode_of(records):
         return _abi.MODE_F32
     if records.dtype == _abi.RECORD64:
         return _abi.MODE_REPLAY64
-    raise TypeError('records must be RECORD32 or RECORD64 structured arrays')
+    if records.dtype == _abi.RECORD64P:
+        return _abi.MODE_POL64
+    raise TypeError('records must be RECORD32, RECORD64 or RECORD64P structured arrays')
 
 
 def write_csv(path, records, n_threads=0):
@@ -75,8 +79,11 @@ def read_csv(path):
         head = f.readline()
         if head.split()[:2] != ['condition', 'wvn[um^-1]']:
             raise ValueError('%s: not a monte_carlo3D CSV' % path)
-        data = np.loadtxt(f, ndmin=2) if os.path.getsize(path) > len(head) else np.zeros((0, 7))
+        ncol = 10 if head.rstrip('\n').endswith('V_n') else 7
+        data = np.loadtxt(f, ndmin=2) if os.path.getsize(path) > len(head) else np.zeros((0, ncol))
     out = {name: data[:, i] for i, name in enumerate(COLUMNS)}
+    if ncol == 10:   # the polarised walk's Q_n, U_n, V_n (monte_carlo3D.py:1637-1646)
+        out['stokes_q'], out['stokes_u'], out['stokes_v'] = data[:, 7], data[:, 8], data[:, 9]
     out['condition'] = out['condition'].astype(np.int32)
     out['n_scat'] = out['n_scat'].astype(np.int64)
     return out

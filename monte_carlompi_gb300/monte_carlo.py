@@ -27,9 +27,15 @@ effective radius is nearest to ``rds_snw``, each photon's wavelength moved to th
 nearest tabulated one, no interpolation; the CSV goes under
 ``output_dir/<shape>/<roughness>/`` named with that effective radius.
 
-Not available (raise): non-sphere shapes without HG and polarised Stokes input
-(they need the Yang et al. 2013 phase matrices, which are not part of the
-reference archive), ``debug`` and ``phase_functions`` (matplotlib figures).
+Non-spherical shapes without HG take the polarised walk (monte_carlo3D.py:
+905-1004, :1282-1342): scattering angles by rejection from the phase matrices
+P11.dat ... P44.dat beside isca.dat, the incident ``stokes_params`` carried
+through every scattering, the CSV with Q_n, U_n, V_n and the name appendix
+'I%d%d%d%d'.  It walks in FP64 on the replay stream (mode 'pol64') whatever
+``mode`` says.  (The Yang et al. 2013 files are not part of the reference
+archive; any files in their layout work.)
+
+Not available (raise): ``debug`` and ``phase_functions`` (matplotlib figures).
 """
 import math
 import os
@@ -110,12 +116,10 @@ class MonteCarlo(object):
             debug=False, Lambertian_surface=False, Lambertian_bottom=True,
             Lambertian_reflectance=1.):
         """Walk n_photon photons and write the per-photon CSV.  ALL VALUES IN MICRONS."""
-        if shape != 'sphere' and not self.HG:
-            raise NotImplementedError('only the Henyey-Greenstein path is built: shape=%r needs '
-                                      'the Yang et al. (2013) phase matrices (pass HG=True for '
-                                      'the HG-forced aspherical path)' % shape)
-        if not np.array_equal(np.asarray(stokes_params), [1, 0, 0, 0]):
-            raise NotImplementedError('HG mode carries the Stokes vector [1, 0, 0, 0] only')
+        polarised = shape != 'sphere' and not self.HG
+        stokes_params = np.asarray(stokes_params, dtype=np.float64)
+        if stokes_params.shape != (4,):
+            raise ValueError('stokes_params must hold I, Q, U, V')
         if debug:
             raise NotImplementedError('debug trajectories are matplotlib figures')
         if self.phase_functions:
@@ -139,8 +143,11 @@ class MonteCarlo(object):
             self.shape_dir = ssp.SHAPE_DIRS[shape]
             self.roughness_dir = ssp.ROUGHNESS_DIRS[roughness]
             subdir = (self.shape_dir, self.roughness_dir)
+        self.initial_stokes_params = stokes_params
         w = self.walker()
         w.set_tables([ice], imp)
+        if polarised:
+            w.set_phase_matrices([ssp.aspherical_phase_table(path, ice, wvl0)])
         cfg = WalkConfig(n_photon=int(n_photon), wvl0=float(wvl0), half_width=float(half_width),
                          theta0_deg=float(theta_0), tau_tot=float(self.tau_tot),
                          imp_cnc=float(self.imp_cnc), rho_snw=float(self.rho_snw),
@@ -149,16 +156,19 @@ class MonteCarlo(object):
                          lambertian_surface=bool(Lambertian_surface),
                          lambertian_bottom=bool(Lambertian_bottom),
                          rds_snw=float(self.snow_effective_radius), ssp_nearest=shape != 'sphere',
+                         polarised=polarised, stokes0=tuple(float(x) for x in stokes_params),
                          **self._overrides(test))
         seed = self.seed
         if seed is None:
             seed = int.from_bytes(os.urandom(8), 'little')
         self.last_seed = seed
-        res = w.walk([cfg], seed, mode=self.mode, records='host')
+        res = w.walk([cfg], seed, mode='pol64' if polarised else self.mode, records='host')
         self.records, self.tallies, self.stats = res.records, res.tallies, res.stats
         if self.write_csv:
+            appendix = 'I%d%d%d%d' % tuple(stokes_params) if polarised else 'HG'   # :123-130
             path = csv_io.output_path(self.output_dir, wvl0, half_width, self.snow_effective_radius,
-                                      n_photon, csv_io.theta0_label(theta_0), subdir=subdir)
+                                      n_photon, csv_io.theta0_label(theta_0), subdir=subdir,
+                                      appendix=appendix)
             csv_io.write_csv(path, res.records)
             self.output_file = path
             print('%s' % path)

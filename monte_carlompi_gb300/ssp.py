@@ -44,6 +44,7 @@ class SSPTable:
     ext_cff_mss: np.ndarray  # m^2/kg
     asm_prm: np.ndarray      # zeros for an impurity table
     wvl_unit: int = WVL_METRES
+    source_rows: object = None  # aspherical: the isca.dat row of each entry
 
     def __post_init__(self):
         self.wvl = np.ascontiguousarray(self.wvl, dtype=np.float64)
@@ -228,7 +229,8 @@ def aspherical_table(path, wvl0, rds_snw, rho_ice=917.0):
     w = wvl[rows][order]
     if np.any(np.diff(w) <= 0):
         raise ValueError('%s: repeated wavelength for RE = %r um' % (path, re_sel))
-    return SSPTable(w, ssa[rows][order], ext[order], asm[rows][order], wvl_unit=WVL_MICRONS), float(re_sel)
+    return (SSPTable(w, ssa[rows][order], ext[order], asm[rows][order], wvl_unit=WVL_MICRONS,
+                     source_rows=rows[order]), float(re_sel))
 
 
 def synthetic_isca_rows(wvls_um, re_um):
@@ -254,3 +256,118 @@ def write_isca(path, rows):
     with open(path, 'w') as f:
         for r in rows:
             f.write('%.4f %r %r %r %r %r %r\n' % tuple(float(x) for x in r))
+
+
+# Phase-matrix elements of the polarised walk (read_phase_matrix_elements,
+# monte_carlo3D.py:145-171, :267-475): P11.dat, P12.dat, P22.dat, P33.dat,
+# P43.dat, P44.dat beside isca.dat.  First line: the scattering angles [deg];
+# then one line per isca.dat row with the element at those angles; P12 ... P44
+# are stored divided by P11.
+PHASE_ELEMENTS = ('P11', 'P12', 'P22', 'P33', 'P43', 'P44')
+
+
+def read_phase_matrix(particle_dir, rows):
+    """The six elements for isca.dat rows `rows` (indices into the file's rows, in
+    the order given): returns (theta_deg[6][n_angle], P[6][len(rows)][n_angle]) with
+    P12 ... P44 multiplied back by P11, as :418-475 do."""
+    thetas, els = [], []
+    for name in PHASE_ELEMENTS:
+        with open(os.path.join(particle_dir, name + '.dat')) as f:
+            head = f.readline().split()
+            lines = f.readlines()
+        thetas.append(np.array([float(t) for t in head], dtype=np.float64))
+        els.append(np.array([[float(v) for v in lines[r].split()[:len(head)]] for r in rows],
+                            dtype=np.float64).reshape(len(rows), len(head)))
+    p11 = els[0]
+    return thetas, [p11] + [e * p11 for e in els[1:]]
+
+
+def synthetic_phase_rows(isca_rows, theta_deg):
+    """Synthetic phase matrices for isca.dat rows (tests and fixtures): P11 a
+    Henyey-Greenstein function with the row's asymmetry parameter; P12/P11 =
+    -0.3 sin^2/(1 + cos^2); P22/P11 = 0.9 + 0.1 cos; P33/P11 = 0.8 cos + 0.1;
+    P43/P11 = 0.05 sin (1 - cos); P44/P11 = 0.85 cos + 0.1.  Returns the six
+    element arrays [n_rows][n_angle] as stored (P12 ... P44 divided by P11)."""
+    th = np.deg2rad(np.asarray(theta_deg, dtype=np.float64))
+    c, s = np.cos(th), np.sin(th)
+    p11 = []
+    for r in isca_rows:
+        g = float(r[6])
+        p11.append((1 - g * g) / (1 + g * g - 2 * g * c) ** 1.5)
+    p11 = np.array(p11)
+    n = p11.shape[0]
+    ratios = [-0.3 * s * s / (1 + c * c), 0.9 + 0.1 * c, 0.8 * c + 0.1, 0.05 * s * (1 - c),
+              0.85 * c + 0.1]
+    return [p11] + [np.tile(q, (n, 1)) for q in ratios]
+
+
+def write_phase_matrix(particle_dir, theta_deg, elements):
+    """Write P11.dat ... P44.dat (element arrays as synthetic_phase_rows returns)."""
+    os.makedirs(particle_dir, exist_ok=True)
+    for name, e in zip(PHASE_ELEMENTS, elements):
+        with open(os.path.join(particle_dir, name + '.dat'), 'w') as f:
+            f.write(' '.join('%r' % float(t) for t in theta_deg) + '\n')
+            for row in e:
+                f.write(' '.join('%r' % float(v) for v in row) + '\n')
+
+
+@dataclass
+class PhaseTable:
+    """Phase matrices of the polarised walk for the rows of an aspherical SSP table
+    (same order), as interpolate_phase_matrix (monte_carlo3D.py:819-883) prepares
+    them: element e (P11, P12, P22, P33, P43, P44) at cos_asc[e] = cos of the file's
+    angles, ascending, with values p_asc[e][row, j] (P12 ... P44 multiplied by P11);
+    the two areas of the rejection sampler split at cos_cutoff, and each row's
+    maxima of |P11| (a1, a2) and |P12| (b1, b2) over them (:929-947)."""
+    cos_asc: list
+    p_asc: list
+    cos_max: float
+    cos_min: float
+    cos_cutoff: float
+    cutoff_idx: int
+    a1: np.ndarray
+    a2: np.ndarray
+    b1: np.ndarray
+    b2: np.ndarray
+
+
+def phase_table(thetas_deg, elements, row_wvl_um, wvl0):
+    """Build a PhaseTable from the six elements' angle grids [deg] and values
+    [n_rows][n_angle] (P12 ... P44 already multiplied by P11; rows in the order of
+    the SSP table whose wavelengths are row_wvl_um).  The area split comes from
+    P11 at wvl0, with the reference's arithmetic (:850-883).  (The reference takes
+    the last drawn wavelength instead when no photon drew wvl0, which a run of more
+    than a handful of photons never meets.)"""
+    cos_desc = [np.cos((np.asarray(t, dtype=np.float64) * np.pi) / 180.) for t in thetas_deg]
+    rows0 = np.where(np.asarray(row_wvl_um) == wvl0)[0]
+    if rows0.size == 0:
+        raise ValueError('wvl0 = %r um is not a row of the table' % (wvl0,))
+    P11 = elements[0][rows0[0]]
+    c11 = cos_desc[0]
+    cos_max, cos_min = c11[0], c11[-1]
+    pct = []
+    n = len(c11)
+    for i, ct in enumerate(c11):
+        if 0 < i < n - 1:
+            m1 = P11[:i + 1].max()
+            m2 = P11[i:].max()
+            a1 = (cos_max - ct) * m1
+            a2 = (ct - cos_min) * m2
+            pct.append(a1 / (a1 + a2))
+        else:
+            pct.append(1e5)
+    cut = int(np.argsort(np.absolute(0.5 - np.array(pct)))[0])
+    p11, p12 = elements[0], elements[1]
+    return PhaseTable(
+        cos_asc=[np.ascontiguousarray(c[::-1]) for c in cos_desc],
+        p_asc=[np.ascontiguousarray(np.asarray(e, dtype=np.float64)[:, ::-1]) for e in elements],
+        cos_max=float(cos_max), cos_min=float(cos_min), cos_cutoff=float(c11[cut]), cutoff_idx=cut,
+        a1=np.absolute(p11[:, :cut + 1]).max(axis=1), a2=np.absolute(p11[:, cut:]).max(axis=1),
+        b1=np.absolute(p12[:, :cut + 1]).max(axis=1), b2=np.absolute(p12[:, cut:]).max(axis=1))
+
+
+def aspherical_phase_table(isca_file, table, wvl0):
+    """The PhaseTable of an aspherical SSP table made by aspherical_table from
+    isca_file: P11.dat ... P44.dat of the same directory, rows of the selected size."""
+    thetas, els = read_phase_matrix(os.path.dirname(isca_file), table.source_rows)
+    return phase_table(thetas, els, table.wvl, wvl0)

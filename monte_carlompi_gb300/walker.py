@@ -14,6 +14,30 @@ from . import _abi
 from .config import configs_to_c
 
 
+# walk modes: (ABI mode, record dtype)
+MODES = {'f32': (_abi.MODE_F32, _abi.RECORD32),
+         'replay64': (_abi.MODE_REPLAY64, _abi.RECORD64),
+         'pol64': (_abi.MODE_POL64, _abi.RECORD64P)}
+
+
+def _phase_c(p, keep):
+    """mcw_phase_table of a monte_carlompi_gb300.ssp.PhaseTable (None: an empty entry)."""
+    c = _abi.PhaseTableC()
+    if p is None:
+        return c
+    cols = [np.ascontiguousarray(a, np.float64) for a in list(p.cos_asc) + list(p.p_asc)]
+    ext = [np.ascontiguousarray(a, np.float64) for a in (p.a1, p.a2, p.b1, p.b2)]
+    keep.extend(cols + ext)
+    c.n_rows = cols[6].shape[0]
+    for e in range(6):
+        c.n_angle[e] = cols[e].size
+        c.cos_asc[e] = cols[e].ctypes.data
+        c.p_asc[e] = cols[6 + e].ctypes.data
+    c.a1, c.a2, c.b1, c.b2 = (a.ctypes.data for a in ext)
+    c.cos_max, c.cos_min, c.cos_cutoff = float(p.cos_max), float(p.cos_min), float(p.cos_cutoff)
+    return c
+
+
 def _table_c(t, keep):
     cols = [np.ascontiguousarray(t.wvl, np.float64), np.ascontiguousarray(t.ss_alb, np.float64),
             np.ascontiguousarray(t.ext_cff_mss, np.float64), np.ascontiguousarray(t.asm_prm, np.float64)]
@@ -106,6 +130,14 @@ class Walker:
     def set_budget(self, seconds):
         _abi.check(self._lib.mcw_set_budget(self._ctx, float(seconds)), self._ctx)
 
+    def set_phase_matrices(self, tables):
+        """Phase matrices of the polarised walk: one ssp.PhaseTable (or None) per ice
+        table of the last set_tables, rows in that table's order."""
+        keep = []
+        arr = (_abi.PhaseTableC * len(tables))(*[_phase_c(t, keep) for t in tables])
+        rc = self._lib.mcw_set_phase_matrices(self._ctx, arr, len(tables))
+        _abi.check(rc, self._ctx)
+
     def walk(self, configs, seed, mode='f32', records='host', out=None, device_ptr=None):
         """Walk every photon of ``configs``.
 
@@ -113,8 +145,9 @@ class Walker:
         ``out``), 'device' (written to ``device_ptr``, a 16-byte aligned device
         address the caller owns) or None.
         """
-        mode_c = _abi.MODE_F32 if mode == 'f32' else _abi.MODE_REPLAY64
-        dtype = _abi.RECORD32 if mode_c == _abi.MODE_F32 else _abi.RECORD64
+        if mode not in MODES:
+            raise ValueError('mode must be one of %s' % ', '.join(sorted(MODES)))
+        mode_c, dtype = MODES[mode]
         cfg = configs_to_c(configs)
         n = len(configs)
         total = int(sum(max(int(c.n_photon), 0) for c in configs))

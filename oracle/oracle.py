@@ -16,7 +16,7 @@ RECORD_DTYPE = np.dtype([
     ('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float64),
     ('theta_n', np.float64), ('phi_n', np.float64), ('path_length', np.float64),
     ('snow_depth', np.float64), ('n_draws', np.int64), ('phi_undefined', np.int32),
-    ('pad', np.int32)])
+    ('pad', np.int32), ('stokes', np.float64, (4,))])
 
 
 class Table(ctypes.Structure):
@@ -33,7 +33,34 @@ class Config(ctypes.Structure):
                 ('R', ctypes.c_double), ('ssa_ice_override', ctypes.c_double),
                 ('g_override', ctypes.c_double), ('ext_ice_override', ctypes.c_double),
                 ('ssa_imp_override', ctypes.c_double), ('ext_imp_override', ctypes.c_double),
-                ('nearest', ctypes.c_int32), ('pad', ctypes.c_int32)]
+                ('nearest', ctypes.c_int32), ('pad', ctypes.c_int32), ('phase', ctypes.c_void_p)]
+
+
+class Phase(ctypes.Structure):
+    _fields_ = [('n_rows', ctypes.c_int32), ('pad', ctypes.c_int32),
+                ('n_angle', ctypes.c_int32 * 6), ('cos_asc', ctypes.c_void_p * 6),
+                ('p_asc', ctypes.c_void_p * 6), ('a1', ctypes.c_void_p), ('a2', ctypes.c_void_p),
+                ('b1', ctypes.c_void_p), ('b2', ctypes.c_void_p), ('cos_max', ctypes.c_double),
+                ('cos_min', ctypes.c_double), ('cos_cutoff', ctypes.c_double),
+                ('stokes0', ctypes.c_double * 4)]
+
+
+def make_phase(pt, stokes0):
+    """ctypes view of a monte_carlompi_gb300.ssp.PhaseTable (keeps its arrays alive)."""
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in pt.cos_asc + pt.p_asc]
+    ext = [np.ascontiguousarray(a, dtype=np.float64) for a in (pt.a1, pt.a2, pt.b1, pt.b2)]
+    ph = Phase()
+    ph.n_rows = pt.p_asc[0].shape[0]
+    for e in range(6):
+        ph.n_angle[e] = keep[e].size
+        ph.cos_asc[e] = keep[e].ctypes.data
+        ph.p_asc[e] = keep[6 + e].ctypes.data
+    ph.a1, ph.a2, ph.b1, ph.b2 = (a.ctypes.data for a in ext)
+    ph.cos_max, ph.cos_min, ph.cos_cutoff = pt.cos_max, pt.cos_min, pt.cos_cutoff
+    for k in range(4):
+        ph.stokes0[k] = float(stokes0[k])
+    ph._keep = keep + ext
+    return ph
 
 
 def build():
@@ -95,11 +122,14 @@ class _Tables:
 def make_config(n_photon, wvl0, half_width, theta0_deg, tau_tot, imp_cnc=0.0, rho_snw=300.0,
                 rho_ice=917.0, lam_surface=False, lam_bottom=True, R=1.0,
                 ssa_ice_override=np.nan, g_override=np.nan, ext_ice_override=np.nan,
-                ssa_imp_override=np.nan, ext_imp_override=np.nan, nearest=False):
-    return Config(int(n_photon), wvl0, half_width, theta0_deg, tau_tot, imp_cnc, rho_snw, rho_ice,
-                  int(bool(lam_surface)), int(bool(lam_bottom)), R, ssa_ice_override,
-                  g_override, ext_ice_override, ssa_imp_override, ext_imp_override,
-                  int(bool(nearest)), 0)
+                ssa_imp_override=np.nan, ext_imp_override=np.nan, nearest=False, phase=None):
+    """phase: a Phase (make_phase) for the polarised walk, or None."""
+    c = Config(int(n_photon), wvl0, half_width, theta0_deg, tau_tot, imp_cnc, rho_snw, rho_ice,
+               int(bool(lam_surface)), int(bool(lam_bottom)), R, ssa_ice_override,
+               g_override, ext_ice_override, ssa_imp_override, ext_imp_override,
+               int(bool(nearest)), 0, None if phase is None else ctypes.addressof(phase))
+    c._phase = phase
+    return c
 
 
 def walk(cfg, ice, imp, seed, p0=0, p1=None, threads=1):
@@ -126,7 +156,31 @@ def config_from_golden(g):
                        p('imp_cnc'), p('rho_snw'), p('rho_ice'), p('lam_surface'),
                        p('lam_bottom'), p('R'), ssa_ice_override=p('ssa_ice_override'),
                        g_override=p('g_override'),
-                       nearest=bool(g['param_ssp_nearest'].item()) if 'param_ssp_nearest' in g else False)
+                       nearest=bool(g['param_ssp_nearest'].item()) if 'param_ssp_nearest' in g else False,
+                       phase=phase_from_golden(g))
+
+
+def phase_from_golden(g):
+    """The polarised walk's phase matrices of a golden fixture (None for the others)."""
+    if 'param_polarised' not in g:
+        return None
+    from monte_carlompi_gb300 import ssp
+    return make_phase(ssp_phase_from_golden(g), g['stokes0'])
+
+
+def ssp_phase_from_golden(g):
+    """PhaseTable of a golden fixture: its stored P rows (P12 ... P44 divided by P11)
+    for the isca.dat rows of the selected size, in the SSP table's order."""
+    from monte_carlompi_gb300 import ssp
+    rows = g['isca_rows']
+    re = 0.75 * rows[:, 2] / rows[:, 3]
+    sel = np.where(re == re[np.argmin(np.abs(re - g['param_rds_selected'].item()))])[0]
+    sel = sel[np.argsort(rows[sel, 0], kind='stable')]
+    st = g['phase_stored']
+    p11 = st[0][sel]
+    els = [p11] + [e[sel] * p11 for e in st[1:]]
+    theta = g['phase_theta']
+    return ssp.phase_table([theta] * 6, els, rows[sel, 0], g['param_wvl0'].item())
 
 
 def tables_from_golden(g):

@@ -101,7 +101,27 @@ typedef struct {
      * takes that point's wavelength for the impurity lookup and wvn */
     int32_t nearest;
     int32_t pad;
+    /* non-NULL: the polarised walk of aspherical grains (HG off), with these phase
+     * matrices for the ice-table rows (requires nearest) */
+    const struct orc_phase *phase;
 } orc_config;
+
+/* Phase matrices of the polarised walk for the rows of the ice table
+ * (interpolate_phase_matrix, monte_carlo3D.py:819-883, and the envelope of the
+ * rejection sampler, :866-883, :933-951).  Element e (P11, P12, P22, P33, P43,
+ * P44) is tabulated at cos_asc[e] (cos of the file's angles, ascending) with
+ * values p_asc[e][row * n_angle[e] + j] (P12 ... P44 multiplied by P11).  cos_max /
+ * cos_min / cos_cutoff and the per-row maxima a1, a2 (|P11| over the two areas)
+ * and b1, b2 (|P12|) are computed by the host exactly as :866-883, :933-951 do. */
+typedef struct orc_phase {
+    int32_t n_rows, pad;
+    int32_t n_angle[6];
+    const double *cos_asc[6];
+    const double *p_asc[6];
+    const double *a1, *a2, *b1, *b2;
+    double cos_max, cos_min, cos_cutoff;
+    double stokes0[4];
+} orc_phase;
 
 typedef struct {
     int32_t condition, n_scat;
@@ -109,6 +129,7 @@ typedef struct {
     int64_t n_draws;      /* uniforms consumed from the walk stream */
     int32_t phi_undefined;/* reference would raise: mux or muy exactly 0 (monte_carlo3D.py:1472-1485) */
     int32_t pad;
+    double stokes[4];     /* final Stokes vector (polarised walk; the incident one otherwise) */
 } orc_record;
 
 /* ---------------------------------------------------------------- lookups */
@@ -152,7 +173,7 @@ double orc_wavelength(uint64_t seed, uint64_t photon, double wvl0, double half_w
 }
 
 /* Per-photon optics: monte_carlo3D.py:1524-1612. */
-typedef struct { double wvl, ssa_ice, ssa_imp, g, ext_cff_mss, P_ext_imp, snow_depth; } orc_optics;
+typedef struct { double wvl, ssa_ice, ssa_imp, g, ext_cff_mss, P_ext_imp, snow_depth; int32_t row; } orc_optics;
 
 /* A wavelength in um in a table's unit: the netCDF lookups compare wvl * 1e-6
  * with metres (monte_carlo3D.py:518, :673); the aspherical one compares um
@@ -169,6 +190,7 @@ static orc_optics photon_optics(const orc_config *c, const orc_table *ice, const
     int32_t i0, i1;
     double ssa_ice, ext_ice, g;
     nearest_two(ice, w, &i0, &i1);
+    o.row = i0;
     if (c->nearest) {
         /* argsort(|wvl - wvl_in|)[0]: ssa_in, Q_ext-derived ext_cff_mss and asm_in of that
          * row (:396-415); the photon's wavelength becomes wvl_in of that row (:399, :1536) */
@@ -201,6 +223,87 @@ static orc_optics photon_optics(const orc_config *c, const orc_table *ice, const
     return o;
 }
 
+/* scipy interp1d (linear) at x of a table with ascending x: searchsorted (left),
+ * clipped to [1, n-1], then the two-term form of interp1d._call_linear. */
+static double interp_n(const double *x, const double *y, int32_t n, double xn)
+{
+    int32_t lo = 0, hi = n;          /* first index with x[i] >= xn */
+    while (lo < hi) {
+        int32_t mid = (lo + hi) / 2;
+        if (x[mid] < xn) lo = mid + 1; else hi = mid;
+    }
+    int32_t k = lo < 1 ? 1 : (lo > n - 1 ? n - 1 : lo);
+    double xl = x[k - 1], xh = x[k], yl = y[k - 1], yh = y[k];
+    return ((xn - xl) / (xh - xl)) * yh + ((xh - xn) / (xh - xl)) * yl;
+}
+
+static double phase_el(const orc_phase *ph, int e, int32_t row, double ct)
+{
+    return interp_n(ph->cos_asc[e], ph->p_asc[e] + (size_t)row * ph->n_angle[e], ph->n_angle[e], ct);
+}
+
+/* rotate_stokes_vector, monte_carlo3D.py:1090-1109 */
+static void rotate_stokes(double angle, const double in[4], double out[4])
+{
+    double d = 2 * angle;
+    double cd = cos(d), sd = sin(d);
+    out[0] = in[0];
+    out[1] = in[1] * cd + in[2] * sd;
+    out[2] = -in[1] * sd + in[2] * cd;
+    out[3] = in[3];
+}
+
+/* Scattering cosine and azimuth of the polarised walk: the two-area rejection
+ * sampler of populate_pdfs, monte_carlo3D.py:922-1004, for the photon's current
+ * Stokes vector st. */
+static void polarised_angles(const orc_phase *ph, int32_t row, const double st[4], orc_stream *s,
+                             double *p_rand, double *phi_rand)
+{
+    double I = st[0], Q = st[1], U = st[2];
+    double two_beta = (Q == 0) ? atan(U / 1e-15) : atan(U / Q);                /* :908-911 */
+    double C = fabs(Q * cos(two_beta) + U * sin(two_beta));                     /* :935 */
+    double max_val1 = fabs(I) * ph->a1[row] + ph->b1[row] * C;                  /* :931-937 */
+    double max_val2 = fabs(I) * ph->a2[row] + ph->b2[row] * C;                  /* :940-947 */
+    double area1 = (ph->cos_max - ph->cos_cutoff) * max_val1;                   /* :949-951 */
+    double area2 = (ph->cos_cutoff - ph->cos_min) * max_val2;
+    double percent_area1 = area1 / (area1 + area2);
+    double area_rand = stream_next(s);                                          /* :953-957 */
+    double cos_theta = stream_next(s);
+    double two_phi = 2 * (stream_next(s) * ORC_TWO_PI);
+    int area;
+    if (area_rand < percent_area1) {                                            /* :963-973 */
+        area = 1;
+        cos_theta = cos_theta * (ph->cos_max - ph->cos_cutoff) + ph->cos_cutoff;
+    } else {
+        area = 2;
+        cos_theta = -cos_theta * (ph->cos_cutoff - ph->cos_min) + ph->cos_cutoff;
+    }
+    double r3 = 1, pf = 0;                                                      /* :976-1001 */
+    int64_t k = 0;
+    while (r3 > pf) {
+        if (k > 0) {
+            area_rand = stream_next(s);
+            if (area_rand < percent_area1) {
+                area = 1;
+                cos_theta = stream_next(s) * (ph->cos_max - ph->cos_cutoff) + ph->cos_cutoff;
+            } else {
+                area = 2;
+                cos_theta = -stream_next(s) * (ph->cos_cutoff - ph->cos_min) + ph->cos_cutoff;
+            }
+            two_phi = stream_next(s) * (4 * ORC_PI);
+        }
+        r3 = 1.000001 * stream_next(s);
+        if (area == 1) r3 = r3 * max_val1;
+        else r3 = r3 * max_val2;
+        double S11 = phase_el(ph, 0, row, cos_theta);
+        double S12 = phase_el(ph, 1, row, cos_theta);
+        pf = I * S11 + S12 * (Q * cos(two_phi) + U * sin(two_phi));
+        k += 1;
+    }
+    *p_rand = cos_theta;
+    *phi_rand = two_phi / 2.;
+}
+
 /* Henyey_Greenstein2, monte_carlo3D.py:790-800. */
 static double hg2(double g, double r)
 {
@@ -227,6 +330,9 @@ void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table 
     double ssa_rand = stream_next(&s);
     double ext_rand = stream_next(&s);
     double p_rand = 0, phi_rand = 0;
+    const orc_phase *ph = c->phase;
+    double st[4] = {1, 0, 0, 0};                                               /* :1132 */
+    if (ph) { st[0] = ph->stokes0[0]; st[1] = ph->stokes0[1]; st[2] = ph->stokes0[2]; st[3] = ph->stokes0[3]; }
 
     double mux_0 = sin(theta0), muy_0 = 0, muz_0 = -cos(theta0);              /* :1121-1124 */
     double muz2_0 = muz_0 * muz_0;
@@ -240,8 +346,12 @@ void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table 
         i += 1;
         i_rand += 1;
         if (i_rand > 1) {                                                      /* :1215-1224 */
-            p_rand = hg2(o.g, stream_next(&s));
-            phi_rand = stream_next(&s) * ORC_TWO_PI;
+            if (ph) {
+                polarised_angles(ph, o.row, st, &s, &p_rand, &phi_rand);
+            } else {
+                p_rand = hg2(o.g, stream_next(&s));
+                phi_rand = stream_next(&s) * ORC_TWO_PI;
+            }
             tau_rand = -log(stream_next(&s));
             ssa_rand = stream_next(&s);
             ext_rand = stream_next(&s);
@@ -284,7 +394,38 @@ void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table 
                 muy_n = (sintheta * (muy_0 * muz_0 * cosphi + mux_0 * sinphi)) / sq + muy_0 * costheta;
                 muz_n = -sq * sintheta * cosphi + muz_0 * costheta;
             }
-            if (bottom_reflection) bottom_reflection = 0;                      /* :1283-1285 */
+            if (bottom_reflection) {                                           /* :1283-1285 */
+                st[0] = 1; st[1] = 0; st[2] = 0; st[3] = 0;
+                bottom_reflection = 0;
+            } else if (ph) {                                                   /* :1287-1342 */
+                double cos2theta = costheta * costheta;
+                double phi_sca = acos(cosphi);
+                double sp[4], sc[4], sm[4];
+                rotate_stokes(phi_sca, st, sp);
+                double P11 = phase_el(ph, 0, o.row, costheta), P12 = phase_el(ph, 1, o.row, costheta);
+                double P22 = phase_el(ph, 2, o.row, costheta), P33 = phase_el(ph, 3, o.row, costheta);
+                double P43 = phase_el(ph, 4, o.row, costheta), P44 = phase_el(ph, 5, o.row, costheta);
+                sc[0] = sp[0] * P11 + sp[1] * P12;
+                sc[1] = sp[0] * P12 + sp[1] * P22;
+                sc[2] = sp[2] * P33 - sp[3] * P43;
+                sc[3] = sp[2] * P43 + sp[3] * P44;
+                double den = sqrt((1 - cos2theta) * (1 - muz_n * muz_n));
+                double cos_i;
+                if (den == 0) {
+                    cos_i = 0;
+                } else {
+                    double num = muz_n * costheta - muz_0;
+                    double sign = (phi_sca >= ORC_PI) ? 1 : -1;
+                    cos_i = num / (sign * den);
+                    if (cos_i < -1) cos_i = -1;
+                    else if (cos_i > 1) cos_i = 1;
+                }
+                double i_2 = acos(cos_i);
+                rotate_stokes(-i_2, sc, sm);
+                double I_merd = sm[0];
+                st[0] = sm[0] / I_merd; st[1] = sm[1] / I_merd;
+                st[2] = sm[2] / I_merd; st[3] = sm[3] / I_merd;
+            }
         } else {                                                               /* :1344-1347 */
             mux_n = mux_0; muy_n = muy_0; muz_n = muz_0;
         }
@@ -336,6 +477,7 @@ void orc_walk_photon(const orc_config *c, const orc_table *ice, const orc_table 
     out->snow_depth = o.snow_depth;
     out->n_draws = (int64_t)s.k;
     out->pad = 0;
+    out->stokes[0] = st[0]; out->stokes[1] = st[1]; out->stokes[2] = st[2]; out->stokes[3] = st[3];
 }
 
 /* Photons [p0, p1) of one run, in order (the loop of monte_carlo3D.py:1613-1616). */

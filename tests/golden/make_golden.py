@@ -86,7 +86,16 @@ CASES = {
     'asph': dict(n_photon=600, wvl0=1.3, half_width=0.085, rds=100.0, theta0=30.0,
                  tau_tot=40.0, imp_cnc=1e-4, lam_bottom=True, R=0.5, seed=0x5EED0016,
                  shape='solid hexagonal column', roughness='smooth', csv=True),
+    # polarised walk of aspherical grains (HG off): the same synthetic isca.dat plus
+    # synthetic P11 ... P44 on a non-uniform angle grid; rejection-sampled scattering
+    # angles and the Stokes vector of a partially polarised incident beam
+    'pol': dict(n_photon=300, wvl0=1.3, half_width=0.085, rds=100.0, theta0=30.0,
+                tau_tot=20.0, lam_bottom=True, R=0.5, seed=0x5EED0017,
+                shape='hexagonal plate', roughness='moderately rough', hg=False,
+                stokes=(1.0, 0.3, 0.2, 0.1), csv=True),
 }
+
+PHASE_THETA = [0.5 * k for k in range(20)] + [10.0 + 2.0 * k for k in range(86)]   # deg, 0 .. 180
 
 ASPH_WVLS = [round(1.0 + 0.025 * i, 4) for i in range(41)]   # 1.0 .. 2.0 um
 ASPH_RE = [60.0, 120.0, 250.0]
@@ -195,7 +204,7 @@ def run_case(name, spec, outdir):
     old_cwd, old_argv = os.getcwd(), sys.argv
     saved = (np.random.rand, np.random.uniform, np.random.normal)
     replay = Replay(spec['seed'])
-    answers, draws = [], []
+    answers, draws, stokes = [], [], []
     try:
         os.chdir(work)
         sys.argv = ['monte_carlo3D']
@@ -208,13 +217,16 @@ def run_case(name, spec, outdir):
             isca_rows = np.array(ssp.synthetic_isca_rows(ASPH_WVLS, ASPH_RE), dtype=np.float64)
             isca = ssp.isca_path(optics, shape, spec['roughness'], spec['wvl0'])
             ssp.write_isca(isca, isca_rows)
+            if not spec.get('hg', True):
+                ssp.write_phase_matrix(os.path.dirname(isca), PHASE_THETA,
+                                       ssp.synthetic_phase_rows(isca_rows, PHASE_THETA))
             # what the library walks: this package's reader of the same file
             ice, re_sel = ssp.aspherical_table(isca, spec['wvl0'], spec['rds'], rho_ice)
             isca_rows = ssp.read_isca(isca)
         model = ref.MonteCarlo(tau_tot=tau_tot, imp_cnc=spec.get('imp_cnc', 0.0),
                                rho_snw=rho_snw, rho_ice=rho_ice,
                                output_dir=os.path.join(work, 'out'), optics_dir=optics,
-                               fi_imp='imp.nc', HG=shape != 'sphere')
+                               fi_imp='imp.nc', HG=shape != 'sphere' and spec.get('hg', True))
         for k, v in spec.get('test', {}).items():
             setattr(model, k, v)
 
@@ -225,6 +237,7 @@ def run_case(name, spec, outdir):
             replay.photon, replay.k = self.photon, 3
             out = orig_walk(self, wvl)
             answers.append(out[:7])
+            stokes.append([float(x) for x in np.asarray(out[7]).ravel()[:4]])
             draws.append(replay.k)
             replay.photon = None
             return out
@@ -244,6 +257,7 @@ def run_case(name, spec, outdir):
             model.run(spec['n_photon'], spec['wvl0'], spec['half_width'], spec['rds'],
                       theta_0=spec['theta0'], test=bool(spec.get('test')),
                       shape=shape, roughness=spec.get('roughness', 'smooth'),
+                      stokes_params=np.array(spec.get('stokes', (1, 0, 0, 0))),
                       Lambertian_surface=spec.get('lam_surface', False),
                       Lambertian_bottom=spec['lam_bottom'],
                       Lambertian_reflectance=spec['R'])
@@ -283,6 +297,12 @@ def run_case(name, spec, outdir):
         params.update(ssp_nearest=1, rds_selected=re_sel)
         extra = dict(ice_unit=np.asarray(ice.wvl_unit), isca_rows=isca_rows,
                      shape=np.asarray(shape), roughness=np.asarray(spec['roughness']))
+    if not spec.get('hg', True):
+        params.update(polarised=1)
+        extra.update(stokes0=np.array(spec['stokes'], dtype=np.float64),
+                     stokes=np.array(stokes, dtype=np.float64),
+                     phase_theta=np.array(PHASE_THETA, dtype=np.float64),
+                     phase_stored=np.array(ssp.synthetic_phase_rows(isca_rows, PHASE_THETA)))
     np.savez_compressed(
         os.path.join(outdir, name + '.npz'),
         **rec, **{'param_' + k: np.asarray(v) for k, v in params.items()},

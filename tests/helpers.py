@@ -48,7 +48,21 @@ def golden_config(g):
                       lambertian_reflectance=p('R'), lambertian_surface=bool(p('lam_surface')),
                       lambertian_bottom=bool(p('lam_bottom')),
                       ssa_ice_override=p('ssa_ice_override'), g_override=p('g_override'),
-                      ssp_nearest=bool(p('ssp_nearest')) if 'param_ssp_nearest' in g else False)
+                      ssp_nearest=bool(p('ssp_nearest')) if 'param_ssp_nearest' in g else False,
+                      polarised='param_polarised' in g,
+                      stokes0=tuple(float(x) for x in g['stokes0']) if 'stokes0' in g else (1.0, 0.0, 0.0, 0.0))
+
+
+def golden_phase(g):
+    """Phase matrices of a polarised golden fixture (None for the others)."""
+    if 'param_polarised' not in g:
+        return None
+    from oracle import oracle
+    return oracle.ssp_phase_from_golden(g)
+
+
+def golden_mode(g):
+    return 'pol64' if 'param_polarised' in g else 'replay64'
 
 
 def golden_tables(g):

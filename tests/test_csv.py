@@ -9,13 +9,15 @@ from tests.conftest import GOLDEN, load_golden
 
 
 def _records64(g):
-    r = np.zeros(g['condition'].size, _abi.RECORD64)
+    r = np.zeros(g['condition'].size, _abi.RECORD64P if 'stokes' in g else _abi.RECORD64)
     for k in ('condition', 'n_scat', 'wvn', 'theta_n', 'phi_n', 'path_length', 'snow_depth'):
         r[k] = g[k]
+    if 'stokes' in g:
+        r['stokes_q'], r['stokes_u'], r['stokes_v'] = g['stokes'][:, 1], g['stokes'][:, 2], g['stokes'][:, 3]
     return r
 
 
-@pytest.mark.parametrize('name', ['cfg1', 'cfg2', 'asph'])
+@pytest.mark.parametrize('name', ['cfg1', 'cfg2', 'asph', 'pol'])
 def test_reference_csv_bytes(name, tmp_path):
     g = load_golden(name)
     ref = open(os.path.join(GOLDEN, name + '.csv'), 'rb').read()

@@ -48,6 +48,36 @@ def test_run_aspherical_hg_reproduces_reference_csv(tmp_path, monkeypatch, capsy
     compare_replay(got, csv_io.read_csv(os.path.join(GOLDEN, 'asph.csv')))
 
 
+def test_run_polarised_reproduces_reference_csv(tmp_path, monkeypatch, capsys):
+    """run(shape=...) with HG off: the polarised walk on the same isca.dat and
+    P11.dat ... P44.dat; the file (name appendix I%d%d%d%d, Q_n U_n V_n columns)
+    holds the reference's photons and Stokes vectors."""
+    g = load_golden('pol')
+    p = lambda k: g['param_' + k].item()  # noqa: E731
+    monkeypatch.chdir(tmp_path)
+    optics = str(tmp_path / 'optics')
+    shape, rough = str(g['shape']), str(g['roughness'])
+    isca = ssp.isca_path(optics, shape, rough, p('wvl0'))
+    ssp.write_isca(isca, g['isca_rows'])
+    ssp.write_phase_matrix(os.path.dirname(isca), g['phase_theta'], list(g['phase_stored']))
+    _, imp = golden_tables(g)
+    ssp.write_netcdf(os.path.join(optics, 'mie', 'snicar', 'imp.nc'), imp, with_asm=False)
+    mc = MonteCarlo(tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'), rho_snw=p('rho_snw'),
+                    rho_ice=p('rho_ice'), output_dir=str(tmp_path / 'out'), optics_dir=optics,
+                    fi_imp='imp.nc', ssp='file', seed=int(p('seed')))
+    mc.run(int(p('n_photon')), p('wvl0'), p('half_width'), p('rds'), theta_0=p('theta0'),
+           stokes_params=g['stokes0'], shape=shape, roughness=rough,
+           Lambertian_bottom=bool(p('lam_bottom')), Lambertian_reflectance=p('R'))
+    printed = capsys.readouterr().out.strip()
+    assert printed.endswith(os.path.join(ssp.SHAPE_DIRS[shape], ssp.ROUGHNESS_DIRS[rough],
+                                         str(g['csv_name'])))
+    got = csv_io.read_csv(printed)
+    compare_replay(got, g)
+    ref = csv_io.read_csv(os.path.join(GOLDEN, 'pol.csv'))
+    for k in ('stokes_q', 'stokes_u', 'stokes_v'):
+        assert np.abs(got[k] - ref[k]).max() < 1e-10
+
+
 @pytest.mark.parametrize('name', ['cfg1', 'cfg2'])
 def test_run_replay_reproduces_reference_csv(tmp_path, monkeypatch, capsys, name):
     """Same tables, same replay stream: the CSV holds the reference's photons."""
@@ -100,13 +130,21 @@ def test_run_test_mode_overrides(tmp_path, monkeypatch):
     assert abs(int(t['n_cond'][1]) / n - 0.09739) < 4 * np.sqrt(0.0974 * 0.9026 / n)
 
 
-def test_unsupported_paths_raise(tmp_path, monkeypatch):
+def test_missing_inputs_and_unsupported_paths_raise(tmp_path, monkeypatch):
+    """Aspherical runs need the database files; debug trajectories (matplotlib) are not
+    built; in HG mode the Stokes vector is carried but never changes, as in the
+    reference (its CSV has no Stokes columns)."""
     monkeypatch.chdir(tmp_path)
-    mc = MonteCarlo(output_dir=str(tmp_path), ssp='synthetic', write_csv=False)
+    mc = MonteCarlo(output_dir=str(tmp_path), ssp='synthetic', write_csv=False,
+                    optics_dir=str(tmp_path / 'none'))
+    with pytest.raises(FileNotFoundError):
+        mc.run(10, 1.3, 0.085, 100, shape='droxtal')            # polarised: isca.dat missing
     with pytest.raises(NotImplementedError):
-        mc.run(10, 1.3, 0.085, 100, shape='droxtal')
-    with pytest.raises(NotImplementedError):
-        mc.run(10, 1.3, 0.085, 100, stokes_params=np.array([1, 1, 0, 0]))
+        mc.run(10, 1.3, 0.085, 100, debug=True)
+    with pytest.raises(ValueError):
+        mc.run(10, 1.3, 0.085, 100, stokes_params=np.array([1, 0, 0]))
+    mc.run(10, 1.3, 0.085, 100, stokes_params=np.array([1, 1, 0, 0]))
+    assert mc.records.size == 10
     with pytest.raises(FileNotFoundError):
         MonteCarlo(output_dir=str(tmp_path), ssp='file', optics_dir=str(tmp_path / 'none'),
                    write_csv=False).run(10, 1.3, 0.085, 100)

@@ -16,7 +16,7 @@ from monte_carlompi_gb300.config import WalkConfig
 from oracle import oracle
 from tests.conftest import golden_names, load_golden
 from tests.helpers import (chi2_two_sample, compare_replay, condition_fractions_agree,
-                           exit_histogram, golden_config, golden_tables)
+                           exit_histogram, golden_config, golden_mode, golden_phase, golden_tables)
 
 pytestmark = pytest.mark.gpu
 
@@ -48,9 +48,38 @@ def test_replay_matches_reference(walker, name):
     g = load_golden(name)
     ice, imp = golden_tables(g)
     walker.set_tables([ice], imp)
-    res = walker.walk([golden_config(g)], int(g['param_seed']), mode='replay64')
+    if golden_phase(g) is not None:
+        walker.set_phase_matrices([golden_phase(g)])
+    res = walker.walk([golden_config(g)], int(g['param_seed']), mode=golden_mode(g))
     compare_replay(res.records, g)
     assert not np.any(res.records['flags'])
+    if 'stokes' in g:   # the polarised walk's Q_n, U_n, V_n
+        got = np.stack([res.records['stokes_q'], res.records['stokes_u'], res.records['stokes_v']], 1)
+        err = np.abs(got - g['stokes'][:, 1:]).max()
+        assert err < 1e-10, err
+
+
+def test_polarised_walk_needs_its_mode_and_tables(walker):
+    """Polarised configs walk in 'pol64' only, with phase matrices attached to their
+    ice table; set_tables drops the matrices of the previous tables."""
+    g = load_golden('pol')
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    cfg = golden_config(g)
+    with pytest.raises(_abi.McwError):
+        walker.walk([cfg], 1, mode='pol64')           # no phase matrices yet
+    walker.set_phase_matrices([golden_phase(g)])
+    with pytest.raises(_abi.McwError):
+        walker.walk([cfg], 1, mode='replay64')
+    with pytest.raises(_abi.McwError):
+        walker.walk([cfg], 1, mode='f32')
+    with pytest.raises(_abi.McwError):
+        walker.walk([dataclasses.replace(cfg, polarised=False)], 1, mode='pol64')
+    r = walker.walk([cfg], 1, mode='pol64')
+    assert r.records.dtype == _abi.RECORD64P and r.records.size == cfg.n_photon
+    walker.set_tables([ice], imp)
+    with pytest.raises(_abi.McwError):
+        walker.walk([cfg], 1, mode='pol64')
 
 
 def test_replay_config2_first_10k_matches_oracle(walker):

@@ -107,3 +107,16 @@ def test_planted_error_is_caught():
     bad['n_scat'][5] += 1
     with pytest.raises(AssertionError):
         compare_replay(bad, g)
+
+
+def test_oracle_polarised_stokes_matches_reference():
+    """The polarised walk's final Stokes vectors (the CSV's Q_n, U_n, V_n) against the
+    reference's own run on the same phase matrices."""
+    g = load_golden('pol')
+    cfg = oracle.config_from_golden(g)
+    ice, imp = oracle.tables_from_golden(g)
+    r = oracle.walk(cfg, ice, imp, int(g['param_seed']))
+    assert np.array_equal(r['condition'], g['condition'])
+    assert np.array_equal(r['n_draws'], g['n_draws'])
+    err = np.abs(r['stokes'] - g['stokes']).max()
+    assert err < 1e-10, err
