@@ -233,6 +233,85 @@ def run_sweep(args):
     return 0
 
 
+POL_WVLS = [round(1.0 + 0.025 * i, 4) for i in range(41)]              # um
+POL_RE = [60.0, 120.0, 250.0]                                            # um
+POL_THETA = [0.5 * k for k in range(20)] + [10.0 + 2.0 * k for k in range(86)]   # deg
+POL_STOKES = (1.0, 0.3, 0.2, 0.1)
+
+
+def pol_workload(n, tmp):
+    """Polarised walk of hexagonal plates (r_eff nearest 100 um -> 120 um), lambda0 1.3 um,
+    FWHM 0.085, theta0 30 deg, tau 20, Lambertian bottom R 0.5, incident Stokes
+    (1, 0.3, 0.2, 0.1); synthetic isca.dat and P11 ... P44 (106 angles) written to tmp."""
+    from monte_carlompi_gb300 import ssp
+    from monte_carlompi_gb300.config import WalkConfig
+    rows = ssp.synthetic_isca_rows(POL_WVLS, POL_RE)
+    isca = ssp.isca_path(tmp, 'hexagonal plate', 'moderately rough', 1.3)
+    ssp.write_isca(isca, rows)
+    ssp.write_phase_matrix(os.path.dirname(isca), POL_THETA, ssp.synthetic_phase_rows(rows, POL_THETA))
+    ice, _ = ssp.aspherical_table(isca, 1.3, 100.0)
+    phase = ssp.aspherical_phase_table(isca, ice, 1.3)
+    lo, hi = ssp.grid_for(1.3, 0.085)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    cfg = WalkConfig(n_photon=n, wvl0=1.3, half_width=0.085, theta0_deg=30.0, tau_tot=20.0,
+                     lambertian_reflectance=0.5, ssp_nearest=True, polarised=True, stokes0=POL_STOKES)
+    return cfg, ice, imp, phase
+
+
+def run_pol(args):
+    """The polarised walk of aspherical grains (FP64, replay stream) against the C
+    oracle of the same walk on the host cores."""
+    import tempfile
+    import torch  # noqa: F401  (CUDA context set-up like the other workloads)
+    from monte_carlompi_gb300.walker import Walker
+    n = 200000
+    with tempfile.TemporaryDirectory() as tmp:
+        cfg, ice, imp, phase = pol_workload(n, tmp)
+    w = Walker(0)
+    w.set_tables([ice], imp)
+    w.set_phase_matrices([phase])
+    for k in range(args.warmup):
+        w.walk([cfg], SEED + k, mode='pol64', records=None)
+    ms, events = [], 0
+    for k in range(args.steps):
+        r = w.walk([cfg], SEED + 100 + k, mode='pol64', records=None)
+        ms.append(r.stats['kernel_ms'])
+        events += r.stats['n_events']
+    w.close()
+    t = float(np.median(ms))
+    line = {'metric': 'photons/s (polarised aspherical walk)', 'workload': 'pol',
+            'value': n / (t / 1e3), 'unit': 'photons/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': t, 'higher_is_better': True, 'dtype': 'f64',
+            'data': 'synthetic',
+            'config': {'workload': '2e5 photons, hexagonal plates (RE 120 um), 1.3 um, FWHM 0.085, '
+                                   '30 deg, tau 20, Lambertian bottom 0.5, Stokes (1, .3, .2, .1); '
+                                   'synthetic isca.dat and P11..P44 (106 angles)',
+                       'mode': 'MCW_MODE_POL64 (FP64, replay stream)'},
+            'scatter_events_per_s': events / args.steps / (t / 1e3)}
+    if not args.no_cpu_baseline:
+        from oracle import oracle
+        if not os.path.exists(oracle.LIB_PATH):
+            oracle.build()
+        cores = cpu_cores()
+        ph = oracle.make_phase(phase, POL_STOKES)
+
+        def sample(m, seed):
+            c = oracle.make_config(m, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot,
+                                   R=0.5, nearest=True, phase=ph)
+            t0 = time.perf_counter()
+            rec = oracle.walk(c, ice, imp, seed, threads=cores)
+            return time.perf_counter() - t0, int(rec['n_scat'].astype(np.int64).sum())
+        dt, _ = sample(2000, SEED + 1)
+        m = int(min(n, max(2000, 2000 * 8.0 / max(dt, 1e-3))))
+        dt, ev = sample(m, SEED)
+        line['cpu_baseline'] = {'value': m / dt, 'unit': 'photons/s', 'cores': cores, 'kind': 'port',
+                                'events_per_s': ev / dt,
+                                'sample': '%d photons of the workload (FP64 C oracle, %d threads, '
+                                          '%.2f s wall)' % (m, cores, dt)}
+    print(json.dumps(line))
+    return 0
+
+
 def run_surrogate(args):
     """Surrogate workload: --surrogate-configs configs (16,384 by default) x 2e5 photons walked
     on the GPU, 5-member ensemble trained on the tensor-core kernels, 512 held-out configs
@@ -539,7 +618,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp'])
+    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol'])
     ap.add_argument('--surrogate-configs', type=int, default=16384)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
@@ -552,6 +631,8 @@ def main():
         return run_surrogate(args)
     if args.workload == 'mlp':
         return run_mlp(args)
+    if args.workload == 'pol':
+        return run_pol(args)
     return run_ours(args)
 
 
