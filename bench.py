@@ -259,8 +259,9 @@ def pol_workload(n, tmp):
 
 
 def run_pol(args):
-    """The polarised walk of aspherical grains (FP64, replay stream) against the C
-    oracle of the same walk on the host cores."""
+    """The polarised walk of aspherical grains: the FP32 production kernel ('pol32',
+    the line's value) and the FP64 replay kernel ('pol64'), against the C oracle of
+    the same walk on the host cores."""
     import tempfile
     import torch  # noqa: F401  (CUDA context set-up like the other workloads)
     from monte_carlompi_gb300.walker import Walker
@@ -270,24 +271,31 @@ def run_pol(args):
     w = Walker(0)
     w.set_tables([ice], imp)
     w.set_phase_matrices([phase])
-    for k in range(args.warmup):
-        w.walk([cfg], SEED + k, mode='pol64', records=None)
-    ms, events = [], 0
-    for k in range(args.steps):
-        r = w.walk([cfg], SEED + 100 + k, mode='pol64', records=None)
-        ms.append(r.stats['kernel_ms'])
-        events += r.stats['n_events']
+
+    def timed(mode, steps):
+        for k in range(args.warmup):
+            w.walk([cfg], SEED + k, mode=mode, records=None)
+        ms, ev = [], 0
+        for k in range(steps):
+            r = w.walk([cfg], SEED + 100 + k, mode=mode, records=None)
+            ms.append(r.stats['kernel_ms'])
+            ev += r.stats['n_events']
+        return float(np.median(ms)), ev / steps
+    t, events_per_step = timed('pol32', args.steps)
+    t64, ev64 = timed('pol64', max(2, args.steps // 3))
     w.close()
-    t = float(np.median(ms))
     line = {'metric': 'photons/s (polarised aspherical walk)', 'workload': 'pol',
             'value': n / (t / 1e3), 'unit': 'photons/s', 'n_gpus': 1, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': t, 'higher_is_better': True, 'dtype': 'f64',
+            'warmup': args.warmup, 'ms_per_step': t, 'higher_is_better': True, 'dtype': 'f32',
             'data': 'synthetic',
             'config': {'workload': '2e5 photons, hexagonal plates (RE 120 um), 1.3 um, FWHM 0.085, '
                                    '30 deg, tau 20, Lambertian bottom 0.5, Stokes (1, .3, .2, .1); '
                                    'synthetic isca.dat and P11..P44 (106 angles)',
-                       'mode': 'MCW_MODE_POL64 (FP64, replay stream)'},
-            'scatter_events_per_s': events / args.steps / (t / 1e3)}
+                       'mode': 'MCW_MODE_POL32 (FP32, Philox4x32-10 stream per photon)'},
+            'scatter_events_per_s': events_per_step / (t / 1e3),
+            'pol64': {'value': n / (t64 / 1e3), 'unit': 'photons/s', 'ms_per_step': t64,
+                      'scatter_events_per_s': ev64 / (t64 / 1e3),
+                      'mode': 'MCW_MODE_POL64 (FP64, replay stream, reference order)'}}
     if not args.no_cpu_baseline:
         from oracle import oracle
         if not os.path.exists(oracle.LIB_PATH):

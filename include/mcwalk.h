@@ -36,6 +36,8 @@ extern "C" {
 #define MCW_MODE_REPLAY64 1  /* FP64 walk on the photon-indexed replay stream, reference order */
 #define MCW_MODE_POL64 2     /* the polarised walk of aspherical grains (HG off): FP64, replay
                                 stream, reference order; records mcw_record64p */
+#define MCW_MODE_POL32 3     /* production polarised walk: FP32, a Philox4x32-10 stream per
+                                photon; records mcw_record32p */
 
 /* where mcw_walk writes per-photon records */
 #define MCW_RECORDS_NONE 0
@@ -153,6 +155,23 @@ typedef struct {
     double stokes_v;
 } mcw_record64p;
 
+/* Per-photon answer of MCW_MODE_POL32: mcw_record32's fields and Q_n, U_n,
+ * V_n.  48 bytes. */
+typedef struct {
+    int32_t condition;
+    int32_t n_scat;
+    float wvn;
+    float theta_n;
+    float phi_n;
+    float path_length;
+    float snow_depth;
+    uint32_t config;
+    float stokes_q;
+    float stokes_u;
+    float stokes_v;
+    float pad;
+} mcw_record32p;
+
 /* Phase matrices of the polarised walk for one ice table (one row per table
  * row, in the order the table was given to mcw_set_tables), as
  * interpolate_phase_matrix (monte_carlo3D.py:819-883) prepares them: element e
@@ -248,10 +267,10 @@ int mcw_set_budget(mcw_ctx *ctx, double seconds);
  * (p = 0 .. n_photon-1) is record sum(n_photon[:c]) + p; its random streams
  * are keyed by (seed, c << 40 | (first_photon + p)), so a run split into
  * shards by first_photon gives the same photons as the whole run.
- * records: mcw_record32 (F32), mcw_record64 (REPLAY64) or mcw_record64p
- * (POL64), or NULL with MCW_RECORDS_NONE.  Polarised configs walk in
- * MCW_MODE_POL64 only, and POL64 walks polarised configs only.  tallies: n_cfg
- * host structs or NULL.  stats: or NULL. */
+ * records: mcw_record32 (F32), mcw_record64 (REPLAY64), mcw_record64p (POL64)
+ * or mcw_record32p (POL32), or NULL with MCW_RECORDS_NONE.  Polarised configs
+ * walk in MCW_MODE_POL32 or MCW_MODE_POL64 only, and those modes walk polarised
+ * configs only.  tallies: n_cfg host structs or NULL.  stats: or NULL. */
 int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed, int32_t mode,
              void *records, int32_t records_where, mcw_tally *tallies, mcw_stats *stats);
 
@@ -282,8 +301,8 @@ int mcw_host_free(void *p);
 /* Per-photon CSV in the reference's format (monte_carlo3D.py:1627-1636):
  * header line, then "%d %r %r %r %d %r %r" rows with Python's shortest
  * round-trip float repr.  mode selects mcw_record32 / mcw_record64, or
- * mcw_record64p with the polarised walk's header and three more columns
- * (Q_n, U_n, V_n, :1637-1646).
+ * mcw_record32p / mcw_record64p with the polarised walk's header and three
+ * more columns (Q_n, U_n, V_n, :1637-1646).
  * mcw_format_csv writes into buf (cap bytes; *used = bytes needed). */
 int mcw_write_csv(const char *path, const void *records, int32_t mode, int64_t n,
                   int32_t n_threads);

@@ -17,6 +17,7 @@ ERRORS = {-1: 'MCW_ERR_ARG', -2: 'MCW_ERR_CUDA', -3: 'MCW_ERR_BUDGET', -4: 'MCW_
 MODE_F32 = 0
 MODE_REPLAY64 = 1
 MODE_POL64 = 2
+MODE_POL32 = 3
 RECORDS_NONE, RECORDS_HOST, RECORDS_DEVICE = 0, 1, 2
 HIST_NTHETA, HIST_NPHI, HIST_BINS = 18, 36, 648
 WVN_FX_SCALE = 4294967296.0
@@ -119,12 +120,18 @@ RECORD64P = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.
                       ('path_length', np.float64), ('snow_depth', np.float64),
                       ('config', np.uint32), ('flags', np.uint32),
                       ('stokes_q', np.float64), ('stokes_u', np.float64), ('stokes_v', np.float64)])
+RECORD32P = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
+                      ('theta_n', np.float32), ('phi_n', np.float32),
+                      ('path_length', np.float32), ('snow_depth', np.float32),
+                      ('config', np.uint32), ('stokes_q', np.float32), ('stokes_u', np.float32),
+                      ('stokes_v', np.float32), ('pad', np.float32)])
 TALLY = np.dtype([('n_cond', np.uint64, 6), ('q_cond_fx', np.uint64, 6), ('n_events', np.uint64),
                   ('max_n_scat', np.uint32), ('reserved', np.uint32),
                   ('bin_wvn_fx', np.uint64, HIST_BINS), ('bin_count', np.uint32, HIST_BINS)])
 POST_STATS = np.dtype([('q_cond_fx', np.uint64, 6), ('n_cond', np.uint64, 6), ('sum_n_scat', np.uint64),
                        ('sum_path_length', np.float64), ('sum_wavelength', np.float64)])
 assert RECORD32.itemsize == 32 and RECORD64.itemsize == 56 and RECORD64P.itemsize == 80
+assert RECORD32P.itemsize == 48
 assert ctypes.sizeof(ConfigC) == 176 and ctypes.sizeof(StatsC) == 80
 
 _lib = None

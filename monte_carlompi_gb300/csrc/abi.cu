@@ -18,6 +18,7 @@ using namespace mcw;
 
 static_assert(sizeof(mcw_config) == 176, "mcw_config layout");
 static_assert(sizeof(mcw_record64p) == 80, "mcw_record64p layout");
+static_assert(sizeof(mcw_record32p) == 48, "mcw_record32p layout");
 static_assert(sizeof(mcw_record32) == 32, "mcw_record32 layout");
 static_assert(sizeof(mcw_record64) == 56, "mcw_record64 layout");
 static_assert(sizeof(mcw_stats) == 80, "mcw_stats layout");
@@ -100,7 +101,7 @@ struct mcw_ctx {
     bool have_tables = false;
     std::vector<std::vector<int32_t>> ice_order;   // row permutation of each ice table (stored ascending)
     // phase matrices of the polarised walk, one per ice table (n_rows 0 = none)
-    DevBuf phasedata, phase_tables;
+    DevBuf phasedata, phase_tables, phasedata32, phase_tables32;
     std::vector<int32_t> phase_rows;
     // workspace
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
@@ -183,11 +184,12 @@ constexpr int32_t kMaxLutPerConfig = 1 << 16;
 int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, int32_t mode, Plan &plan) {
     if (!cfgs || n_cfg <= 0) return set_err(ctx, MCW_ERR_ARG, "need at least one config");
     if (n_cfg > (1 << 23)) return set_err(ctx, MCW_ERR_ARG, "at most 2^23 configs per call");
+    const bool pol_mode = (mode == MCW_MODE_POL64 || mode == MCW_MODE_POL32);
     for (int32_t i = 0; i < n_cfg; ++i) {
-        if (cfgs[i].polarised && mode != MCW_MODE_POL64)
-            return set_err(ctx, MCW_ERR_ARG, "config %d: the polarised walk runs in MCW_MODE_POL64", i);
-        if (!cfgs[i].polarised && mode == MCW_MODE_POL64)
-            return set_err(ctx, MCW_ERR_ARG, "config %d: MCW_MODE_POL64 walks polarised configs only", i);
+        if (cfgs[i].polarised && !pol_mode)
+            return set_err(ctx, MCW_ERR_ARG, "config %d: the polarised walk runs in MCW_MODE_POL32 or MCW_MODE_POL64", i);
+        if (!cfgs[i].polarised && pol_mode)
+            return set_err(ctx, MCW_ERR_ARG, "config %d: the polarised modes walk polarised configs only", i);
         if (cfgs[i].polarised && cfgs[i].ice_table >= 0 && cfgs[i].ice_table < ctx->n_ice &&
             ((int32_t)ctx->phase_rows.size() <= cfgs[i].ice_table || ctx->phase_rows[cfgs[i].ice_table] == 0))
             return set_err(ctx, MCW_ERR_STATE, "config %d: ice table %d has no phase matrices", i,
@@ -585,6 +587,30 @@ int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n)
     }
     CUDA_TRY(ctx, cudaMemcpy(ctx->phasedata.p, host.data(), host.size() * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(ctx, cudaMemcpy(ctx->phase_tables.p, dev.data(), n * sizeof(DevPhase), cudaMemcpyHostToDevice));
+    // float copies for the FP32 polarised walk, same layout
+    std::vector<float> host32(host.begin(), host.end());
+    std::vector<DevPhase32> dev32(n);
+    CUDA_TRY(ctx, ctx->phasedata32.ensure(host32.size() * sizeof(float)));
+    CUDA_TRY(ctx, ctx->phase_tables32.ensure(n * sizeof(DevPhase32)));
+    const float *fbase = (const float *)ctx->phasedata32.p;
+    auto f32 = [&](const double *p) { return p ? fbase + (p - dbase) : nullptr; };
+    for (int32_t t = 0; t < n; ++t) {
+        const DevPhase &d = dev[t];
+        DevPhase32 f{};
+        for (int e = 0; e < 6; ++e) {
+            f.cos_asc[e] = f32(d.cos_asc[e]);
+            f.p_asc[e] = f32(d.p_asc[e]);
+            f.n_angle[e] = d.n_angle[e];
+        }
+        f.a1 = f32(d.a1); f.a2 = f32(d.a2); f.b1 = f32(d.b1); f.b2 = f32(d.b2);
+        f.n_rows = d.n_rows;
+        f.cos_max = (float)d.cos_max;
+        f.cos_min = (float)d.cos_min;
+        f.cos_cutoff = (float)d.cos_cutoff;
+        dev32[t] = f;
+    }
+    CUDA_TRY(ctx, cudaMemcpy(ctx->phasedata32.p, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(ctx->phase_tables32.p, dev32.data(), n * sizeof(DevPhase32), cudaMemcpyHostToDevice));
     for (int32_t t = 0; t < n; ++t) ctx->phase_rows[t] = tabs[t].n_rows;
     return MCW_OK;
 }
@@ -618,7 +644,7 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     if (!ctx) return MCW_ERR_ARG;
     const auto t_start = std::chrono::steady_clock::now();
     if (!ctx->have_tables) return set_err(ctx, MCW_ERR_STATE, "mcw_set_tables has not been called");
-    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64 && mode != MCW_MODE_POL64)
+    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64 && mode != MCW_MODE_POL64 && mode != MCW_MODE_POL32)
         return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
     if (records_where < MCW_RECORDS_NONE || records_where > MCW_RECORDS_DEVICE)
         return set_err(ctx, MCW_ERR_ARG, "unknown records_where %d", records_where);
@@ -635,6 +661,7 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     if (rc) return rc;
     const size_t rec_size = (mode == MCW_MODE_F32)     ? sizeof(mcw_record32)
                             : (mode == MCW_MODE_POL64) ? sizeof(mcw_record64p)
+                            : (mode == MCW_MODE_POL32) ? sizeof(mcw_record32p)
                                                        : sizeof(mcw_record64);
     void *dev_records = nullptr;
     if (records_where == MCW_RECORDS_DEVICE) dev_records = records;
@@ -667,6 +694,16 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
         if (plan.total > 0)
             CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, ctx->sm_count, st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
+    } else if (mode == MCW_MODE_POL32) {
+        // the lookup-table kernel also clears the counters and tallies
+        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
+        WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
+                                (mcw_record32 *)dev_records, 1, seed);
+        wa.phase = (const DevPhase32 *)ctx->phase_tables32.p;
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
+        CUDA_TRY(ctx, launch_walk_pol32(wa, ctx->sm_count, st));
+        CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
+        shape.block = 128;
     } else {
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->tallies.p, 0, n_cfg * sizeof(mcw_tally), st));
         CUDA_TRY(ctx, cudaMemsetAsync(ctx->counters.p, 0, sizeof(Counters), st));

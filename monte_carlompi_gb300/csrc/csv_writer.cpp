@@ -106,7 +106,9 @@ char *put_int(char *p, int64_t v) {
 
 constexpr size_t kMaxRow = 10 * 32 + 16;
 
-bool mode_ok(int32_t mode) { return mode == MCW_MODE_F32 || mode == MCW_MODE_REPLAY64 || mode == MCW_MODE_POL64; }
+bool mode_ok(int32_t mode) {
+    return mode == MCW_MODE_F32 || mode == MCW_MODE_REPLAY64 || mode == MCW_MODE_POL64 || mode == MCW_MODE_POL32;
+}
 
 template <class R>
 size_t format_rows(const R *rec, int64_t n, char *out) {
@@ -126,7 +128,7 @@ size_t format_rows(const R *rec, int64_t n, char *out) {
         p = put_repr(p, r.path_length);
         *p++ = ' ';
         p = put_repr(p, r.snow_depth);
-        if constexpr (std::is_same<R, mcw_record64p>::value) {
+        if constexpr (std::is_same<R, mcw_record64p>::value || std::is_same<R, mcw_record32p>::value) {
             *p++ = ' ';
             p = put_repr(p, r.stokes_q);
             *p++ = ' ';
@@ -142,10 +144,13 @@ size_t format_rows(const R *rec, int64_t n, char *out) {
 size_t format_any(const void *rec, int32_t mode, int64_t off, int64_t n, char *out) {
     if (mode == MCW_MODE_F32) return format_rows(static_cast<const mcw_record32 *>(rec) + off, n, out);
     if (mode == MCW_MODE_POL64) return format_rows(static_cast<const mcw_record64p *>(rec) + off, n, out);
+    if (mode == MCW_MODE_POL32) return format_rows(static_cast<const mcw_record32p *>(rec) + off, n, out);
     return format_rows(static_cast<const mcw_record64 *>(rec) + off, n, out);
 }
 
-const char *header_of(int32_t mode) { return mode == MCW_MODE_POL64 ? kHeaderPol : kHeader; }
+const char *header_of(int32_t mode) {
+    return (mode == MCW_MODE_POL64 || mode == MCW_MODE_POL32) ? kHeaderPol : kHeader;
+}
 
 }  // namespace
 

@@ -13,6 +13,7 @@ constexpr uint32_t kTagWvl = 1;     // replay: wavelength Box-Muller
 constexpr uint32_t kTagStep = 2;    // F32: per-step HG, azimuth, path, albedo draws
 constexpr uint32_t kTagSpecies = 3; // F32: ice/impurity draw (only when imp_cnc > 0)
 constexpr uint32_t kTagBirth = 5;   // F32: wavelength Box-Muller at photon birth
+constexpr uint32_t kTagPol = 6;     // F32 polarised walk: the photon's sequential stream
 
 // Device status bits.
 constexpr uint32_t kStatusBudget = 1u;
@@ -58,6 +59,17 @@ struct DevConfig {
     double stokes0[4];    // polarised walk: incident Stokes vector
 };
 
+// Phase matrices of one ice table for the FP32 polarised walk (float copies).
+struct DevPhase32 {
+    const float *cos_asc[6];
+    const float *p_asc[6];
+    const float *a1, *a2, *b1, *b2;
+    int32_t n_angle[6];
+    int32_t n_rows;
+    int32_t pad;
+    float cos_max, cos_min, cos_cutoff, pad2;
+};
+
 // Phase matrices of one ice table on the device (mcw_phase_table, rows in the
 // device table's order).
 struct DevPhase {
@@ -82,7 +94,7 @@ struct LutEntry {
     float snow_depth; // [m]
     float pad;
     unsigned long long wvn_fx;  // wvn * 2^32, rounded
-    unsigned long long pad2;
+    unsigned long long pad2;    // the nearest ice-table row (the polarised walk's phase-matrix row)
 };
 
 // Per-warp running totals for the warp's current config (shared memory).
@@ -120,6 +132,7 @@ struct WalkArgs {
     uint32_t epoch;              // differs between launches, never 0 (0 marks a taken slot)
     uint32_t drain_cap;          // slots in drain (grid * block)
     uint32_t drain_pad;
+    const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
 };
 
 struct ReplayArgs {
@@ -165,6 +178,8 @@ constexpr int kDrainSlot = 6;
 // (sm_count SMs; a.drain must then hold grid * block slots).
 cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s);
 cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);
+// The FP32 polarised walk (a.phase set, a.records holding mcw_record32p).
+cudaError_t launch_walk_pol32(const WalkArgs &a, int sm_count, cudaStream_t s);
 int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity);
 // The walk and drain kernels (their one parameter is a WalkArgs).
 bool walk_f32_is_kernel(const void *fn);

@@ -53,7 +53,7 @@ __global__ void lut_kernel(const LutArgs a) {
         L.snow_depth = (float)o.snow_depth;
         L.pad = 0.f;
         L.wvn_fx = (unsigned long long)llrint(wvn * 4294967296.0);
-        L.pad2 = 0;
+        L.pad2 = (unsigned long long)o.row;   // the nearest ice-table row (polarised walk)
         a.lut[c.lut_off + j] = L;
     }
 }

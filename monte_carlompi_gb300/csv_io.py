@@ -48,7 +48,9 @@ def _mode_of(records):
         return _abi.MODE_REPLAY64
     if records.dtype == _abi.RECORD64P:
         return _abi.MODE_POL64
-    raise TypeError('records must be RECORD32, RECORD64 or RECORD64P structured arrays')
+    if records.dtype == _abi.RECORD32P:
+        return _abi.MODE_POL32
+    raise TypeError('records must be RECORD32, RECORD64, RECORD32P or RECORD64P structured arrays')
 
 
 def write_csv(path, records, n_threads=0):

@@ -31,9 +31,9 @@ Non-spherical shapes without HG take the polarised walk (monte_carlo3D.py:
 905-1004, :1282-1342): scattering angles by rejection from the phase matrices
 P11.dat ... P44.dat beside isca.dat, the incident ``stokes_params`` carried
 through every scattering, the CSV with Q_n, U_n, V_n and the name appendix
-'I%d%d%d%d'.  It walks in FP64 on the replay stream (mode 'pol64') whatever
-``mode`` says.  (The Yang et al. 2013 files are not part of the reference
-archive; any files in their layout work.)
+'I%d%d%d%d'; ``mode`` 'f32' walks it in FP32 ('pol32'), 'replay64' in FP64 on
+the replay stream ('pol64').  (The Yang et al. 2013 files are not part of the
+reference archive; any files in their layout work.)
 
 Not available (raise): ``debug`` and ``phase_functions`` (matplotlib figures).
 """
@@ -162,7 +162,10 @@ class MonteCarlo(object):
         if seed is None:
             seed = int.from_bytes(os.urandom(8), 'little')
         self.last_seed = seed
-        res = w.walk([cfg], seed, mode='pol64' if polarised else self.mode, records='host')
+        mode = self.mode
+        if polarised:
+            mode = 'pol32' if self.mode == 'f32' else 'pol64'
+        res = w.walk([cfg], seed, mode=mode, records='host')
         self.records, self.tallies, self.stats = res.records, res.tallies, res.stats
         if self.write_csv:
             appendix = 'I%d%d%d%d' % tuple(stokes_params) if polarised else 'HG'   # :123-130

@@ -17,7 +17,8 @@ from .config import configs_to_c
 # walk modes: (ABI mode, record dtype)
 MODES = {'f32': (_abi.MODE_F32, _abi.RECORD32),
          'replay64': (_abi.MODE_REPLAY64, _abi.RECORD64),
-         'pol64': (_abi.MODE_POL64, _abi.RECORD64P)}
+         'pol64': (_abi.MODE_POL64, _abi.RECORD64P),
+         'pol32': (_abi.MODE_POL32, _abi.RECORD32P)}
 
 
 def _phase_c(p, keep):

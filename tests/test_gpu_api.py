@@ -64,7 +64,7 @@ def test_run_polarised_reproduces_reference_csv(tmp_path, monkeypatch, capsys):
     ssp.write_netcdf(os.path.join(optics, 'mie', 'snicar', 'imp.nc'), imp, with_asm=False)
     mc = MonteCarlo(tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'), rho_snw=p('rho_snw'),
                     rho_ice=p('rho_ice'), output_dir=str(tmp_path / 'out'), optics_dir=optics,
-                    fi_imp='imp.nc', ssp='file', seed=int(p('seed')))
+                    fi_imp='imp.nc', ssp='file', mode='replay64', seed=int(p('seed')))
     mc.run(int(p('n_photon')), p('wvl0'), p('half_width'), p('rds'), theta_0=p('theta0'),
            stokes_params=g['stokes0'], shape=shape, roughness=rough,
            Lambertian_bottom=bool(p('lam_bottom')), Lambertian_reflectance=p('R'))

@@ -59,6 +59,38 @@ def test_replay_matches_reference(walker, name):
         assert err < 1e-10, err
 
 
+@pytest.mark.parametrize('n', [100000])
+def test_pol32_statistics_match_oracle(walker, n):
+    """FP32 polarised walk against the oracle's FP64 walk of the reference's algorithm
+    at the same N: condition fractions (4 sigma), exit histogram (chi-square), mean
+    n_scat and the mean final Stokes Q, U, V of the photons leaving the top (4 sigma)."""
+    g = load_golden('pol')
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    walker.set_phase_matrices([golden_phase(g)])
+    cfg = dataclasses.replace(golden_config(g), n_photon=n)
+    rec = walker.walk([cfg], 31, mode='pol32').records
+    from oracle import oracle as orc
+    c = orc.make_config(n, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot, cfg.imp_cnc,
+                        cfg.rho_snw, cfg.rho_ice, cfg.lambertian_surface, cfg.lambertian_bottom,
+                        cfg.lambertian_reflectance, nearest=True, phase=orc.phase_from_golden(g))
+    ref = orc.walk(c, ice, imp, 4321, threads=16)
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    top_g, top_r = rec['condition'] == 1, ref['condition'] == 1
+    x2, dof, p = chi2_two_sample(exit_histogram(rec['theta_n'][top_g], rec['phi_n'][top_g]),
+                                 exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r]))
+    assert p > 1e-4, (x2, dof, p)
+    for a, b in ((rec['n_scat'].astype(np.float64), ref['n_scat'].astype(np.float64)),
+                 (rec['stokes_q'][top_g].astype(np.float64), ref['stokes'][top_r, 1]),
+                 (rec['stokes_u'][top_g].astype(np.float64), ref['stokes'][top_r, 2]),
+                 (rec['stokes_v'][top_g].astype(np.float64), ref['stokes'][top_r, 3])):
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se + 1e-7, (a.mean(), b.mean(), se)
+    # records depend only on (seed, photon): a second launch gives the same photons
+    again = walker.walk([dataclasses.replace(cfg, n_photon=5000)], 31, mode='pol32').records
+    assert np.array_equal(again, rec[:5000])
+
+
 def test_polarised_walk_needs_its_mode_and_tables(walker):
     """Polarised configs walk in 'pol64' only, with phase matrices attached to their
     ice table; set_tables drops the matrices of the previous tables."""
