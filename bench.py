@@ -265,15 +265,15 @@ def run_pol(args):
     import tempfile
     import torch  # noqa: F401  (CUDA context set-up like the other workloads)
     from monte_carlompi_gb300.walker import Walker
-    n = 200000
+    n = 1000000
     with tempfile.TemporaryDirectory() as tmp:
         cfg, ice, imp, phase = pol_workload(n, tmp)
     w = Walker(0)
     w.set_tables([ice], imp)
     w.set_phase_matrices([phase])
 
-    def timed(mode, steps):
-        for k in range(args.warmup):
+    def timed(mode, steps, warmup):
+        for k in range(warmup):
             w.walk([cfg], SEED + k, mode=mode, records=None)
         ms, ev = [], 0
         for k in range(steps):
@@ -281,14 +281,14 @@ def run_pol(args):
             ms.append(r.stats['kernel_ms'])
             ev += r.stats['n_events']
         return float(np.median(ms)), ev / steps
-    t, events_per_step = timed('pol32', args.steps)
-    t64, ev64 = timed('pol64', max(2, args.steps // 3))
+    t, events_per_step = timed('pol32', args.steps, args.warmup)
+    t64, ev64 = timed('pol64', 2, 1)
     w.close()
     line = {'metric': 'photons/s (polarised aspherical walk)', 'workload': 'pol',
             'value': n / (t / 1e3), 'unit': 'photons/s', 'n_gpus': 1, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': t, 'higher_is_better': True, 'dtype': 'f32',
             'data': 'synthetic',
-            'config': {'workload': '2e5 photons, hexagonal plates (RE 120 um), 1.3 um, FWHM 0.085, '
+            'config': {'workload': '1e6 photons, hexagonal plates (RE 120 um), 1.3 um, FWHM 0.085, '
                                    '30 deg, tau 20, Lambertian bottom 0.5, Stokes (1, .3, .2, .1); '
                                    'synthetic isca.dat and P11..P44 (106 angles)',
                        'mode': 'MCW_MODE_POL32 (FP32, Philox4x32-10 stream per photon)'},

@@ -9,9 +9,10 @@
 // sequential stream: Philox4x32-10 blocks (block, kTagPol, stream id), four
 // 32-bit words per block.  Results depend only on (seed, photon stream id).
 //
-// One thread walks one photon at a time; threads claim photons from a global
-// counter (warp-aggregated), so a thread whose photon ends early takes the next
-// instead of idling until the longest walk of its warp is done.
+// One thread walks one photon at a time, one scatter event per loop iteration;
+// a thread whose photon ends claims the next from a global counter (warp-
+// aggregated) in the same iteration, so the lanes of a warp stay together step
+// by step instead of idling until the longest walk of the warp is done.
 //
 // Statistically equivalent restatements (identical distributions):
 //  * the envelope factor |Q cos 2b + U sin 2b| with 2b = arctan(U / Q) (:908-935)
@@ -123,13 +124,29 @@ __device__ __forceinline__ void rotate(float &Q, float &U, float cd, float sd) {
     U = u;
 }
 
-// Walk photon gid; false when the time budget ran out.
-__device__ bool walk_photon(const WalkArgs &a, int64_t gid, unsigned long long t0) {
+// A photon in flight (registers of its lane).
+struct PolPhoton {
+    int64_t gid;
+    const DevPhase32 *ph;
+    int32_t ci, row, i;
+    bool lam_surface, lam_bottom, bref;
+    float tau, R, inv_ext, p_imp, coalb_ice, coalb_imp, wvn, depth;
+    unsigned long long wvn_fx;
+    PolStream s;
+    float dtau_next;
+    uint32_t w_abs, w_ext;
+    float mux, muy, muz, z, path, pathc;
+    float I, Q, U, V;
+};
+
+// Birth of photon gid: wavelength (monte_carlo3D.py:1516-1520), optics row, the
+// initial draws of initial_pdfs (:1035-1038) and the incident direction and Stokes
+// vector (:1121-1132).
+__device__ __forceinline__ void pol_birth(PolPhoton &P, const WalkArgs &a, int64_t gid) {
     const int ci = find_config(a.prefix, a.n_cfg, gid);
     const DevConfig &c = a.cfgs[ci];
     const uint64_t rid = c.rng_base + (uint64_t)(gid - c.offset);
     const uint32_t lo = (uint32_t)rid, hi = (uint32_t)(rid >> 32);
-    // wavelength (monte_carlo3D.py:1516-1520) and its optics row
     const uint4 rb = philox10(make_uint4(0u, kTagBirth, lo, hi), a.keys);
     float sb, cb;
     __sincosf(kTwoPiF * (u01_f32(rb.y) - 0.5f), &sb, &cb);
@@ -138,161 +155,199 @@ __device__ bool walk_photon(const WalkArgs &a, int64_t gid, unsigned long long t
     const LutEntry *e = a.lut + c.lut_off + min(max(kw - c.k_lo, 0), c.lut_n - 1);
     const float4 e0 = __ldg(reinterpret_cast<const float4 *>(e));       // wvn, coalb_ice, coalb_imp, g
     const float4 e1 = __ldg(reinterpret_cast<const float4 *>(e) + 1);   // inv_ext, p_imp, snow_depth, -
-    const unsigned long long wvn_fx = __ldg(&e->wvn_fx);
-    const int row = (int)__ldg(&e->pad2);
-    const DevPhase32 &ph = a.phase[c.ice_table];
-    const bool lam_surface = (c.flags & kFlagLamSurface) != 0;
-    const bool lam_bottom = (c.flags & kFlagLamBottom) != 0;
-    const float tau = c.tau_tot, R = c.R, inv_ext = e1.x, p_imp = e1.y;
-    const float coalb_ice = lam_surface ? 1.f - R : e0.y;               // :1385-1387
-    const float coalb_imp = lam_surface ? 1.f - R : e0.z;
+    P.gid = gid;
+    P.ci = ci;
+    P.ph = a.phase + c.ice_table;
+    P.row = (int)__ldg(&e->pad2);
+    P.i = 0;
+    P.lam_surface = (c.flags & kFlagLamSurface) != 0;
+    P.lam_bottom = (c.flags & kFlagLamBottom) != 0;
+    P.bref = false;
+    P.tau = c.tau_tot;
+    P.R = c.R;
+    P.inv_ext = e1.x;
+    P.p_imp = e1.y;
+    P.coalb_ice = P.lam_surface ? 1.f - P.R : e0.y;                     // :1385-1387
+    P.coalb_imp = P.lam_surface ? 1.f - P.R : e0.z;
+    P.wvn = e0.x;
+    P.depth = e1.z;
+    P.wvn_fx = __ldg(&e->wvn_fx);
+    P.s = PolStream{lo, hi, 0u, 4, make_uint4(0, 0, 0, 0)};
+    P.dtau_next = -__logf(P.s.u(a.keys));
+    P.w_abs = P.s.word(a.keys);
+    P.w_ext = P.s.word(a.keys);
+    P.mux = c.mux0;
+    P.muy = 0.f;
+    P.muz = c.muz0;
+    P.z = 0.f;
+    P.path = 0.f;
+    P.pathc = 0.f;
+    P.I = (float)c.stokes0[0];
+    P.Q = (float)c.stokes0[1];
+    P.U = (float)c.stokes0[2];
+    P.V = (float)c.stokes0[3];
+}
 
-    PolStream s{lo, hi, 0u, 4, make_uint4(0, 0, 0, 0)};
-    // initial_pdfs (:1035-1038): optical path, absorption and species words
-    float dtau_next = -__logf(s.u(a.keys));
-    uint32_t w_abs = s.word(a.keys), w_ext = s.word(a.keys);
-    float mux = c.mux0, muy = 0.f, muz = c.muz0;
-    float z = 0.f, path = 0.f, pathc = 0.f;
-    float I = (float)c.stokes0[0], Q = (float)c.stokes0[1], U = (float)c.stokes0[2], V = (float)c.stokes0[3];
-    bool bref = false;
-    int cond = 0;
-    int32_t i = 0;
+// One scatter event of the photon (monte_carlo3D.py:1212-1466).  Returns the end
+// condition (0: still walking), or -1 when the time budget ran out.
+__device__ __forceinline__ int pol_step(PolPhoton &P, const WalkArgs &a, unsigned long long t0) {
+    const DevPhase32 &ph = *P.ph;
+    P.i += 1;
     float cphi = 0.f, sphi = 0.f, p_cos = 1.f;
-    while (cond == 0) {
-        ++i;
-        if (i > 1) {                                                      // :1215-1224
-            if (!rejection_angles(ph, row, I, Q, U, s, a.keys, p_cos, cphi, sphi, t0, a.budget_ns)) {
-                atomicOr(a.status, kStatusBudget);
-                return false;
-            }
-            dtau_next = -__logf(s.u(a.keys));
-            w_abs = s.word(a.keys);
-            w_ext = s.word(a.keys);
+    if (P.i > 1) {                                                        // :1215-1224
+        if (!rejection_angles(ph, P.row, P.I, P.Q, P.U, P.s, a.keys, p_cos, cphi, sphi, t0, a.budget_ns))
+            return -1;
+        P.dtau_next = -__logf(P.s.u(a.keys));
+        P.w_abs = P.s.word(a.keys);
+        P.w_ext = P.s.word(a.keys);
+    }
+    const float dtau = (P.lam_surface && P.i == 1) ? 0.f : P.dtau_next;  // :1227-1229
+    float nx = P.mux, ny = P.muy, nz = P.muz;
+    if (P.i > 1) {
+        // direction (:1238-1281): Lambertian about the vertical, or the rotation
+        float m0x = P.mux, m0y = P.muy, m0z = P.muz, ct = p_cos;
+        if (P.lam_surface || P.bref) {
+            m0x = 0.f; m0y = 0.f; m0z = 1.f;
+            ct = sqrtf(P.s.u(a.keys));
         }
-        const float dtau = (lam_surface && i == 1) ? 0.f : dtau_next;   // :1227-1229
-        float nx = mux, ny = muy, nz = muz;
-        if (i > 1) {
-            // direction (:1238-1281): Lambertian about the vertical, or the rotation
-            float m0x = mux, m0y = muy, m0z = muz, ct = p_cos;
-            if (lam_surface || bref) {
-                m0x = 0.f; m0y = 0.f; m0z = 1.f;
-                ct = sqrtf(s.u(a.keys));
-            }
-            const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
-            if (fabsf(m0z) > 0.99999f) {
-                const float sg = copysignf(1.f, m0z);
-                nx = st * cphi;
-                ny = sg * st * sphi;
-                nz = sg * ct;
-            } else {
-                const float s2 = fmaf(-m0z, m0z, 1.f);
-                const float tq = st * rsqrtf(s2);
-                nx = fmaf(tq, fmaf(m0x * m0z, cphi, -m0y * sphi), m0x * ct);
-                ny = fmaf(tq, fmaf(m0y * m0z, cphi, m0x * sphi), m0y * ct);
-                nz = fmaf(-s2 * rsqrtf(s2) * st, cphi, m0z * ct);
-                const float inv = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
-                nx *= inv; ny *= inv; nz *= inv;
-            }
-            // Stokes vector (:1282-1342)
-            if (bref) {
-                I = 1.f; Q = 0.f; U = 0.f; V = 0.f;
-                bref = false;
-            } else {
-                // into the scattering plane: phi_sca = arccos(cphi) in [0, pi]
-                const float sps = sqrtf(fmaxf(0.f, fmaf(-cphi, cphi, 1.f)));
-                rotate(Q, U, fmaf(2.f * cphi, cphi, -1.f), 2.f * sps * cphi);
-                const float P11 = phase_el(ph, 0, row, ct), P12 = phase_el(ph, 1, row, ct);
-                const float P22 = phase_el(ph, 2, row, ct), P33 = phase_el(ph, 3, row, ct);
-                const float P43 = phase_el(ph, 4, row, ct), P44 = phase_el(ph, 5, row, ct);
-                const float Is = fmaf(I, P11, Q * P12), Qs = fmaf(I, P12, Q * P22);
-                const float Us = fmaf(U, P33, -V * P43), Vs = fmaf(U, P43, V * P44);
-                // back to the meridian plane of the new direction
-                const float den = sqrtf(fmaf(-ct, ct, 1.f) * fmaf(-nz, nz, 1.f));
-                float cos_i = 0.f;
-                if (den != 0.f) {
-                    const float sign = (cphi == -1.f) ? 1.f : -1.f;   // phi_sca >= pi only at cos phi = -1
-                    cos_i = fminf(fmaxf(__fdividef(fmaf(nz, ct, -m0z), sign * den), -1.f), 1.f);
-                }
-                const float si = sqrtf(fmaxf(0.f, fmaf(-cos_i, cos_i, 1.f)));
-                float Qm = Qs, Um = Us;
-                rotate(Qm, Um, fmaf(2.f * cos_i, cos_i, -1.f), -2.f * si * cos_i);
-                const float inv_i = 1.f / Is;
-                I = 1.f;
-                Q = Qm * inv_i;
-                U = Um * inv_i;
-                V = Vs * inv_i;
-            }
+        const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
+        if (fabsf(m0z) > 0.99999f) {
+            const float sg = copysignf(1.f, m0z);
+            nx = st * cphi;
+            ny = sg * st * sphi;
+            nz = sg * ct;
+        } else {
+            const float s2 = fmaf(-m0z, m0z, 1.f);
+            const float rs = rsqrtf(s2);
+            const float tq = st * rs;
+            nx = fmaf(tq, fmaf(m0x * m0z, cphi, -m0y * sphi), m0x * ct);
+            ny = fmaf(tq, fmaf(m0y * m0z, cphi, m0x * sphi), m0y * ct);
+            nz = fmaf(-s2 * rs * st, cphi, m0z * ct);
+            const float inv = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
+            nx *= inv; ny *= inv; nz *= inv;
         }
-        // move, path, boundaries, absorption (:1349-1466)
-        float zn = fmaf(dtau, nz, z);
-        const float inc = dtau * inv_ext;
-        {
-            const float y = inc - pathc;
-            const float tt = path + y;
-            pathc = (tt - path) - y;
-            path = tt;
-        }
-        mux = nx; muy = ny; muz = nz;
-        const bool imp = (float)w_ext * kTwo32Inv < p_imp;
-        const float coalb = imp ? coalb_imp : coalb_ice;
-        if (zn > 0.f) {
-            cond = 1;
-            path -= __fdividef(zn, zn - z) * inc;
-        } else if (zn < -tau) {
-            path -= __fdividef(zn + tau, zn - z) * inc;
-            zn = -tau;
-            if (lam_bottom && s.u(a.keys) <= R) bref = true;
-            else cond = (i == 1) ? 3 : 2;
-        } else if ((float)w_abs * kTwo32Inv < coalb) {
-            cond = imp ? 5 : 4;
-        }
-        z = zn;
-        if ((i & 1023) == 0 && global_ns() - t0 > a.budget_ns) {
-            atomicOr(a.status, kStatusBudget);
-            return false;
+        // Stokes vector (:1282-1342)
+        if (P.bref) {
+            P.I = 1.f; P.Q = 0.f; P.U = 0.f; P.V = 0.f;
+            P.bref = false;
+        } else {
+            // into the scattering plane: phi_sca = arccos(cphi) in [0, pi]
+            const float sps = sqrtf(fmaxf(0.f, fmaf(-cphi, cphi, 1.f)));
+            float Q = P.Q, U = P.U;
+            rotate(Q, U, fmaf(2.f * cphi, cphi, -1.f), 2.f * sps * cphi);
+            const float P11 = phase_el(ph, 0, P.row, ct), P12 = phase_el(ph, 1, P.row, ct);
+            const float P22 = phase_el(ph, 2, P.row, ct), P33 = phase_el(ph, 3, P.row, ct);
+            const float P43 = phase_el(ph, 4, P.row, ct), P44 = phase_el(ph, 5, P.row, ct);
+            const float Is = fmaf(P.I, P11, Q * P12), Qs = fmaf(P.I, P12, Q * P22);
+            const float Us = fmaf(U, P33, -P.V * P43), Vs = fmaf(U, P43, P.V * P44);
+            // back to the meridian plane of the new direction
+            const float den = sqrtf(fmaf(-ct, ct, 1.f) * fmaf(-nz, nz, 1.f));
+            float cos_i = 0.f;
+            if (den != 0.f) {
+                const float sign = (cphi == -1.f) ? 1.f : -1.f;   // phi_sca >= pi only at cos phi = -1
+                cos_i = fminf(fmaxf(__fdividef(fmaf(nz, ct, -m0z), sign * den), -1.f), 1.f);
+            }
+            const float si = sqrtf(fmaxf(0.f, fmaf(-cos_i, cos_i, 1.f)));
+            float Qm = Qs, Um = Us;
+            rotate(Qm, Um, fmaf(2.f * cos_i, cos_i, -1.f), -2.f * si * cos_i);
+            const float inv_i = 1.f / Is;
+            P.I = 1.f;
+            P.Q = Qm * inv_i;
+            P.U = Um * inv_i;
+            P.V = Vs * inv_i;
         }
     }
-    const float theta = acosf(fminf(fmaxf(muz, -1.f), 1.f));
+    // move, path, boundaries, absorption (:1349-1466)
+    float zn = fmaf(dtau, nz, P.z);
+    const float inc = dtau * P.inv_ext;
+    {
+        const float y = inc - P.pathc;
+        const float tt = P.path + y;
+        P.pathc = (tt - P.path) - y;
+        P.path = tt;
+    }
+    P.mux = nx; P.muy = ny; P.muz = nz;
+    const bool imp = (float)P.w_ext * kTwo32Inv < P.p_imp;
+    const float coalb = imp ? P.coalb_imp : P.coalb_ice;
+    int cond = 0;
+    if (zn > 0.f) {
+        cond = 1;
+        P.path -= __fdividef(zn, zn - P.z) * inc;
+    } else if (zn < -P.tau) {
+        P.path -= __fdividef(zn + P.tau, zn - P.z) * inc;
+        zn = -P.tau;
+        if (P.lam_bottom && P.s.u(a.keys) <= P.R) P.bref = true;
+        else cond = (P.i == 1) ? 3 : 2;
+    } else if ((float)P.w_abs * kTwo32Inv < coalb) {
+        cond = imp ? 5 : 4;
+    }
+    P.z = zn;
+    return cond;
+}
+
+// Record and tallies of a photon that ended with condition cond.
+__device__ __forceinline__ void pol_finish(const PolPhoton &P, const WalkArgs &a, int cond) {
+    const float theta = acosf(fminf(fmaxf(P.muz, -1.f), 1.f));
     float phi = 0.f;
-    if (i > 1) {
-        phi = atan2f(muy, mux);
+    if (P.i > 1) {
+        phi = atan2f(P.muy, P.mux);
         if (phi < 0.f) phi += kTwoPiF;
         if (phi >= kTwoPiF) phi = 0.f;
     }
     if (a.records) {
         mcw_record32p r;
         r.condition = cond;
-        r.n_scat = i - 1;
-        r.wvn = e0.x;
+        r.n_scat = P.i - 1;
+        r.wvn = P.wvn;
         r.theta_n = theta;
         r.phi_n = phi;
-        r.path_length = path;
-        r.snow_depth = e1.z;
-        r.config = (uint32_t)ci;
-        r.stokes_q = Q;
-        r.stokes_u = U;
-        r.stokes_v = V;
+        r.path_length = P.path;
+        r.snow_depth = P.depth;
+        r.config = (uint32_t)P.ci;
+        r.stokes_q = P.Q;
+        r.stokes_u = P.U;
+        r.stokes_v = P.V;
         r.pad = 0.f;
-        reinterpret_cast<mcw_record32p *>(a.records)[gid] = r;
+        reinterpret_cast<mcw_record32p *>(a.records)[P.gid] = r;
     }
-    tally_global(a.tallies + ci, cond, i - 1, wvn_fx, theta, phi);
-    return true;
+    tally_global(a.tallies + P.ci, cond, P.i - 1, P.wvn_fx, theta, phi);
 }
 
+// One loop iteration is one scatter event of each lane's photon; a lane whose
+// photon ends claims the next one in the same iteration, so the lanes of a warp
+// stay together step by step instead of waiting for the warp's longest walk.
 __global__ void __launch_bounds__(kPolBlock) walk_pol32_kernel(const WalkArgs a) {
     const unsigned long long t0 = global_ns();
     const int lane = threadIdx.x & 31;
-    for (;;) {
-        // claim the next photon; lanes that arrive together share one atomic
-        const unsigned m = __activemask();
-        const int leader = __ffs(m) - 1;
-        unsigned long long base = 0;
-        if (lane == leader) base = atomicAdd(a.work, (unsigned long long)__popc(m));
-        base = __shfl_sync(m, base, leader);
-        const unsigned long long g = base + __popc(m & ((1u << lane) - 1u));
-        if (g >= (unsigned long long)a.total) break;
-        if (*(volatile unsigned int *)a.status & kStatusBudget) break;
-        if (!walk_photon(a, (int64_t)g, t0)) break;
+    PolPhoton P;
+    bool have = false;
+    for (uint32_t it = 0;; ++it) {
+        if (!have) {
+            // claim the next photon; lanes that arrive together share one atomic
+            const unsigned m = __activemask();
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.work, (unsigned long long)__popc(m));
+            base = __shfl_sync(m, base, leader);
+            const unsigned long long g = base + __popc(m & ((1u << lane) - 1u));
+            if (g >= (unsigned long long)a.total) break;
+            pol_birth(P, a, (int64_t)g);
+            have = true;
+        }
+        const int cond = pol_step(P, a, t0);
+        if (cond < 0) {
+            atomicOr(a.status, kStatusBudget);
+            break;
+        }
+        if (cond > 0) {
+            pol_finish(P, a, cond);
+            have = false;
+        }
+        if ((it & 1023u) == 1023u &&
+            (global_ns() - t0 > a.budget_ns || (*(volatile unsigned int *)a.status & kStatusBudget))) {
+            atomicOr(a.status, kStatusBudget);
+            break;
+        }
     }
 }
 
