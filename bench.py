@@ -291,7 +291,7 @@ def run_pol(args):
             'config': {'workload': '1e6 photons, hexagonal plates (RE 120 um), 1.3 um, FWHM 0.085, '
                                    '30 deg, tau 20, Lambertian bottom 0.5, Stokes (1, .3, .2, .1); '
                                    'synthetic isca.dat and P11..P44 (106 angles)',
-                       'mode': 'MCW_MODE_POL32 (FP32, Philox4x32-10 stream per photon)'},
+                       'mode': 'MCW_MODE_POL32 (FP32, Philox4x32-10 blocks per step and per rejection candidate)'},
             'scatter_events_per_s': events_per_step / (t / 1e3),
             'pol64': {'value': n / (t64 / 1e3), 'unit': 'photons/s', 'ms_per_step': t64,
                       'scatter_events_per_s': ev64 / (t64 / 1e3),

@@ -13,7 +13,9 @@ constexpr uint32_t kTagWvl = 1;     // replay: wavelength Box-Muller
 constexpr uint32_t kTagStep = 2;    // F32: per-step HG, azimuth, path, albedo draws
 constexpr uint32_t kTagSpecies = 3; // F32: ice/impurity draw (only when imp_cnc > 0)
 constexpr uint32_t kTagBirth = 5;   // F32: wavelength Box-Muller at photon birth
-constexpr uint32_t kTagPol = 6;     // F32 polarised walk: the photon's sequential stream
+constexpr uint32_t kTagPolStep = 6;  // F32 polarised walk: a step's path, absorption, species, Lambertian words
+constexpr uint32_t kTagPolRefl = 7;  // F32 polarised walk: a step's bottom reflectance draw
+constexpr uint32_t kTagPolCand = 8;  // F32 polarised walk: rejection candidate j of a step (word y = 8 | j << 8)
 
 // Device status bits.
 constexpr uint32_t kStatusBudget = 1u;

@@ -4,15 +4,24 @@
 // Every step draws its scattering angles by rejection from the phase matrix of
 // the photon's wavelength row, for the photon's current Stokes vector, and the
 // Stokes vector is rotated into the scattering plane, scattered by the phase
-// matrix and rotated back after every scattering.  The number of uniforms a
-// step takes depends on the rejection loop, so each photon reads its own
-// sequential stream: Philox4x32-10 blocks (block, kTagPol, stream id), four
-// 32-bit words per block.  Results depend only on (seed, photon stream id).
+// matrix and rotated back after every scattering.
 //
-// One thread walks one photon at a time, one scatter event per loop iteration;
-// a thread whose photon ends claims the next from a global counter (warp-
-// aggregated) in the same iteration, so the lanes of a warp stay together step
-// by step instead of idling until the longest walk of the warp is done.
+// Random numbers are indexed, not sequential: step n of a photon takes one
+// Philox4x32-10 block (n, kTagPolStep, stream id) for its optical path,
+// absorption, species and Lambertian words, one (n, kTagPolRefl, id) for a
+// bottom reflectance draw, and rejection candidate j one block
+// (n, kTagPolCand | j << 8, id) for its area, cosine, azimuth and acceptance
+// words; the accepted candidate is the lowest-indexed one that passes.  So any
+// lane can test any photon's candidates, and results depend only on (seed,
+// photon stream id).
+//
+// One thread walks one photon, one scatter event per loop iteration; a lane
+// whose photon ends claims the next from a global counter in the same iteration
+// (warp-aggregated), and lanes without a photon stay in the loop as helpers.
+// The rejection runs as warp-wide rounds: the n photons still looking for an
+// angle share the 32 lanes (lane l tests candidate jbase + l / n of photon
+// l % n), so a step costs a few rounds instead of the slowest lane's candidate
+// count, and the last walks of a launch get the whole warp.
 //
 // Statistically equivalent restatements (identical distributions):
 //  * the envelope factor |Q cos 2b + U sin 2b| with 2b = arctan(U / Q) (:908-935)
@@ -42,25 +51,7 @@ constexpr float kTwoPiF = 6.28318530717958648f;
 constexpr float kPiF = 3.14159265358979324f;
 constexpr float kTwo32Inv = 2.3283064365386963e-10f;  // 2^-32
 constexpr int kPolBlock = 128;
-
-// The photon's sequential uniforms: Philox4x32-10 (block, kTagPol, id lo, id hi).
-struct PolStream {
-    uint32_t lo, hi, block;
-    int k;
-    uint4 x;
-
-    __device__ __forceinline__ uint32_t word(const PhiloxKeys &ks) {
-        if (k == 4) {
-            x = philox10(make_uint4(block++, kTagPol, lo, hi), ks);
-            k = 0;
-        }
-        const uint32_t w = k == 0 ? x.x : (k == 1 ? x.y : (k == 2 ? x.z : x.w));
-        ++k;
-        return w;
-    }
-    // uniform in [2^-24, 1 - 2^-24]
-    __device__ __forceinline__ float u(const PhiloxKeys &ks) { return u01_f32(word(ks)); }
-};
+constexpr uint32_t kMaxCandidates = 1u << 24;          // candidate index range of a step
 
 // scipy interp1d (linear) on an ascending grid: the segment of the first grid
 // point >= xn (clipped to [1, n - 1]), linear between its ends.
@@ -88,33 +79,6 @@ __device__ __forceinline__ void azimuth(float u, float &c, float &s) {
     s = -sn;
 }
 
-// One step's scattering cosine and azimuth: the two-area rejection sampler of
-// populate_pdfs (monte_carlo3D.py:922-1004) for Stokes vector (I, Q, U).
-// Returns false if the time budget ran out.
-__device__ bool rejection_angles(const DevPhase32 &ph, int row, float I, float Q, float U, PolStream &s,
-                                 const PhiloxKeys &ks, float &cos_theta, float &cphi, float &sphi,
-                                 unsigned long long t0, unsigned long long budget_ns) {
-    const float C = sqrtf(fmaf(Q, Q, U * U));
-    const float max_val1 = fmaf(fabsf(I), __ldg(ph.a1 + row), __ldg(ph.b1 + row) * C);
-    const float max_val2 = fmaf(fabsf(I), __ldg(ph.a2 + row), __ldg(ph.b2 + row) * C);
-    const float w1 = ph.cos_max - ph.cos_cutoff, w2 = ph.cos_cutoff - ph.cos_min;
-    const float area1 = w1 * max_val1, area2 = w2 * max_val2;
-    const float percent_area1 = __fdividef(area1, area1 + area2);
-    for (uint32_t k = 0;; ++k) {
-        const bool one = s.u(ks) < percent_area1;
-        const float uc = s.u(ks);
-        azimuth(s.u(ks), cphi, sphi);
-        cos_theta = one ? fmaf(uc, w1, ph.cos_cutoff) : fmaf(-uc, w2, ph.cos_cutoff);
-        const float r3 = 1.000001f * s.u(ks) * (one ? max_val1 : max_val2);
-        const float S11 = phase_el(ph, 0, row, cos_theta);
-        const float S12 = phase_el(ph, 1, row, cos_theta);
-        const float c2 = fmaf(2.f * cphi, cphi, -1.f), s2 = 2.f * sphi * cphi;
-        const float pf = fmaf(I, S11, S12 * fmaf(Q, c2, U * s2));
-        if (!(r3 > pf)) return true;
-        if ((k & 255u) == 255u && global_ns() - t0 > budget_ns) return false;
-    }
-}
-
 // Rotate a Stokes vector by an angle whose doubled cosine / sine are (cd, sd)
 // (rotate_stokes_vector, monte_carlo3D.py:1090-1109).
 __device__ __forceinline__ void rotate(float &Q, float &U, float cd, float sd) {
@@ -129,28 +93,32 @@ struct PolPhoton {
     int64_t gid;
     const DevPhase32 *ph;
     int32_t ci, row, i;
+    uint32_t lo, hi;
     bool lam_surface, lam_bottom, bref;
     float tau, R, inv_ext, p_imp, coalb_ice, coalb_imp, wvn, depth;
     unsigned long long wvn_fx;
-    PolStream s;
-    float dtau_next;
-    uint32_t w_abs, w_ext;
+    uint4 sb;        // the current step's block (path, absorption, species, Lambertian)
     float mux, muy, muz, z, path, pathc;
     float I, Q, U, V;
 };
 
+__device__ __forceinline__ uint4 step_block(const PolPhoton &P, uint32_t n, uint32_t tag, const WalkArgs &a) {
+    return philox10(make_uint4(n, tag, P.lo, P.hi), a.keys);
+}
+
 // Birth of photon gid: wavelength (monte_carlo3D.py:1516-1520), optics row, the
-// initial draws of initial_pdfs (:1035-1038) and the incident direction and Stokes
-// vector (:1121-1132).
+// incident direction and Stokes vector (:1121-1132) and step 1's draws
+// (initial_pdfs, :1035-1038).
 __device__ __forceinline__ void pol_birth(PolPhoton &P, const WalkArgs &a, int64_t gid) {
     const int ci = find_config(a.prefix, a.n_cfg, gid);
     const DevConfig &c = a.cfgs[ci];
     const uint64_t rid = c.rng_base + (uint64_t)(gid - c.offset);
-    const uint32_t lo = (uint32_t)rid, hi = (uint32_t)(rid >> 32);
-    const uint4 rb = philox10(make_uint4(0u, kTagBirth, lo, hi), a.keys);
-    float sb, cb;
-    __sincosf(kTwoPiF * (u01_f32(rb.y) - 0.5f), &sb, &cb);
-    const float zb = sqrtf(-2.f * __logf(u01_f32(rb.x))) * cb;
+    P.lo = (uint32_t)rid;
+    P.hi = (uint32_t)(rid >> 32);
+    const uint4 rb = philox10(make_uint4(0u, kTagBirth, P.lo, P.hi), a.keys);
+    float sbn, cbn;
+    __sincosf(kTwoPiF * (u01_f32(rb.y) - 0.5f), &sbn, &cbn);
+    const float zb = sqrtf(-2.f * __logf(u01_f32(rb.x))) * cbn;
     const int kw = __float2int_rn(fmaf(c.sigma_100, zb, c.wvl0_100));
     const LutEntry *e = a.lut + c.lut_off + min(max(kw - c.k_lo, 0), c.lut_n - 1);
     const float4 e0 = __ldg(reinterpret_cast<const float4 *>(e));       // wvn, coalb_ice, coalb_imp, g
@@ -172,10 +140,6 @@ __device__ __forceinline__ void pol_birth(PolPhoton &P, const WalkArgs &a, int64
     P.wvn = e0.x;
     P.depth = e1.z;
     P.wvn_fx = __ldg(&e->wvn_fx);
-    P.s = PolStream{lo, hi, 0u, 4, make_uint4(0, 0, 0, 0)};
-    P.dtau_next = -__logf(P.s.u(a.keys));
-    P.w_abs = P.s.word(a.keys);
-    P.w_ext = P.s.word(a.keys);
     P.mux = c.mux0;
     P.muy = 0.f;
     P.muz = c.muz0;
@@ -188,27 +152,54 @@ __device__ __forceinline__ void pol_birth(PolPhoton &P, const WalkArgs &a, int64
     P.V = (float)c.stokes0[3];
 }
 
-// One scatter event of the photon (monte_carlo3D.py:1212-1466).  Returns the end
-// condition (0: still walking), or -1 when the time budget ran out.
-__device__ __forceinline__ int pol_step(PolPhoton &P, const WalkArgs &a, unsigned long long t0) {
+// The envelope of the rejection sampler for the photon's Stokes vector
+// (populate_pdfs, monte_carlo3D.py:929-951).
+struct Envelope {
+    float max1, max2, pa1;
+};
+
+__device__ __forceinline__ Envelope envelope(const PolPhoton &P) {
     const DevPhase32 &ph = *P.ph;
-    P.i += 1;
-    float cphi = 0.f, sphi = 0.f, p_cos = 1.f;
-    if (P.i > 1) {                                                        // :1215-1224
-        if (!rejection_angles(ph, P.row, P.I, P.Q, P.U, P.s, a.keys, p_cos, cphi, sphi, t0, a.budget_ns))
-            return -1;
-        P.dtau_next = -__logf(P.s.u(a.keys));
-        P.w_abs = P.s.word(a.keys);
-        P.w_ext = P.s.word(a.keys);
-    }
-    const float dtau = (P.lam_surface && P.i == 1) ? 0.f : P.dtau_next;  // :1227-1229
+    const float C = sqrtf(fmaf(P.Q, P.Q, P.U * P.U));
+    Envelope v;
+    v.max1 = fmaf(fabsf(P.I), __ldg(ph.a1 + P.row), __ldg(ph.b1 + P.row) * C);
+    v.max2 = fmaf(fabsf(P.I), __ldg(ph.a2 + P.row), __ldg(ph.b2 + P.row) * C);
+    const float area1 = (ph.cos_max - ph.cos_cutoff) * v.max1;
+    const float area2 = (ph.cos_cutoff - ph.cos_min) * v.max2;
+    v.pa1 = __fdividef(area1, area1 + area2);
+    return v;
+}
+
+// Candidate j of step n (:953-1001): its cosine and azimuth, and whether it passes.
+__device__ __forceinline__ bool candidate(const DevPhase32 &ph, int row, float I, float Q, float U,
+                                          const Envelope &v, uint32_t n, uint32_t j, uint32_t lo, uint32_t hi,
+                                          const PhiloxKeys &ks, float &cos_theta, float &cphi, float &sphi) {
+    const uint4 r = philox10(make_uint4(n, kTagPolCand | (j << 8), lo, hi), ks);
+    const bool one = u01_f32(r.x) < v.pa1;
+    const float uc = u01_f32(r.y);
+    azimuth(u01_f32(r.z), cphi, sphi);
+    cos_theta = one ? fmaf(uc, ph.cos_max - ph.cos_cutoff, ph.cos_cutoff)
+                    : fmaf(-uc, ph.cos_cutoff - ph.cos_min, ph.cos_cutoff);
+    const float r3 = 1.000001f * u01_f32(r.w) * (one ? v.max1 : v.max2);
+    const float S11 = phase_el(ph, 0, row, cos_theta);
+    const float S12 = phase_el(ph, 1, row, cos_theta);
+    const float c2 = fmaf(2.f * cphi, cphi, -1.f), s2 = 2.f * sphi * cphi;
+    const float pf = fmaf(I, S11, S12 * fmaf(Q, c2, U * s2));
+    return !(r3 > pf);
+}
+
+// The rest of the step (monte_carlo3D.py:1227-1466) with its scattering angles.
+// Returns the end condition (0: still walking).
+__device__ __forceinline__ int pol_step_post(PolPhoton &P, const WalkArgs &a, float p_cos, float cphi, float sphi) {
+    const DevPhase32 &ph = *P.ph;
+    const float dtau = (P.lam_surface && P.i == 1) ? 0.f : -__logf(u01_f32(P.sb.x));   // :1227-1229
     float nx = P.mux, ny = P.muy, nz = P.muz;
     if (P.i > 1) {
         // direction (:1238-1281): Lambertian about the vertical, or the rotation
         float m0x = P.mux, m0y = P.muy, m0z = P.muz, ct = p_cos;
         if (P.lam_surface || P.bref) {
             m0x = 0.f; m0y = 0.f; m0z = 1.f;
-            ct = sqrtf(P.s.u(a.keys));
+            ct = sqrtf(u01_f32(P.sb.w));
         }
         const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
         if (fabsf(m0z) > 0.99999f) {
@@ -267,7 +258,7 @@ __device__ __forceinline__ int pol_step(PolPhoton &P, const WalkArgs &a, unsigne
         P.path = tt;
     }
     P.mux = nx; P.muy = ny; P.muz = nz;
-    const bool imp = (float)P.w_ext * kTwo32Inv < P.p_imp;
+    const bool imp = (float)P.sb.z * kTwo32Inv < P.p_imp;
     const float coalb = imp ? P.coalb_imp : P.coalb_ice;
     int cond = 0;
     if (zn > 0.f) {
@@ -276,9 +267,9 @@ __device__ __forceinline__ int pol_step(PolPhoton &P, const WalkArgs &a, unsigne
     } else if (zn < -P.tau) {
         P.path -= __fdividef(zn + P.tau, zn - P.z) * inc;
         zn = -P.tau;
-        if (P.lam_bottom && P.s.u(a.keys) <= P.R) P.bref = true;
+        if (P.lam_bottom && u01_f32(step_block(P, (uint32_t)P.i, kTagPolRefl, a).x) <= P.R) P.bref = true;
         else cond = (P.i == 1) ? 3 : 2;
-    } else if ((float)P.w_abs * kTwo32Inv < coalb) {
+    } else if ((float)P.sb.y * kTwo32Inv < coalb) {
         cond = imp ? 5 : 4;
     }
     P.z = zn;
@@ -313,40 +304,125 @@ __device__ __forceinline__ void pol_finish(const PolPhoton &P, const WalkArgs &a
     tally_global(a.tallies + P.ci, cond, P.i - 1, P.wvn_fx, theta, phi);
 }
 
-// One loop iteration is one scatter event of each lane's photon; a lane whose
-// photon ends claims the next one in the same iteration, so the lanes of a warp
-// stay together step by step instead of waiting for the warp's longest walk.
+// Warp-synchronous: every lane of the warp stays in the loop until none has a
+// photon left, so the rejection rounds and claims can use the whole warp.
 __global__ void __launch_bounds__(kPolBlock) walk_pol32_kernel(const WalkArgs a) {
     const unsigned long long t0 = global_ns();
     const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
     PolPhoton P;
-    bool have = false;
+    bool have = false, exhausted = false;
     for (uint32_t it = 0;; ++it) {
-        if (!have) {
-            // claim the next photon; lanes that arrive together share one atomic
-            const unsigned m = __activemask();
-            const int leader = __ffs(m) - 1;
+        // ---- claims: lanes without a photon take the next ones, one atomic per warp
+        const unsigned need = __ballot_sync(0xffffffffu, !have && !exhausted);
+        if (need) {
             unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(a.work, (unsigned long long)__popc(m));
-            base = __shfl_sync(m, base, leader);
-            const unsigned long long g = base + __popc(m & ((1u << lane) - 1u));
-            if (g >= (unsigned long long)a.total) break;
-            pol_birth(P, a, (int64_t)g);
-            have = true;
+            if (lane == __ffs(need) - 1) base = atomicAdd(a.work, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+            if (!have && !exhausted) {
+                const unsigned long long g = base + __popc(need & lt_mask);
+                if (g < (unsigned long long)a.total) {
+                    pol_birth(P, a, (int64_t)g);
+                    have = true;
+                } else {
+                    exhausted = true;
+                }
+            }
         }
-        const int cond = pol_step(P, a, t0);
-        if (cond < 0) {
-            atomicOr(a.status, kStatusBudget);
-            break;
+        if (!__any_sync(0xffffffffu, have)) break;
+
+        // ---- this step's draws; scattering angles for steps after the first
+        bool pending = false;
+        Envelope env{0.f, 0.f, 0.f};
+        uint32_t jbase = 0;
+        float p_cos = 1.f, cphi = 0.f, sphi = 0.f;
+        if (have) {
+            P.i += 1;
+            P.sb = step_block(P, (uint32_t)P.i, kTagPolStep, a);
+            if (P.i > 1) {
+                env = envelope(P);
+                pending = true;
+            }
         }
-        if (cond > 0) {
-            pol_finish(P, a, cond);
-            have = false;
+        // ---- rejection rounds (:953-1001): the n pending photons share the lanes;
+        // lane l tests candidate jbase + l / n of the photon of rank l % n, and a
+        // photon takes its lowest-indexed passing candidate
+        unsigned pend = __ballot_sync(0xffffffffu, pending);
+        for (uint32_t round = 0; pend; ++round) {
+            const int np = __popc(pend);
+            const int r = lane % np, q = lane / np;
+            const int owner = __fns(pend, 0, r + 1);
+            const int o_row = __shfl_sync(0xffffffffu, P.row, owner);
+            const float o_I = __shfl_sync(0xffffffffu, P.I, owner);
+            const float o_Q = __shfl_sync(0xffffffffu, P.Q, owner);
+            const float o_U = __shfl_sync(0xffffffffu, P.U, owner);
+            Envelope o_env;
+            o_env.max1 = __shfl_sync(0xffffffffu, env.max1, owner);
+            o_env.max2 = __shfl_sync(0xffffffffu, env.max2, owner);
+            o_env.pa1 = __shfl_sync(0xffffffffu, env.pa1, owner);
+            const uint32_t o_n = (uint32_t)__shfl_sync(0xffffffffu, P.i, owner);
+            const uint32_t o_lo = __shfl_sync(0xffffffffu, P.lo, owner);
+            const uint32_t o_hi = __shfl_sync(0xffffffffu, P.hi, owner);
+            const uint32_t o_j = __shfl_sync(0xffffffffu, jbase, owner) + (uint32_t)q;
+            const DevPhase32 *o_ph = reinterpret_cast<const DevPhase32 *>(
+                __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(P.ph), owner));
+            float c_cos, c_cphi, c_sphi;
+            const bool pass = candidate(*o_ph, o_row, o_I, o_Q, o_U, o_env, o_n, o_j, o_lo, o_hi, a.keys,
+                                        c_cos, c_cphi, c_sphi);
+            const unsigned acc = __ballot_sync(0xffffffffu, pass);
+            int src = lane;
+            bool got = false;
+            if (pending) {
+                const int me = __popc(pend & lt_mask);
+                unsigned group = 0;
+                for (int l = me; l < 32; l += np) group |= 1u << l;
+                const unsigned hit = acc & group;
+                if (hit) {
+                    src = __ffs(hit) - 1;
+                    got = true;
+                } else {
+                    jbase += (uint32_t)__popc(group);
+                }
+            }
+            const float w_cos = __shfl_sync(0xffffffffu, c_cos, src);
+            const float w_cphi = __shfl_sync(0xffffffffu, c_cphi, src);
+            const float w_sphi = __shfl_sync(0xffffffffu, c_sphi, src);
+            if (got) {
+                p_cos = w_cos;
+                cphi = w_cphi;
+                sphi = w_sphi;
+                pending = false;
+            } else if (pending && jbase >= kMaxCandidates) {
+                atomicOr(a.status, kStatusStream);   // a candidate range no envelope should need
+                pending = false;
+            }
+            pend = __ballot_sync(0xffffffffu, pending);
+            if ((round & 255u) == 255u) {
+                int over = 0;
+                if (lane == 0) over = global_ns() - t0 > a.budget_ns;
+                if (__shfl_sync(0xffffffffu, over, 0)) {
+                    if (lane == 0) atomicOr(a.status, kStatusBudget);
+                    return;
+                }
+            }
         }
-        if ((it & 1023u) == 1023u &&
-            (global_ns() - t0 > a.budget_ns || (*(volatile unsigned int *)a.status & kStatusBudget))) {
-            atomicOr(a.status, kStatusBudget);
-            break;
+
+        // ---- the rest of the step; finished photons leave their records
+        if (have) {
+            const int cond = pol_step_post(P, a, p_cos, cphi, sphi);
+            if (cond > 0) {
+                pol_finish(P, a, cond);
+                have = false;
+            }
+        }
+        if ((it & 1023u) == 1023u) {
+            int stop = 0;
+            if (lane == 0)
+                stop = (global_ns() - t0 > a.budget_ns) || (*(volatile unsigned int *)a.status & kStatusBudget);
+            if (__shfl_sync(0xffffffffu, stop, 0)) {
+                if (lane == 0) atomicOr(a.status, kStatusBudget);
+                return;
+            }
         }
     }
 }
