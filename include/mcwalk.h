@@ -319,7 +319,8 @@ typedef struct {
 } mcw_post_stats;
 
 /* Post-processing of records on the device (records: host or device pointer, see
- * records_where; mode selects mcw_record32 / mcw_record64; photons are grouped by
+ * records_where; mode selects mcw_record32 / mcw_record64 / mcw_record32p /
+ * mcw_record64p, whose Stokes columns it does not read; photons are grouped by
  * their config field, which must be < n_cfg): the wvn-weighted condition-1 exit
  * zenith histogram with np.histogram's binning of [0, pi/2] into n_bins bins
  * (post_processing.py:73-77 brf, :132-134 polar BRFs), and per-config sums for

@@ -770,7 +770,8 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
 int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t mode, int64_t n, int32_t n_cfg,
              int32_t n_bins, uint64_t *bin_wvn_fx, uint32_t *bin_count, mcw_post_stats *stats) {
     if (!ctx) return MCW_ERR_ARG;
-    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64) return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
+    if (mode != MCW_MODE_F32 && mode != MCW_MODE_REPLAY64 && mode != MCW_MODE_POL64 && mode != MCW_MODE_POL32)
+        return set_err(ctx, MCW_ERR_ARG, "unknown mode %d", mode);
     if (records_where != MCW_RECORDS_HOST && records_where != MCW_RECORDS_DEVICE)
         return set_err(ctx, MCW_ERR_ARG, "records must be on the host or the device");
     if (n < 0 || (n > 0 && !records) || n_cfg <= 0 || n_bins < 0 || n_bins > (1 << 20) || !stats ||
@@ -778,7 +779,11 @@ int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t m
         return set_err(ctx, MCW_ERR_ARG, "invalid post-processing arguments");
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    const size_t rec_size = (mode == MCW_MODE_F32) ? sizeof(mcw_record32) : sizeof(mcw_record64);
+    const size_t rec_size = (mode == MCW_MODE_F32)     ? sizeof(mcw_record32)
+                            : (mode == MCW_MODE_POL32) ? sizeof(mcw_record32p)
+                            : (mode == MCW_MODE_POL64) ? sizeof(mcw_record64p)
+                                                       : sizeof(mcw_record64);
+    const bool f64 = (mode == MCW_MODE_REPLAY64 || mode == MCW_MODE_POL64);
     const size_t b_bins = (size_t)n_cfg * n_bins * sizeof(unsigned long long);
     const size_t b_cnt = (size_t)n_cfg * n_bins * sizeof(unsigned int);
     const size_t b_cnt_pad = (b_cnt + 255) & ~size_t(255);
@@ -792,7 +797,7 @@ int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t m
         drec = ctx->records.p;
     }
     CUDA_TRY(ctx, cudaMemsetAsync(dev, 0, b_bins + b_cnt_pad + b_stats, st));
-    CUDA_TRY(ctx, launch_post(drec, mode == MCW_MODE_REPLAY64, n, n_cfg, n_bins, (unsigned long long *)dev,
+    CUDA_TRY(ctx, launch_post(drec, f64, rec_size, n, n_cfg, n_bins, (unsigned long long *)dev,
                               (unsigned int *)(dev + b_bins), (mcw_post_stats *)(dev + b_bins + b_cnt_pad),
                               ctx->sm_count, st));
     if (n_bins > 0) {

@@ -170,8 +170,10 @@ struct LutArgs {
 const char *config_problem(const mcw_config &c, int32_t n_ice);
 
 // Kernel launchers (defined in the .cu files).
-cudaError_t launch_post(const void *recs, bool f64, int64_t n, int n_cfg, int n_bins, unsigned long long *bins_fx,
-                        unsigned int *bins_cnt, mcw_post_stats *stats, int sms, cudaStream_t s);
+// recs: n records of `stride` bytes starting with an mcw_record64 (f64) or mcw_record32.
+cudaError_t launch_post(const void *recs, bool f64, size_t stride, int64_t n, int n_cfg, int n_bins,
+                        unsigned long long *bins_fx, unsigned int *bins_cnt, mcw_post_stats *stats, int sms,
+                        cudaStream_t s);
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
 // Photons the walk hands over to its drain queue are packed as this many float4.
 constexpr int kDrainSlot = 6;

@@ -30,19 +30,21 @@ __device__ __forceinline__ int np_bin(double x, int n, double step) {
     return i;
 }
 
+// recs: records of stride bytes whose leading fields are an mcw_record64 (kF64) or an
+// mcw_record32 (the polarised records extend them).
 template <bool kF64>
-__global__ void post_kernel(const void *recs, int64_t n, int n_cfg, int n_bins, double step,
+__global__ void post_kernel(const void *recs, size_t stride, int64_t n, int n_cfg, int n_bins, double step,
                             unsigned long long *bins_fx, unsigned int *bins_cnt, mcw_post_stats *stats) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int cond, nscat;
         uint32_t cfg;
         double wvn, theta, path;
         if (kF64) {
-            const mcw_record64 r = static_cast<const mcw_record64 *>(recs)[i];
+            const mcw_record64 r = *reinterpret_cast<const mcw_record64 *>(static_cast<const char *>(recs) + i * stride);
             cond = r.condition; nscat = r.n_scat; cfg = r.config;
             wvn = r.wvn; theta = r.theta_n; path = r.path_length;
         } else {
-            const mcw_record32 r = static_cast<const mcw_record32 *>(recs)[i];
+            const mcw_record32 r = *reinterpret_cast<const mcw_record32 *>(static_cast<const char *>(recs) + i * stride);
             cond = r.condition; nscat = r.n_scat; cfg = r.config;
             wvn = r.wvn; theta = r.theta_n; path = r.path_length;
         }
@@ -66,14 +68,15 @@ __global__ void post_kernel(const void *recs, int64_t n, int n_cfg, int n_bins, 
 
 }  // namespace
 
-cudaError_t launch_post(const void *recs, bool f64, int64_t n, int n_cfg, int n_bins, unsigned long long *bins_fx,
-                        unsigned int *bins_cnt, mcw_post_stats *stats, int sms, cudaStream_t s) {
+cudaError_t launch_post(const void *recs, bool f64, size_t stride, int64_t n, int n_cfg, int n_bins,
+                        unsigned long long *bins_fx, unsigned int *bins_cnt, mcw_post_stats *stats, int sms,
+                        cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     const double step = (kPi / 2) / (double)(n_bins > 0 ? n_bins : 1);
     const int64_t want = (n + 255) / 256;
     const int grid = (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
-    if (f64) post_kernel<true><<<grid, 256, 0, s>>>(recs, n, n_cfg, n_bins, step, bins_fx, bins_cnt, stats);
-    else post_kernel<false><<<grid, 256, 0, s>>>(recs, n, n_cfg, n_bins, step, bins_fx, bins_cnt, stats);
+    if (f64) post_kernel<true><<<grid, 256, 0, s>>>(recs, stride, n, n_cfg, n_bins, step, bins_fx, bins_cnt, stats);
+    else post_kernel<false><<<grid, 256, 0, s>>>(recs, stride, n, n_cfg, n_bins, step, bins_fx, bins_cnt, stats);
     return cudaGetLastError();
 }
 

@@ -27,10 +27,15 @@ def calculate_bins(active_area=1.0, d_dome=175.0):
 
 
 def zenith_brf(walker, records, n_bins=None, n_cfg=None):
-    """Per-config 1-D BRF and albedo statistics of a record array (RECORD32 or RECORD64,
-    host numpy array) using the device kernel of ``walker``'s context."""
+    """Per-config 1-D BRF and albedo statistics of a record array (RECORD32, RECORD64 or
+    the polarised RECORD32P / RECORD64P, host numpy array) using the device kernel of
+    ``walker``'s context."""
     rec = np.ascontiguousarray(records)
-    mode = _abi.MODE_F32 if rec.dtype == _abi.RECORD32 else _abi.MODE_REPLAY64
+    modes = {_abi.RECORD32: _abi.MODE_F32, _abi.RECORD64: _abi.MODE_REPLAY64,
+             _abi.RECORD32P: _abi.MODE_POL32, _abi.RECORD64P: _abi.MODE_POL64}
+    if rec.dtype not in modes:
+        raise TypeError('records must be RECORD32, RECORD64, RECORD32P or RECORD64P')
+    mode = modes[rec.dtype]
     if n_bins is None:
         n_bins = calculate_bins()
     if n_cfg is None:

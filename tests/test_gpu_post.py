@@ -49,6 +49,21 @@ def test_golden_records_match_numpy(walker, n_bins):
     _check(out, rec, n_bins)
 
 
+def test_polarised_records_match_numpy(walker):
+    """The polarised walks' records (their leading columns are the HG records') go
+    through the same post-processing, FP64 and FP32."""
+    from tests.helpers import golden_config, golden_phase, golden_tables
+    g = load_golden('pol')
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    walker.set_phase_matrices([golden_phase(g)])
+    for mode in ('pol64', 'pol32'):
+        cfg = dataclasses.replace(golden_config(g), n_photon=20000)
+        rec = walker.walk([cfg], 9, mode=mode).records
+        out = post.zenith_brf(walker, rec, 137)
+        _check(out, rec, 137)
+
+
 def test_walk_records_match_numpy(walker):
     lo, hi = ssp.grid_for(1.55, 0.085)
     walker.set_tables([ssp.synthetic_ice_table(250.0, lo, hi)], ssp.synthetic_impurity_table(lo, hi))
