@@ -91,6 +91,52 @@ def test_pol32_statistics_match_oracle(walker, n):
     assert np.array_equal(again, rec[:5000])
 
 
+POL_VARIANTS = {
+    # a Lambertian surface: the phase-matrix update at Lambertian angles (:1238-1342)
+    'lamsurf': dict(lambertian_surface=True, lambertian_reflectance=0.7),
+    # impurities: the species draw and condition 5
+    'imp': dict(imp_cnc=2e-4),
+    # no bottom reflection: conditions 2 and 3 from a thin slab
+    'nobottom': dict(lambertian_bottom=False, tau_tot=3.0),
+}
+
+
+@pytest.mark.parametrize('variant', sorted(POL_VARIANTS))
+def test_polarised_variants_match_oracle(walker, variant):
+    """Branches of the polarised walk the golden run does not reach: the FP64 replay
+    equals the oracle photon by photon (condition, n_scat bit-exact; Stokes within
+    1e-10), and the FP32 walk agrees with the oracle statistically."""
+    g = load_golden('pol')
+    ice, imp = golden_tables(g)
+    walker.set_tables([ice], imp)
+    walker.set_phase_matrices([golden_phase(g)])
+    from oracle import oracle as orc
+    cfg = dataclasses.replace(golden_config(g), n_photon=4000, **POL_VARIANTS[variant])
+    c = orc.make_config(cfg.n_photon, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot,
+                        cfg.imp_cnc, cfg.rho_snw, cfg.rho_ice, cfg.lambertian_surface,
+                        cfg.lambertian_bottom, cfg.lambertian_reflectance, nearest=True,
+                        phase=orc.phase_from_golden(g))
+    ref = orc.walk(c, ice, imp, 77, threads=16)
+    got = walker.walk([cfg], 77, mode='pol64').records
+    compare_replay(got, ref)
+    st = np.stack([got['stokes_q'], got['stokes_u'], got['stokes_v']], 1)
+    assert np.abs(st - ref['stokes'][:, 1:]).max() < 1e-10
+    big = dataclasses.replace(cfg, n_photon=100000)
+    rec = walker.walk([big], 5, mode='pol32').records
+    c.n_photon = big.n_photon
+    ref = orc.walk(c, ice, imp, 55, threads=16)
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    for a, b in ((rec['n_scat'].astype(np.float64), ref['n_scat'].astype(np.float64)),
+                 (rec['stokes_q'].astype(np.float64), ref['stokes'][:, 1]),
+                 (rec['stokes_u'].astype(np.float64), ref['stokes'][:, 2])):
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se + 1e-7, (variant, a.mean(), b.mean(), se)
+    if variant == 'imp':
+        assert np.any(rec['condition'] == 5) and np.any(ref['condition'] == 5)
+    if variant == 'nobottom':
+        assert np.any(rec['condition'] == 2)
+
+
 def test_polarised_walk_needs_its_mode_and_tables(walker):
     """Polarised configs walk in 'pol64' only, with phase matrices attached to their
     ice table; set_tables drops the matrices of the previous tables."""
