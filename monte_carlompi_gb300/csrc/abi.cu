@@ -604,6 +604,15 @@ int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n)
         }
         f.a1 = f32(d.a1); f.a2 = f32(d.a2); f.b1 = f32(d.b1); f.b2 = f32(d.b2);
         f.n_rows = d.n_rows;
+        f.shared_grid = 0;
+        if (d.n_rows > 0) {
+            const mcw_phase_table &p = tabs[t];
+            bool same = true;
+            for (int e = 1; e < 6 && same; ++e)
+                same = p.n_angle[e] == p.n_angle[0] &&
+                       memcmp(p.cos_asc[e], p.cos_asc[0], p.n_angle[0] * sizeof(double)) == 0;
+            f.shared_grid = same ? 1 : 0;
+        }
         f.cos_max = (float)d.cos_max;
         f.cos_min = (float)d.cos_min;
         f.cos_cutoff = (float)d.cos_cutoff;

@@ -68,7 +68,7 @@ struct DevPhase32 {
     const float *a1, *a2, *b1, *b2;
     int32_t n_angle[6];
     int32_t n_rows;
-    int32_t pad;
+    int32_t shared_grid;         // 1: the six elements share one cos grid (one search serves all)
     float cos_max, cos_min, cos_cutoff, pad2;
 };
 

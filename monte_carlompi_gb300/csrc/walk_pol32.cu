@@ -70,6 +70,24 @@ __device__ __forceinline__ float phase_el(const DevPhase32 &ph, int e, int row, 
     return interp32(ph.cos_asc[e], ph.p_asc[e] + (size_t)row * ph.n_angle[e], ph.n_angle[e], ct);
 }
 
+// The segment interp32 would use: first grid point >= xn, clipped to [1, n - 1].
+__device__ __forceinline__ int segment32(const float *x, int n, float xn) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(x + mid) < xn) lo = mid + 1; else hi = mid;
+    }
+    return min(max(lo, 1), n - 1);
+}
+
+// Element e at xn in segment k of the grid the elements share.
+__device__ __forceinline__ float phase_at(const DevPhase32 &ph, int e, int row, int k, float xn) {
+    const float *x = ph.cos_asc[0];
+    const float *y = ph.p_asc[e] + (size_t)row * ph.n_angle[0];
+    const float xl = __ldg(x + k - 1), xh = __ldg(x + k), yl = __ldg(y + k - 1), yh = __ldg(y + k);
+    return fmaf(__fdividef(xn - xl, xh - xl), yh - yl, yl);
+}
+
 // cos / sin of an azimuth 2 pi u, u in (0, 1): sincos of the angle shifted into
 // [-pi, pi) (where the fast intrinsic is accurate), negated back.
 __device__ __forceinline__ void azimuth(float u, float &c, float &s) {
@@ -181,8 +199,15 @@ __device__ __forceinline__ bool candidate(const DevPhase32 &ph, int row, float I
     cos_theta = one ? fmaf(uc, ph.cos_max - ph.cos_cutoff, ph.cos_cutoff)
                     : fmaf(-uc, ph.cos_cutoff - ph.cos_min, ph.cos_cutoff);
     const float r3 = 1.000001f * u01_f32(r.w) * (one ? v.max1 : v.max2);
-    const float S11 = phase_el(ph, 0, row, cos_theta);
-    const float S12 = phase_el(ph, 1, row, cos_theta);
+    float S11, S12;
+    if (ph.shared_grid) {
+        const int k = segment32(ph.cos_asc[0], ph.n_angle[0], cos_theta);
+        S11 = phase_at(ph, 0, row, k, cos_theta);
+        S12 = phase_at(ph, 1, row, k, cos_theta);
+    } else {
+        S11 = phase_el(ph, 0, row, cos_theta);
+        S12 = phase_el(ph, 1, row, cos_theta);
+    }
     const float c2 = fmaf(2.f * cphi, cphi, -1.f), s2 = 2.f * sphi * cphi;
     const float pf = fmaf(I, S11, S12 * fmaf(Q, c2, U * s2));
     return !(r3 > pf);
@@ -226,9 +251,16 @@ __device__ __forceinline__ int pol_step_post(PolPhoton &P, const WalkArgs &a, fl
             const float sps = sqrtf(fmaxf(0.f, fmaf(-cphi, cphi, 1.f)));
             float Q = P.Q, U = P.U;
             rotate(Q, U, fmaf(2.f * cphi, cphi, -1.f), 2.f * sps * cphi);
-            const float P11 = phase_el(ph, 0, P.row, ct), P12 = phase_el(ph, 1, P.row, ct);
-            const float P22 = phase_el(ph, 2, P.row, ct), P33 = phase_el(ph, 3, P.row, ct);
-            const float P43 = phase_el(ph, 4, P.row, ct), P44 = phase_el(ph, 5, P.row, ct);
+            float Pe[6];
+            if (ph.shared_grid) {
+                const int k = segment32(ph.cos_asc[0], ph.n_angle[0], ct);
+#pragma unroll
+                for (int e = 0; e < 6; ++e) Pe[e] = phase_at(ph, e, P.row, k, ct);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 6; ++e) Pe[e] = phase_el(ph, e, P.row, ct);
+            }
+            const float P11 = Pe[0], P12 = Pe[1], P22 = Pe[2], P33 = Pe[3], P43 = Pe[4], P44 = Pe[5];
             const float Is = fmaf(P.I, P11, Q * P12), Qs = fmaf(P.I, P12, Q * P22);
             const float Us = fmaf(U, P33, -P.V * P43), Vs = fmaf(U, P43, P.V * P44);
             // back to the meridian plane of the new direction

@@ -137,6 +137,44 @@ def test_polarised_variants_match_oracle(walker, variant):
         assert np.any(rec['condition'] == 2)
 
 
+def test_polarised_walk_with_separate_element_grids(walker):
+    """P33 tabulated on a grid of its own (every other angle): the walks look it up on
+    that grid; FP64 replay equals the oracle photon by photon, FP32 agrees statistically."""
+    from monte_carlompi_gb300 import ssp as S
+    from oracle import oracle as orc
+    g = load_golden('pol')
+    ice, imp = golden_tables(g)
+    pt = golden_phase(g)
+    theta = g['phase_theta']
+    keep = np.r_[np.arange(0, theta.size - 1, 2), theta.size - 1]      # keeps 0 and 180 deg
+    rows = [e[:, ::-1] for e in pt.p_asc]                               # back to descending cos
+    els = rows[:3] + [rows[3][:, keep]] + rows[4:]
+    thetas = [theta] * 3 + [theta[keep]] + [theta] * 2
+    pt2 = S.phase_table(thetas, els, ice.wvl, g['param_wvl0'].item())
+    assert pt2.cos_asc[3].size == keep.size
+    walker.set_tables([ice], imp)
+    walker.set_phase_matrices([pt2])
+    cfg = dataclasses.replace(golden_config(g), n_photon=3000)
+    c = orc.make_config(cfg.n_photon, cfg.wvl0, cfg.half_width, cfg.theta0_deg, cfg.tau_tot,
+                        cfg.imp_cnc, cfg.rho_snw, cfg.rho_ice, cfg.lambertian_surface,
+                        cfg.lambertian_bottom, cfg.lambertian_reflectance, nearest=True,
+                        phase=orc.make_phase(pt2, g['stokes0']))
+    ref = orc.walk(c, ice, imp, 8, threads=16)
+    got = walker.walk([cfg], 8, mode='pol64').records
+    compare_replay(got, ref)
+    st = np.stack([got['stokes_q'], got['stokes_u'], got['stokes_v']], 1)
+    assert np.abs(st - ref['stokes'][:, 1:]).max() < 1e-10
+    big = dataclasses.replace(cfg, n_photon=100000)
+    rec = walker.walk([big], 6, mode='pol32').records
+    c.n_photon = big.n_photon
+    ref = orc.walk(c, ice, imp, 66, threads=16)
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    for a, b in ((rec['stokes_q'].astype(np.float64), ref['stokes'][:, 1]),
+                 (rec['stokes_u'].astype(np.float64), ref['stokes'][:, 2])):
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se + 1e-7
+
+
 def test_polarised_walk_needs_its_mode_and_tables(walker):
     """Polarised configs walk in 'pol64' only, with phase matrices attached to their
     ice table; set_tables drops the matrices of the previous tables."""
