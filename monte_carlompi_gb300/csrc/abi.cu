@@ -101,7 +101,7 @@ struct mcw_ctx {
     bool have_tables = false;
     std::vector<std::vector<int32_t>> ice_order;   // row permutation of each ice table (stored ascending)
     // phase matrices of the polarised walk, one per ice table (n_rows 0 = none)
-    DevBuf phasedata, phase_tables, phasedata32, phase_tables32;
+    DevBuf phasedata, phase_tables, phasedata32, phase_tables32, phase_seeds;
     std::vector<int32_t> phase_rows;
     // workspace
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
@@ -594,6 +594,8 @@ int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n)
     CUDA_TRY(ctx, ctx->phase_tables32.ensure(n * sizeof(DevPhase32)));
     const float *fbase = (const float *)ctx->phasedata32.p;
     auto f32 = [&](const double *p) { return p ? fbase + (p - dbase) : nullptr; };
+    std::vector<uint16_t> seeds((size_t)n * kPhaseBuckets, 0);
+    CUDA_TRY(ctx, ctx->phase_seeds.ensure(seeds.size() * sizeof(uint16_t)));
     for (int32_t t = 0; t < n; ++t) {
         const DevPhase &d = dev[t];
         DevPhase32 f{};
@@ -612,6 +614,22 @@ int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n)
                 same = p.n_angle[e] == p.n_angle[0] &&
                        memcmp(p.cos_asc[e], p.cos_asc[0], p.n_angle[0] * sizeof(double)) == 0;
             f.shared_grid = same ? 1 : 0;
+            if (same && p.n_angle[0] <= 65535) {
+                // bucket seeds on the float copy of the grid (what the kernel compares)
+                const int32_t m = p.n_angle[0];
+                const float lo = (float)p.cos_asc[0][0], hi = (float)p.cos_asc[0][m - 1];
+                const float scale = (float)kPhaseBuckets / (hi - lo);
+                uint16_t *sd = &seeds[(size_t)t * kPhaseBuckets];
+                int32_t j = 0;
+                for (int b = 0; b < kPhaseBuckets; ++b) {
+                    const float edge = lo + (float)b / scale;
+                    while (j < m && (float)p.cos_asc[0][j] < edge) ++j;
+                    sd[b] = (uint16_t)j;
+                }
+                f.seed = (const uint16_t *)ctx->phase_seeds.p + (size_t)t * kPhaseBuckets;
+                f.seed_lo = lo;
+                f.seed_scale = scale;
+            }
         }
         f.cos_max = (float)d.cos_max;
         f.cos_min = (float)d.cos_min;
@@ -619,6 +637,7 @@ int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n)
         dev32[t] = f;
     }
     CUDA_TRY(ctx, cudaMemcpy(ctx->phasedata32.p, host32.data(), host32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(ctx, cudaMemcpy(ctx->phase_seeds.p, seeds.data(), seeds.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     CUDA_TRY(ctx, cudaMemcpy(ctx->phase_tables32.p, dev32.data(), n * sizeof(DevPhase32), cudaMemcpyHostToDevice));
     for (int32_t t = 0; t < n; ++t) ctx->phase_rows[t] = tabs[t].n_rows;
     return MCW_OK;

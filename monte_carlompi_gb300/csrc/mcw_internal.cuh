@@ -70,7 +70,12 @@ struct DevPhase32 {
     int32_t n_rows;
     int32_t shared_grid;         // 1: the six elements share one cos grid (one search serves all)
     float cos_max, cos_min, cos_cutoff, pad2;
+    // seeds of the search on the shared grid: seed[b] = first grid index with
+    // cos >= the lower edge of bucket b, kPhaseBuckets buckets uniform on [cos_min, cos_max]
+    const uint16_t *seed;
+    float seed_lo, seed_scale;
 };
+constexpr int kPhaseBuckets = 2048;
 
 // Phase matrices of one ice table on the device (mcw_phase_table, rows in the
 // device table's order).

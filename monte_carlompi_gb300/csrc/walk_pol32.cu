@@ -80,6 +80,19 @@ __device__ __forceinline__ int segment32(const float *x, int n, float xn) {
     return min(max(lo, 1), n - 1);
 }
 
+// The same segment on the shared grid, the search seeded by its bucket: probe down
+// while the point before is still >= xn, then up while the point is < xn.
+__device__ __forceinline__ int segment_seeded(const DevPhase32 &ph, float xn) {
+    const float *x = ph.cos_asc[0];
+    const int n = ph.n_angle[0];
+    if (!ph.seed) return segment32(x, n, xn);
+    const int b = min(max(__float2int_rd((xn - ph.seed_lo) * ph.seed_scale), 0), kPhaseBuckets - 1);
+    int k = __ldg(ph.seed + b);
+    while (k > 0 && __ldg(x + k - 1) >= xn) --k;
+    while (k < n && __ldg(x + k) < xn) ++k;
+    return min(max(k, 1), n - 1);
+}
+
 // Element e at xn in segment k of the grid the elements share.
 __device__ __forceinline__ float phase_at(const DevPhase32 &ph, int e, int row, int k, float xn) {
     const float *x = ph.cos_asc[0];
@@ -201,7 +214,7 @@ __device__ __forceinline__ bool candidate(const DevPhase32 &ph, int row, float I
     const float r3 = 1.000001f * u01_f32(r.w) * (one ? v.max1 : v.max2);
     float S11, S12;
     if (ph.shared_grid) {
-        const int k = segment32(ph.cos_asc[0], ph.n_angle[0], cos_theta);
+        const int k = segment_seeded(ph, cos_theta);
         S11 = phase_at(ph, 0, row, k, cos_theta);
         S12 = phase_at(ph, 1, row, k, cos_theta);
     } else {
@@ -253,7 +266,7 @@ __device__ __forceinline__ int pol_step_post(PolPhoton &P, const WalkArgs &a, fl
             rotate(Q, U, fmaf(2.f * cphi, cphi, -1.f), 2.f * sps * cphi);
             float Pe[6];
             if (ph.shared_grid) {
-                const int k = segment32(ph.cos_asc[0], ph.n_angle[0], ct);
+                const int k = segment_seeded(ph, ct);
 #pragma unroll
                 for (int e = 0; e < 6; ++e) Pe[e] = phase_at(ph, e, P.row, k, ct);
             } else {
