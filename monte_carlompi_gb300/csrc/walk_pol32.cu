@@ -355,7 +355,10 @@ __global__ void __launch_bounds__(kPolBlock) walk_pol32_kernel(const WalkArgs a)
     const unsigned long long t0 = global_ns();
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    PolPhoton P;
+    // lanes without a photon still source the round's shuffles (their values are
+    // never selected), so the state starts defined
+    PolPhoton P{};
+    P.ph = a.phase;
     bool have = false, exhausted = false;
     for (uint32_t it = 0;; ++it) {
         // ---- claims: lanes without a photon take the next ones, one atomic per warp
