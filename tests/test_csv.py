@@ -75,3 +75,25 @@ def test_read_back(tmp_path):
     d = csv_io.read_csv(str(p))
     assert np.array_equal(d['condition'], g['condition'])
     assert np.array_equal(d['path_length'], g['path_length'])
+
+
+def test_polarised_fp32_rows():
+    """mcw_record32p: the polarised header and ten columns, each float the shortest
+    repr that reads back to the FP32 value (like the FP32 HG records)."""
+    rng = np.random.default_rng(7)
+    rec = np.zeros(200, _abi.RECORD32P)
+    rec['condition'] = rng.integers(1, 6, 200)
+    rec['n_scat'] = rng.integers(0, 1000, 200)
+    for k in ('wvn', 'theta_n', 'phi_n', 'path_length', 'snow_depth', 'stokes_q', 'stokes_u', 'stokes_v'):
+        rec[k] = rng.standard_normal(200).astype(np.float32)
+    text = csv_io.format_csv(rec).decode()
+    lines = text.splitlines()
+    assert lines[0] == ('condition wvn[um^-1] theta_n phi_n n_scat path_length[m], snow_depth[m], '
+                        'Q_n, U_n, V_n')
+    for r, line in zip(rec, lines[1:]):
+        f = line.split()
+        assert len(f) == 10 and int(f[0]) == r['condition'] and int(f[4]) == r['n_scat']
+        for tok, k in zip(f[1:4] + f[5:], ('wvn', 'theta_n', 'phi_n', 'path_length', 'snow_depth',
+                                           'stokes_q', 'stokes_u', 'stokes_v')):
+            assert np.float32(float(tok)) == r[k]
+            assert tok == repr(float(tok))
