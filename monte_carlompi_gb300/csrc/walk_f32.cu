@@ -65,11 +65,12 @@ constexpr float kTwo33Inv = 1.16415321826934814e-10f; // 2^-33
 constexpr uint32_t kFlagReflect = 8u;                  // bottom reflection pending
 constexpr int kSmemCfgMax = 256;                       // configs staged in shared memory
 constexpr int kFinishCap = 64;                         // finish queue entries per warp
-#ifndef MCW_LONG_WALK
-#define MCW_LONG_WALK 1024
+#ifndef MCW_BLOCK_WALK
+#define MCW_BLOCK_WALK 256
 #endif
-// steps after which a walk still going once the supply is exhausted leaves for the drain queue
-constexpr int kLongWalk = MCW_LONG_WALK;
+// steps after which a photon (not on a Lambertian surface) walks in warp-wide blocks
+// of 32 steps (block_pass); a multiple of 4, so every path reaches it at a round edge
+constexpr int kBlockWalk = MCW_BLOCK_WALK;
 #ifndef MCW_STEPS_PER_ROUND
 #define MCW_STEPS_PER_ROUND 4
 #endif
@@ -124,6 +125,12 @@ struct Photon {
     float inv_ext, coalb_ice, coalb_imp, p_imp;
     float hg_a, hg_b, hg_c, hg_d, hg_e;  // 1+g^2, 1-g^2, 1-g, 2g, 1/(2g); hg_d == 0: isotropic
 };
+
+// A photon walks in block mode (block_pass) from kBlockWalk steps on, except on a
+// Lambertian surface (whose directions do not follow from the previous one).
+__device__ __forceinline__ bool in_block_mode(const Photon &P) {
+    return P.cfg >= 0 && P.i >= kBlockWalk && !(P.flags & kFlagLamSurface);
+}
 
 // A photon handed to the drain queue: kDrainSlot = 6 float4 (.w of the last: epoch).
 __device__ __forceinline__ void pack_photon(float4 *d, const Photon &P) {
@@ -491,7 +498,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
     // 1 <= n_act <= kSparseWarp; S = 2^ls
     const int ls = max(kLogStepsPerRound, 5 - (32 - __clz(n_act - 1)));
     const int S = 1 << ls;
-    const bool me = P.cfg >= 0;
+    const bool me = (act >> lane) & 1u;
     const int rank = __popc(act & lt_mask);
     if (me) {
         q.rmeta[3 * rank] = make_uint4((uint32_t)P.rid, (uint32_t)(P.rid >> 32), (uint32_t)P.i, P.flags);
@@ -528,6 +535,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
         // rounds (a lane whose photon ended keeps its final state), so one step's
         // rotation overlaps the previous step's boundary tests
         for (int k0 = 0; k0 < S; k0 += kStepsPerRound) {
+            if (in_block_mode(P)) break;                        // block mode from kBlockWalk on
             const int t0 = (rank << ls) + k0;
             float4 xs[kStepsPerRound], ys[kStepsPerRound];
 #pragma unroll
@@ -558,6 +566,167 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
     }
     __syncwarp();
     return cond;
+}
+
+// ---- block mode: the walk beyond kBlockWalk steps (block_pass)
+//
+// Photons this long are deep in a weakly absorbing slab and still have hundreds
+// to millions of steps to go; walked one step at a time they set the end of a
+// launch.  A block pass advances one photon by up to 32 steps with the whole
+// warp: lane k draws step k's angles, optical path and absorption word (the
+// same Philox blocks as the step-by-step walk), builds the local rotation
+// R_k = Rz(phi_k) Ry(theta_k) (as a unit quaternion) and the warp composes
+// P_k = R_1 ... R_k with an inclusive shuffle scan (products of rotations are
+// associative), so step k's direction is O_0 P_k e_z for the photon's frame O_0; positions and path
+// lengths are shuffle-scan sums; the first boundary crossing or absorption
+// (ballot) ends the pass there, as the step-by-step walk would.  The direction
+// is carried in a moving frame (O_0 built from the direction by the branchless
+// orthonormal basis of Duff et al. 2017) instead of the z-referenced formula:
+// with a uniform azimuth both give the same distribution of walks.  A photon
+// enters block mode at exactly kBlockWalk steps on every path (the dense and
+// sparse rounds and the drain walk stop there), so records stay independent of
+// the launch shape.
+
+__device__ __forceinline__ Photon shfl_photon(const Photon &P, int src) {
+    Photon Q;
+    Q.rid = __shfl_sync(0xffffffffu, P.rid, src);
+    Q.cfg = __shfl_sync(0xffffffffu, P.cfg, src);
+    Q.lut = __shfl_sync(0xffffffffu, P.lut, src);
+    Q.i = __shfl_sync(0xffffffffu, P.i, src);
+    Q.flags = __shfl_sync(0xffffffffu, P.flags, src);
+    Q.mux = __shfl_sync(0xffffffffu, P.mux, src);
+    Q.muy = __shfl_sync(0xffffffffu, P.muy, src);
+    Q.muz = __shfl_sync(0xffffffffu, P.muz, src);
+    Q.z = __shfl_sync(0xffffffffu, P.z, src);
+    Q.path = __shfl_sync(0xffffffffu, P.path, src);
+    Q.pathc = __shfl_sync(0xffffffffu, P.pathc, src);
+    Q.tau = __shfl_sync(0xffffffffu, P.tau, src);
+    Q.R = __shfl_sync(0xffffffffu, P.R, src);
+    Q.inv_ext = __shfl_sync(0xffffffffu, P.inv_ext, src);
+    Q.coalb_ice = __shfl_sync(0xffffffffu, P.coalb_ice, src);
+    Q.coalb_imp = __shfl_sync(0xffffffffu, P.coalb_imp, src);
+    Q.p_imp = __shfl_sync(0xffffffffu, P.p_imp, src);
+    Q.hg_a = __shfl_sync(0xffffffffu, P.hg_a, src);
+    Q.hg_b = __shfl_sync(0xffffffffu, P.hg_b, src);
+    Q.hg_c = __shfl_sync(0xffffffffu, P.hg_c, src);
+    Q.hg_d = __shfl_sync(0xffffffffu, P.hg_d, src);
+    Q.hg_e = __shfl_sync(0xffffffffu, P.hg_e, src);
+    return Q;
+}
+
+// Hamilton product a b of quaternions stored as (.x, .y, .z, .w) = (w, x, y, z),
+// every operation rounded as written (the pass is inlined in two kernels and
+// must give the same bits in both).
+__device__ __forceinline__ float4 qmul(const float4 a, const float4 b) {
+    return make_float4(
+        fmaf(-a.y, b.y, fmaf(-a.z, b.z, fmaf(-a.w, b.w, __fmul_rn(a.x, b.x)))),   // w
+        fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.z, b.w, -__fmul_rn(a.w, b.z)))),     // x
+        fmaf(a.x, b.z, fmaf(-a.y, b.w, fmaf(a.z, b.x, __fmul_rn(a.w, b.y)))),     // y
+        fmaf(a.x, b.w, fmaf(a.y, b.z, fmaf(-a.z, b.y, __fmul_rn(a.w, b.x)))));    // z
+}
+
+// One block pass over photon Q, held alike by every lane of the warp: steps
+// Q.i + 1 .. Q.i + 32, ended early by the first top or bottom crossing or
+// absorption.  Lane k's rotation Rz(phi) Ry(theta) is the unit quaternion
+// (c_p c_t, -s_p s_t, c_p s_t, s_p c_t) of the half angles; an inclusive
+// shuffle scan of Hamilton products gives the composed rotations.  Q is updated
+// alike on every lane; returns the end condition (0: still walking, or
+// reflected at the bottom).  Warp-collective.
+__device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
+    const uint32_t n = (uint32_t)Q.i + 1u + (uint32_t)lane;
+    const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
+    const float4 uu = step_uniforms(r);
+    const float dtau = -__logf(uu.z);                                   // :1014
+    const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
+    // after a bottom reflection the pass starts in the lab frame and its first step
+    // takes the Lambertian direction about the vertical (:1238-1250)
+    const bool reflected = (Q.flags & kFlagReflect) != 0;
+    const bool lamb = reflected && lane == 0;
+    const float ct = lamb ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
+    const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));      // cos(theta / 2)
+    const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));      // sin(theta / 2)
+    float sph, cph;                                                     // half the azimuth, uniform
+    __sincosf(__fmul_rn(3.14159265358979324f, __fsub_rn(uu.y, 0.5f)), &sph, &cph);
+    float4 q = make_float4(__fmul_rn(cph, ch), -__fmul_rn(sph, sh), __fmul_rn(cph, sh), __fmul_rn(sph, ch));
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        float4 l;
+        l.x = __shfl_up_sync(0xffffffffu, q.x, off);
+        l.y = __shfl_up_sync(0xffffffffu, q.y, off);
+        l.z = __shfl_up_sync(0xffffffffu, q.z, off);
+        l.w = __shfl_up_sync(0xffffffffu, q.w, off);
+        if (lane >= off) q = qmul(l, q);                                // earlier steps on the left
+    }
+    // q = (w, x, y, z) of R_1 ... R_k; its third column is the direction in the frame
+    const float c0 = __fmul_rn(2.f, fmaf(q.y, q.w, __fmul_rn(q.x, q.z)));
+    const float c1 = __fmul_rn(2.f, fmaf(q.z, q.w, -__fmul_rn(q.x, q.y)));
+    const float c2 = fmaf(-2.f, fmaf(q.y, q.y, __fmul_rn(q.z, q.z)), 1.f);
+    // the frame O_0 = (e1, e2, d0) of the pass
+    float e1x = 1.f, e1y = 0.f, e1z = 0.f, e2x = 0.f, e2y = 1.f, e2z = 0.f, d0x = 0.f, d0y = 0.f, d0z = 1.f;
+    if (!reflected) {
+        const float inv = rsqrtf(fmaf(Q.mux, Q.mux, fmaf(Q.muy, Q.muy, __fmul_rn(Q.muz, Q.muz))));
+        d0x = __fmul_rn(Q.mux, inv); d0y = __fmul_rn(Q.muy, inv); d0z = __fmul_rn(Q.muz, inv);
+        const float sg = copysignf(1.f, d0z);
+        const float aa = -1.f / __fadd_rn(sg, d0z);
+        const float bb = __fmul_rn(__fmul_rn(d0x, d0y), aa);
+        e1x = fmaf(__fmul_rn(sg, d0x), __fmul_rn(d0x, aa), 1.f); e1y = __fmul_rn(sg, bb); e1z = -__fmul_rn(sg, d0x);
+        e2x = bb; e2y = fmaf(d0y, __fmul_rn(d0y, aa), sg); e2z = -d0y;
+    }
+    const float dx = fmaf(e1x, c0, fmaf(e2x, c1, __fmul_rn(d0x, c2)));
+    const float dy = fmaf(e1y, c0, fmaf(e2y, c1, __fmul_rn(d0y, c2)));
+    const float dz = fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2)));
+    // positions and path lengths: inclusive scan sums
+    float zs = __fmul_rn(dtau, dz);
+    const float inc = __fmul_rn(dtau, Q.inv_ext);
+    float ps = inc;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float zu = __shfl_up_sync(0xffffffffu, zs, off);
+        const float pu = __shfl_up_sync(0xffffffffu, ps, off);
+        if (lane >= off) { zs = __fadd_rn(zs, zu); ps = __fadd_rn(ps, pu); }
+    }
+    const float zprev_s = __shfl_up_sync(0xffffffffu, zs, 1);
+    const float zk = __fadd_rn(Q.z, zs);
+    const float zprev = lane == 0 ? Q.z : __fadd_rn(Q.z, zprev_s);
+    // the first event: a crossing, else absorption (1 - u < 1 - ssa, :1461-1466)
+    const bool top = zk > 0.f;
+    const bool bot = zk < -Q.tau;
+    const bool absb = !top && !bot && uu.w < (imp ? Q.coalb_imp : Q.coalb_ice);
+    const unsigned ev = __ballot_sync(0xffffffffu, top || bot || absb);
+    const int e = ev ? __ffs(ev) - 1 : 31;
+    // the photon's state after step e, taken from lane e
+    const float nx = __shfl_sync(0xffffffffu, dx, e), ny = __shfl_sync(0xffffffffu, dy, e);
+    const float nz = __shfl_sync(0xffffffffu, dz, e);
+    const float ze = __shfl_sync(0xffffffffu, zk, e), zp = __shfl_sync(0xffffffffu, zprev, e);
+    const float pe = __shfl_sync(0xffffffffu, ps, e), ince = __shfl_sync(0xffffffffu, inc, e);
+    const unsigned what = __shfl_sync(0xffffffffu, (top ? 1u : 0u) | (bot ? 2u : 0u) | (imp ? 4u : 0u) |
+                                                     ((uu.w < Q.R) ? 8u : 0u), e);
+    Q.i += e + 1;
+    {   // compensated path sum
+        const float y = __fsub_rn(pe, Q.pathc);
+        const float tt = __fadd_rn(Q.path, y);
+        Q.pathc = __fsub_rn(__fsub_rn(tt, Q.path), y);
+        Q.path = tt;
+    }
+    const float inv = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, __fmul_rn(nz, nz))));
+    Q.mux = __fmul_rn(nx, inv); Q.muy = __fmul_rn(ny, inv); Q.muz = __fmul_rn(nz, inv);
+    Q.flags &= ~kFlagReflect;
+    Q.z = ze;
+    if (!ev) return 0;
+    if (what & 1u) {                                                    // :1390-1397
+        Q.path = fmaf(-__fdividef(ze, __fsub_rn(ze, zp)), ince, Q.path);
+        return 1;
+    }
+    if (what & 2u) {                                                    // :1399-1459
+        Q.path = fmaf(-__fdividef(__fadd_rn(ze, Q.tau), __fsub_rn(ze, zp)), ince, Q.path);
+        Q.z = -Q.tau;
+        if ((Q.flags & kFlagLamBottom) && (what & 8u)) {
+            Q.flags |= kFlagReflect;
+            return 0;
+        }
+        return 2;
+    }
+    return (what & 4u) ? 5 : 4;
 }
 
 // Exact warp sum of 64-bit values below 2^47.
@@ -711,11 +880,10 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
         if (idle == 0xffffffffu && exhausted && n_birth == 0) break;
 
         // ---- drain handover, once the supply is exhausted: the photons of a nearly
-        // empty warp, and any photon already kLongWalk steps long (likely to walk much
-        // longer), go to the queue to be walked with a whole warp each
+        // empty warp go to the queue to be walked with a whole warp each
         if (a.drain_below > 0 && exhausted && n_birth == 0) {
             const bool whole = __popc(~idle) <= a.drain_below;
-            const bool leave = P.cfg >= 0 && (whole || P.i >= kLongWalk);
+            const bool leave = P.cfg >= 0 && whole;
             const unsigned lm = __ballot_sync(0xffffffffu, leave);
             if (lm) {
                 unsigned base = 0;
@@ -740,8 +908,9 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
         // ---- kStepsPerRound scatter events per active lane of a well-filled warp;
         // their Philox blocks are independent of the walk, so they are computed
         // together first.  A sparse warp runs sparse_round instead.
-        const unsigned act = ~idle;
-        const bool me_active = P.cfg >= 0;
+        const unsigned bmask = __ballot_sync(0xffffffffu, in_block_mode(P));
+        const unsigned act = ~idle & ~bmask;
+        const bool me_active = (act >> lane) & 1u;
         const int n_act = __popc(act);
         int cond = 0;
         if (n_act <= kSparseWarp) {
@@ -769,6 +938,23 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
                 P.z = Q.z;
                 P.pathc = Q.pathc;
                 cond = alive ? c : cond;
+            }
+        }
+
+        // ---- photons past kBlockWalk steps: one block pass (up to 32 steps) each,
+        // walked by the whole warp
+        for (unsigned pend = bmask; pend; pend &= pend - 1) {
+            const int src = __ffs(pend) - 1;
+            Photon Q = shfl_photon(P, src);
+            const int c = block_pass(Q, a, lane);
+            if (lane == src) {
+                P.i = Q.i;
+                P.flags = Q.flags;
+                P.mux = Q.mux; P.muy = Q.muy; P.muz = Q.muz;
+                P.z = Q.z;
+                P.path = Q.path;
+                P.pathc = Q.pathc;
+                cond = c;
             }
         }
 
@@ -844,6 +1030,10 @@ __device__ __forceinline__ bool drain_walk(const float4 *slot, FinishSlot *fin, 
     unpack_photon(P, v);
     int cond = 0;
     while (cond == 0) {
+        if (in_block_mode(P)) {
+            cond = block_pass(P, a, lane);
+            continue;
+        }
         // direction-independent part of steps P.i + 1 .. P.i + 32, one per lane
         const uint32_t n = (uint32_t)P.i + 1u + (uint32_t)lane;
         const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)P.rid, (uint32_t)(P.rid >> 32)), a.keys);
@@ -858,6 +1048,7 @@ __device__ __forceinline__ bool drain_walk(const float4 *slot, FinishSlot *fin, 
         // so every fourth step renormalises, as in the main loop
 #pragma unroll
         for (int k = 0; k < 32; ++k) {
+            if ((k & 3) == 0 && in_block_mode(P)) break;               // block mode from kBlockWalk on
             const float4 x = pbuf[2 * k], y = pbuf[2 * k + 1];
             StepPre s;
             s.ct_hg = x.x, s.st_hg = x.y, s.ct_l = x.z, s.st_l = x.w;

@@ -353,6 +353,32 @@ def test_f32_long_walks_same_records_with_and_without_drain(walker):
     assert np.array_equal(a.records, b.records) and np.array_equal(a.tallies, b.tallies)
 
 
+def test_f32_block_mode_statistics_match_oracle(walker):
+    """Deep, weakly absorbing snow (lambda 1.0 um, r_eff 50 um, tau ~980): nearly every
+    photon in four walks thousands of steps, all past the first 256 in warp-wide block passes.
+    Condition fractions, exit histogram, mean n_scat and mean path length agree with
+    the oracle's step-by-step FP64 walk of the reference algorithm."""
+    lo, hi = ssp.grid_for(1.0, 0.085)
+    ice = ssp.synthetic_ice_table(50.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = 0.1 * ssp.ext_cff_mss_sphere(50.0) * 300.0
+    cfg = WalkConfig(n_photon=20000, wvl0=1.0, half_width=0.085, theta0_deg=30.0, tau_tot=tau,
+                     lambertian_reflectance=0.5)
+    walker.set_tables([ice], imp)
+    rec = walker.walk([cfg], 13, mode='f32').records
+    ref = oracle_run(cfg, ice, imp, 31)
+    assert np.mean(rec["n_scat"] > 256) > 0.2
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    top_g, top_r = rec['condition'] == 1, ref['condition'] == 1
+    x2, dof, p = chi2_two_sample(exit_histogram(rec['theta_n'][top_g], rec['phi_n'][top_g]),
+                                 exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r]))
+    assert p > 1e-4, (x2, dof, p)
+    for a, b in ((rec['n_scat'].astype(np.float64), ref['n_scat'].astype(np.float64)),
+                 (rec['path_length'].astype(np.float64), ref['path_length'])):
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se, (a.mean(), b.mean(), se)
+
+
 def test_records_into_pinned_host_memory(walker):
     """Pinned host buffers are written by the walk directly (no copy after the kernel);
     their records equal those copied into pageable memory, in both modes."""
