@@ -69,7 +69,7 @@ constexpr int kFinishCap = 64;                         // finish queue entries p
 #define MCW_BLOCK_WALK 256
 #endif
 // steps after which a photon (not on a Lambertian surface) walks in warp-wide blocks
-// of 32 steps (block_pass); a multiple of 4, so every path reaches it at a round edge
+// of kBlockSteps steps (block_pass); a multiple of 4, so every path reaches it at a round edge
 constexpr int kBlockWalk = MCW_BLOCK_WALK;
 #ifndef MCW_STEPS_PER_ROUND
 #define MCW_STEPS_PER_ROUND 4
@@ -572,9 +572,9 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
 //
 // Photons this long are deep in a weakly absorbing slab and still have hundreds
 // to millions of steps to go; walked one step at a time they set the end of a
-// launch.  A block pass advances one photon by up to 32 steps with the whole
-// warp: lane k draws step k's angles, optical path and absorption word (the
-// same Philox blocks as the step-by-step walk), builds the local rotation
+// launch.  A block pass advances one photon by up to kBlockSteps steps with the
+// whole warp: lane k draws its steps' angles, optical path and absorption words
+// (the same Philox blocks as the step-by-step walk), builds the local rotation
 // R_k = Rz(phi_k) Ry(theta_k) (as a unit quaternion) and the warp composes
 // P_k = R_1 ... R_k with an inclusive shuffle scan (products of rotations are
 // associative), so step k's direction is O_0 P_k e_z for the photon's frame O_0; positions and path
@@ -625,29 +625,54 @@ __device__ __forceinline__ float4 qmul(const float4 a, const float4 b) {
         fmaf(a.x, b.w, fmaf(a.y, b.z, fmaf(-a.z, b.y, __fmul_rn(a.w, b.x)))));    // z
 }
 
+#ifndef MCW_BLOCK_LANE_STEPS
+#define MCW_BLOCK_LANE_STEPS 2
+#endif
+// steps per lane in a block pass: a pass covers 32 * kLaneSteps steps
+constexpr int kLaneSteps = MCW_BLOCK_LANE_STEPS;
+constexpr int kBlockSteps = 32 * kLaneSteps;
+
 // One block pass over photon Q, held alike by every lane of the warp: steps
-// Q.i + 1 .. Q.i + 32, ended early by the first top or bottom crossing or
-// absorption.  Lane k's rotation Rz(phi) Ry(theta) is the unit quaternion
-// (c_p c_t, -s_p s_t, c_p s_t, s_p c_t) of the half angles; an inclusive
-// shuffle scan of Hamilton products gives the composed rotations.  Q is updated
-// alike on every lane; returns the end condition (0: still walking, or
+// Q.i + 1 .. Q.i + kBlockSteps, lane l taking steps kLaneSteps l .. + kLaneSteps - 1,
+// ended early by the first top or bottom crossing or absorption.  Each step's
+// rotation Rz(phi) Ry(theta) is the unit quaternion (c_p c_t, -s_p s_t, c_p s_t,
+// s_p c_t) of the half angles; a lane multiplies its own, an inclusive shuffle
+// scan of the lane products (Hamilton products) composes them across lanes, and
+// the lane's exclusive prefix times its local products gives every step's
+// composed rotation.  Positions and path lengths are scanned the same way.  Q is
+// updated alike on every lane; returns the end condition (0: still walking, or
 // reflected at the bottom).  Warp-collective.
 __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
-    const uint32_t n = (uint32_t)Q.i + 1u + (uint32_t)lane;
-    const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
-    const float4 uu = step_uniforms(r);
-    const float dtau = -__logf(uu.z);                                   // :1014
-    const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
-    // after a bottom reflection the pass starts in the lab frame and its first step
-    // takes the Lambertian direction about the vertical (:1238-1250)
     const bool reflected = (Q.flags & kFlagReflect) != 0;
-    const bool lamb = reflected && lane == 0;
-    const float ct = lamb ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
-    const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));      // cos(theta / 2)
-    const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));      // sin(theta / 2)
-    float sph, cph;                                                     // half the azimuth, uniform
-    __sincosf(__fmul_rn(3.14159265358979324f, __fsub_rn(uu.y, 0.5f)), &sph, &cph);
-    float4 q = make_float4(__fmul_rn(cph, ch), -__fmul_rn(sph, sh), __fmul_rn(cph, sh), __fmul_rn(sph, ch));
+    float4 qs[kLaneSteps];                   // the steps' rotations, then their prefixes
+    float dtau[kLaneSteps];
+    unsigned absm = 0, reflm = 0, impm = 0;  // per step: absorbed, reflectance draw, species
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        const uint32_t n = (uint32_t)Q.i + 1u + (uint32_t)(kLaneSteps * lane + t);
+        const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
+        const float4 uu = step_uniforms(r);
+        dtau[t] = -__logf(uu.z);                                        // :1014
+        const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
+        // absorption as 1 - u < 1 - ssa (:1461-1466); on a bottom crossing the same
+        // word is the reflectance draw
+        absm |= (uu.w < (imp ? Q.coalb_imp : Q.coalb_ice) ? 1u : 0u) << t;
+        reflm |= (uu.w < Q.R ? 1u : 0u) << t;
+        impm |= (imp ? 1u : 0u) << t;
+        // after a bottom reflection the pass starts in the lab frame and its first
+        // step takes the Lambertian direction about the vertical (:1238-1250)
+        const bool lamb = reflected && lane == 0 && t == 0;
+        const float ct = lamb ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
+        const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));  // cos(theta / 2)
+        const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));  // sin(theta / 2)
+        float sph, cph;                                                 // half the azimuth, uniform
+        __sincosf(__fmul_rn(3.14159265358979324f, __fsub_rn(uu.y, 0.5f)), &sph, &cph);
+        qs[t] = make_float4(__fmul_rn(cph, ch), -__fmul_rn(sph, sh), __fmul_rn(cph, sh), __fmul_rn(sph, ch));
+    }
+    // the lane's product, scanned across the lanes; then each step's prefix
+    float4 q = qs[0];
+#pragma unroll
+    for (int t = 1; t < kLaneSteps; ++t) q = qmul(q, qs[t]);
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
         float4 l;
@@ -657,10 +682,19 @@ __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane
         l.w = __shfl_up_sync(0xffffffffu, q.w, off);
         if (lane >= off) q = qmul(l, q);                                // earlier steps on the left
     }
-    // q = (w, x, y, z) of R_1 ... R_k; its third column is the direction in the frame
-    const float c0 = __fmul_rn(2.f, fmaf(q.y, q.w, __fmul_rn(q.x, q.z)));
-    const float c1 = __fmul_rn(2.f, fmaf(q.z, q.w, -__fmul_rn(q.x, q.y)));
-    const float c2 = fmaf(-2.f, fmaf(q.y, q.y, __fmul_rn(q.z, q.z)), 1.f);
+    {
+        float4 x;                                                       // exclusive prefix
+        x.x = __shfl_up_sync(0xffffffffu, q.x, 1);
+        x.y = __shfl_up_sync(0xffffffffu, q.y, 1);
+        x.z = __shfl_up_sync(0xffffffffu, q.z, 1);
+        x.w = __shfl_up_sync(0xffffffffu, q.w, 1);
+        if (lane == 0) x = make_float4(1.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < kLaneSteps; ++t) {
+            x = qmul(x, qs[t]);
+            qs[t] = x;
+        }
+    }
     // the frame O_0 = (e1, e2, d0) of the pass
     float e1x = 1.f, e1y = 0.f, e1z = 0.f, e2x = 0.f, e2y = 1.f, e2z = 0.f, d0x = 0.f, d0y = 0.f, d0z = 1.f;
     if (!reflected) {
@@ -672,36 +706,84 @@ __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane
         e1x = fmaf(__fmul_rn(sg, d0x), __fmul_rn(d0x, aa), 1.f); e1y = __fmul_rn(sg, bb); e1z = -__fmul_rn(sg, d0x);
         e2x = bb; e2y = fmaf(d0y, __fmul_rn(d0y, aa), sg); e2z = -d0y;
     }
-    const float dx = fmaf(e1x, c0, fmaf(e2x, c1, __fmul_rn(d0x, c2)));
-    const float dy = fmaf(e1y, c0, fmaf(e2y, c1, __fmul_rn(d0y, c2)));
-    const float dz = fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2)));
-    // positions and path lengths: inclusive scan sums
-    float zs = __fmul_rn(dtau, dz);
-    const float inc = __fmul_rn(dtau, Q.inv_ext);
-    float ps = inc;
+    // each step's vertical move (O_0 times the third column of its composed
+    // rotation, z row), and the lane's sums of the position and path increments
+    float dz[kLaneSteps];
+    float zs = 0.f, ps = 0.f;
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        const float4 p = qs[t];
+        const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
+        const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
+        const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
+        dz[t] = __fmul_rn(dtau[t], fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2))));
+        zs = t == 0 ? dz[t] : __fadd_rn(zs, dz[t]);
+        const float inc = __fmul_rn(dtau[t], Q.inv_ext);
+        ps = t == 0 ? inc : __fadd_rn(ps, inc);
+    }
+    // scan of the lane sums; the lane's exclusive prefix
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
         const float zu = __shfl_up_sync(0xffffffffu, zs, off);
         const float pu = __shfl_up_sync(0xffffffffu, ps, off);
         if (lane >= off) { zs = __fadd_rn(zs, zu); ps = __fadd_rn(ps, pu); }
     }
-    const float zprev_s = __shfl_up_sync(0xffffffffu, zs, 1);
-    const float zk = __fadd_rn(Q.z, zs);
-    const float zprev = lane == 0 ? Q.z : __fadd_rn(Q.z, zprev_s);
-    // the first event: a crossing, else absorption (1 - u < 1 - ssa, :1461-1466)
-    const bool top = zk > 0.f;
-    const bool bot = zk < -Q.tau;
-    const bool absb = !top && !bot && uu.w < (imp ? Q.coalb_imp : Q.coalb_ice);
-    const unsigned ev = __ballot_sync(0xffffffffu, top || bot || absb);
+    float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
+    if (lane == 0) { zx = 0.f; px = 0.f; }
+    // the lane's first event (a crossing, else absorption), or its last step; the
+    // local sums repeat the additions above exactly
+    int first = kLaneSteps, ts = kLaneSteps - 1;
+    unsigned what_l = 0;
+    float zk_l = 0.f, zp_l = 0.f, pk_l = 0.f;
+    {
+        float zl = 0.f, pl = 0.f;
+#pragma unroll
+        for (int t = 0; t < kLaneSteps; ++t) {
+            const float zp = t == 0 ? __fadd_rn(Q.z, zx) : __fadd_rn(Q.z, __fadd_rn(zx, zl));
+            const float inc = __fmul_rn(dtau[t], Q.inv_ext);
+            zl = t == 0 ? dz[t] : __fadd_rn(zl, dz[t]);
+            pl = t == 0 ? inc : __fadd_rn(pl, inc);
+            const float zk = __fadd_rn(Q.z, __fadd_rn(zx, zl));
+            const bool top = zk > 0.f;
+            const bool bot = zk < -Q.tau;
+            const bool absb = !top && !bot && ((absm >> t) & 1u);
+            const bool event = top || bot || absb;
+            if (first == kLaneSteps && (event || t == kLaneSteps - 1)) {
+                if (event) first = t;
+                ts = t;
+                what_l = (top ? 1u : 0u) | (bot ? 2u : 0u) | (((impm >> t) & 1u) << 2) | (((reflm >> t) & 1u) << 3);
+                zk_l = zk;
+                zp_l = zp;
+                pk_l = __fadd_rn(px, pl);
+            }
+        }
+    }
+    // the direction after step ts
+    float ex, ey, ez, ei;
+    {
+        float4 p = qs[0];
+        float dt = dtau[0];
+#pragma unroll
+        for (int t = 1; t < kLaneSteps; ++t)
+            if (t == ts) { p = qs[t]; dt = dtau[t]; }
+        const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
+        const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
+        const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
+        ex = fmaf(e1x, c0, fmaf(e2x, c1, __fmul_rn(d0x, c2)));
+        ey = fmaf(e1y, c0, fmaf(e2y, c1, __fmul_rn(d0y, c2)));
+        ez = fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2)));
+        ei = __fmul_rn(dt, Q.inv_ext);
+    }
+    const unsigned ev = __ballot_sync(0xffffffffu, first < kLaneSteps);
     const int e = ev ? __ffs(ev) - 1 : 31;
-    // the photon's state after step e, taken from lane e
-    const float nx = __shfl_sync(0xffffffffu, dx, e), ny = __shfl_sync(0xffffffffu, dy, e);
-    const float nz = __shfl_sync(0xffffffffu, dz, e);
-    const float ze = __shfl_sync(0xffffffffu, zk, e), zp = __shfl_sync(0xffffffffu, zprev, e);
-    const float pe = __shfl_sync(0xffffffffu, ps, e), ince = __shfl_sync(0xffffffffu, inc, e);
-    const unsigned what = __shfl_sync(0xffffffffu, (top ? 1u : 0u) | (bot ? 2u : 0u) | (imp ? 4u : 0u) |
-                                                     ((uu.w < Q.R) ? 8u : 0u), e);
-    Q.i += e + 1;
+    // the photon's state after the event step, taken from lane e
+    const int te = __shfl_sync(0xffffffffu, first, e);
+    const float nx = __shfl_sync(0xffffffffu, ex, e), ny = __shfl_sync(0xffffffffu, ey, e);
+    const float nz = __shfl_sync(0xffffffffu, ez, e);
+    const float ze = __shfl_sync(0xffffffffu, zk_l, e), zp = __shfl_sync(0xffffffffu, zp_l, e);
+    const float pe = __shfl_sync(0xffffffffu, pk_l, e), ince = __shfl_sync(0xffffffffu, ei, e);
+    const unsigned what = __shfl_sync(0xffffffffu, what_l, e);
+    Q.i += kLaneSteps * e + (ev ? te : kLaneSteps - 1) + 1;
     {   // compensated path sum
         const float y = __fsub_rn(pe, Q.pathc);
         const float tt = __fadd_rn(Q.path, y);
@@ -811,7 +893,7 @@ __device__ __noinline__ void drain_serve(FinishSlot *fin, WarpTally &tally, floa
                                          const WalkArgs &a, unsigned long long t0, int lane);
 
 template <bool kImpurity>
-__global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
+__global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -941,7 +1023,7 @@ __global__ void __launch_bounds__(256, 1) walk_f32_kernel(const WalkArgs a) {
             }
         }
 
-        // ---- photons past kBlockWalk steps: one block pass (up to 32 steps) each,
+        // ---- photons past kBlockWalk steps: one block pass (up to kBlockSteps steps) each,
         // walked by the whole warp
         for (unsigned pend = bmask; pend; pend &= pend - 1) {
             const int src = __ffs(pend) - 1;
