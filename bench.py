@@ -515,7 +515,7 @@ def run_ours(args):
     tuned = w.autotune([cfg], seed=11)
     tuned.pop('ms')
     w.set_launch(**tuned)
-    kernels_per_walk = 3 if tuned['drain_below'] > 0 else 2   # lookup table, walk, drain
+    kernels_per_walk = 3 if tuned['drain_from'] > 0 else 2   # lookup table, walk, drain
     dev_records = torch.empty(n * RECORD_BYTES, dtype=torch.uint8, device='cuda')
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device='cuda')
 

@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-#define MCW_ABI_VERSION 2
+#define MCW_ABI_VERSION 3
 
 /* status codes */
 #define MCW_OK 0
@@ -222,12 +222,13 @@ typedef struct {
 
 /* Launch shape of the FP32 walk (persistent grid). */
 typedef struct {
-    int32_t block_size;    /* threads per block, multiple of 32, 32..1024 */
+    int32_t block_size;    /* threads per block, multiple of 32, 32..256 */
     int32_t blocks_per_sm; /* resident blocks per SM to launch (0 = occupancy maximum) */
     int32_t regen_chunk;   /* refill a warp once this many lanes are idle (1..32) */
-    int32_t drain_below;   /* once every photon has started, a warp with at most this many
-                              walking photons hands them to a queue served by whole warps,
-                              one photon each (0..32; 0 = never, the default) */
+    int32_t drain_from;    /* once every photon has started, a photon past this many steps
+                              leaves the walk for a queue walked after it by a whole thread
+                              block per photon (0 = never; else 256..2^30; default 4096).
+                              Records do not depend on it. */
 } mcw_launch;
 
 /* Library identity.  No reference counterpart. */
@@ -281,7 +282,9 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
 int mcw_brf(const mcw_tally *tallies, int32_t n_cfg, double *brf, double *albedo);
 
 /* Time launch shapes on (a sample of) these configs and keep the fastest in
- * the context.  No reference counterpart (the reference has no tuning). */
+ * the context: block size, resident blocks and refill chunk first, then
+ * drain_from (0, 512, 1024, 4096) for that shape.  No reference counterpart
+ * (the reference has no tuning). */
 int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
                  mcw_launch *best, double *best_ms);
 

@@ -85,7 +85,7 @@ class StatsC(ctypes.Structure):
 
 class LaunchC(ctypes.Structure):
     _fields_ = [('block_size', ctypes.c_int32), ('blocks_per_sm', ctypes.c_int32),
-                ('regen_chunk', ctypes.c_int32), ('drain_below', ctypes.c_int32)]
+                ('regen_chunk', ctypes.c_int32), ('drain_from', ctypes.c_int32)]
 
 
 class GemmC(ctypes.Structure):

@@ -80,10 +80,9 @@ struct Plan {
 struct Counters {
     unsigned long long work;
     unsigned int status;
-    unsigned int drain_count;   // drain-queue slots reserved
-    unsigned int drain_next;    // next drain ticket
-    unsigned int warps_done;    // walk warps past their photon loop
-    unsigned int pad[3];
+    unsigned int drain_count;   // drain-queue slots written
+    unsigned int drain_next;    // the drain kernel's next slot
+    unsigned int pad[4];
 };
 
 }  // namespace
@@ -107,9 +106,8 @@ struct mcw_ctx {
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
     HostBuf h_stage, h_tallies, h_counters;
     int32_t max_ice_n = 0;
-    mcw_launch launch{256, 0, 8, 0};
+    mcw_launch launch{256, 0, 8, 4096};
     double budget_s = 300.0;
-    uint32_t epoch = 0;   // drain-queue epoch of the last launch
 };
 
 struct mcw_graph {
@@ -340,29 +338,18 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &l
     wa.keys = philox_schedule(seed);
     wa.drain_count = &cn->drain_count;
     wa.drain_next = &cn->drain_next;
-    wa.warps_done = &cn->warps_done;
     return wa;
-}
-
-// A fresh epoch for the drain queue of one launch (never 0, the mark of a taken slot).
-uint32_t next_epoch(mcw_ctx *ctx) {
-    if (++ctx->epoch == 0) ++ctx->epoch;
-    return ctx->epoch;
 }
 
 // Attach the drain queue (one slot per thread of the walk grid) when handover is on.
 int attach_drain(mcw_ctx *ctx, WalkArgs &wa, DevBuf &drain, const Shape &shape) {
     wa.drain = nullptr;
-    wa.drain_below = 0;
-    if (ctx->launch.drain_below <= 0) return MCW_OK;
-    void *old = drain.p;
+    wa.drain_from = 0;
+    if (ctx->launch.drain_from <= 0) return MCW_OK;
     CUDA_TRY(ctx, drain.ensure((size_t)shape.grid * shape.block * kDrainSlot * sizeof(float4)));
-    // slots are recognised by their epoch word: a new buffer starts cleared
-    if (drain.p != old) CUDA_TRY(ctx, cudaMemsetAsync(drain.p, 0, drain.cap, ctx->stream));
     wa.drain = (float4 *)drain.p;
     wa.drain_cap = (uint32_t)((size_t)shape.grid * shape.block);
-    wa.drain_below = ctx->launch.drain_below;
-    wa.epoch = next_epoch(ctx);
+    wa.drain_from = ctx->launch.drain_from;
     return MCW_OK;
 }
 
@@ -649,7 +636,8 @@ int mcw_set_launch(mcw_ctx *ctx, const mcw_launch *l) {
         return set_err(ctx, MCW_ERR_ARG, "block_size must be a multiple of 32 in [32, 256]");
     if (l->blocks_per_sm < 0 || l->blocks_per_sm > 64) return set_err(ctx, MCW_ERR_ARG, "blocks_per_sm must be in [0, 64]");
     if (l->regen_chunk < 1 || l->regen_chunk > 32) return set_err(ctx, MCW_ERR_ARG, "regen_chunk must be in [1, 32]");
-    if (l->drain_below < 0 || l->drain_below > 32) return set_err(ctx, MCW_ERR_ARG, "drain_below must be in [0, 32]");
+    if (l->drain_from != 0 && (l->drain_from < 256 || l->drain_from > (1 << 30)))
+        return set_err(ctx, MCW_ERR_ARG, "drain_from must be 0 (off) or in [256, 2^30]");
     ctx->launch = *l;
     return MCW_OK;
 }
@@ -877,7 +865,7 @@ int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t s
         for (int bi = 0; bi < 2; ++bi) {
             if (bi == 1 && bps_opts[1] == bps_opts[0]) continue;
             for (int ch : chunks) {
-                mcw_launch l{b, bps_opts[bi], ch, saved.drain_below};
+                mcw_launch l{b, bps_opts[bi], ch, saved.drain_from};
                 ctx->launch = l;
                 mcw_stats s;
                 double t = 0;
@@ -894,6 +882,29 @@ int mcw_autotune(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t s
                     win = l;
                 }
             }
+        }
+    }
+    // then the drain handover for the winning shape
+    const int32_t drains[] = {0, 512, 1024, 4096};
+    const mcw_launch shape = win;
+    for (int32_t d : drains) {
+        if (d == shape.drain_from) continue;
+        mcw_launch l = shape;
+        l.drain_from = d;
+        ctx->launch = l;
+        mcw_stats s;
+        double t = 0;
+        for (int rep = 0; rep < 2; ++rep) {
+            int rc = mcw_walk(ctx, cfgs, n_cfg, seed + rep, MCW_MODE_F32, nullptr, MCW_RECORDS_NONE, nullptr, &s);
+            if (rc) {
+                ctx->launch = saved;
+                return rc;
+            }
+            if (rep) t = s.kernel_ms;
+        }
+        if (t < win_ms) {
+            win_ms = t;
+            win = l;
         }
     }
     ctx->launch = win;
@@ -975,7 +986,6 @@ int mcw_graph_launch(mcw_graph *g, uint64_t seed, mcw_tally *tallies, mcw_stats 
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     g->args.keys = philox_schedule(seed);
-    if (g->args.drain) g->args.epoch = next_epoch(ctx);
     for (size_t i = 0; i < g->walk_nodes.size(); ++i) {
         void *kp[1] = {&g->args};
         cudaKernelNodeParams p = g->walk_params[i];

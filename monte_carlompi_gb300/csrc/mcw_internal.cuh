@@ -126,19 +126,15 @@ struct WalkArgs {
     mcw_tally *tallies;          // n_cfg device tallies
     unsigned long long budget_ns;
     PhiloxKeys keys;
-    // drain handover: once the photon supply is exhausted, a warp with at most
-    // drain_below active lanes writes its photons to drain (kDrainSlot float4
-    // each; the last word of a slot is `epoch`, written after the rest) and then
-    // walks handed-over photons with the whole warp; the drain kernel after the
-    // walk takes any left.  drain == null or drain_below == 0: no handover.
+    // drain handover: once the photon supply is exhausted, photons past drain_from
+    // steps (in block mode) leave the walk for drain (kDrainSlot float4 each, at
+    // most one per thread of the walk grid); the drain kernel after the walk walks
+    // each with a whole thread block.  drain == null or drain_from == 0: no handover.
     float4 *drain;
-    unsigned int *drain_count;   // slots reserved
-    unsigned int *drain_next;    // next ticket
-    unsigned int *warps_done;    // warps of the walk grid past their photon loop
-    int32_t drain_below;
-    uint32_t epoch;              // differs between launches, never 0 (0 marks a taken slot)
+    unsigned int *drain_count;   // slots written
+    unsigned int *drain_next;    // the drain kernel's next slot
+    int32_t drain_from;
     uint32_t drain_cap;          // slots in drain (grid * block)
-    uint32_t drain_pad;
     const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
 };
 
@@ -183,7 +179,7 @@ cudaError_t launch_lut(const LutArgs &a, cudaStream_t s);
 // Photons the walk hands over to its drain queue are packed as this many float4.
 constexpr int kDrainSlot = 6;
 // impurity: some config has imp_cnc > 0 (the kernel instance with the species draw).
-// Launches the walk and, when a.drain_below > 0, the drain kernel after it
+// Launches the walk and, when a.drain_from > 0, the drain kernel after it
 // (sm_count SMs; a.drain must then hold grid * block slots).
 cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s);
 cudaError_t launch_walk_replay(const ReplayArgs &a, cudaStream_t s);

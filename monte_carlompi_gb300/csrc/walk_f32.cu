@@ -21,14 +21,14 @@
 // steps of a lone photon) and each photon's lane then runs only the chain that
 // remains (rotation, move, boundaries).
 //
-// Optionally (WalkArgs::drain_below > 0) a warp that is down to drain_below
-// photons hands them over (their state packed into a device queue) and then
-// serves the queue, walking one handed-over photon at a time with the whole warp.
-// A warp leaves once every warp is past its photon loop and no slot is left for
-// it, or after kDrainIdleNs without its slot arriving; the drain kernel launched
-// after the walk takes whatever is left, so no warp ever waits on one that may not
-// run.  The arithmetic of a step is the same on every path, so records do not
-// depend on where or how a photon ends its walk.
+// Photons past kBlockWalk steps walk in block passes of up to 512 steps, a warp
+// per photon.  Optionally (WalkArgs::drain_from > 0), once the photon supply is
+// exhausted, a photon past drain_from steps leaves the walk (its state packed
+// into a device queue) and the drain kernel launched after the walk gives each
+// such photon a whole thread block, a warp per 64 steps of every pass.  Nothing
+// waits on anything: the queue is complete when the drain kernel starts.  The
+// arithmetic of a step and of a pass is the same on every path, so records do
+// not depend on where or how a photon ends its walk.
 //
 // Per step (monte_carloMPI/monte_carlo3D.py:1212-1466, HG branch) one
 // Philox4x32-10 block keyed by (step, photon) supplies the four uniforms the
@@ -68,8 +68,8 @@ constexpr int kFinishCap = 64;                         // finish queue entries p
 #ifndef MCW_BLOCK_WALK
 #define MCW_BLOCK_WALK 256
 #endif
-// steps after which a photon (not on a Lambertian surface) walks in warp-wide blocks
-// of kBlockSteps steps (block_pass); a multiple of 4, so every path reaches it at a round edge
+// steps after which a photon (not on a Lambertian surface) walks in block passes
+// (block_pass); a multiple of 4, so every path reaches it at a round edge
 constexpr int kBlockWalk = MCW_BLOCK_WALK;
 #ifndef MCW_STEPS_PER_ROUND
 #define MCW_STEPS_PER_ROUND 4
@@ -132,7 +132,7 @@ __device__ __forceinline__ bool in_block_mode(const Photon &P) {
     return P.cfg >= 0 && P.i >= kBlockWalk && !(P.flags & kFlagLamSurface);
 }
 
-// A photon handed to the drain queue: kDrainSlot = 6 float4 (.w of the last: epoch).
+// A photon handed to the drain queue: kDrainSlot = 6 float4.
 __device__ __forceinline__ void pack_photon(float4 *d, const Photon &P) {
     d[0] = make_float4(__uint_as_float((uint32_t)P.rid), __uint_as_float((uint32_t)(P.rid >> 32)),
                        __int_as_float(P.cfg), __int_as_float(P.lut));
@@ -568,24 +568,363 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
     return cond;
 }
 
-// ---- block mode: the walk beyond kBlockWalk steps (block_pass)
+// ---- block mode: the walk beyond kBlockWalk steps (block_pass, cta_pass)
 //
 // Photons this long are deep in a weakly absorbing slab and still have hundreds
 // to millions of steps to go; walked one step at a time they set the end of a
-// launch.  A block pass advances one photon by up to kBlockSteps steps with the
-// whole warp: lane k draws its steps' angles, optical path and absorption words
-// (the same Philox blocks as the step-by-step walk), builds the local rotation
-// R_k = Rz(phi_k) Ry(theta_k) (as a unit quaternion) and the warp composes
-// P_k = R_1 ... R_k with an inclusive shuffle scan (products of rotations are
-// associative), so step k's direction is O_0 P_k e_z for the photon's frame O_0; positions and path
-// lengths are shuffle-scan sums; the first boundary crossing or absorption
-// (ballot) ends the pass there, as the step-by-step walk would.  The direction
-// is carried in a moving frame (O_0 built from the direction by the branchless
-// orthonormal basis of Duff et al. 2017) instead of the z-referenced formula:
-// with a uniform azimuth both give the same distribution of walks.  A photon
-// enters block mode at exactly kBlockWalk steps on every path (the dense and
-// sparse rounds and the drain walk stop there), so records stay independent of
-// the launch shape.
+// launch.  A block pass advances one photon by up to kPassSteps = 512 steps from
+// one frame O_0 (built from the direction by the branchless orthonormal basis of
+// Duff et al. 2017; the lab frame after a bottom reflection).  The pass is cut
+// into kPassChunks chunks of 32 lanes x kLaneSteps steps.  Lane l of chunk c draws
+// its steps' angles, optical path and absorption words (the same Philox blocks,
+// counter = step, as the step-by-step walk) and turns each step's rotation
+// R = Rz(phi) Ry(theta) into a unit quaternion; the lane's product, an inclusive
+// shuffle scan of Hamilton products across the chunk (rotations compose
+// associatively) and the product W_c of the earlier chunks' totals give every
+// step's composed rotation P_k = R_1 ... R_k, so step k's direction is
+// O_0 P_k e_z.  Vertical positions and path lengths are scan sums the same way,
+// and the first top/bottom crossing or absorption ends the pass there, as the
+// step-by-step walk would.  The moving frame replaces the z-referenced rotation
+// formula: with a uniform azimuth both give the same distribution of walks.
+//
+// The chunks' totals are combined in chunk order (W_{c+1} = W_c * T_c, sums
+// likewise), so a warp that walks the chunks one after the other (block_pass,
+// stopping at the first chunk with an event) and a thread block whose warps take
+// one chunk each (cta_pass, in the drain kernel) do the same arithmetic: records
+// do not depend on which walks a photon.  A photon enters block mode at exactly
+// kBlockWalk steps on every path (the dense and sparse rounds stop there).
+
+#ifndef MCW_BLOCK_LANE_STEPS
+#define MCW_BLOCK_LANE_STEPS 2
+#endif
+constexpr int kLaneSteps = MCW_BLOCK_LANE_STEPS;          // steps per lane in a chunk
+constexpr int kChunkSteps = 32 * kLaneSteps;              // steps per chunk (one warp)
+constexpr int kPassChunks = 8;                            // chunks per block pass
+constexpr int kPassSteps = kPassChunks * kChunkSteps;     // steps per block pass
+constexpr int kCtaWalkThreads = 32 * kPassChunks;         // the drain kernel's block: a warp per chunk
+
+// Hamilton product a b of quaternions stored as (.x, .y, .z, .w) = (w, x, y, z),
+// every operation rounded as written (a pass must give the same bits in every
+// kernel that walks it).
+__device__ __forceinline__ float4 qmul(const float4 a, const float4 b) {
+    return make_float4(
+        fmaf(-a.y, b.y, fmaf(-a.z, b.z, fmaf(-a.w, b.w, __fmul_rn(a.x, b.x)))),   // w
+        fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.z, b.w, -__fmul_rn(a.w, b.z)))),     // x
+        fmaf(a.x, b.z, fmaf(-a.y, b.w, fmaf(a.z, b.x, __fmul_rn(a.w, b.y)))),     // y
+        fmaf(a.x, b.w, fmaf(a.y, b.z, fmaf(-a.z, b.y, __fmul_rn(a.w, b.x)))));    // z
+}
+
+__device__ __forceinline__ float4 q_identity() { return make_float4(1.f, 0.f, 0.f, 0.f); }
+
+__device__ __forceinline__ float4 shfl_q(const float4 q, int src) {
+    return make_float4(__shfl_sync(0xffffffffu, q.x, src), __shfl_sync(0xffffffffu, q.y, src),
+                       __shfl_sync(0xffffffffu, q.z, src), __shfl_sync(0xffffffffu, q.w, src));
+}
+
+// Inclusive scan of the lanes' quaternions, earlier lanes on the left.
+__device__ __forceinline__ float4 warp_scan_q(float4 q, int lane) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        float4 l;
+        l.x = __shfl_up_sync(0xffffffffu, q.x, off);
+        l.y = __shfl_up_sync(0xffffffffu, q.y, off);
+        l.z = __shfl_up_sync(0xffffffffu, q.z, off);
+        l.w = __shfl_up_sync(0xffffffffu, q.w, off);
+        if (lane >= off) q = qmul(l, q);
+    }
+    return q;
+}
+
+// Inclusive scan of two sums across the lanes.
+__device__ __forceinline__ void warp_scan_2(float &x, float &y, int lane) {
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const float xu = __shfl_up_sync(0xffffffffu, x, off);
+        const float yu = __shfl_up_sync(0xffffffffu, y, off);
+        if (lane >= off) { x = __fadd_rn(x, xu); y = __fadd_rn(y, yu); }
+    }
+}
+
+// The frame O_0 = (e1, e2, d0) of a pass.
+struct PassFrame {
+    float e1x, e1y, e1z, e2x, e2y, e2z, d0x, d0y, d0z;
+};
+
+__device__ __forceinline__ PassFrame pass_frame(const Photon &Q, bool reflected) {
+    PassFrame F{1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
+    if (!reflected) {
+        const float inv = rsqrtf(fmaf(Q.mux, Q.mux, fmaf(Q.muy, Q.muy, __fmul_rn(Q.muz, Q.muz))));
+        F.d0x = __fmul_rn(Q.mux, inv); F.d0y = __fmul_rn(Q.muy, inv); F.d0z = __fmul_rn(Q.muz, inv);
+        const float sg = copysignf(1.f, F.d0z);
+        const float aa = -1.f / __fadd_rn(sg, F.d0z);
+        const float bb = __fmul_rn(__fmul_rn(F.d0x, F.d0y), aa);
+        F.e1x = fmaf(__fmul_rn(sg, F.d0x), __fmul_rn(F.d0x, aa), 1.f);
+        F.e1y = __fmul_rn(sg, bb);
+        F.e1z = -__fmul_rn(sg, F.d0x);
+        F.e2x = bb;
+        F.e2y = fmaf(F.d0y, __fmul_rn(F.d0y, aa), sg);
+        F.e2z = -F.d0y;
+    }
+    return F;
+}
+
+// One lane's steps of a chunk: their rotations (then their composed rotations),
+// optical paths, and per step the absorption, reflectance and species bits.
+struct LaneSteps {
+    float4 qs[kLaneSteps];
+    float dtau[kLaneSteps];
+    unsigned absm, reflm, impm;
+};
+
+// Draw steps s0 .. s0 + kLaneSteps - 1 of photon Q; lamb: the first of them takes
+// the Lambertian direction about the vertical (the first step after a bottom
+// reflection, :1238-1250).
+__device__ __forceinline__ void lane_draw(LaneSteps &L, const Photon &Q, uint32_t s0, bool lamb, const WalkArgs &a) {
+    L.absm = L.reflm = L.impm = 0;
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        const uint32_t n = s0 + (uint32_t)t;
+        const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
+        const float4 uu = step_uniforms(r);
+        L.dtau[t] = -__logf(uu.z);                                      // :1014
+        const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
+        // absorption as 1 - u < 1 - ssa (:1461-1466); on a bottom crossing the same
+        // word is the reflectance draw
+        L.absm |= (uu.w < (imp ? Q.coalb_imp : Q.coalb_ice) ? 1u : 0u) << t;
+        L.reflm |= (uu.w < Q.R ? 1u : 0u) << t;
+        L.impm |= (imp ? 1u : 0u) << t;
+        const float ct = (lamb && t == 0) ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
+        const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));  // cos(theta / 2)
+        const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));  // sin(theta / 2)
+        float sph, cph;                                                 // half the azimuth, uniform
+        __sincosf(__fmul_rn(3.14159265358979324f, __fsub_rn(uu.y, 0.5f)), &sph, &cph);
+        L.qs[t] = make_float4(__fmul_rn(cph, ch), -__fmul_rn(sph, sh), __fmul_rn(cph, sh), __fmul_rn(sph, ch));
+    }
+}
+
+__device__ __forceinline__ float4 lane_product(const LaneSteps &L) {
+    float4 q = L.qs[0];
+#pragma unroll
+    for (int t = 1; t < kLaneSteps; ++t) q = qmul(q, L.qs[t]);
+    return q;
+}
+
+// x: the rotation up to the lane's first step; the lane's rotations become the
+// composed rotations of its steps.
+__device__ __forceinline__ void lane_prefixes(LaneSteps &L, float4 x) {
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        x = qmul(x, L.qs[t]);
+        L.qs[t] = x;
+    }
+}
+
+// The direction after a step of composed rotation p (O_0 p e_z).
+__device__ __forceinline__ float3 pass_dir(const PassFrame &F, const float4 p) {
+    const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
+    const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
+    const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
+    return make_float3(fmaf(F.e1x, c0, fmaf(F.e2x, c1, __fmul_rn(F.d0x, c2))),
+                       fmaf(F.e1y, c0, fmaf(F.e2y, c1, __fmul_rn(F.d0y, c2))),
+                       fmaf(F.e1z, c0, fmaf(F.e2z, c1, __fmul_rn(F.d0z, c2))));
+}
+
+// Each step's vertical move, and the lane's sums of the moves and path increments.
+__device__ __forceinline__ void lane_moves(const LaneSteps &L, const PassFrame &F, float inv_ext,
+                                           float (&dz)[kLaneSteps], float &zs, float &ps) {
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        const float4 p = L.qs[t];
+        const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
+        const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
+        const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
+        dz[t] = __fmul_rn(L.dtau[t], fmaf(F.e1z, c0, fmaf(F.e2z, c1, __fmul_rn(F.d0z, c2))));
+        const float inc = __fmul_rn(L.dtau[t], inv_ext);
+        zs = t == 0 ? dz[t] : __fadd_rn(zs, dz[t]);
+        ps = t == 0 ? inc : __fadd_rn(ps, inc);
+    }
+}
+
+// The lane's first event (a crossing, else absorption) or, without one, its last
+// step: the step (ts), the event bits, z after and before the step, the path up to
+// it.  zx, px: the moves and path before the lane's first step of the pass.
+struct LaneEvent {
+    int first, ts;        // first: the event step, kLaneSteps if none
+    unsigned what;        // 1 top, 2 bottom, 4 species impurity, 8 reflectance draw passed
+    float zk, zp, pk;
+};
+
+__device__ __forceinline__ LaneEvent lane_event(const LaneSteps &L, const float (&dz)[kLaneSteps], const Photon &Q,
+                                                float zx, float px) {
+    LaneEvent E{kLaneSteps, kLaneSteps - 1, 0u, 0.f, 0.f, 0.f};
+    float zl = 0.f, pl = 0.f;
+#pragma unroll
+    for (int t = 0; t < kLaneSteps; ++t) {
+        const float zp = t == 0 ? __fadd_rn(Q.z, zx) : __fadd_rn(Q.z, __fadd_rn(zx, zl));
+        const float inc = __fmul_rn(L.dtau[t], Q.inv_ext);
+        zl = t == 0 ? dz[t] : __fadd_rn(zl, dz[t]);
+        pl = t == 0 ? inc : __fadd_rn(pl, inc);
+        const float zk = __fadd_rn(Q.z, __fadd_rn(zx, zl));
+        const bool top = zk > 0.f;
+        const bool bot = zk < -Q.tau;
+        const bool absb = !top && !bot && ((L.absm >> t) & 1u);
+        const bool event = top || bot || absb;
+        if (E.first == kLaneSteps && (event || t == kLaneSteps - 1)) {
+            if (event) E.first = t;
+            E.ts = t;
+            E.what = (top ? 1u : 0u) | (bot ? 2u : 0u) | (((L.impm >> t) & 1u) << 2) | (((L.reflm >> t) & 1u) << 3);
+            E.zk = zk;
+            E.zp = zp;
+            E.pk = __fadd_rn(px, pl);
+        }
+    }
+    return E;
+}
+
+// The direction (x, y, z) and path increment (w) of the lane's step ts.
+__device__ __forceinline__ float4 lane_step_dir(const LaneSteps &L, const PassFrame &F, int ts, float inv_ext) {
+    float4 p = L.qs[0];
+    float dt = L.dtau[0];
+#pragma unroll
+    for (int t = 1; t < kLaneSteps; ++t)
+        if (t == ts) { p = L.qs[t]; dt = L.dtau[t]; }
+    const float3 d = pass_dir(F, p);
+    return make_float4(d.x, d.y, d.z, __fmul_rn(dt, inv_ext));
+}
+
+// The end of a pass: the photon advanced `adv` steps; dir: the direction and path
+// increment of the last step, ze / zp: z after / before it, pe: the pass's path
+// length, what: its event bits (ev: an event ended the pass).  Returns the end
+// condition (0: still walking, or reflected at the bottom).
+__device__ __forceinline__ int pass_end(Photon &Q, int adv, bool ev, const float4 dir, float ze, float zp, float pe,
+                                        unsigned what) {
+    Q.i += adv;
+    {   // compensated path sum
+        const float y = __fsub_rn(pe, Q.pathc);
+        const float tt = __fadd_rn(Q.path, y);
+        Q.pathc = __fsub_rn(__fsub_rn(tt, Q.path), y);
+        Q.path = tt;
+    }
+    const float inv = rsqrtf(fmaf(dir.x, dir.x, fmaf(dir.y, dir.y, __fmul_rn(dir.z, dir.z))));
+    Q.mux = __fmul_rn(dir.x, inv); Q.muy = __fmul_rn(dir.y, inv); Q.muz = __fmul_rn(dir.z, inv);
+    Q.flags &= ~kFlagReflect;
+    Q.z = ze;
+    if (!ev) return 0;
+    if (what & 1u) {                                                    // :1390-1397
+        Q.path = fmaf(-__fdividef(ze, __fsub_rn(ze, zp)), dir.w, Q.path);
+        return 1;
+    }
+    if (what & 2u) {                                                    // :1399-1459
+        Q.path = fmaf(-__fdividef(__fadd_rn(ze, Q.tau), __fsub_rn(ze, zp)), dir.w, Q.path);
+        Q.z = -Q.tau;
+        if ((Q.flags & kFlagLamBottom) && (what & 8u)) {
+            Q.flags |= kFlagReflect;
+            return 0;
+        }
+        return 2;
+    }
+    return (what & 4u) ? 5 : 4;
+}
+
+// One block pass over photon Q, held alike by every lane of the warp, the chunks
+// walked one after the other until the first with an event.  Q is updated alike
+// on every lane; returns the end condition.  Warp-collective.
+__device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
+    const bool reflected = (Q.flags & kFlagReflect) != 0;
+    const PassFrame F = pass_frame(Q, reflected);
+    float4 W = q_identity();               // rotation of the earlier chunks
+    float Wz = 0.f, Wp = 0.f;              // their vertical moves and path increments
+    for (int c = 0;; ++c) {
+        LaneSteps L;
+        lane_draw(L, Q, (uint32_t)Q.i + 1u + (uint32_t)(kChunkSteps * c + kLaneSteps * lane),
+                  reflected && c == 0 && lane == 0, a);
+        const float4 qi = warp_scan_q(lane_product(L), lane);
+        float4 xl = shfl_q(qi, (lane + 31) & 31);
+        if (lane == 0) xl = q_identity();
+        lane_prefixes(L, qmul(W, xl));
+        float dz[kLaneSteps], zs, ps;
+        lane_moves(L, F, Q.inv_ext, dz, zs, ps);
+        warp_scan_2(zs, ps, lane);
+        float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
+        if (lane == 0) { zx = 0.f; px = 0.f; }
+        const LaneEvent E = lane_event(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
+        const unsigned ev = __ballot_sync(0xffffffffu, E.first < kLaneSteps);
+        if (ev || c == kPassChunks - 1) {
+            const int e = ev ? __ffs(ev) - 1 : 31;
+            const float4 d = lane_step_dir(L, F, E.ts, Q.inv_ext);
+            const float4 dir = make_float4(__shfl_sync(0xffffffffu, d.x, e), __shfl_sync(0xffffffffu, d.y, e),
+                                           __shfl_sync(0xffffffffu, d.z, e), __shfl_sync(0xffffffffu, d.w, e));
+            const int ts = __shfl_sync(0xffffffffu, E.ts, e);
+            const float ze = __shfl_sync(0xffffffffu, E.zk, e), zp = __shfl_sync(0xffffffffu, E.zp, e);
+            const float pe = __shfl_sync(0xffffffffu, E.pk, e);
+            const unsigned what = __shfl_sync(0xffffffffu, E.what, e);
+            return pass_end(Q, kChunkSteps * c + kLaneSteps * e + ts + 1, ev != 0, dir, ze, zp, pe, what);
+        }
+        W = qmul(W, shfl_q(qi, 31));
+        Wz = __fadd_rn(Wz, __shfl_sync(0xffffffffu, zs, 31));
+        Wp = __fadd_rn(Wp, __shfl_sync(0xffffffffu, ps, 31));
+    }
+}
+
+// Shared memory of a block walking one photon in block passes (cta_pass).
+struct CtaPassShared {
+    float4 wq[kPassChunks];     // each chunk's rotation
+    float2 wzp[kPassChunks];    // each chunk's vertical move and path length
+    int wev[kPassChunks];       // each chunk's first lane with an event (32: none)
+    float4 dir;                 // the last step's direction and path increment
+    float4 zzp;                 // z after and before it, the pass's path length, event bits
+    int adv, ev;
+};
+
+// One block pass over photon Q, held alike by every thread of a block of
+// kCtaWalkThreads, warp w taking chunk w: the same arithmetic as block_pass.  Q is
+// updated alike on every thread; returns the end condition.  Block-collective.
+__device__ __forceinline__ int cta_pass(Photon &Q, const WalkArgs &a, CtaPassShared &S, int warp, int lane) {
+    const bool reflected = (Q.flags & kFlagReflect) != 0;
+    const PassFrame F = pass_frame(Q, reflected);
+    LaneSteps L;
+    lane_draw(L, Q, (uint32_t)Q.i + 1u + (uint32_t)(kChunkSteps * warp + kLaneSteps * lane),
+              reflected && warp == 0 && lane == 0, a);
+    const float4 qi = warp_scan_q(lane_product(L), lane);
+    if (lane == 31) S.wq[warp] = qi;
+    __syncthreads();
+    float4 W = q_identity();
+    for (int c = 0; c < warp; ++c) W = qmul(W, S.wq[c]);
+    float4 xl = shfl_q(qi, (lane + 31) & 31);
+    if (lane == 0) xl = q_identity();
+    lane_prefixes(L, qmul(W, xl));
+    float dz[kLaneSteps], zs, ps;
+    lane_moves(L, F, Q.inv_ext, dz, zs, ps);
+    warp_scan_2(zs, ps, lane);
+    if (lane == 31) S.wzp[warp] = make_float2(zs, ps);
+    __syncthreads();
+    float Wz = 0.f, Wp = 0.f;
+    for (int c = 0; c < warp; ++c) {
+        const float2 t = S.wzp[c];
+        Wz = __fadd_rn(Wz, t.x);
+        Wp = __fadd_rn(Wp, t.y);
+    }
+    float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
+    if (lane == 0) { zx = 0.f; px = 0.f; }
+    const LaneEvent E = lane_event(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
+    const unsigned ev = __ballot_sync(0xffffffffu, E.first < kLaneSteps);
+    if (lane == 0) S.wev[warp] = ev ? __ffs(ev) - 1 : 32;
+    __syncthreads();
+    int ec = kPassChunks - 1, el = 31;
+    bool any = false;
+    for (int c = kPassChunks - 1; c >= 0; --c) {
+        const int l = S.wev[c];
+        if (l < 32) { ec = c; el = l; any = true; }
+    }
+    if (warp == ec && lane == el) {
+        S.dir = lane_step_dir(L, F, E.ts, Q.inv_ext);
+        S.zzp = make_float4(E.zk, E.zp, E.pk, __uint_as_float(E.what));
+        S.adv = kChunkSteps * ec + kLaneSteps * el + E.ts + 1;
+    }
+    __syncthreads();
+    const float4 zzp = S.zzp;
+    return pass_end(Q, S.adv, any, S.dir, zzp.x, zzp.y, zzp.z, __float_as_uint(zzp.w));
+}
 
 __device__ __forceinline__ Photon shfl_photon(const Photon &P, int src) {
     Photon Q;
@@ -614,202 +953,6 @@ __device__ __forceinline__ Photon shfl_photon(const Photon &P, int src) {
     return Q;
 }
 
-// Hamilton product a b of quaternions stored as (.x, .y, .z, .w) = (w, x, y, z),
-// every operation rounded as written (the pass is inlined in two kernels and
-// must give the same bits in both).
-__device__ __forceinline__ float4 qmul(const float4 a, const float4 b) {
-    return make_float4(
-        fmaf(-a.y, b.y, fmaf(-a.z, b.z, fmaf(-a.w, b.w, __fmul_rn(a.x, b.x)))),   // w
-        fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.z, b.w, -__fmul_rn(a.w, b.z)))),     // x
-        fmaf(a.x, b.z, fmaf(-a.y, b.w, fmaf(a.z, b.x, __fmul_rn(a.w, b.y)))),     // y
-        fmaf(a.x, b.w, fmaf(a.y, b.z, fmaf(-a.z, b.y, __fmul_rn(a.w, b.x)))));    // z
-}
-
-#ifndef MCW_BLOCK_LANE_STEPS
-#define MCW_BLOCK_LANE_STEPS 2
-#endif
-// steps per lane in a block pass: a pass covers 32 * kLaneSteps steps
-constexpr int kLaneSteps = MCW_BLOCK_LANE_STEPS;
-constexpr int kBlockSteps = 32 * kLaneSteps;
-
-// One block pass over photon Q, held alike by every lane of the warp: steps
-// Q.i + 1 .. Q.i + kBlockSteps, lane l taking steps kLaneSteps l .. + kLaneSteps - 1,
-// ended early by the first top or bottom crossing or absorption.  Each step's
-// rotation Rz(phi) Ry(theta) is the unit quaternion (c_p c_t, -s_p s_t, c_p s_t,
-// s_p c_t) of the half angles; a lane multiplies its own, an inclusive shuffle
-// scan of the lane products (Hamilton products) composes them across lanes, and
-// the lane's exclusive prefix times its local products gives every step's
-// composed rotation.  Positions and path lengths are scanned the same way.  Q is
-// updated alike on every lane; returns the end condition (0: still walking, or
-// reflected at the bottom).  Warp-collective.
-__device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
-    const bool reflected = (Q.flags & kFlagReflect) != 0;
-    float4 qs[kLaneSteps];                   // the steps' rotations, then their prefixes
-    float dtau[kLaneSteps];
-    unsigned absm = 0, reflm = 0, impm = 0;  // per step: absorbed, reflectance draw, species
-#pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
-        const uint32_t n = (uint32_t)Q.i + 1u + (uint32_t)(kLaneSteps * lane + t);
-        const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
-        const float4 uu = step_uniforms(r);
-        dtau[t] = -__logf(uu.z);                                        // :1014
-        const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
-        // absorption as 1 - u < 1 - ssa (:1461-1466); on a bottom crossing the same
-        // word is the reflectance draw
-        absm |= (uu.w < (imp ? Q.coalb_imp : Q.coalb_ice) ? 1u : 0u) << t;
-        reflm |= (uu.w < Q.R ? 1u : 0u) << t;
-        impm |= (imp ? 1u : 0u) << t;
-        // after a bottom reflection the pass starts in the lab frame and its first
-        // step takes the Lambertian direction about the vertical (:1238-1250)
-        const bool lamb = reflected && lane == 0 && t == 0;
-        const float ct = lamb ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
-        const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));  // cos(theta / 2)
-        const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));  // sin(theta / 2)
-        float sph, cph;                                                 // half the azimuth, uniform
-        __sincosf(__fmul_rn(3.14159265358979324f, __fsub_rn(uu.y, 0.5f)), &sph, &cph);
-        qs[t] = make_float4(__fmul_rn(cph, ch), -__fmul_rn(sph, sh), __fmul_rn(cph, sh), __fmul_rn(sph, ch));
-    }
-    // the lane's product, scanned across the lanes; then each step's prefix
-    float4 q = qs[0];
-#pragma unroll
-    for (int t = 1; t < kLaneSteps; ++t) q = qmul(q, qs[t]);
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        float4 l;
-        l.x = __shfl_up_sync(0xffffffffu, q.x, off);
-        l.y = __shfl_up_sync(0xffffffffu, q.y, off);
-        l.z = __shfl_up_sync(0xffffffffu, q.z, off);
-        l.w = __shfl_up_sync(0xffffffffu, q.w, off);
-        if (lane >= off) q = qmul(l, q);                                // earlier steps on the left
-    }
-    {
-        float4 x;                                                       // exclusive prefix
-        x.x = __shfl_up_sync(0xffffffffu, q.x, 1);
-        x.y = __shfl_up_sync(0xffffffffu, q.y, 1);
-        x.z = __shfl_up_sync(0xffffffffu, q.z, 1);
-        x.w = __shfl_up_sync(0xffffffffu, q.w, 1);
-        if (lane == 0) x = make_float4(1.f, 0.f, 0.f, 0.f);
-#pragma unroll
-        for (int t = 0; t < kLaneSteps; ++t) {
-            x = qmul(x, qs[t]);
-            qs[t] = x;
-        }
-    }
-    // the frame O_0 = (e1, e2, d0) of the pass
-    float e1x = 1.f, e1y = 0.f, e1z = 0.f, e2x = 0.f, e2y = 1.f, e2z = 0.f, d0x = 0.f, d0y = 0.f, d0z = 1.f;
-    if (!reflected) {
-        const float inv = rsqrtf(fmaf(Q.mux, Q.mux, fmaf(Q.muy, Q.muy, __fmul_rn(Q.muz, Q.muz))));
-        d0x = __fmul_rn(Q.mux, inv); d0y = __fmul_rn(Q.muy, inv); d0z = __fmul_rn(Q.muz, inv);
-        const float sg = copysignf(1.f, d0z);
-        const float aa = -1.f / __fadd_rn(sg, d0z);
-        const float bb = __fmul_rn(__fmul_rn(d0x, d0y), aa);
-        e1x = fmaf(__fmul_rn(sg, d0x), __fmul_rn(d0x, aa), 1.f); e1y = __fmul_rn(sg, bb); e1z = -__fmul_rn(sg, d0x);
-        e2x = bb; e2y = fmaf(d0y, __fmul_rn(d0y, aa), sg); e2z = -d0y;
-    }
-    // each step's vertical move (O_0 times the third column of its composed
-    // rotation, z row), and the lane's sums of the position and path increments
-    float dz[kLaneSteps];
-    float zs = 0.f, ps = 0.f;
-#pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
-        const float4 p = qs[t];
-        const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
-        const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
-        const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
-        dz[t] = __fmul_rn(dtau[t], fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2))));
-        zs = t == 0 ? dz[t] : __fadd_rn(zs, dz[t]);
-        const float inc = __fmul_rn(dtau[t], Q.inv_ext);
-        ps = t == 0 ? inc : __fadd_rn(ps, inc);
-    }
-    // scan of the lane sums; the lane's exclusive prefix
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const float zu = __shfl_up_sync(0xffffffffu, zs, off);
-        const float pu = __shfl_up_sync(0xffffffffu, ps, off);
-        if (lane >= off) { zs = __fadd_rn(zs, zu); ps = __fadd_rn(ps, pu); }
-    }
-    float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
-    if (lane == 0) { zx = 0.f; px = 0.f; }
-    // the lane's first event (a crossing, else absorption), or its last step; the
-    // local sums repeat the additions above exactly
-    int first = kLaneSteps, ts = kLaneSteps - 1;
-    unsigned what_l = 0;
-    float zk_l = 0.f, zp_l = 0.f, pk_l = 0.f;
-    {
-        float zl = 0.f, pl = 0.f;
-#pragma unroll
-        for (int t = 0; t < kLaneSteps; ++t) {
-            const float zp = t == 0 ? __fadd_rn(Q.z, zx) : __fadd_rn(Q.z, __fadd_rn(zx, zl));
-            const float inc = __fmul_rn(dtau[t], Q.inv_ext);
-            zl = t == 0 ? dz[t] : __fadd_rn(zl, dz[t]);
-            pl = t == 0 ? inc : __fadd_rn(pl, inc);
-            const float zk = __fadd_rn(Q.z, __fadd_rn(zx, zl));
-            const bool top = zk > 0.f;
-            const bool bot = zk < -Q.tau;
-            const bool absb = !top && !bot && ((absm >> t) & 1u);
-            const bool event = top || bot || absb;
-            if (first == kLaneSteps && (event || t == kLaneSteps - 1)) {
-                if (event) first = t;
-                ts = t;
-                what_l = (top ? 1u : 0u) | (bot ? 2u : 0u) | (((impm >> t) & 1u) << 2) | (((reflm >> t) & 1u) << 3);
-                zk_l = zk;
-                zp_l = zp;
-                pk_l = __fadd_rn(px, pl);
-            }
-        }
-    }
-    // the direction after step ts
-    float ex, ey, ez, ei;
-    {
-        float4 p = qs[0];
-        float dt = dtau[0];
-#pragma unroll
-        for (int t = 1; t < kLaneSteps; ++t)
-            if (t == ts) { p = qs[t]; dt = dtau[t]; }
-        const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
-        const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
-        const float c2 = fmaf(-2.f, fmaf(p.y, p.y, __fmul_rn(p.z, p.z)), 1.f);
-        ex = fmaf(e1x, c0, fmaf(e2x, c1, __fmul_rn(d0x, c2)));
-        ey = fmaf(e1y, c0, fmaf(e2y, c1, __fmul_rn(d0y, c2)));
-        ez = fmaf(e1z, c0, fmaf(e2z, c1, __fmul_rn(d0z, c2)));
-        ei = __fmul_rn(dt, Q.inv_ext);
-    }
-    const unsigned ev = __ballot_sync(0xffffffffu, first < kLaneSteps);
-    const int e = ev ? __ffs(ev) - 1 : 31;
-    // the photon's state after the event step, taken from lane e
-    const int te = __shfl_sync(0xffffffffu, first, e);
-    const float nx = __shfl_sync(0xffffffffu, ex, e), ny = __shfl_sync(0xffffffffu, ey, e);
-    const float nz = __shfl_sync(0xffffffffu, ez, e);
-    const float ze = __shfl_sync(0xffffffffu, zk_l, e), zp = __shfl_sync(0xffffffffu, zp_l, e);
-    const float pe = __shfl_sync(0xffffffffu, pk_l, e), ince = __shfl_sync(0xffffffffu, ei, e);
-    const unsigned what = __shfl_sync(0xffffffffu, what_l, e);
-    Q.i += kLaneSteps * e + (ev ? te : kLaneSteps - 1) + 1;
-    {   // compensated path sum
-        const float y = __fsub_rn(pe, Q.pathc);
-        const float tt = __fadd_rn(Q.path, y);
-        Q.pathc = __fsub_rn(__fsub_rn(tt, Q.path), y);
-        Q.path = tt;
-    }
-    const float inv = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, __fmul_rn(nz, nz))));
-    Q.mux = __fmul_rn(nx, inv); Q.muy = __fmul_rn(ny, inv); Q.muz = __fmul_rn(nz, inv);
-    Q.flags &= ~kFlagReflect;
-    Q.z = ze;
-    if (!ev) return 0;
-    if (what & 1u) {                                                    // :1390-1397
-        Q.path = fmaf(-__fdividef(ze, __fsub_rn(ze, zp)), ince, Q.path);
-        return 1;
-    }
-    if (what & 2u) {                                                    // :1399-1459
-        Q.path = fmaf(-__fdividef(__fadd_rn(ze, Q.tau), __fsub_rn(ze, zp)), ince, Q.path);
-        Q.z = -Q.tau;
-        if ((Q.flags & kFlagLamBottom) && (what & 8u)) {
-            Q.flags |= kFlagReflect;
-            return 0;
-        }
-        return 2;
-    }
-    return (what & 4u) ? 5 : 4;
-}
 
 // Exact warp sum of 64-bit values below 2^47.
 __device__ __forceinline__ unsigned long long warp_sum_u64(unsigned long long v) {
@@ -889,9 +1032,6 @@ __device__ __noinline__ void finish_batch(const FinishSlot *fin, WarpTally &tall
     }
 }
 
-__device__ __noinline__ void drain_serve(FinishSlot *fin, WarpTally &tally, float4 *pbuf, int &n_fin,
-                                         const WalkArgs &a, unsigned long long t0, int lane);
-
 template <bool kImpurity>
 __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -961,30 +1101,28 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         }
         if (idle == 0xffffffffu && exhausted && n_birth == 0) break;
 
-        // ---- drain handover, once the supply is exhausted: the photons of a nearly
-        // empty warp go to the queue to be walked with a whole warp each
-        if (a.drain_below > 0 && exhausted && n_birth == 0) {
-            const bool whole = __popc(~idle) <= a.drain_below;
-            const bool leave = P.cfg >= 0 && whole;
+        // ---- drain handover, once the supply is exhausted: photons past drain_from
+        // steps go to the queue, walked after this kernel with a thread block each
+        // (a lane hands over at most one photon: it takes none afterwards)
+        if (a.drain_from > 0 && exhausted && n_birth == 0) {
+            const bool leave = in_block_mode(P) && P.i >= a.drain_from;
             const unsigned lm = __ballot_sync(0xffffffffu, leave);
             if (lm) {
                 unsigned base = 0;
                 if (lane == 0) base = atomicAdd(a.drain_count, (unsigned)__popc(lm));
                 base = __shfl_sync(0xffffffffu, base, 0);
-                if (leave) {
-                    float4 *slot = a.drain + (size_t)(base + __popc(lm & lt_mask)) * kDrainSlot;
+                const unsigned slot_i = base + __popc(lm & lt_mask);
+                if (leave && slot_i < a.drain_cap) {
+                    float4 *slot = a.drain + (size_t)slot_i * kDrainSlot;
                     float4 v[kDrainSlot];
                     pack_photon(v, P);
 #pragma unroll
-                    for (int k = 0; k < kDrainSlot - 1; ++k) __stcg(&slot[k], v[k]);
-                    __threadfence();
-                    v[kDrainSlot - 1].w = __uint_as_float(a.epoch);
-                    __stcg(&slot[kDrainSlot - 1], v[kDrainSlot - 1]);
+                    for (int k = 0; k < kDrainSlot; ++k) __stcg(&slot[k], v[k]);
                     P.cfg = -1;
                 }
-                idle |= lm;
+                idle |= __ballot_sync(0xffffffffu, leave && slot_i < a.drain_cap);
             }
-            if (whole) break;
+            if (idle == 0xffffffffu) break;
         }
 
         // ---- kStepsPerRound scatter events per active lane of a well-filled warp;
@@ -1023,8 +1161,8 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
             }
         }
 
-        // ---- photons past kBlockWalk steps: one block pass (up to kBlockSteps steps) each,
-        // walked by the whole warp
+        // ---- photons past kBlockWalk steps: one block pass (up to kPassSteps steps)
+        // each, walked by the whole warp
         for (unsigned pend = bmask; pend; pend &= pend - 1) {
             const int src = __ffs(pend) - 1;
             Photon Q = shfl_photon(P, src);
@@ -1084,170 +1222,88 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         }
     }
     __syncwarp();
-    if (a.drain_below > 0) {
-        // this warp is past its photon loop; then it serves the drain queue
-        if (lane == 0) {
-            __threadfence();
-            atomicAdd(a.warps_done, 1u);
-        }
-        __syncwarp();
-        drain_serve(q.fin, q.tally, q.pbuf, n_fin, a, t0, lane);
-        __syncwarp();
-    }
     if (n_fin > 0) finish_batch(q.fin, q.tally, 0, n_fin, a, scfg, prefix, staged, lane);
     warp_tally_flush(q.tally, a.tallies, lane);
 }
 
-constexpr unsigned long long kDrainIdleNs = 2000000ull;  // a serving warp waits at most 2 ms for its slot
-
-// Walk the photon in drain slot `slot` with the whole warp and push it to the
-// warp's finish queue (n_fin entries).  Returns false if the time budget ran out.
-__device__ __forceinline__ bool drain_walk(const float4 *slot, FinishSlot *fin, WarpTally &tally, float4 *pbuf,
-                                           int &n_fin, const WalkArgs &a, unsigned long long t0, int lane) {
-    float4 v[kDrainSlot];
-#pragma unroll
-    for (int k = 0; k < kDrainSlot; ++k) v[k] = __ldcg(&slot[k]);
-    // every lane holds the same photon; the chain below runs on all of them alike
-    Photon P;
-    unpack_photon(P, v);
-    int cond = 0;
-    while (cond == 0) {
-        if (in_block_mode(P)) {
-            cond = block_pass(P, a, lane);
-            continue;
-        }
-        // direction-independent part of steps P.i + 1 .. P.i + 32, one per lane
-        const uint32_t n = (uint32_t)P.i + 1u + (uint32_t)lane;
-        const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)P.rid, (uint32_t)(P.rid >> 32)), a.keys);
-        const StepPre t = step_pre(r, make_float4(P.hg_a, P.hg_b, P.hg_c, P.hg_d), P.hg_e);
-        __syncwarp();
-        pbuf[2 * lane] = make_float4(t.ct_hg, t.st_hg, t.ct_l, t.st_l);
-        pbuf[2 * lane + 1] = make_float4(t.sp, t.cp, t.dtau, t.u4);
-        const bool imp_t = (P.flags & kFlagImpurity) && impurity_draw(P.rid, n, P.p_imp, a);
-        const unsigned impm = __ballot_sync(0xffffffffu, imp_t);
-        __syncwarp();
-        // P.i is a multiple of 4 here (photons leave the main loop between rounds),
-        // so every fourth step renormalises, as in the main loop
-#pragma unroll
-        for (int k = 0; k < 32; ++k) {
-            if ((k & 3) == 0 && in_block_mode(P)) break;               // block mode from kBlockWalk on
-            const float4 x = pbuf[2 * k], y = pbuf[2 * k + 1];
-            StepPre s;
-            s.ct_hg = x.x, s.st_hg = x.y, s.ct_l = x.z, s.st_l = x.w;
-            s.sp = y.x, s.cp = y.y, s.dtau = y.z, s.u4 = y.w;
-            cond = step_post(P, s, (impm >> k) & 1u, (k & 3) == 3);
-            if (cond != 0) break;
-        }
-        int over = 0;
-        if (lane == 0)
-            over = (global_ns() - t0 > a.budget_ns) || (*(volatile unsigned int *)a.status & kStatusBudget);
-        if (__shfl_sync(0xffffffffu, over, 0)) {
-            if (lane == 0) atomicOr(a.status, kStatusBudget);
-            return false;
-        }
-    }
-    if (lane == 0) {
-        FinishSlot f;
-        f.rid_lo = (uint32_t)P.rid;
-        f.rid_hi = (uint32_t)(P.rid >> 32);
-        f.cfg = (uint32_t)P.cfg;
-        f.lut = (uint32_t)P.lut;
-        f.n_step = P.i;
-        f.cond = cond;
-        f.mux = P.mux;
-        f.muy = P.muy;
-        f.muz = P.muz;
-        f.path = P.path;
-        f.pad0 = f.pad1 = 0.f;
-        copy_f4<3>(&fin[n_fin], &f);
-    }
-    __syncwarp();
-    if (++n_fin >= 32) {
-        finish_batch(fin, tally, n_fin - 32, 32, a, nullptr, a.prefix, false, lane);
-        n_fin -= 32;
-    }
-    return true;
-}
-
-// Serve the drain queue from a warp of the walk grid: take a ticket (the next
-// slot), wait for that slot to be written (polling the slot itself, with growing
-// pauses), mark it taken and walk it; repeat.  Leave when every warp of the grid is
-// past its photon loop and no slot is left for the ticket, or after kDrainIdleNs
-// without the slot arriving (the drain kernel then walks it).  Warp-collective.
-__device__ __noinline__ void drain_serve(FinishSlot *fin, WarpTally &tally, float4 *pbuf, int &n_fin,
-                                         const WalkArgs &a, unsigned long long t0, int lane) {
-    const unsigned total_warps = gridDim.x * (blockDim.x >> 5);
-    for (;;) {
-        unsigned j = 0;
-        int go = 0;
-        if (lane == 0) j = atomicAdd(a.drain_next, 1u);
-        // a ticket past the buffer can never be filled: leave without touching memory
-        if (__shfl_sync(0xffffffffu, j, 0) >= a.drain_cap) break;
-        if (lane == 0) {
-            float4 *slot = a.drain + (size_t)j * kDrainSlot;
-            const unsigned long long w0 = global_ns();
-            unsigned pause = 32;
-            for (uint32_t it = 0;; ++it) {
-                if (__float_as_uint(__ldcg(&slot[kDrainSlot - 1]).w) == a.epoch) {
-                    // taken (0 is never an epoch): the drain kernel must not walk it again
-                    float4 last = __ldcg(&slot[kDrainSlot - 1]);
-                    last.w = __uint_as_float(0u);
-                    __stcg(&slot[kDrainSlot - 1], last);
-                    go = 1;
-                    break;
-                }
-                if ((it & 15u) == 0u) {
-                    const unsigned done = *(volatile unsigned int *)a.warps_done;
-                    __threadfence();
-                    if (done >= total_warps && j >= *(volatile unsigned int *)a.drain_count) break;
-                }
-                const unsigned long long now = global_ns();
-                if (now - w0 > kDrainIdleNs) break;
-                if (now - t0 > a.budget_ns || (*(volatile unsigned int *)a.status & kStatusBudget)) {
-                    atomicOr(a.status, kStatusBudget);
-                    break;
-                }
-                __nanosleep(pause);
-                pause = min(pause * 2u, 2048u);
-            }
-        }
-        if (!__shfl_sync(0xffffffffu, go, 0)) break;
-        __threadfence();
-        j = __shfl_sync(0xffffffffu, j, 0);
-        if (!drain_walk(a.drain + (size_t)j * kDrainSlot, fin, tally, pbuf, n_fin, a, t0, lane)) break;
-    }
-}
-
-// Shared memory of one drain-kernel warp.
-struct DrainWarp {
+// Shared memory of a drain-kernel block.
+struct DrainBlock {
+    CtaPassShared pass;
     FinishSlot fin[32];
-    float4 pbuf[2 * 32];
     WarpTally tally;
+    unsigned job;
+    int stop;
 };
 
-// After the walk: slots written but never taken (normally none; the walk's own
-// warps serve the queue) are walked here.
-__global__ void __launch_bounds__(256) drain_kernel(const WalkArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// After the walk: every photon handed over to the drain queue is walked to its end
+// by a whole block (cta_pass), one photon after another; finished photons go
+// through warp 0's finish queue.  The queue is complete when this kernel starts.
+__global__ void __launch_bounds__(kCtaWalkThreads) drain_kernel(const WalkArgs a) {
+    __shared__ DrainBlock S;
     const int lane = threadIdx.x & 31;
-    DrainWarp &d = reinterpret_cast<DrainWarp *>(smem)[threadIdx.x >> 5];
-    warp_tally_reset(d.tally, lane);
-    __syncwarp();
-    const unsigned cnt = *a.drain_count;
+    const int warp = threadIdx.x >> 5;
+    const unsigned cnt = min(*(volatile unsigned int *)a.drain_count, a.drain_cap);
+    if (blockIdx.x >= cnt) return;          // blocks past the queue length would find no photon
+    if (warp == 0) warp_tally_reset(S.tally, lane);
     const unsigned long long t0 = global_ns();
     int n_fin = 0;
-    const unsigned nw = gridDim.x * (blockDim.x >> 5);
-    for (unsigned j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < cnt; j += nw) {
-        const float4 *slot = a.drain + (size_t)j * kDrainSlot;
-        if (__float_as_uint(__ldcg(&slot[kDrainSlot - 1]).w) != a.epoch) continue;   // taken, or never written
-        if (!drain_walk(slot, d.fin, d.tally, d.pbuf, n_fin, a, t0, lane)) break;
+    for (;;) {
+        if (threadIdx.x == 0) S.job = atomicAdd(a.drain_next, 1u);
+        __syncthreads();
+        const unsigned j = S.job;
+        if (j >= cnt) break;
+        float4 v[kDrainSlot];
+#pragma unroll
+        for (int k = 0; k < kDrainSlot; ++k) v[k] = __ldcg(&a.drain[(size_t)j * kDrainSlot + k]);
+        Photon P;
+        unpack_photon(P, v);
+        int cond = 0;
+        bool over = false;
+        for (uint32_t pass = 1; cond == 0; ++pass) {
+            cond = cta_pass(P, a, S.pass, warp, lane);
+            if ((pass & 63u) == 0u) {
+                // time budget (watchdog; never a truncation in normal runs)
+                if (threadIdx.x == 0)
+                    S.stop = (global_ns() - t0 > a.budget_ns) || (*(volatile unsigned int *)a.status & kStatusBudget);
+                __syncthreads();
+                over = S.stop != 0;
+                __syncthreads();
+                if (over) break;
+            }
+        }
+        if (over) {
+            if (threadIdx.x == 0) atomicOr(a.status, kStatusBudget);
+            break;
+        }
+        if (warp == 0) {
+            if (lane == 0) {
+                FinishSlot f;
+                f.rid_lo = (uint32_t)P.rid;
+                f.rid_hi = (uint32_t)(P.rid >> 32);
+                f.cfg = (uint32_t)P.cfg;
+                f.lut = (uint32_t)P.lut;
+                f.n_step = P.i;
+                f.cond = cond;
+                f.mux = P.mux;
+                f.muy = P.muy;
+                f.muz = P.muz;
+                f.path = P.path;
+                f.pad0 = f.pad1 = 0.f;
+                copy_f4<3>(&S.fin[n_fin], &f);
+            }
+            __syncwarp();
+            if (++n_fin >= 32) {
+                finish_batch(S.fin, S.tally, n_fin - 32, 32, a, nullptr, a.prefix, false, lane);
+                n_fin -= 32;
+            }
+        }
     }
-    __syncwarp();
-    if (n_fin > 0) finish_batch(d.fin, d.tally, 0, n_fin, a, nullptr, a.prefix, false, lane);
-    warp_tally_flush(d.tally, a.tallies, lane);
+    if (warp == 0) {
+        __syncwarp();
+        if (n_fin > 0) finish_batch(S.fin, S.tally, 0, n_fin, a, nullptr, a.prefix, false, lane);
+        warp_tally_flush(S.tally, a.tallies, lane);
+    }
 }
-
-constexpr int kDrainBlock = 256;
 
 size_t smem_bytes(int block, int n_cfg) {
     const size_t cfg = n_cfg <= kSmemCfgMax ? (size_t)n_cfg * (sizeof(CfgF32) + sizeof(int64_t)) : 0;
@@ -1286,9 +1342,16 @@ cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int bloc
     if (impurity) walk_f32_kernel<true><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
     else walk_f32_kernel<false><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
     e = cudaGetLastError();
-    if (e != cudaSuccess || a.drain_below <= 0 || !a.drain) return e;
-    // the drain kernel for slots still unwalked (normally none): one block per SM
-    drain_kernel<<<std::max(1, sm_count), kDrainBlock, sizeof(DrainWarp) * (kDrainBlock / 32), s>>>(a);
+    if (e != cudaSuccess || a.drain_from <= 0 || !a.drain) return e;
+    // the drain kernel: as many blocks as fit at once, each taking the handed-over
+    // photons one at a time
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drain_kernel, kCtaWalkThreads, 0);
+        if (e != cudaSuccess) return e;
+        per_sm = std::max(1, per_sm);
+    }
+    drain_kernel<<<std::max(1, sm_count) * per_sm, kCtaWalkThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 

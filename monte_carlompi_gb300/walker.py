@@ -113,20 +113,21 @@ class Walker:
         _abi.check(rc, self._ctx)
         self._tables_keep = keep
 
-    def set_launch(self, block_size=256, blocks_per_sm=0, regen_chunk=8, drain_below=None):
-        """Launch shape of the FP32 walk; drain_below: once every photon has started, a warp
-        with at most this many walking photons hands them to a queue served by whole warps
-        (0 = never; None keeps the current value)."""
-        if drain_below is None:
-            drain_below = self.get_launch()['drain_below']
-        l = _abi.LaunchC(block_size, blocks_per_sm, regen_chunk, drain_below)
+    def set_launch(self, block_size=256, blocks_per_sm=0, regen_chunk=8, drain_from=None):
+        """Launch shape of the FP32 walk; drain_from: once every photon has started, a photon
+        past this many steps leaves the walk for a queue walked after it by a whole thread
+        block per photon (0 = never, else >= 256; None keeps the current value).  Records do
+        not depend on the launch shape."""
+        if drain_from is None:
+            drain_from = self.get_launch()['drain_from']
+        l = _abi.LaunchC(block_size, blocks_per_sm, regen_chunk, drain_from)
         _abi.check(self._lib.mcw_set_launch(self._ctx, ctypes.byref(l)), self._ctx)
 
     def get_launch(self):
         l = _abi.LaunchC()
         _abi.check(self._lib.mcw_get_launch(self._ctx, ctypes.byref(l)), self._ctx)
         return dict(block_size=l.block_size, blocks_per_sm=l.blocks_per_sm, regen_chunk=l.regen_chunk,
-                    drain_below=l.drain_below)
+                    drain_from=l.drain_from)
 
     def set_budget(self, seconds):
         _abi.check(self._lib.mcw_set_budget(self._ctx, float(seconds)), self._ctx)
@@ -181,7 +182,7 @@ class Walker:
                                     ctypes.byref(ms))
         _abi.check(rc, self._ctx)
         return dict(block_size=best.block_size, blocks_per_sm=best.blocks_per_sm,
-                    regen_chunk=best.regen_chunk, drain_below=best.drain_below, ms=ms.value)
+                    regen_chunk=best.regen_chunk, drain_from=best.drain_from, ms=ms.value)
 
     def graph(self, configs, device_ptr=None):
         return SweepGraph(self, configs, device_ptr)

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_version():
     L = _abi.load()
-    assert L.mcw_abi_version() == 2
+    assert L.mcw_abi_version() == 3
     assert b'sm_103a' in L.mcw_version()
 
 

@@ -280,16 +280,17 @@ def test_f32_known_answer_slab(walker):
 
 def test_f32_same_records_for_any_launch_shape(walker):
     """Records and tallies do not depend on the launch shape, nor on which photons end
-    their walk in the drain queue (drain_below 0: none; 32: whole warps)."""
+    their walk in the drain queue (drain_from 0: none; 256: every photon in block mode
+    once the supply is exhausted)."""
     cfg, ice, imp = cfg2_geometry(100000)
     walker.set_tables([ice], imp)
     saved = walker.get_launch()
     try:
-        walker.set_launch(256, 0, 8, 8)
+        walker.set_launch(256, 0, 8, 512)
         a = walker.walk([cfg], 77, mode='f32')
         walker.set_launch(128, 2, 1, 0)
         b = walker.walk([cfg], 77, mode='f32')
-        walker.set_launch(64, 1, 32, 32)
+        walker.set_launch(64, 1, 32, 256)
         c = walker.walk([cfg], 77, mode='f32')
     finally:
         walker.set_launch(**saved)
@@ -332,8 +333,9 @@ def test_f32_sparse_rounds_same_records(walker, n):
 
 def test_f32_long_walks_same_records_with_and_without_drain(walker):
     """Weakly absorbing, deep snow (lambda 1.0 um, r_eff 50 um, tau ~1000: walks of
-    thousands of steps): the walks that leave for the drain queue end exactly as they
-    would in the main loop."""
+    thousands of steps): the walks that leave for the drain queue, whose block passes a
+    thread block computes a warp per chunk, end exactly as they would in the main loop,
+    where one warp computes the chunks one after the other."""
     lo, hi = ssp.grid_for(1.0, 0.085)
     ice = ssp.synthetic_ice_table(50.0, lo, hi)
     imp = ssp.synthetic_impurity_table(lo, hi)
@@ -345,12 +347,15 @@ def test_f32_long_walks_same_records_with_and_without_drain(walker):
     try:
         walker.set_launch(256, 0, 8, 0)
         a = walker.walk([cfg], 5, mode='f32')
-        walker.set_launch(256, 0, 8, 4)
+        walker.set_launch(256, 0, 8, 256)
         b = walker.walk([cfg], 5, mode='f32')
+        walker.set_launch(128, 1, 4, 2048)
+        c = walker.walk([cfg], 5, mode='f32')
     finally:
         walker.set_launch(**saved)
     assert int(a.records['n_scat'].max()) > 4096
     assert np.array_equal(a.records, b.records) and np.array_equal(a.tallies, b.tallies)
+    assert np.array_equal(a.records, c.records) and np.array_equal(a.tallies, c.tallies)
 
 
 def test_f32_block_mode_statistics_match_oracle(walker):
