@@ -233,6 +233,49 @@ def run_sweep(args):
     return 0
 
 
+def run_lone(args):
+    """The latency of one photon's walk: single-photon launches of a nearly
+    non-absorbing, semi-infinite slab (single-scattering albedo 0.99995, tau 1e7,
+    normal incidence) over 30 seeds, the kernel time fitted against n_scat; walked in
+    its warp (drain_from 0) and by a whole block in the drain kernel (drain_from 256).
+    Records are the same either way.  The first drain-kernel launch of the run walks
+    the longest of the 30 photons (the one to capture with ncu -k drain_kernel -c 1)."""
+    import dataclasses
+    import torch  # noqa: F401  (CUDA context set-up like the other workloads)
+    from monte_carlompi_gb300.walker import Walker
+    cfg, ice, imp = workload(1)
+    lone = dataclasses.replace(cfg, ssa_ice_override=0.99995, tau_tot=1e7, theta0_deg=0.0)
+    peaks, _ = measured_peaks()
+    mhz = float(peaks.get('sm_max_mhz', 2070.0))
+    w = Walker(0)
+    w.set_tables([ice], imp)
+    out, recs = {}, {}
+    longest = SEED
+    for drain in (0, 256):
+        w.set_launch(128, 4, 1, drain)
+        w.walk([lone], longest, records=None)
+        xs, ys, rs = [], [], []
+        for s in range(30):
+            r = w.walk([lone], SEED + 100 + s)
+            xs.append(int(r.records['n_scat'][0]))
+            ys.append(r.stats['kernel_ms'])
+            rs.append(r.records.tobytes())
+        longest = SEED + 100 + int(np.argmax(xs))
+        xs, ys = np.array(xs, dtype=np.float64), np.array(ys)
+        slope = np.linalg.lstsq(np.vstack([xs, np.ones_like(xs)]).T, ys, rcond=None)[0][0]
+        out[drain] = {'cycles_per_step': slope * 1e-3 * mhz * 1e6, 'max_n_scat': int(xs.max())}
+        recs[drain] = rs
+    w.close()
+    print(json.dumps({'metric': 'cycles per scatter event of one photon walked alone', 'workload': 'lone',
+                      'value': out[256]['cycles_per_step'], 'unit': 'SM cycles/step',
+                      'higher_is_better': False, 'dtype': 'f32', 'data': 'synthetic',
+                      'config': {'workload': '1 photon x 30 seeds: ssa 0.99995, tau 1e7, theta0 0, '
+                                             'r_eff 250 um, 1.55 um', 'sm_mhz': mhz},
+                      'in_warp': out[0], 'drain_block': out[256],
+                      'same_records': recs[0] == recs[256]}))
+    return 0
+
+
 POL_WVLS = [round(1.0 + 0.025 * i, 4) for i in range(41)]              # um
 POL_RE = [60.0, 120.0, 250.0]                                            # um
 POL_THETA = [0.5 * k for k in range(20)] + [10.0 + 2.0 * k for k in range(86)]   # deg
@@ -626,7 +669,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
-    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol'])
+    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol', 'lone'])
     ap.add_argument('--surrogate-configs', type=int, default=16384)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
@@ -641,6 +684,8 @@ def main():
         return run_mlp(args)
     if args.workload == 'pol':
         return run_pol(args)
+    if args.workload == 'lone':
+        return run_lone(args)
     return run_ours(args)
 
 
