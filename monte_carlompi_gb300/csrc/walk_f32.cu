@@ -179,7 +179,7 @@ struct WarpQueues {
     BirthSlot birth[32];
     FinishSlot fin[kFinishCap];
     uint4 rmeta[3 * kSparseWarp];             // sparse round: each photon's stream, step and constants
-    float4 pbuf[2 * kSparseSlots];            // sparse round and drain: StepPre of up to 64 steps
+    float4 pbuf[2 * kSparseSlots];            // sparse round: StepPre of up to 64 steps
     WarpTally tally;
 };
 
@@ -402,10 +402,10 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     return cond;
 }
 
-// The same scatter event as step(), split for the drain path: the part that does
-// not depend on the photon's direction or position (everything drawn from the
-// step's Philox block and the photon's phase-function constants), computed for 32
-// steps at once on the 32 lanes of a warp, and the chain that does.  Every value is
+// The same scatter event as step(), split for the sparse rounds: the part that
+// does not depend on the photon's direction or position (everything drawn from the
+// step's Philox block and the photon's phase-function constants), computed for up
+// to 32 steps at once across the lanes of a warp, and the chain that does.  Every value is
 // the same function of the same inputs as in step(): st is sqrt(1 - ct^2) of the
 // selected cosine whichever way the selection is made.
 struct StepPre {

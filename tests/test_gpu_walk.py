@@ -528,6 +528,41 @@ def test_budget_stops_the_kernel_and_context_survives(walker):
     assert int(ok.tallies[0]['n_cond'][1:].sum()) == 1000
 
 
+@pytest.mark.parametrize('launch', [(512, 0, 8, 0), (96, 0, 8, 0), (256, -1, 8, 0), (256, 0, 0, 0),
+                                    (256, 0, 33, 0), (256, 0, 8, 100), (256, 0, 8, -1)])
+def test_invalid_launch_shapes_are_refused(walker, launch):
+    saved = walker.get_launch()
+    with pytest.raises(_abi.McwError, match='MCW_ERR_ARG'):
+        walker.set_launch(*launch)
+    assert walker.get_launch() == saved
+
+
+def test_budget_stops_the_drain_kernel_too(walker):
+    """Deep, weakly absorbing snow with every photon past 256 steps handed to the drain
+    kernel: a 0.1 ms budget stops the walk and the drain kernel (which checks it every 64
+    block passes), the call raises, and the next walk is complete."""
+    lo, hi = ssp.grid_for(1.0, 0.085)
+    ice = ssp.synthetic_ice_table(50.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = 0.1 * ssp.ext_cff_mss_sphere(50.0) * 300.0
+    cfg = WalkConfig(n_photon=20000, wvl0=1.0, half_width=0.085, theta0_deg=30.0, tau_tot=tau,
+                     lambertian_reflectance=0.5)
+    walker.set_tables([ice], imp)
+    saved = walker.get_launch()
+    walker.set_launch(256, 0, 8, 256)
+    walker.set_budget(1e-4)
+    try:
+        with pytest.raises(_abi.BudgetExceeded):
+            walker.walk([cfg], 2, mode='f32', records=None)
+    finally:
+        walker.set_budget(300.0)
+    try:
+        ok = walker.walk([dataclasses.replace(cfg, n_photon=2000)], 2, mode='f32')
+    finally:
+        walker.set_launch(**saved)
+    assert int(ok.tallies[0]['n_cond'][1:].sum()) == 2000
+
+
 @pytest.mark.parametrize('bad', [dict(n_photon=-1), dict(wvl0=0.0), dict(half_width=-0.1),
                                  dict(theta0_deg=90.0), dict(tau_tot=0.0), dict(imp_cnc=1.5),
                                  dict(lambertian_reflectance=1.5), dict(ice_table=3),
