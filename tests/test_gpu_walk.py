@@ -528,7 +528,7 @@ def test_budget_stops_the_kernel_and_context_survives(walker):
     assert int(ok.tallies[0]['n_cond'][1:].sum()) == 1000
 
 
-@pytest.mark.parametrize('launch', [(512, 0, 8, 0), (96, 0, 8, 0), (256, -1, 8, 0), (256, 0, 0, 0),
+@pytest.mark.parametrize('launch', [(512, 0, 8, 0), (48, 0, 8, 0), (256, -1, 8, 0), (256, 0, 0, 0),
                                     (256, 0, 33, 0), (256, 0, 8, 100), (256, 0, 8, -1)])
 def test_invalid_launch_shapes_are_refused(walker, launch):
     saved = walker.get_launch()
