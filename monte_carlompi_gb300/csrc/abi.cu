@@ -672,9 +672,6 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     if (rc) return rc;
     CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
-    uint64_t h2d = 0;
-    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
-    if (rc) return rc;
     const size_t rec_size = (mode == MCW_MODE_F32)     ? sizeof(mcw_record32)
                             : (mode == MCW_MODE_POL64) ? sizeof(mcw_record64p)
                             : (mode == MCW_MODE_POL32) ? sizeof(mcw_record32p)
@@ -697,15 +694,20 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
             dev_records = ctx->records.p;
         }
     }
+    // the launch shape first (occupancy queries, allocations): once the copies and
+    // kernels below are queued, nothing on the host stands between them
     Shape shape{0, 0, 0, 0};
+    if (mode == MCW_MODE_F32) shape = pick_shape(ctx, ctx->launch, plan);
+    uint64_t h2d = 0;
+    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
+    if (rc) return rc;
     if (mode == MCW_MODE_F32) {
-        // the lookup-table kernel also clears the counters and tallies
-        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
-        shape = pick_shape(ctx, ctx->launch, plan);
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
         rc = attach_drain(ctx, wa, ctx->drain, shape);
         if (rc) return rc;
+        // the lookup-table kernel also clears the counters and tallies
+        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
         if (plan.total > 0)
             CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, ctx->sm_count, st));

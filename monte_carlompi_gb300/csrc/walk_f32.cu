@@ -51,6 +51,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <set>
+#include <tuple>
 
 #include "mcw_internal.cuh"
 #include "tally.cuh"
@@ -1310,24 +1315,49 @@ size_t smem_bytes(int block, int n_cfg) {
     return sizeof(WarpQueues) * (size_t)(block / 32) + cfg;
 }
 
+// The walk kernels may use up to 200 KB of dynamic shared memory; set once per device.
 cudaError_t allow_smem() {
-    cudaError_t e = cudaFuncSetAttribute(walk_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    static std::mutex m;
+    static std::set<int> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(walk_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    std::lock_guard<std::mutex> g(m);
+    if (done.count(dev)) return cudaSuccess;
+    e = cudaFuncSetAttribute(walk_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(walk_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) done.insert(dev);
+    return e;
 }
 
 }  // namespace
 
 size_t walk_f32_smem_bytes(int block, int n_cfg) { return smem_bytes(block, n_cfg); }
 
+// Resident blocks per SM of the walk kernel; the occupancy query is made once per
+// device, block size, shared-memory size and kernel instance.
 int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity) {
-    int n = 0;
     if (allow_smem() != cudaSuccess) return 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     const size_t smem = smem_bytes(block, n_cfg);
+    static std::mutex m;
+    static std::map<std::tuple<int, int, size_t, bool>, int> cache;
+    const auto key = std::make_tuple(dev, block, smem, impurity);
+    {
+        std::lock_guard<std::mutex> g(m);
+        const auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    int n = 0;
     const cudaError_t e = impurity
         ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<true>, block, smem)
         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<false>, block, smem);
-    return e == cudaSuccess ? n : 0;
+    if (e != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> g(m);
+    cache[key] = n;
+    return n;
 }
 
 bool walk_f32_is_kernel(const void *fn) {
@@ -1345,11 +1375,13 @@ cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int bloc
     if (e != cudaSuccess || a.drain_from <= 0 || !a.drain) return e;
     // the drain kernel: as many blocks as fit at once, each taking the handed-over
     // photons one at a time
-    static int per_sm = 0;
+    static std::atomic<int> per_sm_cached{0};
+    int per_sm = per_sm_cached.load();
     if (per_sm == 0) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drain_kernel, kCtaWalkThreads, 0);
         if (e != cudaSuccess) return e;
         per_sm = std::max(1, per_sm);
+        per_sm_cached.store(per_sm);
     }
     drain_kernel<<<std::max(1, sm_count) * per_sm, kCtaWalkThreads, 0, s>>>(a);
     return cudaGetLastError();
