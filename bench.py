@@ -476,6 +476,9 @@ def run_inverse(ens, walker, n_obs):
     known = raw[:, 1:]
     res = I.retrieve(ens, walker, obs, known)
     err = np.abs(res['r_eff'] / raw[:, 0] - 1)
+    # the same with the fallback decided on the spread of the retrieved r_eff
+    res_r = I.retrieve(ens, walker, obs, known, criterion='r_eff')
+    err_r = np.abs(res_r['r_eff'] / raw[:, 0] - 1)
     # the same retrieval with plain Monte Carlo only, on a subset
     n_sub = min(64, n_obs)
     t0 = _t.perf_counter()
@@ -498,7 +501,19 @@ def run_inverse(ens, walker, n_obs):
                         'surrogate_path_err_median_same_subset': float(np.median(err[:n_sub])),
                         'seconds_per_retrieval': t_mc / n_sub, 'brf_evals': evals},
             'speedup_per_retrieval_vs_mc': (t_mc / n_sub) / (t_sur / n_obs),
-            'seconds_obs_generation': t_obs}
+            'seconds_obs_generation': t_obs,
+            'criterion': 'BRF ensemble spread > 2%',
+            'r_eff_criterion': {
+                'criterion': 'ensemble spread of the retrieved r_eff > 2%',
+                'flagged_for_mc': float(res_r['flagged'].mean()),
+                'r_eff_rel_err': {'median': float(np.median(err_r)), 'p90': float(np.percentile(err_r, 90))},
+                'r_eff_rel_err_unflagged_median':
+                    float(np.median(err_r[~res_r['flagged']])) if np.any(~res_r['flagged']) else None,
+                'r_eff_rel_err_flagged_median':
+                    float(np.median(err_r[res_r['flagged']])) if np.any(res_r['flagged']) else None,
+                'seconds': {'surrogate_gn': res_r['seconds_net'], 'mc_fallback': res_r['seconds_mc']},
+                'brf_evals_mc_fallback': res_r['mc_brf_evals'],
+                'spread_r_eff_median': float(np.median(res_r['spread_r_eff']))}}
 
 
 def run_reference(args):

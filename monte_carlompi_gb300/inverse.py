@@ -4,10 +4,14 @@ Given observed 648-bin BRFs with known wavelength, incident zenith and depth,
 find r_eff.  Each iteration evaluates the ensemble and the Jacobian
 d BRF / d log r_eff in forward mode through the surrogate's tensor-core kernels
 (`surrogate.forward_tangent`: the input is one scalar, so one tangent pass replaces a
-backward pass per output bin).  Retrievals whose ensemble spread at the
-solution exceeds ``spread_tol`` fall back to plain Monte Carlo: the same
-Gauss-Newton iteration with BRFs and central-difference Jacobians from the GPU
-walk.  The reference has no inverse; this consumes the same BRF definition
+backward pass per output bin).  Retrievals whose ensemble spread at the solution
+exceeds ``spread_tol`` fall back to plain Monte Carlo: the same Gauss-Newton
+iteration with BRFs and central-difference Jacobians from the GPU walk.  The spread
+is either that of the members' BRFs (criterion 'brf': weighted RMS of their standard
+deviation over the weighted RMS BRF) or that of the retrieved quantity (criterion
+'r_eff': each member's BRF, taken through the Gauss-Newton normal equation at the
+solution, gives the log r_eff that member would move the answer to; their standard
+deviation is the surrogate's own relative uncertainty in r_eff).  The reference has no inverse; this consumes the same BRF definition
 (post_processing.py:73-81, 2-D form).
 """
 import math
@@ -61,9 +65,19 @@ def _gn_update(f, jac, obs, s, w, damping=1e-3, max_step=0.7):
     return np.clip(s + step, LOG_R[0], LOG_R[1])
 
 
+def logr_spread(f_members, jac, w):
+    """Standard deviation over the members of the log r_eff shift that takes the
+    ensemble-mean BRF to each member's BRF, linearised at the solution:
+    ds_m = sum_b w_b J_b (f_mb - mean_b) / sum_b w_b J_b^2.  f_members [M, n, bins],
+    jac [n, bins] (d BRF / d log r), w [1, bins] or [bins]."""
+    dev = f_members - f_members.mean(0, keepdims=True)
+    ds = (w * jac * dev).sum(2) / np.maximum((w * jac * jac).sum(1), 1e-300)
+    return ds.std(0)
+
+
 def surrogate_gn(ens, obs, known, iters=6):
     """Gauss-Newton on s = log r_eff through the surrogate; starts from the best of a
-    16-point grid.  Returns (s, brf at s, ensemble spread at s)."""
+    16-point grid.  Returns (s, brf at s, BRF spread at s, log r_eff spread at s)."""
     n = obs.shape[0]
     w = S.bin_weights()[None, :]
     grid = np.linspace(LOG_R[0], LOG_R[1], 16)
@@ -79,7 +93,9 @@ def surrogate_gn(ens, obs, known, iters=6):
         f, jac = _brf_and_jacobian(ens, s, known)
         s = _gn_update(f, jac, obs, s, w)
     pred, _, spread = ens.predict(np.column_stack([np.exp(s), known]))
-    return s, pred, spread
+    _, jac = _brf_and_jacobian(ens, s, known)
+    members, _ = ens.predict_members(np.column_stack([np.exp(s), known]))
+    return s, pred, spread, logr_spread(members, jac, w)
 
 
 def mc_gn(walker, obs, known, s0, n_photon=1000000, iters=3, h=0.05, seed=0x5EED0055):
@@ -111,12 +127,16 @@ def mc_retrieve(walker, obs, known, grid=16, iters=4, n_photon=1000000, seed=0x5
     return s, evals + rows.shape[0]
 
 
-def retrieve(ens, walker, obs, known, spread_tol=0.02, mc_photons=1000000):
-    """Surrogate retrieval with Monte Carlo fallback.  Returns dict of results and timings."""
+def retrieve(ens, walker, obs, known, spread_tol=0.02, mc_photons=1000000, criterion='brf'):
+    """Surrogate retrieval with Monte Carlo fallback where the ensemble spread exceeds
+    spread_tol: of the BRF (criterion 'brf') or of r_eff (criterion 'r_eff').  Returns
+    dict of results and timings."""
+    if criterion not in ('brf', 'r_eff'):
+        raise ValueError("criterion must be 'brf' or 'r_eff'")
     t0 = time.perf_counter()
-    s, _, spread = surrogate_gn(ens, obs, known)
+    s, _, spread, spread_r = surrogate_gn(ens, obs, known)
     t_net = time.perf_counter() - t0
-    flagged = spread > spread_tol
+    flagged = (spread if criterion == 'brf' else spread_r) > spread_tol
     t0 = time.perf_counter()
     mc_evals = 0
     if np.any(flagged):
@@ -124,5 +144,5 @@ def retrieve(ens, walker, obs, known, spread_tol=0.02, mc_photons=1000000):
         s = s.copy()
         s[flagged] = s_mc
     t_mc = time.perf_counter() - t0
-    return dict(r_eff=np.exp(s), flagged=flagged, spread=spread, seconds_net=t_net, seconds_mc=t_mc,
-                mc_brf_evals=mc_evals)
+    return dict(r_eff=np.exp(s), flagged=flagged, spread=spread, spread_r_eff=spread_r, seconds_net=t_net,
+                seconds_mc=t_mc, mc_brf_evals=mc_evals, criterion=criterion)

@@ -369,8 +369,8 @@ class Ensemble:
     def __init__(self, members):
         self.members = members
 
-    def predict(self, raw):
-        """Mean BRF [n, 648], mean albedo [n], relative ensemble spread of the BRF [n]."""
+    def predict_members(self, raw):
+        """Each member's BRF [members, n, 648] and albedo [members, n]."""
         import torch
         x = torch.from_numpy(encode(*np.asarray(raw, np.float64).T)).cuda()
         outs = []
@@ -379,7 +379,11 @@ class Ensemble:
             outs.append(ys.cpu().numpy())
         outs = np.stack(outs)
         brfs, albs = zip(*[from_target(o) for o in outs])
-        brfs, albs = np.stack(brfs), np.stack(albs)
+        return np.stack(brfs), np.stack(albs)
+
+    def predict(self, raw):
+        """Mean BRF [n, 648], mean albedo [n], relative ensemble spread of the BRF [n]."""
+        brfs, albs = self.predict_members(raw)
         mean_brf = brfs.mean(0)
         w = bin_weights()
         # member spread in the units of rel_rms: weighted RMS std over weighted RMS BRF

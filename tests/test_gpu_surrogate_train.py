@@ -76,7 +76,8 @@ def test_gauss_newton_recovers_r_eff_on_network_brfs(trained):
     raw = surrogate.sample_inputs(64, 303)
     raw[:, 1] = rng.uniform(1.4, 1.8, 64)          # absorbing wavelengths: r_eff is well constrained
     obs, _, _ = ens.predict(raw)
-    s, _, _ = inverse.surrogate_gn(ens, obs, raw[:, 1:])
+    s, _, spread, spread_r = inverse.surrogate_gn(ens, obs, raw[:, 1:])
     err = np.abs(np.exp(s) / raw[:, 0] - 1)
     assert np.median(err) < 0.01, np.median(err)
     assert np.all(np.isfinite(s)) and np.all(s >= math.log(50) - 1e-9)
+    assert np.all(np.isfinite(spread)) and np.all(np.isfinite(spread_r)) and np.all(spread_r >= 0)
