@@ -12,6 +12,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, '_lib', 'libmcwalk.so')
 
 MCW_OK = 0
+ABI_VERSION = 3          # MCW_ABI_VERSION of include/mcwalk.h these bindings follow
 ERRORS = {-1: 'MCW_ERR_ARG', -2: 'MCW_ERR_CUDA', -3: 'MCW_ERR_BUDGET', -4: 'MCW_ERR_STREAM',
           -5: 'MCW_ERR_OOM', -6: 'MCW_ERR_STATE'}
 MODE_F32 = 0
@@ -190,6 +191,9 @@ def load(path=None):
         f = getattr(L, name)
         f.argtypes = args
         f.restype = res
+    if L.mcw_abi_version() != ABI_VERSION:
+        raise RuntimeError('%s has ABI version %d, these bindings need %d; rebuild it with '
+                           '`python -m monte_carlompi_gb300.build`' % (p, L.mcw_abi_version(), ABI_VERSION))
     if path is None:
         _lib = L
     return L

@@ -34,6 +34,14 @@ def test_version():
     assert b'sm_103a' in L.mcw_version()
 
 
+def test_bindings_follow_the_header_abi_version():
+    """The ctypes bindings state the header's MCW_ABI_VERSION, and loading refuses a
+    library of another version (checked when the library is loaded)."""
+    hdr = open(os.path.join(os.path.dirname(__file__), '..', 'include', 'mcwalk.h')).read()
+    m = re.search(r'#define MCW_ABI_VERSION (\d+)', hdr)
+    assert m and int(m.group(1)) == _abi.ABI_VERSION
+
+
 def test_create_without_gpu_fails_cleanly():
     try:
         import torch
