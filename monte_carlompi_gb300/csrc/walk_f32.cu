@@ -44,8 +44,11 @@
 //  * absorption tests 1 - u < 1 - ssa on a 32-bit uniform, so small
 //    co-albedos (1e-6) are resolved; likewise the species test;
 //  * the azimuth is uniform on (-pi, pi) instead of (0, 2 pi);
-//  * the direction is renormalised after every rotation and the pole branch
-//    (:1262-1269) is taken for |mu_z| > 0.99999 instead of |mu_z| == 1;
+//  * the direction is renormalised once per 4-step round (and at the end of
+//    every block pass) and the pole branch (:1262-1269) is taken for
+//    |mu_z| > 0.99999 instead of |mu_z| == 1;
+//  * past kBlockWalk steps the directions are composed in a moving frame
+//    (block passes) instead of the z-referenced rotation formula (:1270-1281);
 //  * phi_n = atan2(mu_y, mu_x) mapped to [0, 2 pi) (the quadrant arctan of
 //    :1472-1485, defined on the axes too).
 #include <cuda_runtime.h>
