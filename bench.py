@@ -524,9 +524,9 @@ def run_reference(args):
     from oracle import oracle
     if not os.path.exists(oracle.LIB_PATH):
         oracle.build()
-    n = 100000
-    for _ in range(args.warmup):
-        oracle_sample(20000, cores, seed=SEED + 7)
+    n = N_PER_GPU   # the whole workload each step (about 0.2-0.3 s on 16 cores)
+    for k in range(args.warmup):
+        oracle_sample(20000, cores, seed=SEED + 7 + k)
     times, events = [], 0
     for k in range(args.steps):
         dt, ev = oracle_sample(n, cores, seed=SEED + k)
@@ -539,12 +539,14 @@ def run_reference(args):
         'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': 1e3 * tot / args.steps, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-        'config': dict(CONFIG_DESC, sample_photons_per_step=n,
+        'config': dict(CONFIG_DESC, photons_per_step=n,
                        mode='FP64 replay stream of the reference algorithm (C oracle on the host cores)'),
         'scatter_events_per_s': events / tot,
         'cpu_baseline': {'value': value, 'unit': 'photons/s', 'cores': cores, 'kind': 'port',
-                         'sample': '%d photons per step of the workload (FP64 C oracle, '
-                                   '%d threads)' % (n, cores)},
+                         'sample': 'all %d photons of the workload each step (FP64 C oracle, '
+                                   '%d threads, np.array_split shares as parallelize.py:14-15)' % (n, cores),
+                         'python_reference': 'not run: the reference is a Python checkout without an '
+                                             'installer and is absent on the GPU host'},
         'e2e': {'value': value, 'unit': 'photons/s', 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': 0},
     }
@@ -582,23 +584,41 @@ def run_ours(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    def step():
-        return w.walk([cfg], SEED, mode='f32', records='device', device_ptr=dev_records.data_ptr())
+    def step(seed):
+        return w.walk([cfg], seed, mode='f32', records='device', device_ptr=dev_records.data_ptr())
 
-    for _ in range(args.warmup):
-        step()
+    for k in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step(SEED + 1000 + k)
+    # host wall time of one walk (with its flush), to size the timed region
+    t0 = time.perf_counter()
+    for k in range(10):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step(SEED + 1100 + k)
+    wall_per_walk = (time.perf_counter() - t0) / 10
+    # inner repeats: each timed step walks the 1e6 photons `repeats` times (a new seed
+    # and an L2 flush before each walk), so that the timed region lasts about 2 s and
+    # the clock sampler sees it under load
+    repeats = args.repeats or max(1, int(np.ceil(2.5 / max(1e-5, wall_per_walk * args.steps))))
+    if world > 1:
+        rt = torch.tensor([repeats], device='cuda')
+        torch.distributed.all_reduce(rt, op=torch.distributed.ReduceOp.MAX)
+        repeats = int(rt.item())
     clocks = Clocks(dev)
     clocks.start()
     barrier()
     dev_ms, kern_ms, events, launches = [], [], 0, 0
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        r = step()
-        dev_ms.append(r.stats['device_ms'])
-        kern_ms.append(r.stats['kernel_ms'])
-        events += r.stats['n_events']
-        launches += kernels_per_walk
+    for k in range(args.steps):
+        for j in range(repeats):
+            flush.zero_()
+            torch.cuda.synchronize()
+            r = step(SEED + k * repeats + j)
+            dev_ms.append(r.stats['device_ms'])
+            kern_ms.append(r.stats['kernel_ms'])
+            events += r.stats['n_events']
+            launches += kernels_per_walk
     barrier()
     clk = clocks.stop()
     t_dev = sum(dev_ms) / 1e3
@@ -611,15 +631,16 @@ def run_ours(args):
     _abi.check(_abi.load().mcw_host_alloc(n * RECORD_BYTES, ctypes.byref(host_ptr)), what='host alloc')
     host_buf = (ctypes.c_char * (n * RECORD_BYTES)).from_address(host_ptr.value)
     host_rec = np.frombuffer(host_buf, dtype=_abi.RECORD32, count=n)
-    for _ in range(max(1, args.warmup)):
-        w.walk([cfg], SEED, mode='f32', records='host', out=host_rec)
+    for k in range(max(1, args.warmup)):
+        w.walk([cfg], SEED + 2000 + k, mode='f32', records='host', out=host_rec)
     barrier()
     e2e_t, h2d, d2h = [], 0, 0
-    for _ in range(args.steps):
+    e2e_calls = args.steps * min(repeats, 20)
+    for k in range(e2e_calls):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = w.walk([cfg], SEED, mode='f32', records='host', out=host_rec)
+        r = w.walk([cfg], SEED + 3000 + k, mode='f32', records='host', out=host_rec)
         e2e_t.append(time.perf_counter() - t0)
         h2d, d2h = r.stats['h2d_bytes'], r.stats['d2h_bytes']
     barrier()
@@ -634,13 +655,14 @@ def run_ours(args):
         local_stats[:3] = t.cpu().numpy()
         local_stats[3] = float(ev.item())
     t_dev, t_kern, t_e2e, events_all = local_stats
-    photons_all = N_PER_GPU * world * args.steps
+    walks = args.steps * repeats
+    photons_all = N_PER_GPU * world * walks
     value = photons_all / t_dev
     if rank == 0:
         peaks, src = measured_peaks()
         sm_max = float(peaks.get('sm_max_mhz') or 2070.0)
-        ev_per_launch = events_all / args.steps / world
-        kern_s = t_kern / args.steps
+        ev_per_launch = events_all / walks / world
+        kern_s = t_kern / walks
         achieved = ev_per_launch * ALG_INST_PER_EVENT / kern_s / 1e12
         peak = 152 * 4 * 32 * sm_max * 1e6 / 1e12
         rec_gbs = (n * RECORD_BYTES) / kern_s / 1e9
@@ -649,13 +671,23 @@ def run_ours(args):
             'metric': METRIC, 'value': value, 'unit': 'photons/s', 'n_gpus': world,
             'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1e3 * t_dev / args.steps,
             'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-            'data': 'synthetic', 'config': dict(CONFIG_DESC, parallelism='replicas x%d' % world, launch=tuned),
+            'data': 'synthetic',
+            'config': dict(CONFIG_DESC, parallelism='replicas x%d' % world, launch=tuned,
+                           walks_per_step=repeats,
+                           step='%d walks of the 1e6 photons, each with its own seed and an L2 flush '
+                                'before it' % repeats,
+                           lookup_table='built by the first walk of a config and reused while the '
+                                        'configs and SSP tables are unchanged (mcw_walk)'),
+            'ms_per_walk': 1e3 * t_dev / walks,
             'scatter_events_per_s': events_all / t_dev,
-            'kernel_ms_per_step': 1e3 * kern_s,
+            'kernel_ms_per_walk': 1e3 * kern_s,
             'clocks': clk,
             'gpu_launches': launches,
-            'e2e': {'value': photons_all / t_e2e, 'unit': 'photons/s',
-                    'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
+            'e2e': {'value': N_PER_GPU * world * e2e_calls / t_e2e, 'unit': 'photons/s',
+                    'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
+                    'calls': e2e_calls,
+                    'path': 'Walker.walk -> mcw_walk, records written into pinned host memory, '
+                            'tallies copied back; host wall clock per call'},
             'roofline': {
                 'bound': 'issue', 'achieved': achieved, 'peak': peak, 'unit': 'Tinst/s',
                 'frac': achieved / peak,
@@ -684,6 +716,8 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--repeats', type=int, default=0,
+                    help='walks per timed step (0: enough for about 2 s of timed work)')
     ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol', 'lone'])
     ap.add_argument('--surrogate-configs', type=int, default=16384)
     ap.add_argument('--surrogate-epochs', type=int, default=300)

@@ -257,7 +257,10 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice,
  * P44.dat reads of get_aspherical_SSPs (monte_carlo3D.py:145-171, :267-475). */
 int mcw_set_phase_matrices(mcw_ctx *ctx, const mcw_phase_table *tabs, int32_t n);
 
-/* Launch shape and time budget of later walks. */
+/* Launch shape and time budget of later walks.  The budget of a new context
+ * (and of every mcw_walk_noalloc call) is MCW_DEFAULT_BUDGET_S: a walk still
+ * running after it stops, and the call returns MCW_ERR_BUDGET. */
+#define MCW_DEFAULT_BUDGET_S 300.0
 int mcw_set_launch(mcw_ctx *ctx, const mcw_launch *launch);
 int mcw_get_launch(const mcw_ctx *ctx, mcw_launch *launch);
 int mcw_set_budget(mcw_ctx *ctx, double seconds);
@@ -350,9 +353,12 @@ int mcw_post(mcw_ctx *ctx, const void *records, int32_t records_where, int32_t m
  * (about 107 KB per GPU, held until the process exits) shared by all calls on
  * a device, so calls that overlap on the GPU race; the first call on a device
  * resolves the array's address and should come before any stream capture.
- * Sizes beyond MCW_NOALLOC_MAX_LUT and unsorted tables return MCW_ERR_ARG.
+ * Sizes beyond MCW_NOALLOC_MAX_LUT return MCW_ERR_ARG; so do tables whose
+ * wavelengths are not strictly ascending, whose values are not finite, or
+ * whose ice extinction is not > 0 (checked on the device before the walk
+ * starts).  The time budget is MCW_DEFAULT_BUDGET_S (MCW_ERR_BUDGET).
  * Same records and tally as mcw_walk with one config and this seed.
- * Synchronises the stream before returning. */
+ * Synchronises the stream twice (after the table check and at the end). */
 int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_dev, const mcw_ssp_table *imp_dev,
                      uint64_t seed, mcw_record32 *records_dev, mcw_tally *tally_dev, void *stream);
 

@@ -22,6 +22,8 @@ MODE_POL32 = 3
 RECORDS_NONE, RECORDS_HOST, RECORDS_DEVICE = 0, 1, 2
 HIST_NTHETA, HIST_NPHI, HIST_BINS = 18, 36, 648
 WVN_FX_SCALE = 4294967296.0
+NOALLOC_MAX_LUT = 2048       # MCW_NOALLOC_MAX_LUT: wavelength grid points of mcw_walk_noalloc
+DEFAULT_BUDGET_S = 300.0     # MCW_DEFAULT_BUDGET_S: time budget of a new context
 
 # names every build of the library must export (the entry points of mcwalk.h)
 EXPORTS = ['mcw_abi_version', 'mcw_version', 'mcw_create', 'mcw_destroy', 'mcw_last_error',

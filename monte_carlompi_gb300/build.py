@@ -18,6 +18,9 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, 'csrc')
 BUILD = os.path.join(PKG, '_build')
+if os.environ.get('MCW_DEFINES'):
+    BUILD = os.path.join(PKG, '_build', 'defines_' + ''.join(
+        c if c.isalnum() else '_' for c in os.environ['MCW_DEFINES']))
 LIBDIR = os.path.join(PKG, '_lib')
 LIB = os.path.join(LIBDIR, 'libmcwalk.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -26,6 +29,9 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NO_FMAD = {'walk_replay.cu', 'ssp_lut.cu'}
 # the FP32 production walk: flush denormals, approximate division and square root
 FAST_F32 = {'walk_f32.cu': ['-ftz=true', '-prec-div=false', '-prec-sqrt=false']}
+# tuning builds: extra -D flags for the CUDA units (e.g. MCW_DEFINES="-DMCW_BLOCK_WALK=128");
+# objects of such a build go to a directory of their own
+DEFINES = os.environ.get('MCW_DEFINES', '').split()
 
 
 def nvcc():
@@ -52,7 +58,7 @@ def _compile(src, verbose):
     if not _stale(obj, src):
         return obj, None
     if name.endswith('.cu'):
-        cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
+        cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', *DEFINES, '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
         if name in NO_FMAD:
             cmd.insert(-4, '--fmad=false')
         for flag in FAST_F32.get(name, []):
@@ -84,11 +90,16 @@ def build(force=False, verbose=False):
         for _, log in results:
             if log:
                 print(log, file=sys.stderr)
-    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+    stamp = LIB + '.objdir'     # which object directory the library was linked from
+    same_dir = os.path.exists(stamp) and open(stamp).read() == BUILD
+    if force or not same_dir or not os.path.exists(LIB) or \
+            any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [nvcc(), *ARCH, '-shared', '-o', LIB, *objs, '-lpthread']
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError('link failed: %s\n%s%s' % (' '.join(cmd), r.stdout, r.stderr))
+        with open(stamp, 'w') as f:
+            f.write(BUILD)
     return LIB
 
 

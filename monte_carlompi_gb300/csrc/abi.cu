@@ -106,8 +106,13 @@ struct mcw_ctx {
     DevBuf cfgs, lut, tallies, counters, records, post, drain;
     HostBuf h_stage, h_tallies, h_counters;
     int32_t max_ice_n = 0;
+    // the plan (configs + prefix bytes) whose lookup table ctx->lut holds, for
+    // the tables of version tables_version; empty when none does
+    std::vector<unsigned char> lut_plan;
+    uint64_t tables_version = 0, lut_tables_version = 0;
+    void *lut_cfgs_ptr = nullptr, *lut_ptr = nullptr;
     mcw_launch launch{256, 0, 8, 4096};
-    double budget_s = 300.0;
+    double budget_s = MCW_DEFAULT_BUDGET_S;
 };
 
 struct mcw_graph {
@@ -304,9 +309,20 @@ int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBu
     return MCW_OK;
 }
 
+// The plan's bytes as uploaded (configs, then prefix): equal bytes and equal
+// tables give an equal lookup table.
+std::vector<unsigned char> plan_bytes(const Plan &plan) {
+    const size_t bc = plan.cfgs.size() * sizeof(DevConfig), bp = plan.prefix.size() * sizeof(int64_t);
+    std::vector<unsigned char> v(bc + bp);
+    memcpy(v.data(), plan.cfgs.data(), bc);
+    memcpy(v.data() + bc, plan.prefix.data(), bp);
+    return v;
+}
+
 LutArgs lut_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBuf &tallies,
                  DevBuf &counters) {
     LutArgs la;
+    la.clear_only = 0;
     la.cfgs = (const DevConfig *)cfgs.p;
     la.n_cfg = (int32_t)plan.cfgs.size();
     la.stage_doubles = ctx->max_ice_n + ctx->imp.n;
@@ -426,6 +442,7 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
             if (!std::isfinite(t.wvl[i]) || !std::isfinite(t.ss_alb[i]) || !std::isfinite(t.ext_cff_mss[i]))
                 return "non-finite table value";
             if (need_asm && !std::isfinite(t.asm_prm[i])) return "non-finite table value";
+            if (need_asm && !(t.ext_cff_mss[i] > 0)) return "ice extinction must be > 0";
         }
         return nullptr;
     };
@@ -499,6 +516,7 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     for (int32_t i = 0; i < n_ice; ++i) order_of(ice[i], ctx->ice_order[i]);
     ctx->phase_rows.assign(n_ice, 0);   // phase matrices belong to the previous tables
     ctx->have_tables = true;
+    ctx->tables_version++;
     return MCW_OK;
 }
 
@@ -699,22 +717,49 @@ int mcw_walk(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, uint64_t seed,
     Shape shape{0, 0, 0, 0};
     if (mode == MCW_MODE_F32) shape = pick_shape(ctx, ctx->launch, plan);
     uint64_t h2d = 0;
-    rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
-    if (rc) return rc;
+    // a call on the configs and tables of the previous F32 / POL32 call finds their
+    // launch data and lookup table in place: no upload, and the lookup-table kernel
+    // only clears the counters and tallies
+    const bool lut_mode = (mode == MCW_MODE_F32 || mode == MCW_MODE_POL32);
+    std::vector<unsigned char> pb;
+    if (lut_mode) pb = plan_bytes(plan);
+    const bool cached = lut_mode && !ctx->lut_plan.empty() && ctx->lut_tables_version == ctx->tables_version &&
+                        ctx->lut_cfgs_ptr == ctx->cfgs.p && ctx->lut_ptr == ctx->lut.p && ctx->lut_plan == pb;
+    if (cached) {
+        CUDA_TRY(ctx, ctx->tallies.ensure((size_t)n_cfg * sizeof(mcw_tally)));
+        CUDA_TRY(ctx, ctx->counters.ensure(sizeof(Counters)));
+        CUDA_TRY(ctx, cudaEventRecord(ctx->evs, st));
+    } else {
+        ctx->lut_plan.clear();   // the upload below replaces the launch data
+        rc = upload_plan(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters, st, ctx->evs, &h2d);
+        if (rc) return rc;
+    }
+    auto lut_launch = [&]() -> int {
+        LutArgs la = lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters);
+        la.clear_only = cached ? 1 : 0;
+        CUDA_TRY(ctx, launch_lut(la, st));
+        if (!cached) {
+            ctx->lut_plan = pb;
+            ctx->lut_tables_version = ctx->tables_version;
+            ctx->lut_cfgs_ptr = ctx->cfgs.p;
+            ctx->lut_ptr = ctx->lut.p;
+        }
+        return MCW_OK;
+    };
     if (mode == MCW_MODE_F32) {
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, shape.chunk, seed);
         rc = attach_drain(ctx, wa, ctx->drain, shape);
         if (rc) return rc;
         // the lookup-table kernel also clears the counters and tallies
-        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
+        if ((rc = lut_launch())) return rc;
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, st));
         if (plan.total > 0)
             CUDA_TRY(ctx, launch_walk_f32(wa, plan.impurity, shape.grid, shape.block, ctx->sm_count, st));
         CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, st));
     } else if (mode == MCW_MODE_POL32) {
         // the lookup-table kernel also clears the counters and tallies
-        CUDA_TRY(ctx, launch_lut(lut_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters), st));
+        if ((rc = lut_launch())) return rc;
         WalkArgs wa = walk_args(ctx, plan, ctx->cfgs, ctx->lut, ctx->tallies, ctx->counters,
                                 (mcw_record32 *)dev_records, 1, seed);
         wa.phase = (const DevPhase32 *)ctx->phase_tables32.p;

@@ -165,6 +165,7 @@ struct LutArgs {
     const DevTable *ice;
     mcw_tally *tallies;          // n_cfg tallies to clear, or null
     uint32_t *counters;          // work counter and status to clear, or null
+    int32_t clear_only;          // 1: clear tallies and counters, leave the table as it is
 };
 
 // Why a config is invalid (nullptr when valid); n_ice = number of ice tables.

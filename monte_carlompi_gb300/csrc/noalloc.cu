@@ -16,7 +16,14 @@
 // the GPU (two streams, or two threads) race on it: serialise them.  The
 // first call on a device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call
-// before any stream capture.
+// before any stream capture.  Later calls look the address up again unless
+// their stream is capturing, so a device reset between calls is harmless.
+//
+// The caller's tables are checked on the device (ascending, distinct and
+// finite wavelengths, finite values, ice extinction > 0) by the set-up kernel,
+// and the call returns MCW_ERR_ARG before the lookup-table and walk kernels
+// are launched when they fail.  The walk's time budget is the library's
+// default, MCW_DEFAULT_BUDGET_S.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -53,11 +60,19 @@ static __device__ __align__(256) unsigned char g_scratch[sizeof(NoAllocScratch)]
 std::mutex g_mu;
 NoAllocScratch *g_ptr[kMaxDevices] = {};
 
+// One table column entry is usable: finite (and > 0 where positive is required).
+__device__ __forceinline__ bool entry_ok(const double *col, int i, bool positive) {
+    const double v = col[i];
+    return isfinite(v) && (!positive || v > 0.0);
+}
+
 // Fill the scratch for this call from kernel parameters: zero the counters
 // (and the caller's tally), store the config and table descriptors, and check
-// that the tables are strictly increasing (the device lookups binary-search).
+// the tables as mcw_set_tables checks host tables: finite values, strictly
+// increasing wavelengths (the device lookups binary-search), and an ice
+// extinction > 0 (its reciprocal sets the path length).
 __global__ void noalloc_setup(NoAllocScratch *s, const DevConfig cfg, const DevTable ice, const DevTable imp,
-                              int lut_n, mcw_tally *tally) {
+                              mcw_tally *tally) {
     const int t = threadIdx.x;
     if (t == 0) {
         s->counters.work = 0;
@@ -72,19 +87,33 @@ __global__ void noalloc_setup(NoAllocScratch *s, const DevConfig cfg, const DevT
     for (int i = t; i < (int)(sizeof(mcw_tally) / 4); i += blockDim.x) tw[i] = 0u;
     __syncthreads();
     bool bad = false;
-    for (int i = t + 1; i < ice.n; i += blockDim.x) bad |= !(ice.wvl[i] > ice.wvl[i - 1]);
-    for (int i = t + 1; i < imp.n; i += blockDim.x) bad |= !(imp.wvl[i] > imp.wvl[i - 1]);
+    for (int i = t; i < ice.n; i += blockDim.x) {
+        bad |= !(entry_ok(ice.wvl, i, false) && entry_ok(ice.ssa, i, false) && entry_ok(ice.ext, i, true) &&
+                 entry_ok(ice.asm_, i, false));
+        if (i > 0) bad |= !(ice.wvl[i] > ice.wvl[i - 1]);
+    }
+    for (int i = t; i < imp.n; i += blockDim.x) {
+        bad |= !(entry_ok(imp.wvl, i, false) && entry_ok(imp.ssa, i, false) && entry_ok(imp.ext, i, false));
+        if (i > 0) bad |= !(imp.wvl[i] > imp.wvl[i - 1]);
+    }
     if (bad) atomicOr(&s->counters.bad_table, 1u);
 }
 
-int scratch_for_device(int dev, NoAllocScratch **out) {
+// Device address of g_scratch on the current device.  Resolved on every call
+// whose stream is not capturing (cudaGetSymbolAddress allocates nothing), so a
+// context torn down and recreated between calls gets the new address; a call
+// made during capture uses the address of the last call outside it.
+int scratch_for_device(int dev, cudaStream_t st, NoAllocScratch **out) {
     if (dev < 0 || dev >= kMaxDevices) return MCW_ERR_ARG;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const bool capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone;
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_ptr[dev]) {
+    if (!capturing) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return MCW_ERR_CUDA;
         g_ptr[dev] = static_cast<NoAllocScratch *>(p);
     }
+    if (!g_ptr[dev]) return MCW_ERR_STATE;   // first call on this device made during a capture
     *out = g_ptr[dev];
     return MCW_OK;
 }
@@ -159,12 +188,19 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return MCW_ERR_CUDA;
     NoAllocScratch *s = nullptr;
-    int rc = scratch_for_device(dev, &s);
+    int rc = scratch_for_device(dev, st, &s);
     if (rc) return rc;
     mcw_tally *tally = tally_dev ? tally_dev : &s->tally;
 
-    noalloc_setup<<<1, 256, 0, st>>>(s, d, ice, imp, d.lut_n, tally);
+    noalloc_setup<<<1, 256, 0, st>>>(s, d, ice, imp, tally);
     if (cudaGetLastError() != cudaSuccess) return MCW_ERR_CUDA;
+    // tables are checked before anything reads them
+    unsigned int bad_table = 0;
+    if (cudaMemcpyAsync(&bad_table, &s->counters.bad_table, sizeof(bad_table), cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+        return MCW_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return MCW_ERR_CUDA;
+    if (bad_table) return MCW_ERR_ARG;
     LutArgs la;
     la.cfgs = &s->cfg;
     la.n_cfg = 1;
@@ -176,6 +212,7 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     la.ice = &s->ice;
     la.tallies = nullptr;   // cleared by noalloc_setup
     la.counters = nullptr;
+    la.clear_only = 0;
     if (launch_lut(la, st) != cudaSuccess) return MCW_ERR_CUDA;
     if (c.n_photon > 0) {
         WalkArgs wa{};   // no drain handover: its queue would need an allocation
@@ -189,7 +226,7 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
         wa.status = &s->counters.status;
         wa.records = records_dev;
         wa.tallies = tally;
-        wa.budget_ns = 300ull * 1000000000ull;
+        wa.budget_ns = (unsigned long long)(MCW_DEFAULT_BUDGET_S * 1e9);
         wa.keys = philox_schedule(seed);
         int sms = 0;
         if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return MCW_ERR_CUDA;
@@ -204,7 +241,6 @@ extern "C" int mcw_walk_noalloc(const mcw_config *cfg, const mcw_ssp_table *ice_
     NoAllocCounters h;
     if (cudaMemcpyAsync(&h, &s->counters, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess) return MCW_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return MCW_ERR_CUDA;
-    if (h.bad_table) return MCW_ERR_ARG;
     if (h.status & kStatusBudget) return MCW_ERR_BUDGET;
     return MCW_OK;
 }

@@ -18,7 +18,8 @@ namespace {
 
 // One block per config: clears the call's counters and the config's tally
 // (they must start at zero), stages the wavelength columns of its tables in
-// shared memory when they fit, then fills the config's grid points.
+// shared memory when they fit, then fills the config's grid points (unless
+// clear_only: a repeated call on the same configs and tables).
 __global__ void lut_kernel(const LutArgs a) {
     extern __shared__ double s_wvl[];
     const int ci = blockIdx.x;
@@ -29,6 +30,7 @@ __global__ void lut_kernel(const LutArgs a) {
     }
     if (a.counters && ci == 0)
         for (int i = threadIdx.x; i < a.counters_words; i += blockDim.x) a.counters[i] = 0u;
+    if (a.clear_only) return;   // the table of these configs is already in place
     DevTable ice = a.ice[c.ice_table];
     DevTable imp = a.imp;
     if (a.stage) {
@@ -62,7 +64,7 @@ __global__ void lut_kernel(const LutArgs a) {
 
 cudaError_t launch_lut(const LutArgs &a, cudaStream_t s) {
     if (a.n_cfg <= 0) return cudaSuccess;
-    const size_t smem = a.stage ? (size_t)a.stage_doubles * sizeof(double) : 0;
+    const size_t smem = (a.stage && !a.clear_only) ? (size_t)a.stage_doubles * sizeof(double) : 0;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(lut_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

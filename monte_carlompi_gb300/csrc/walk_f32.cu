@@ -38,15 +38,21 @@
 // needs them.  Results depend only on (seed, photon stream id): any launch
 // shape, any number of GPUs or replicas gives the same records.
 //
-// Statistically equivalent restatements (identical distributions):
+// Restatements whose distributions equal the reference's in exact arithmetic
+// (the FP32 walk then differs from it by rounding and by the resolution of its
+// draws: 2^-23 for the angle uniforms, 2^-32 for the path and absorption ones):
 //  * the Lambertian direction (p(theta) ~ sin 2 theta, :1238-1250) is drawn by
 //    inversion, cos theta = sqrt(u), instead of rejection;
 //  * absorption tests 1 - u < 1 - ssa on a 32-bit uniform, so small
 //    co-albedos (1e-6) are resolved; likewise the species test;
 //  * the azimuth is uniform on (-pi, pi) instead of (0, 2 pi);
+//  * the rotation (:1270-1281) takes sqrt(mu_x^2 + mu_y^2) where the reference
+//    writes sqrt(1 - mu_z^2): equal for a unit direction, and with it the
+//    rotation's frame stays orthogonal next to the pole, where 1 - mu_z^2 loses
+//    its digits in FP32.  The pole branch (:1262-1269) is taken when that
+//    horizontal part is exactly 0, the reference's mu_z == +-1;
 //  * the direction is renormalised once per 4-step round (and at the end of
-//    every block pass) and the pole branch (:1262-1269) is taken for
-//    |mu_z| > 0.99999 instead of |mu_z| == 1;
+//    every block pass), which only removes rounding drift;
 //  * past kBlockWalk steps the directions are composed in a moving frame
 //    (block passes) instead of the z-referenced rotation formula (:1270-1281);
 //  * phi_n = atan2(mu_y, mu_x) mapped to [0, 2 pi) (the quadrant arctan of
@@ -302,11 +308,22 @@ __device__ __forceinline__ float hg_cos(const float u1, const float hg_a, const 
 
 __device__ __forceinline__ float sin_of(const float ct) { return sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f))); }
 
+// Squared horizontal part of a direction, mu_x^2 + mu_y^2 (= 1 - mu_z^2 for a
+// unit direction).  0 exactly on the vertical: the pole case of the reference
+// (mu_z == +-1, monte_carlo3D.py:1262-1269); the kernel flushes denormals, so a
+// non-zero value is at least FLT_MIN and its reciprocal square root is finite.
+__device__ __forceinline__ float horiz2(const float mx, const float my) { return fmaf(mx, mx, __fmul_rn(my, my)); }
+constexpr float kFltMin = 1.17549435e-38f;
+
 // General rotation of direction m by polar cosine/sine (ct, st) and azimuth
-// (cp, sp) (monte_carlo3D.py:1270-1281), renormalised when `renorm`.
-__device__ __forceinline__ float3 rotate(const float mx, const float my, const float mz, const float ct,
-                                         const float st, const float cp, const float sp, const bool renorm) {
-    const float s2 = fmaxf(fmaf(-mz, mz, 1.f), 1e-12f);
+// (cp, sp) (monte_carlo3D.py:1270-1281), renormalised when `renorm`; s2 =
+// horiz2(mx, my).  With s = sqrt(s2) taken from m's own horizontal part, the
+// frame (m, (mx mz / s, my mz / s, -s), (-my / s, mx / s, 0)) is orthogonal and
+// its second vector is as long as m, however close m is to the vertical.
+__device__ __forceinline__ float3 rotate(const float mx, const float my, const float mz, const float s2in,
+                                         const float ct, const float st, const float cp, const float sp,
+                                         const bool renorm) {
+    const float s2 = fmaxf(s2in, kFltMin);
     const float rs = rsqrtf(s2);
     const float tq = __fmul_rn(st, rs);
     // x and y as pairs: (mx mz cp - my sp, my mz cp + mx sp), then tq * that + (mx ct, my ct)
@@ -360,9 +377,10 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     const float mx = lamb ? 0.f : P.mux;
     const float my = lamb ? 0.f : P.muy;
     const float mz = lamb ? 1.f : P.muz;
-    float3 g = rotate(mx, my, mz, ct, st, cp, sp, renorm);
-    // pole, taken for |mu_z| > 0.99999 (rare: a branch)
-    if (fabsf(mz) > 0.99999f) g = pole_dir(copysignf(1.f, mz), ct, st, cp, sp);
+    const float s2 = horiz2(mx, my);
+    float3 g = rotate(mx, my, mz, s2, ct, st, cp, sp, renorm);
+    // pole: the direction is exactly vertical (rare: a branch)
+    if (!(s2 > 0.f)) g = pole_dir(copysignf(1.f, mz), ct, st, cp, sp);
     const float nx = first ? mx : g.x;
     const float ny = first ? my : g.y;
     const float nz = first ? mz : g.z;
@@ -455,10 +473,11 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     // depends on the previous step's bottom test): a Lambertian direction is the
     // pole case of mu = (0, 0, 1) and is selected afterwards, so only that select
     // sits on the chain between steps.  Same values as step().
-    const float3 g = rotate(P.mux, P.muy, P.muz, s.ct_hg, s.st_hg, s.cp, s.sp, renorm);
+    const float s2 = horiz2(P.mux, P.muy);
+    const float3 g = rotate(P.mux, P.muy, P.muz, s2, s.ct_hg, s.st_hg, s.cp, s.sp, renorm);
     const float3 pd = pole_dir(copysignf(1.f, P.muz), s.ct_hg, s.st_hg, s.cp, s.sp);
     const float3 ld = pole_dir(1.f, s.ct_l, s.st_l, s.cp, s.sp);
-    const bool pole = fabsf(P.muz) > 0.99999f;
+    const bool pole = !(s2 > 0.f);
     const float nx = first ? P.mux : (lamb ? ld.x : (pole ? pd.x : g.x));
     const float ny = first ? P.muy : (lamb ? ld.y : (pole ? pd.y : g.y));
     const float nz = first ? P.muz : (lamb ? ld.z : (pole ? pd.z : g.z));

@@ -240,13 +240,17 @@ __device__ __forceinline__ int pol_step_post(PolPhoton &P, const WalkArgs &a, fl
             ct = sqrtf(u01_f32(P.sb.w));
         }
         const float st = sqrtf(fmaxf(0.f, fmaf(-ct, ct, 1.f)));
-        if (fabsf(m0z) > 0.99999f) {
+        // sqrt(mu_x^2 + mu_y^2) stands for sqrt(1 - mu_z^2) (equal for a unit
+        // direction; the frame stays orthogonal next to the pole in FP32); the
+        // pole formula when it is 0 (or below FLT_MIN, where the reciprocal square
+        // root would not be finite), the reference's mu_z == +-1
+        const float s2 = fmaf(m0x, m0x, m0y * m0y);
+        if (!(s2 >= 1.17549435e-38f)) {
             const float sg = copysignf(1.f, m0z);
             nx = st * cphi;
             ny = sg * st * sphi;
             nz = sg * ct;
         } else {
-            const float s2 = fmaf(-m0z, m0z, 1.f);
             const float rs = rsqrtf(s2);
             const float tq = st * rs;
             nx = fmaf(tq, fmaf(m0x * m0z, cphi, -m0y * sphi), m0x * ct);

@@ -71,6 +71,38 @@ def build():
 _lib = None
 
 
+ULP_LIB_PATH = os.path.join(HERE, '_build', 'liboracle_walk_ulp.so')
+_ulp_lib = None
+
+
+def _bind(L):
+    L.orc_uniform.restype = ctypes.c_double
+    L.orc_uniform.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64]
+    L.orc_wavelength.restype = ctypes.c_double
+    L.orc_wavelength.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_double, ctypes.c_double]
+    L.orc_philox4x32_10.argtypes = [ctypes.c_void_p] * 3
+    L.orc_walk_range.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Table),
+                                 ctypes.POINTER(Table), ctypes.c_uint64, ctypes.c_int64,
+                                 ctypes.c_int64, ctypes.c_void_p]
+    L.orc_walk_threads.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(Table),
+                                   ctypes.POINTER(Table), ctypes.c_uint64, ctypes.c_int64,
+                                   ctypes.c_int, ctypes.c_void_p]
+    L.orc_walk_threads.restype = ctypes.c_int
+    return L
+
+
+def ulp_lib():
+    """The oracle built with log, sin and cos moved by one ulp (a stand-in for a
+    different libm, such as CUDA's on the GPU): tests measure how far one-ulp
+    differences carry through the walk."""
+    global _ulp_lib
+    if _ulp_lib is None:
+        if not os.path.exists(ULP_LIB_PATH):
+            build()
+        _ulp_lib = _bind(ctypes.CDLL(ULP_LIB_PATH))
+    return _ulp_lib
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -132,20 +164,22 @@ def make_config(n_photon, wvl0, half_width, theta0_deg, tau_tot, imp_cnc=0.0, rh
     return c
 
 
-def walk(cfg, ice, imp, seed, p0=0, p1=None, threads=1):
-    """FP64 replay walk of photons [p0, p1) -> structured array (RECORD_DTYPE)."""
+def walk(cfg, ice, imp, seed, p0=0, p1=None, threads=1, ulp=False):
+    """FP64 replay walk of photons [p0, p1) -> structured array (RECORD_DTYPE).
+    ulp: walk with the one-ulp libm stand-in (ulp_lib) instead."""
     if p1 is None:
         p1 = cfg.n_photon
+    L = ulp_lib() if ulp else lib()
     tabs = _Tables(ice, imp)
     out = np.zeros(p1 - p0, dtype=RECORD_DTYPE)
     if threads > 1 and p0 == 0:
-        rc = lib().orc_walk_threads(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
+        rc = L.orc_walk_threads(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
                                     int(seed), int(p1), int(threads), out.ctypes.data)
         if rc:
             raise RuntimeError('oracle thread start failed')
     else:
-        lib().orc_walk_range(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
-                             int(seed), int(p0), int(p1), out.ctypes.data)
+        L.orc_walk_range(ctypes.byref(cfg), ctypes.byref(tabs.ice), ctypes.byref(tabs.imp),
+                         int(seed), int(p0), int(p1), out.ctypes.data)
     return out
 
 

@@ -17,6 +17,27 @@
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
+
+#ifdef ORC_ULP_PERTURB
+/* Test build only (liboracle_walk_ulp.so): log, sin and cos results moved by one
+ * ulp up or down (or left alone), chosen by a hash of the argument.  It stands in
+ * for a different libm (CUDA's on the GPU against glibc here), to measure how far
+ * one-ulp differences carry through the walk. */
+static double orc_ulp_(double r, double x)
+{
+    union { double d; uint64_t u; } a;
+    a.d = x;
+    const int k = (int)((a.u * 0x9E3779B97F4A7C15ull) >> 62);
+    return k == 1 ? nextafter(r, INFINITY) : k == 2 ? nextafter(r, -INFINITY) : r;
+}
+static double orc_log_(double x) { return orc_ulp_(log(x), x); }
+static double orc_sin_(double x) { return orc_ulp_(sin(x), x); }
+static double orc_cos_(double x) { return orc_ulp_(cos(x), x); }
+#define log(x) orc_log_(x)
+#define sin(x) orc_sin_(x)
+#define cos(x) orc_cos_(x)
+#endif
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 

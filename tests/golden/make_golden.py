@@ -1,11 +1,11 @@
 #!/usr/bin/env python
 """Generate golden per-photon fixtures by running the UNMODIFIED reference.
 
-Run in a container that has the reference checkout (default
-``/root/reference``; override with ``MC_REFERENCE``)::
+Run where a checkout of the reference exists, naming it with ``--reference``
+or the ``MC_REFERENCE`` environment variable::
 
-    python tests/golden/make_golden.py            # all cases
-    python tests/golden/make_golden.py kat cfg1   # selected cases
+    python tests/golden/make_golden.py --reference <checkout>            # all cases
+    python tests/golden/make_golden.py --reference <checkout> kat cfg1   # selected cases
 
 The reference (monte_carloMPI/monte_carlo3D.py) is imported as-is.  A small
 harness supplies what it needs to run here:
@@ -44,7 +44,7 @@ sys.path.insert(0, REPO)
 from oracle import philox  # noqa: E402
 from monte_carlompi_gb300 import ssp  # noqa: E402
 
-REFERENCE = os.environ.get('MC_REFERENCE', '/root/reference')
+REFERENCE = os.environ.get('MC_REFERENCE')   # checkout of the reference; or --reference
 
 # name -> run parameters.  depth_m is converted to tau_tot with the synthetic
 # extinction (tau = depth * ext_cff_mss * rho_snw); tau_tot given directly wins.
@@ -54,9 +54,20 @@ CASES = {
     'cfg1': dict(n_photon=1000, wvl0=1.3, half_width=0.085, rds=100.0, theta0=0.0,
                  depth_m=0.5, table_nm=(1200, 1400), lam_bottom=True, R=0.5,
                  seed=0x5EED0001, csv=True),
+    # the same run at the driver's own size, 10,000 packets (monte_carlo3D-run.py:18);
+    # its first 1,000 photons are cfg1's (the replay stream is photon-indexed)
+    'cfg1_10k': dict(n_photon=10000, wvl0=1.3, half_width=0.085, rds=100.0, theta0=0.0,
+                     depth_m=0.5, table_nm=(1200, 1400), lam_bottom=True, R=0.5,
+                     seed=0x5EED0001, csv=False),
     # convergence-size geometry: r 250 um, 1.55 um, 60 deg, 0.10 m
     'cfg2': dict(n_photon=1000, wvl0=1.55, half_width=0.085, rds=250.0, theta0=60.0,
                  depth_m=0.10, lam_bottom=True, R=0.5, seed=0x5EED0002, csv=True),
+    # the last 1,000 photons of the 1e6-photon convergence run (photons 999,000 ..
+    # 999,999, the share np.array_split gives the last of 1,000 ranks,
+    # parallelize.py:14-15): the replay stream far into a run
+    'cfg2_tail': dict(n_photon=1000, first_photon=999000, wvl0=1.55, half_width=0.085,
+                      rds=250.0, theta0=60.0, depth_m=0.10, lam_bottom=True, R=0.5,
+                      seed=0x5EED0002, csv=False),
     # thin slab: exercises conditions 2 and 3 and the Lambertian bottom
     'thin': dict(n_photon=2000, wvl0=1.55, half_width=0.085, rds=1500.0, theta0=60.0,
                  depth_m=0.02, lam_bottom=True, R=0.5, seed=0x5EED0010, csv=False),
@@ -130,8 +141,9 @@ def _install_stubs():
 class Replay:
     """Answers np.random calls from the photon-indexed Philox replay stream."""
 
-    def __init__(self, seed):
+    def __init__(self, seed, first_photon=0):
         self.seed = seed
+        self.first = first_photon        # global index of the run's photon 0
         self.photon = None
         self.k = 0
         self.initial_calls = None
@@ -144,7 +156,8 @@ class Replay:
             for _ in range(n):
                 c = self.initial_calls
                 self.initial_calls += 1
-                out.append(float(philox.replay_uniform(self.seed, philox.TAG_WALK, c // 3, c % 3)))
+                out.append(float(philox.replay_uniform(self.seed, philox.TAG_WALK,
+                                                       self.first + c // 3, c % 3)))
             return np.array(out)
         if self.photon is None:
             raise RuntimeError('uniform drawn outside a photon')
@@ -169,7 +182,7 @@ class Replay:
 
     def normal(self, loc=0.0, scale=1.0, size=None):
         n = int(np.prod(size))
-        z = philox.replay_normal(self.seed, np.arange(n, dtype=np.uint64))
+        z = philox.replay_normal(self.seed, np.arange(self.first, self.first + n, dtype=np.uint64))
         return (loc + scale * z).reshape(size)
 
 
@@ -203,7 +216,7 @@ def run_case(name, spec, outdir):
     work = tempfile.mkdtemp(prefix='mcgold_')
     old_cwd, old_argv = os.getcwd(), sys.argv
     saved = (np.random.rand, np.random.uniform, np.random.normal)
-    replay = Replay(spec['seed'])
+    replay = Replay(spec['seed'], spec.get('first_photon', 0))
     answers, draws, stokes = [], [], []
     try:
         os.chdir(work)
@@ -234,7 +247,7 @@ def run_case(name, spec, outdir):
         orig_init = ref.MonteCarlo.initial_pdfs
 
         def walk(self, wvl):
-            replay.photon, replay.k = self.photon, 3
+            replay.photon, replay.k = replay.first + self.photon, 3
             out = orig_walk(self, wvl)
             answers.append(out[:7])
             stokes.append([float(x) for x in np.asarray(out[7]).ravel()[:4]])
@@ -285,7 +298,7 @@ def run_case(name, spec, outdir):
         condition=a[:, 0].astype(np.int32), wvn=a[:, 1], theta_n=a[:, 2], phi_n=a[:, 3],
         n_scat=a[:, 4].astype(np.int32), path_length=a[:, 5], snow_depth=a[:, 6],
         n_draws=np.array(draws, dtype=np.int64))
-    params = dict(n_photon=spec['n_photon'], wvl0=spec['wvl0'], half_width=spec['half_width'],
+    params = dict(n_photon=spec['n_photon'], first_photon=spec.get('first_photon', 0), wvl0=spec['wvl0'], half_width=spec['half_width'],
                   rds=spec['rds'], theta0=spec['theta0'], tau_tot=tau_tot,
                   imp_cnc=spec.get('imp_cnc', 0.0), rho_snw=rho_snw, rho_ice=rho_ice,
                   lam_surface=int(spec.get('lam_surface', False)),
@@ -319,6 +332,11 @@ def run_case(name, spec, outdir):
 
 
 def main(argv):
+    global REFERENCE
+    if argv[:1] == ['--reference']:
+        REFERENCE, argv = argv[1], argv[2:]
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, 'monte_carloMPI')):
+        sys.exit('name the reference checkout: --reference <dir> or MC_REFERENCE=<dir>')
     names = argv or list(CASES)
     for name in names:
         run_case(name, CASES[name], HERE)

@@ -6,14 +6,25 @@ from monte_carlompi_gb300.config import WalkConfig
 
 FLOAT_RTOL = 1e-12   # FP64 replay: float fields, relative
 ANGLE_ATOL = 1e-12   # FP64 replay: direction cosines rebuilt from theta_n / phi_n
+# Runs of 1e6 photons: the reference's rotation divides by sqrt(1 - mu_z^2), so a
+# one-ulp difference between two libms (CUDA's and glibc's sin, cos, log) grows by
+# 1 / sin(theta) at directions near the vertical, and among ~4e7 rotations a few come
+# close enough to carry it past 1e-12.  The oracle against its own one-ulp stand-in
+# (oracle.walk(..., ulp=True)) measures 4.3e-12 at most on config 2's 1e6 photons, 6
+# above 1e-12 (tests/test_oracle.py); the full runs are held to FULL_RUN_ANGLE_ATOL for
+# every photon and to ANGLE_ATOL for all but FULL_RUN_ANGLE_FRAC of them.
+FULL_RUN_ANGLE_ATOL = 1e-11
+FULL_RUN_ANGLE_FRAC = 1e-4
 
 
-def compare_replay(got, ref, skip_phi_undefined=True):
+def compare_replay(got, ref, skip_phi_undefined=True, angle_atol=ANGLE_ATOL):
     """Replay parity: condition and n_scat bit-exact; wvn, path_length and
     snow_depth within FLOAT_RTOL (path_length relative to max(|path|, depth));
     angles compared through the direction they
     encode (cos theta, sin theta cos phi, sin theta sin phi), because arccos
-    and the quadrant arctan are ill-conditioned near the poles and axes.
+    and the quadrant arctan are ill-conditioned near the poles and axes, within
+    angle_atol; err['direction_frac_over'] is the fraction of photons whose
+    direction differs by more than ANGLE_ATOL.
     Returns a dict of maximum errors; raises AssertionError on failure."""
     assert np.array_equal(np.asarray(got['condition']), np.asarray(ref['condition']))
     assert np.array_equal(np.asarray(got['n_scat']), np.asarray(ref['n_scat']))
@@ -36,13 +47,15 @@ def compare_replay(got, ref, skip_phi_undefined=True):
     db = np.stack([np.cos(th_b), np.sin(th_b) * np.cos(ph_b), np.sin(th_b) * np.sin(ph_b)])
     e = np.abs(da - db)[:, ok]
     err['direction'] = float(e.max()) if e.size else 0.0
-    assert err['direction'] <= ANGLE_ATOL, err
+    err['direction_frac_over'] = float(np.mean(e.max(0) > ANGLE_ATOL)) if e.size else 0.0
+    assert err['direction'] <= angle_atol, err
     return err
 
 
 def golden_config(g):
     p = lambda k: g['param_' + k].item()  # noqa: E731
     return WalkConfig(n_photon=int(p('n_photon')), wvl0=p('wvl0'), half_width=p('half_width'),
+                      first_photon=int(p('first_photon')) if 'param_first_photon' in g else 0,
                       theta0_deg=p('theta0'), tau_tot=p('tau_tot'), imp_cnc=p('imp_cnc'),
                       rho_snw=p('rho_snw'), rho_ice=p('rho_ice'),
                       lambertian_reflectance=p('R'), lambertian_surface=bool(p('lam_surface')),

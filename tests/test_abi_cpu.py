@@ -40,6 +40,11 @@ def test_bindings_follow_the_header_abi_version():
     hdr = open(os.path.join(os.path.dirname(__file__), '..', 'include', 'mcwalk.h')).read()
     m = re.search(r'#define MCW_ABI_VERSION (\d+)', hdr)
     assert m and int(m.group(1)) == _abi.ABI_VERSION
+    for name, value in (('MCW_NOALLOC_MAX_LUT', _abi.NOALLOC_MAX_LUT),
+                        ('MCW_DEFAULT_BUDGET_S', _abi.DEFAULT_BUDGET_S),
+                        ('MCW_HIST_BINS', _abi.HIST_BINS)):
+        m = re.search(r'#define %s ([0-9.]+)' % name, hdr)
+        assert m and float(m.group(1)) == value, name
 
 
 def test_create_without_gpu_fails_cleanly():

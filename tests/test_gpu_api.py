@@ -78,9 +78,12 @@ def test_run_polarised_reproduces_reference_csv(tmp_path, monkeypatch, capsys):
         assert np.abs(got[k] - ref[k]).max() < 1e-10
 
 
-@pytest.mark.parametrize('name', ['cfg1', 'cfg2'])
+@pytest.mark.parametrize('name', ['cfg1', 'cfg2', 'cfg1_10k'])
 def test_run_replay_reproduces_reference_csv(tmp_path, monkeypatch, capsys, name):
-    """Same tables, same replay stream: the CSV holds the reference's photons."""
+    """Same tables, same replay stream: the CSV holds the reference's photons.  cfg1_10k
+    is config 1 at the driver's 10,000 packets (monte_carlo3D-run.py:18): all its rows
+    match the reference's answers, and its first 1,000 rows match the reference's own
+    CSV of cfg1."""
     g = load_golden(name)
     p = lambda k: g['param_' + k].item()  # noqa: E731
     monkeypatch.chdir(tmp_path)
@@ -95,11 +98,15 @@ def test_run_replay_reproduces_reference_csv(tmp_path, monkeypatch, capsys, name
     assert os.path.basename(printed) == str(g['csv_name'])
     got = csv_io.read_csv(printed)
     compare_replay(got, g)
-    ref = csv_io.read_csv(os.path.join(GOLDEN, name + '.csv'))
-    compare_replay(got, ref)
     text = open(printed, 'rb').read()
     assert text.startswith(csv_io.HEADER.encode())
     assert text.count(b'\n') == int(p('n_photon')) + 1
+    ref_csv = os.path.join(GOLDEN, name + '.csv')
+    if os.path.exists(ref_csv):
+        compare_replay(got, csv_io.read_csv(ref_csv))
+    else:
+        first = {k: v[:1000] for k, v in got.items()}
+        compare_replay(first, csv_io.read_csv(os.path.join(GOLDEN, 'cfg1.csv')))
 
 
 def test_run_f32_synthetic_and_albedo(tmp_path, monkeypatch, capsys):

@@ -15,8 +15,9 @@ from monte_carlompi_gb300 import _abi, replicas, ssp
 from monte_carlompi_gb300.config import WalkConfig
 from oracle import oracle
 from tests.conftest import golden_names, load_golden
-from tests.helpers import (chi2_two_sample, compare_replay, condition_fractions_agree,
-                           exit_histogram, golden_config, golden_mode, golden_phase, golden_tables)
+from tests.helpers import (FULL_RUN_ANGLE_ATOL, FULL_RUN_ANGLE_FRAC, chi2_two_sample, compare_replay,
+                           condition_fractions_agree, exit_histogram, golden_config, golden_mode,
+                           golden_phase, golden_tables)
 
 pytestmark = pytest.mark.gpu
 
@@ -198,13 +199,23 @@ def test_polarised_walk_needs_its_mode_and_tables(walker):
         walker.walk([cfg], 1, mode='pol64')
 
 
-def test_replay_config2_first_10k_matches_oracle(walker):
-    cfg, ice, imp = cfg2_geometry(10000)
+def test_replay_config2_full_run_matches_oracle_and_reference(walker):
+    """Config 2 at its full size (monte_carlo3D.py:1212-1490 for 1,000,000 photons):
+    every photon of the FP64 replay walk equals the oracle's (condition and n_scat
+    bit-exact, float fields within 1e-12), and the last 1,000 photons equal the
+    reference's own run of them (photons 999,000 .. 999,999 of the same stream)."""
+    g = load_golden('cfg2_tail')
+    ice, imp = golden_tables(g)
+    cfg = dataclasses.replace(golden_config(g), first_photon=0, n_photon=1000000)
     walker.set_tables([ice], imp)
-    res = walker.walk([cfg], 0x5EED0002, mode='replay64')
-    ref = oracle_run(cfg, ice, imp, 0x5EED0002)
-    err = compare_replay(res.records, ref)
+    res = walker.walk([cfg], int(g['param_seed']), mode='replay64')
+    ref = oracle_run(cfg, ice, imp, int(g['param_seed']))
+    err = compare_replay(res.records, ref, angle_atol=FULL_RUN_ANGLE_ATOL)
     assert err['path_length'] < 1e-12
+    assert err['direction_frac_over'] <= FULL_RUN_ANGLE_FRAC, err
+    compare_replay(res.records[999000:], g)
+    # the FP64 walk reaches the bottom: the full run exercises conditions 1, 2 and 4
+    assert set(np.unique(res.records['condition'])) >= {1, 4}
 
 
 def test_replay_shard_equals_slice(walker):
@@ -223,6 +234,10 @@ STAT_CASES = {
     # name: (config builder, N)
     'cfg2': (lambda: cfg2_geometry(0), 200000),
     'thin': (lambda: cfg2_geometry(0, depth=0.02, rds=1500.0), 200000),
+    # normal incidence on the thin slab: every photon starts exactly on the vertical
+    # (the pole branch) and near-vertical directions are common
+    'thin0': (lambda: tuple([dataclasses.replace(cfg2_geometry(0, depth=0.02, rds=1500.0)[0], theta0_deg=0.0)])
+              + cfg2_geometry(0, depth=0.02, rds=1500.0)[1:], 1000000),
 }
 
 
@@ -232,10 +247,13 @@ def _golden_case(name, n):
     return dataclasses.replace(golden_config(g), n_photon=n), ice, imp
 
 
-@pytest.mark.parametrize('case,n', [('cfg2', 200000), ('thin', 200000), ('kat', 200000),
+@pytest.mark.parametrize('case,n', [('cfg2', 1000000), ('thin', 1000000), ('thin0', 1000000), ('kat', 200000),
                                     ('imp', 100000), ('lamsurf', 50000), ('edge', 50000),
-                                    ('cfg1', 20000), ('asph', 100000)])
+                                    ('cfg1', 10000), ('cfg1', 40000), ('asph', 100000)])
 def test_f32_statistics_match_oracle(walker, case, n):
+    """The FP32 walk against the oracle's FP64 walk of the reference algorithm at the
+    same N: config 2 and its thin-slab variant at the 1,000,000 photons the bench walks,
+    config 1 at its 10,000 (and at 40,000 for more power)."""
     if case in STAT_CASES:
         cfg, ice, imp = STAT_CASES[case][0]()
         cfg = dataclasses.replace(cfg, n_photon=n)
@@ -523,7 +541,7 @@ def test_budget_stops_the_kernel_and_context_survives(walker):
         with pytest.raises(_abi.BudgetExceeded):
             walker.walk([dataclasses.replace(cfg, n_photon=2000)], 1, mode='replay64', records=None)
     finally:
-        walker.set_budget(300.0)
+        walker.set_budget(_abi.DEFAULT_BUDGET_S)
     ok = walker.walk([dataclasses.replace(cfg, n_photon=1000)], 1, mode='f32')
     assert int(ok.tallies[0]['n_cond'][1:].sum()) == 1000
 
@@ -555,7 +573,7 @@ def test_budget_stops_the_drain_kernel_too(walker):
         with pytest.raises(_abi.BudgetExceeded):
             walker.walk([cfg], 2, mode='f32', records=None)
     finally:
-        walker.set_budget(300.0)
+        walker.set_budget(_abi.DEFAULT_BUDGET_S)
     try:
         ok = walker.walk([dataclasses.replace(cfg, n_photon=2000)], 2, mode='f32')
     finally:
