@@ -70,7 +70,7 @@ int mcw_mlp_adam(float *w, const float *g, float *m, float *v, void *w16, int64_
 
 /* Error flags of the tensor-core path on the current device (bit 0: an MMA completion
  * wait of the tcgen05 GEMM ran out of time and the kernel left early; bit 1: the same in
- * mcw_mlp_forward); clear != 0 resets them. */
+ * mcw_mlp_forward; bit 2: the same in mcw_mlp_gemm_grouped); clear != 0 resets them. */
 int mcw_mlp_status(int32_t clear, uint32_t *flags);
 
 /* y (bf16) = x (f32), n elements. */
@@ -101,6 +101,98 @@ int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2,
  * bytes of the output stream. */
 int mcw_mlp_forward_f16(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
                         const float *b4, const void *blob, void *y, int32_t ldy, void *stream);
+
+/* ---- training engine: one Adam step of an ensemble in a fixed sequence of launches.
+ * "groups" are independent problems of the same shape (ensemble members) whose
+ * operands lie stride_* elements apart; strides and leading dimensions count
+ * elements. */
+
+/* C[g] = A[g] B[g]^T for g < groups on the tcgen05 tensor cores, A bf16 [m, k] and B
+ * bf16 [n, k] both K-major (rows lda / ldb apart), operand tiles staged by TMA.
+ * Rules of the copies: a and b 16-byte aligned, lda, ldb, stride_a and stride_b
+ * multiples of 8 with stride >= ld * rows; rows past m / n and columns past k read as
+ * zero.  Epilogues as mcw_mlp_gemm (bias and aux per group: bias + g * stride_bias,
+ * aux + g * stride_aux + i * ldaux), and for MCW_EPI_BIAS_SILU / MCW_EPI_DSILU an
+ * optional bf16 transposed copy of the bf16 output, ct [n, m] with leading dimension
+ * ldct.  splits > 1 (MCW_EPI_F32 only): K is cut into `splits` whole-64 ranges and
+ * range s writes its partial product at c + s * stride_split (mcw_mlp_reduce_splits
+ * adds them); splits must equal ceil(c / ceil(c / splits)) for c = ceil(k / 64). */
+typedef struct {
+    int32_t m, n, k;
+    int32_t groups;
+    int32_t splits;
+    int32_t epilogue;
+    const void *a;
+    int64_t lda, stride_a;
+    const void *b;
+    int64_t ldb, stride_b;
+    const float *bias;
+    int64_t stride_bias;
+    const float *aux;
+    int64_t ldaux, stride_aux;
+    void *c;
+    int64_t ldc, stride_c, stride_split;
+    void *c2;
+    int64_t ldc2, stride_c2;
+    void *ct;
+    int64_t ldct, stride_ct;
+} McwGemmGrouped;
+
+int mcw_mlp_gemm_grouped(const McwGemmGrouped *p, void *stream);
+
+/* dst[g][i][j] = sum over s < splits of src[s * stride_split + g * stride_src + i * ld_src + j]. */
+int mcw_mlp_reduce_splits(const float *src, int64_t stride_split, int64_t stride_src, int64_t ld_src, float *dst,
+                          int64_t stride_dst, int64_t ld_dst, int32_t splits, int32_t groups, int32_t m, int32_t n,
+                          void *stream);
+
+/* mcw_mlp_loss for `groups` outputs y[g] against t[g] (loss[g] += ...), the gradient as
+ * f32 g32 and bf16 g16 [m, n] (leading dimension ldg) and bf16 transposed g16t [n, m]
+ * (leading dimension ldgt). */
+int mcw_mlp_loss_grouped(const float *y, int64_t ldy, int64_t stride_y, const float *t, int64_t ldt,
+                         int64_t stride_t, const float *w, int32_t groups, int32_t m, int32_t n, float *g32,
+                         int64_t ldg, int64_t stride_g32, void *g16, int64_t stride_g16, void *g16t, int64_t ldgt,
+                         int64_t stride_g16t, float *loss, void *stream);
+
+/* Column sums of up to four gradient matrices (bias gradients):
+ * out[g * stride_out + out_offset + j] = sum over i < m of g[g * stride + i * ld + j], j < n. */
+typedef struct {
+    const float *g;
+    int64_t ld, stride;
+    int64_t out_offset;
+    int32_t n;
+    int32_t pad;
+} McwColsumLayer;
+
+int mcw_mlp_colsum_grouped(const McwColsumLayer *layers, int32_t n_layers, int32_t groups, int32_t m, float *out,
+                           int64_t stride_out, void *stream);
+
+/* A block of the flat parameters whose bf16 copy is also kept transposed:
+ * wt[offset_t + c * ld_t + o] = w[offset + o * cols + c] for o < rows, c < cols. */
+typedef struct {
+    int64_t offset, offset_t, ld_t;
+    int32_t rows, cols;
+} McwTransposeBlock;
+
+/* mcw_mlp_adam over `groups` flat parameter vectors of n elements (w, g, m, v and the
+ * bf16 copy w16 each g * n apart), the learning rate and the 1-based step read from
+ * device memory (lr_dev, step_dev); wt (stride_t per group) receives the transposed
+ * bf16 copies of up to four blocks. */
+int mcw_mlp_adam_grouped(float *w, const float *g, float *m, float *v, void *w16, int64_t n, int32_t groups,
+                         const float *lr_dev, const int32_t *step_dev, float beta1, float beta2, float eps,
+                         void *wt, int64_t stride_t, const McwTransposeBlock *blocks, int32_t n_blocks,
+                         void *stream);
+
+/* The batch of a step: for g < groups and i < batch, row r = perm[g * n_rows + c * batch + i]
+ * (c = *counter_dev) of x_all (bf16 [n_rows, 16]) and t_all (f32, leading dimension
+ * ldt_all, n_out columns) into x (bf16 [batch, 16]), xt (bf16 [16, batch]) and t
+ * (leading dimension ldt).  Rows past n_rows are skipped. */
+int mcw_mlp_gather(const void *x_all, const float *t_all, int64_t ldt_all, int32_t n_out, const int32_t *perm,
+                   int64_t n_rows, const int32_t *counter_dev, int32_t batch, int32_t groups, void *x,
+                   int64_t stride_x, void *xt, int64_t stride_xt, float *t, int64_t ldt, int64_t stride_t,
+                   void *stream);
+
+/* *counter_dev += 1 and *step_dev += 1 (the end of a captured step). */
+int mcw_mlp_advance(int32_t *counter_dev, int32_t *step_dev, void *stream);
 
 #ifdef __cplusplus
 }

@@ -102,12 +102,40 @@ class GemmC(ctypes.Structure):
                 ('engine', ctypes.c_int32)]
 
 
+class GemmGroupedC(ctypes.Structure):
+    """McwGemmGrouped of include/mcw_mlp.h."""
+    _fields_ = [('m', ctypes.c_int32), ('n', ctypes.c_int32), ('k', ctypes.c_int32),
+                ('groups', ctypes.c_int32), ('splits', ctypes.c_int32), ('epilogue', ctypes.c_int32),
+                ('a', ctypes.c_void_p), ('lda', ctypes.c_int64), ('stride_a', ctypes.c_int64),
+                ('b', ctypes.c_void_p), ('ldb', ctypes.c_int64), ('stride_b', ctypes.c_int64),
+                ('bias', ctypes.c_void_p), ('stride_bias', ctypes.c_int64),
+                ('aux', ctypes.c_void_p), ('ldaux', ctypes.c_int64), ('stride_aux', ctypes.c_int64),
+                ('c', ctypes.c_void_p), ('ldc', ctypes.c_int64), ('stride_c', ctypes.c_int64),
+                ('stride_split', ctypes.c_int64),
+                ('c2', ctypes.c_void_p), ('ldc2', ctypes.c_int64), ('stride_c2', ctypes.c_int64),
+                ('ct', ctypes.c_void_p), ('ldct', ctypes.c_int64), ('stride_ct', ctypes.c_int64)]
+
+
+class ColsumLayerC(ctypes.Structure):
+    """McwColsumLayer of include/mcw_mlp.h."""
+    _fields_ = [('g', ctypes.c_void_p), ('ld', ctypes.c_int64), ('stride', ctypes.c_int64),
+                ('out_offset', ctypes.c_int64), ('n', ctypes.c_int32), ('pad', ctypes.c_int32)]
+
+
+class TransposeBlockC(ctypes.Structure):
+    """McwTransposeBlock of include/mcw_mlp.h."""
+    _fields_ = [('offset', ctypes.c_int64), ('offset_t', ctypes.c_int64), ('ld_t', ctypes.c_int64),
+                ('rows', ctypes.c_int32), ('cols', ctypes.c_int32)]
+
+
 EPI_F32, EPI_BIAS_F32, EPI_BIAS_SILU, EPI_DSILU = 0, 1, 2, 3
 ENGINE_MMA_SYNC, ENGINE_TCGEN05 = 0, 1
 
 # entry points of include/mcw_mlp.h
 MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16',
-               'mcw_mlp_status', 'mcw_mlp_pack', 'mcw_mlp_forward', 'mcw_mlp_forward_f16']
+               'mcw_mlp_status', 'mcw_mlp_pack', 'mcw_mlp_forward', 'mcw_mlp_forward_f16',
+               'mcw_mlp_gemm_grouped', 'mcw_mlp_reduce_splits', 'mcw_mlp_loss_grouped',
+               'mcw_mlp_colsum_grouped', 'mcw_mlp_adam_grouped', 'mcw_mlp_gather', 'mcw_mlp_advance']
 MLP_PACK_BYTES = 5 * 256 * 256 * 2 + 256 * 16 * 2
 
 RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
@@ -188,6 +216,17 @@ def load(path=None):
         'mcw_mlp_pack': ([vp, vp, vp, vp, vp, vp], ctypes.c_int),
         'mcw_mlp_forward': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
         'mcw_mlp_forward_f16': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
+        'mcw_mlp_gemm_grouped': ([ctypes.POINTER(GemmGroupedC), vp], ctypes.c_int),
+        'mcw_mlp_reduce_splits': ([vp, i64, i64, i64, vp, i64, i64, i32, i32, i32, i32, vp], ctypes.c_int),
+        'mcw_mlp_loss_grouped': ([vp, i64, i64, vp, i64, i64, vp, i32, i32, i32, vp, i64, i64, vp, i64,
+                                  vp, i64, i64, vp, vp], ctypes.c_int),
+        'mcw_mlp_colsum_grouped': ([ctypes.POINTER(ColsumLayerC), i32, i32, i32, vp, i64, vp], ctypes.c_int),
+        'mcw_mlp_adam_grouped': ([vp, vp, vp, vp, vp, i64, i32, vp, vp, ctypes.c_float, ctypes.c_float,
+                                  ctypes.c_float, vp, i64, ctypes.POINTER(TransposeBlockC), i32, vp],
+                                 ctypes.c_int),
+        'mcw_mlp_gather': ([vp, vp, i64, i32, vp, i64, vp, i32, i32, vp, i64, vp, i64, vp, i64, i64, vp],
+                           ctypes.c_int),
+        'mcw_mlp_advance': ([vp, vp, vp], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

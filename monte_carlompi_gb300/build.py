@@ -18,9 +18,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, 'csrc')
 BUILD = os.path.join(PKG, '_build')
-if os.environ.get('MCW_DEFINES'):
-    BUILD = os.path.join(PKG, '_build', 'defines_' + ''.join(
-        c if c.isalnum() else '_' for c in os.environ['MCW_DEFINES']))
+VARIANT = os.path.join(BUILD, 'defines_' + ''.join(
+    c if c.isalnum() else '_' for c in os.environ['MCW_DEFINES'])) if os.environ.get('MCW_DEFINES') else BUILD
 LIBDIR = os.path.join(PKG, '_lib')
 LIB = os.path.join(LIBDIR, 'libmcwalk.so')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
@@ -29,9 +28,10 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NO_FMAD = {'walk_replay.cu', 'ssp_lut.cu'}
 # the FP32 production walk: flush denormals, approximate division and square root
 FAST_F32 = {'walk_f32.cu': ['-ftz=true', '-prec-div=false', '-prec-sqrt=false']}
-# tuning builds: extra -D flags for the CUDA units (e.g. MCW_DEFINES="-DMCW_BLOCK_WALK=128");
-# objects of such a build go to a directory of their own
+# tuning builds: extra -D flags for the FP32 walk (e.g. MCW_DEFINES="-DMCW_BLOCK_WALK=128");
+# its object goes to a directory of its own, the other units are shared with the default build
 DEFINES = os.environ.get('MCW_DEFINES', '').split()
+DEFINE_UNITS = {'walk_f32.cu'}
 
 
 def nvcc():
@@ -54,11 +54,12 @@ def _stale(obj, src):
 
 def _compile(src, verbose):
     name = os.path.basename(src)
-    obj = os.path.join(BUILD, name + '.o')
+    obj = os.path.join(VARIANT if name in DEFINE_UNITS else BUILD, name + '.o')
     if not _stale(obj, src):
         return obj, None
     if name.endswith('.cu'):
-        cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', *DEFINES, '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
+        defs = DEFINES if name in DEFINE_UNITS else []
+        cmd = [nvcc(), *ARCH, '-O3', '-lineinfo', '-std=c++17', *defs, '-Xcompiler', '-fPIC', '-c', src, '-o', obj]
         if name in NO_FMAD:
             cmd.insert(-4, '--fmad=false')
         for flag in FAST_F32.get(name, []):
@@ -76,11 +77,13 @@ def _compile(src, verbose):
 def build(force=False, verbose=False):
     """Compile every unit under csrc/ and link libmcwalk.so.  Returns its path."""
     os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(VARIANT, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, '*.cu')) + glob.glob(os.path.join(CSRC, '*.cpp')))
     if force:
         for s in srcs:
-            o = os.path.join(BUILD, os.path.basename(s) + '.o')
+            o = os.path.join(VARIANT if os.path.basename(s) in DEFINE_UNITS else BUILD,
+                             os.path.basename(s) + '.o')
             if os.path.exists(o):
                 os.remove(o)
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
@@ -91,7 +94,7 @@ def build(force=False, verbose=False):
             if log:
                 print(log, file=sys.stderr)
     stamp = LIB + '.objdir'     # which object directory the library was linked from
-    same_dir = os.path.exists(stamp) and open(stamp).read() == BUILD
+    same_dir = os.path.exists(stamp) and open(stamp).read() == VARIANT
     if force or not same_dir or not os.path.exists(LIB) or \
             any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [nvcc(), *ARCH, '-shared', '-o', LIB, *objs, '-lpthread']
@@ -99,7 +102,7 @@ def build(force=False, verbose=False):
         if r.returncode != 0:
             raise RuntimeError('link failed: %s\n%s%s' % (' '.join(cmd), r.stdout, r.stderr))
         with open(stamp, 'w') as f:
-            f.write(BUILD)
+            f.write(VARIANT)
     return LIB
 
 

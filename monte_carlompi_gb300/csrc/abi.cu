@@ -72,6 +72,11 @@ struct HostBuf {
 struct Plan {
     std::vector<DevConfig> cfgs;
     std::vector<int64_t> prefix;
+    // the order in which the FP32 walk hands out photons: configs whose walks are
+    // expected to run longest first (claim_cfg[k] = config taken k-th, claim_prefix
+    // its cumulative photon counts); records do not depend on it
+    std::vector<int64_t> claim_prefix;
+    std::vector<int32_t> claim_cfg;
     int64_t total = 0;
     int32_t lut_total = 0;
     bool impurity = false;  // some config has imp_cnc > 0
@@ -99,6 +104,9 @@ struct mcw_ctx {
     int32_t n_ice = 0;
     bool have_tables = false;
     std::vector<std::vector<int32_t>> ice_order;   // row permutation of each ice table (stored ascending)
+    // host copy of the device tables (the claim order's estimate of walk lengths)
+    std::vector<double> h_tab;
+    std::vector<DevTable> h_ice;                   // offsets into h_tab (pointers unused)
     // phase matrices of the polarised walk, one per ice table (n_rows 0 = none)
     DevBuf phasedata, phase_tables, phasedata32, phase_tables32, phase_seeds;
     std::vector<int32_t> phase_rows;
@@ -184,6 +192,53 @@ const char *check_config(const mcw_config &c, int32_t n_ice) {
 
 constexpr int32_t kMaxLutPerConfig = 1 << 16;
 
+// Linear interpolation of column col (1 ss_alb, 3 asm_prm) of ice table t at
+// wavelength x [um], clamped to the table's ends (host copy; ordering only).
+double host_column(const mcw_ctx *ctx, int32_t t, int col, double x_um) {
+    const DevTable &d = ctx->h_ice[t];
+    const double *base = ctx->h_tab.data() + (d.wvl - (const double *)ctx->tabdata.p);
+    const double *w = base, *v = base + (size_t)col * d.n;
+    const double x = d.unit == MCW_WVL_METRES ? x_um * 1e-6 : x_um;
+    if (x <= w[0]) return v[0];
+    if (x >= w[d.n - 1]) return v[d.n - 1];
+    const int32_t hi = (int32_t)(std::upper_bound(w, w + d.n, x) - w);
+    const double f = (x - w[hi - 1]) / (w[hi] - w[hi - 1]);
+    return v[hi - 1] + f * (v[hi] - v[hi - 1]);
+}
+
+// Expected length (scatter events) of a config's longest walks, for the claim
+// order: absorption ends a walk after about 1 / (1 - ssa) events (the smallest
+// co-albedo within 2 sigma of the centre wavelength), a slab of optical depth tau
+// after about tau^2 (1 - g) (diffusion across it).  Only the ranking matters.
+double walk_length_estimate(const mcw_ctx *ctx, const mcw_config &c) {
+    const double sigma = c.half_width / 2.355;
+    double coalb = 1.0, g = 0.0;
+    for (int k = -2; k <= 2; k += 2) {
+        const double x = c.wvl0 + k * sigma;
+        const double ssa = std::isnan(c.ssa_ice_override) ? host_column(ctx, c.ice_table, 1, x) : c.ssa_ice_override;
+        coalb = std::min(coalb, 1.0 - ssa);
+        if (k == 0) g = std::isnan(c.g_override) ? host_column(ctx, c.ice_table, 3, x) : c.g_override;
+    }
+    if (c.lambertian_surface) return 1.0 / std::max(1.0 - c.lambertian_reflectance, 1e-9);
+    const double absorb = 1.0 / std::max(coalb, 1e-12);
+    const double slab = c.tau_tot * c.tau_tot * std::max(1.0 - g, 1e-3) + c.tau_tot;
+    return std::min(absorb, slab);
+}
+
+// Claim order of a plan: longest expected walks first (stable: ties keep the
+// callers' order).
+void make_claim_order(const mcw_ctx *ctx, const mcw_config *cfgs, Plan &plan) {
+    const int32_t n = (int32_t)plan.cfgs.size();
+    std::vector<double> key(n);
+    for (int32_t i = 0; i < n; ++i) key[i] = (n > 1 && !ctx->h_ice.empty()) ? walk_length_estimate(ctx, cfgs[i]) : 0.0;
+    plan.claim_cfg.resize(n);
+    for (int32_t i = 0; i < n; ++i) plan.claim_cfg[i] = i;
+    std::stable_sort(plan.claim_cfg.begin(), plan.claim_cfg.end(),
+                     [&](int32_t a, int32_t b) { return key[a] > key[b]; });
+    plan.claim_prefix.assign(n + 1, 0);
+    for (int32_t k = 0; k < n; ++k) plan.claim_prefix[k + 1] = plan.claim_prefix[k] + plan.cfgs[plan.claim_cfg[k]].n_photon;
+}
+
 int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, int32_t mode, Plan &plan) {
     if (!cfgs || n_cfg <= 0) return set_err(ctx, MCW_ERR_ARG, "need at least one config");
     if (n_cfg > (1 << 23)) return set_err(ctx, MCW_ERR_ARG, "at most 2^23 configs per call");
@@ -260,6 +315,7 @@ int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, int32_t mode,
     plan.prefix[n_cfg] = off;
     plan.total = off;
     plan.lut_total = lut_off;
+    make_claim_order(ctx, cfgs, plan);
     return MCW_OK;
 }
 
@@ -291,7 +347,8 @@ int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBu
     const size_t n_cfg = plan.cfgs.size();
     const size_t b_cfg = n_cfg * sizeof(DevConfig);
     const size_t off = prefix_offset(n_cfg);
-    const size_t b_all = off + (n_cfg + 1) * sizeof(int64_t);
+    // configs | prefix (n + 1) | claim_prefix (n + 1) | claim_cfg (n)
+    const size_t b_all = off + 2 * (n_cfg + 1) * sizeof(int64_t) + n_cfg * sizeof(int32_t);
     CUDA_TRY(ctx, cfgs.ensure(b_all));
     CUDA_TRY(ctx, lut.ensure(std::max<size_t>(1, plan.lut_total) * sizeof(LutEntry)));
     CUDA_TRY(ctx, tallies.ensure(n_cfg * sizeof(mcw_tally)));
@@ -303,6 +360,8 @@ int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBu
     memcpy(h, plan.cfgs.data(), b_cfg);
     memset(h + b_cfg, 0, off - b_cfg);
     memcpy(h + off, plan.prefix.data(), (n_cfg + 1) * sizeof(int64_t));
+    memcpy(h + off + (n_cfg + 1) * sizeof(int64_t), plan.claim_prefix.data(), (n_cfg + 1) * sizeof(int64_t));
+    memcpy(h + off + 2 * (n_cfg + 1) * sizeof(int64_t), plan.claim_cfg.data(), n_cfg * sizeof(int32_t));
     if (start) CUDA_TRY(ctx, cudaEventRecord(start, st));
     if (h2d) *h2d = b_all;
     CUDA_TRY(ctx, cudaMemcpyAsync(cfgs.p, h, b_all, cudaMemcpyHostToDevice, st));
@@ -313,9 +372,12 @@ int upload_plan(mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &lut, DevBu
 // tables give an equal lookup table.
 std::vector<unsigned char> plan_bytes(const Plan &plan) {
     const size_t bc = plan.cfgs.size() * sizeof(DevConfig), bp = plan.prefix.size() * sizeof(int64_t);
-    std::vector<unsigned char> v(bc + bp);
+    const size_t bk = plan.claim_cfg.size() * sizeof(int32_t);
+    std::vector<unsigned char> v(bc + 2 * bp + bk);
     memcpy(v.data(), plan.cfgs.data(), bc);
     memcpy(v.data() + bc, plan.prefix.data(), bp);
+    memcpy(v.data() + bc + bp, plan.claim_prefix.data(), bp);
+    memcpy(v.data() + bc + 2 * bp, plan.claim_cfg.data(), bk);
     return v;
 }
 
@@ -341,6 +403,8 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &l
     WalkArgs wa{};
     wa.cfgs = (const DevConfig *)cfgs.p;
     wa.prefix = (const int64_t *)((const char *)cfgs.p + prefix_offset(plan.cfgs.size()));
+    wa.claim_prefix = wa.prefix + (plan.cfgs.size() + 1);
+    wa.claim_cfg = (const int32_t *)(wa.claim_prefix + (plan.cfgs.size() + 1));
     wa.lut = (const LutEntry *)lut.p;
     wa.n_cfg = (int32_t)plan.cfgs.size();
     wa.regen_chunk = chunk;
@@ -508,6 +572,8 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     put(*imp, dimp);
     CUDA_TRY(ctx, cudaMemcpy(ctx->tabdata.p, host.data(), total * sizeof(double), cudaMemcpyHostToDevice));
     CUDA_TRY(ctx, cudaMemcpy(ctx->ice_tables.p, tabs.data(), n_ice * sizeof(DevTable), cudaMemcpyHostToDevice));
+    ctx->h_tab = host;
+    ctx->h_ice = tabs;
     ctx->imp = dimp;
     ctx->n_ice = n_ice;
     ctx->max_ice_n = 0;

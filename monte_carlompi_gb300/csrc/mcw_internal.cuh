@@ -116,6 +116,11 @@ struct WarpTally {
 struct WalkArgs {
     const DevConfig *cfgs;
     const int64_t *prefix;       // n_cfg + 1 global photon offsets
+    // claim order: the walk hands out photons of config claim_cfg[k] for claim ids
+    // claim_prefix[k] .. claim_prefix[k + 1] - 1 (null: configs in order, claim id =
+    // record index)
+    const int64_t *claim_prefix;
+    const int32_t *claim_cfg;
     const LutEntry *lut;
     int32_t n_cfg;
     int32_t regen_chunk;

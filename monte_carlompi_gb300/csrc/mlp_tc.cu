@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
+#include <mutex>
 
 #include "../../include/mcw_mlp.h"
 
@@ -309,8 +311,17 @@ __global__ void __launch_bounds__(128) gemm_tc_kernel(const McwGemm p, unsigned 
 static __device__ unsigned int g_tc_err;
 
 unsigned int *tc_err_flag() {
+    // looked up once per device (no runtime call while a stream is being captured)
+    static std::mutex mu;
+    static std::map<int, unsigned int *> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_tc_err) != cudaSuccess) return nullptr;
+    cache[dev] = static_cast<unsigned int *>(p);
     return static_cast<unsigned int *>(p);
 }
 

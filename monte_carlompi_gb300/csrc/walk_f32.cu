@@ -1069,13 +1069,21 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     const bool staged = a.n_cfg <= kSmemCfgMax;
     CfgF32 *scfg = reinterpret_cast<CfgF32 *>(smem + sizeof(WarpQueues) * nwarps);
     int64_t *sprefix = reinterpret_cast<int64_t *>(scfg + (staged ? a.n_cfg : 0));
+    int64_t *sclaim = sprefix + (staged ? a.n_cfg : 0);
+    int32_t *sclaim_cfg = reinterpret_cast<int32_t *>(sclaim + (staged ? a.n_cfg : 0));
+    const bool ordered = a.claim_prefix != nullptr;
     if (staged) {
         for (int c = threadIdx.x; c < a.n_cfg; c += blockDim.x) {
             scfg[c] = make_cfg(a.cfgs[c]);
             sprefix[c] = a.prefix[c];
+            sclaim[c] = ordered ? a.claim_prefix[c] : a.prefix[c];
+            sclaim_cfg[c] = ordered ? a.claim_cfg[c] : c;
         }
     }
     const int64_t *prefix = staged ? sprefix : a.prefix;
+    // photons are handed out in claim order (longest expected walks first)
+    const int64_t *claim = staged ? sclaim : (ordered ? a.claim_prefix : a.prefix);
+    const int32_t *claim_cfg = staged ? sclaim_cfg : a.claim_cfg;
     WarpQueues &q = queues[warp];
     warp_tally_reset(q.tally, lane);
     __syncthreads();
@@ -1106,9 +1114,10 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
                 if (left <= want) exhausted = true;
                 if (lane < valid) {
                     const int64_t g = (int64_t)base + lane;
-                    const int ci = find_config(prefix, a.n_cfg, g);
+                    const int k = find_config(claim, a.n_cfg, g);
+                    const int ci = claim_cfg ? claim_cfg[k] : k;
                     const CfgF32 c = staged ? scfg[ci] : make_cfg(a.cfgs[ci]);
-                    birth(q.birth[cnt + lane], g - prefix[ci], ci, c, a);
+                    birth(q.birth[cnt + lane], g - claim[k], ci, c, a);
                 }
                 cnt += valid;
                 __syncwarp();
@@ -1333,7 +1342,8 @@ __global__ void __launch_bounds__(kCtaWalkThreads) drain_kernel(const WalkArgs a
 }
 
 size_t smem_bytes(int block, int n_cfg) {
-    const size_t cfg = n_cfg <= kSmemCfgMax ? (size_t)n_cfg * (sizeof(CfgF32) + sizeof(int64_t)) : 0;
+    const size_t cfg =
+        n_cfg <= kSmemCfgMax ? (size_t)n_cfg * (sizeof(CfgF32) + 2 * sizeof(int64_t) + sizeof(int32_t)) : 0;
     return sizeof(WarpQueues) * (size_t)(block / 32) + cfg;
 }
 

@@ -318,6 +318,306 @@ class SurrogateMLP:
         return loss
 
 
+# ------------------------------------------------------------------ training engine
+
+IN_PAD = 16        # layer-1 inputs padded to 16: one 16-byte TMA row, one MMA K step
+OUT_PITCH = 656    # 649 outputs rounded up to 8 (16-byte bf16 rows)
+
+
+def _align8(n):
+    return (n + 7) // 8 * 8
+
+
+def flat_layout():
+    """Layout of one member's parameters in the training engine's flat vectors.
+
+    Returns (lay, P, tlay, T): lay['W%d'] = (offset, rows, cols) of W_l [out, in]
+    (layer 1's inputs padded to IN_PAD columns, held at zero), lay['b%d'] = (offset, n);
+    P elements per member; tlay['W%d'] = (offset, ld) of the transposed bf16 copy
+    W_l^T [in, ld] (ld = out rounded up to 8) of W2, W3, W4, the B operands of the
+    backward products; T elements per member.  Every block starts on 8 elements."""
+    lay, off = {}, 0
+    for layer, (fan_in, fan_out) in enumerate(zip(DIMS[:-1], DIMS[1:])):
+        k = IN_PAD if layer == 0 else fan_in
+        lay['W%d' % layer] = (off, fan_out, k)
+        off = _align8(off + fan_out * k)
+        lay['b%d' % layer] = (off, fan_out)
+        off = _align8(off + fan_out)
+    tlay, toff = {}, 0
+    for layer in (1, 2, 3):
+        _, rows, cols = lay['W%d' % layer]
+        ld = _align8(rows)
+        tlay['W%d' % layer] = (toff, ld)
+        toff += cols * ld
+    return lay, off, tlay, toff
+
+
+def _dw_splits(rows):
+    """Split-K of the weight-gradient products over `rows` batch rows: about 1,024 rows
+    per split, at most 64 splits, in the form mcw_mlp_gemm_grouped accepts."""
+    chunks = (rows + 63) // 64
+    want = max(1, min(64, rows // 1024))
+    per = (chunks + want - 1) // want
+    return (chunks + per - 1) // per
+
+
+class EnsembleTrainer:
+    """Adam steps of every member of an ensemble at once on the training engine
+    (include/mcw_mlp.h): per step one gather of the members' batches, the four forward
+    products (bias + SiLU epilogues keeping pre-activations and transposed
+    activations), the loss, the weight- and input-gradient products, the bias
+    gradients, Adam over the flat parameters and the step counter, each one launch for
+    all members.  Parameters live in flat [members, P] vectors (flat_layout).  The step
+    is captured in a CUDA graph on first use and replayed; learning rate, step count and
+    batch counter are device scalars, so the graph never changes."""
+
+    def __init__(self, members, batch, x_all, t_all, w_out, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8,
+                 use_graph=True):
+        import torch
+        self.torch = torch
+        self.members = members
+        self.G = len(members)
+        self.B = int(batch)
+        self.beta1, self.beta2, self.eps = beta1, beta2, eps
+        self.use_graph = use_graph
+        self.graph = None
+        G, B = self.G, self.B
+        self.lay, self.P, self.tlay, self.T = flat_layout()
+        dev = 'cuda'
+        f32, bf16, i32 = torch.float32, torch.bfloat16, torch.int32
+        # parameters, gradients, Adam moments and the bf16 copies (zeros in the padding)
+        self.params = torch.zeros((G, self.P), dtype=f32, device=dev)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.grad = torch.zeros_like(self.params)
+        for g, net in enumerate(members):
+            for layer in range(4):
+                o, rows, cols = self.lay['W%d' % layer]
+                w = net.params[2 * layer]
+                blk = self.params[g, o:o + rows * cols].view(rows, cols)
+                blk[:, :w.shape[1]].copy_(w)
+                ob, nb = self.lay['b%d' % layer]
+                self.params[g, ob:ob + nb].copy_(net.params[2 * layer + 1])
+                mw, vw = net.m[2 * layer], net.v[2 * layer]
+                self.m[g, o:o + rows * cols].view(rows, cols)[:, :w.shape[1]].copy_(mw)
+                self.v[g, o:o + rows * cols].view(rows, cols)[:, :w.shape[1]].copy_(vw)
+                self.m[g, ob:ob + nb].copy_(net.m[2 * layer + 1])
+                self.v[g, ob:ob + nb].copy_(net.v[2 * layer + 1])
+        self.w16 = self.params.to(bf16)
+        self.wt = torch.zeros((G, self.T), dtype=bf16, device=dev)
+        for layer in (1, 2, 3):
+            o, rows, cols = self.lay['W%d' % layer]
+            to, ld = self.tlay['W%d' % layer]
+            self.wt[:, to:to + cols * ld].view(G, cols, ld)[:, :, :rows].copy_(
+                self.w16[:, o:o + rows * cols].view(G, rows, cols).transpose(1, 2))
+        # data (inputs padded to IN_PAD, bf16) and the step's batch
+        n_rows = x_all.shape[0]
+        if n_rows < B:
+            raise ValueError('fewer rows (%d) than the batch (%d)' % (n_rows, B))
+        self.n_rows = n_rows
+        self.x_all = torch.zeros((n_rows, IN_PAD), dtype=bf16, device=dev)
+        self.x_all[:, :DIMS[0]].copy_(x_all.to(bf16))
+        self.t_all = t_all.contiguous().float()
+        self.w_out = w_out.contiguous().float()
+        self.perm = torch.zeros((G, n_rows), dtype=i32, device=dev)
+        self.counter = torch.zeros(1, dtype=i32, device=dev)
+        self.step = torch.full((1,), max(int(net.step) for net in members) + 1, dtype=i32, device=dev)
+        self.lr = torch.full((1,), float(lr), dtype=f32, device=dev)
+        self.loss = torch.zeros(G, dtype=f32, device=dev)
+        H, N = DIMS[1], DIMS[-1]
+        self.x16 = torch.zeros((G, B, IN_PAD), dtype=bf16, device=dev)
+        self.xt = torch.zeros((G, IN_PAD, B), dtype=bf16, device=dev)
+        self.t = torch.zeros((G, B, N), dtype=f32, device=dev)
+        self.h = [torch.zeros((G, B, H), dtype=bf16, device=dev) for _ in range(3)]
+        self.ht = [torch.zeros((G, H, B), dtype=bf16, device=dev) for _ in range(3)]
+        self.z = [torch.zeros((G, B, H), dtype=f32, device=dev) for _ in range(3)]
+        self.y = torch.zeros((G, B, OUT_PITCH), dtype=f32, device=dev)
+        # output gradient (pitch 656, the pad columns stay zero) and hidden-layer gradients
+        self.g32 = [torch.zeros((G, B, H), dtype=f32, device=dev) for _ in range(3)] + \
+                   [torch.zeros((G, B, OUT_PITCH), dtype=f32, device=dev)]
+        self.g16 = [torch.zeros((G, B, H), dtype=bf16, device=dev) for _ in range(3)] + \
+                   [torch.zeros((G, B, OUT_PITCH), dtype=bf16, device=dev)]
+        self.gt = [torch.zeros((G, H, B), dtype=bf16, device=dev) for _ in range(3)] + \
+                  [torch.zeros((G, OUT_PITCH, B), dtype=bf16, device=dev)]
+        self.splits = _dw_splits(B)
+        if self.splits > 1:
+            largest = max(rows * cols for (_, rows, cols) in (self.lay['W%d' % q] for q in range(4)))
+            self.part = torch.zeros((self.splits, G, largest), dtype=f32, device=dev)
+        self._build_calls()
+
+    # ---- the calls of one step, built once (pointers never change)
+    def _gemm(self, epi, m, n, k, a, lda, sa, b, ldb, sb, c, ldc, sc, bias=None, aux=None, ldaux=0, saux=0,
+              c2=None, ldc2=0, sc2=0, ct=None, ldct=0, sct=0, splits=1, s_split=0):
+        ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+        bias_p = bias if isinstance(bias, int) else ptr(bias)
+        return _abi.GemmGroupedC(m, n, k, self.G, splits, epi, a if isinstance(a, int) else ptr(a), lda, sa,
+                                 b if isinstance(b, int) else ptr(b), ldb, sb, bias_p, self.P,
+                                 ptr(aux), ldaux, saux, c if isinstance(c, int) else ptr(c), ldc, sc, s_split,
+                                 ptr(c2), ldc2, sc2, ptr(ct), ldct, sct)
+
+    def _build_calls(self):
+        G, B, P, T = self.G, self.B, self.P, self.T
+        H, N = DIMS[1], DIMS[-1]
+        lay, tlay = self.lay, self.tlay
+        w16 = self.w16.data_ptr()
+        wt = self.wt.data_ptr()
+        par = self.params.data_ptr()
+        grd = self.grad.data_ptr()
+        bf, f4 = 2, 4
+        fwd = []
+        a, lda, sa = self.x16, IN_PAD, B * IN_PAD
+        for layer in range(3):
+            o, rows, cols = lay['W%d' % layer]
+            ob, _ = lay['b%d' % layer]
+            fwd.append(self._gemm(_abi.EPI_BIAS_SILU, B, rows, cols, a, lda, sa, w16 + o * bf, cols, P,
+                                  self.h[layer], H, B * H, bias=par + ob * f4, c2=self.z[layer], ldc2=H,
+                                  sc2=B * H, ct=self.ht[layer], ldct=B, sct=H * B))
+            a, lda, sa = self.h[layer], H, B * H
+        o, rows, cols = lay['W3']
+        ob, _ = lay['b3']
+        fwd.append(self._gemm(_abi.EPI_BIAS_F32, B, N, H, self.h[2], H, B * H, w16 + o * bf, H, P,
+                              self.y, OUT_PITCH, B * OUT_PITCH, bias=par + ob * f4))
+        self.fwd_calls = fwd
+        bwd, reduce = [], []
+        # gradient of layer l's output: g[l] (layer 4: g[3], pitch 656)
+        acts_t = [self.xt] + self.ht          # transposed inputs of layers 1..4
+        for layer in (3, 2, 1, 0):
+            o, rows, cols = lay['W%d' % layer]
+            gt = self.gt[layer]
+            gpitch = OUT_PITCH if layer == 3 else H
+            # dW_l[o, i] = sum_b G[b, o] X[b, i]: A = G^T [rows, B], B = X^T [cols, B]
+            if self.splits == 1:
+                bwd.append(self._gemm(_abi.EPI_F32, rows, cols, B, gt, B, gpitch * B, acts_t[layer], B,
+                                      cols * B, grd + o * f4, cols, P))
+            else:
+                bwd.append(self._gemm(_abi.EPI_F32, rows, cols, B, gt, B, gpitch * B, acts_t[layer], B,
+                                      cols * B, self.part, cols, self.part.shape[2], splits=self.splits,
+                                      s_split=G * self.part.shape[2]))
+                reduce.append((len(bwd) - 1, (self.part.data_ptr(), G * self.part.shape[2], self.part.shape[2],
+                                              cols, grd + o * f4, P, cols, self.splits, G, rows, cols)))
+            if layer == 0:
+                break
+            # G_{l-1} = (G_l W_l) * silu'(Z_{l-1}): A = G_l [B, gpitch], B = W_l^T [cols, ld]
+            to, ld = tlay['W%d' % layer]
+            bwd.append(self._gemm(_abi.EPI_DSILU, B, cols, rows, self.g16[layer], gpitch, B * gpitch,
+                                  wt + to * bf, ld, T, self.g16[layer - 1], H, B * H, aux=self.z[layer - 1],
+                                  ldaux=H, saux=B * H, c2=self.g32[layer - 1], ldc2=H, sc2=B * H,
+                                  ct=self.gt[layer - 1], ldct=B, sct=H * B))
+        self.bwd_calls = bwd
+        self.reduce_after = dict(reduce)
+        cols = (_abi.ColsumLayerC * 4)()
+        for layer in range(4):
+            ob, nb = lay['b%d' % layer]
+            pitch = OUT_PITCH if layer == 3 else H
+            cols[layer] = _abi.ColsumLayerC(self.g32[layer].data_ptr(), pitch, B * pitch, ob, nb, 0)
+        self.colsum_layers = cols
+        tb = (_abi.TransposeBlockC * 3)()
+        for q, layer in enumerate((1, 2, 3)):
+            o, rows, cols_ = lay['W%d' % layer]
+            to, ld = tlay['W%d' % layer]
+            tb[q] = _abi.TransposeBlockC(o, to, ld, rows, cols_)
+        self.transpose_blocks = tb
+
+    def _check(self, rc, what):
+        if rc:
+            raise _abi.McwError(rc, '%s failed' % what)
+
+    def _launch(self, adam=True):
+        """The kernels of one step on the current stream (no host synchronisation)."""
+        torch = self.torch
+        L = _abi.load()
+        st = _stream(torch)
+        G, B = self.G, self.B
+        N = DIMS[-1]
+        self._check(L.mcw_mlp_gather(self.x_all.data_ptr(), self.t_all.data_ptr(), self.t_all.shape[1], N,
+                                     self.perm.data_ptr(), self.n_rows, self.counter.data_ptr(), B, G,
+                                     self.x16.data_ptr(), B * IN_PAD, self.xt.data_ptr(), IN_PAD * B,
+                                     self.t.data_ptr(), N, B * N, st), 'mcw_mlp_gather')
+        for c in self.fwd_calls:
+            self._check(L.mcw_mlp_gemm_grouped(ctypes.byref(c), st), 'forward GEMM')
+        self.loss.zero_()
+        self._check(L.mcw_mlp_loss_grouped(self.y.data_ptr(), OUT_PITCH, B * OUT_PITCH, self.t.data_ptr(), N,
+                                           B * N, self.w_out.data_ptr(), G, B, N, self.g32[3].data_ptr(),
+                                           OUT_PITCH, B * OUT_PITCH, self.g16[3].data_ptr(), B * OUT_PITCH,
+                                           self.gt[3].data_ptr(), B, OUT_PITCH * B, self.loss.data_ptr(), st),
+                    'mcw_mlp_loss_grouped')
+        for i, c in enumerate(self.bwd_calls):
+            self._check(L.mcw_mlp_gemm_grouped(ctypes.byref(c), st), 'backward GEMM')
+            if i in self.reduce_after:
+                self._check(L.mcw_mlp_reduce_splits(*self.reduce_after[i], st), 'mcw_mlp_reduce_splits')
+        self._check(L.mcw_mlp_colsum_grouped(self.colsum_layers, 4, G, B, self.grad.data_ptr(), self.P, st),
+                    'mcw_mlp_colsum_grouped')
+        if not adam:
+            return
+        self._check(L.mcw_mlp_adam_grouped(self.params.data_ptr(), self.grad.data_ptr(), self.m.data_ptr(),
+                                           self.v.data_ptr(), self.w16.data_ptr(), self.P, G, self.lr.data_ptr(),
+                                           self.step.data_ptr(), self.beta1, self.beta2, self.eps,
+                                           self.wt.data_ptr(), self.T, self.transpose_blocks, 3, st),
+                    'mcw_mlp_adam_grouped')
+        self._check(L.mcw_mlp_advance(self.counter.data_ptr(), self.step.data_ptr(), st), 'mcw_mlp_advance')
+
+    def set_epoch(self, perms, lr):
+        """Row order of each member for the next len(rows) // batch steps, and the learning rate."""
+        torch = self.torch
+        self.perm.copy_(torch.as_tensor(np.asarray(perms, np.int32)))
+        self.counter.zero_()
+        self.lr.fill_(float(lr))
+
+    def run_step(self):
+        """One Adam step of every member (graph replay after the first)."""
+        torch = self.torch
+        if not self.use_graph:
+            self._launch()
+            return
+        if self.graph is None:
+            # an eager step first: one-time set-up (module loading, kernel attributes)
+            # must not happen inside the capture; then undo it
+            saved = [t.clone() for t in (self.params, self.m, self.v, self.w16, self.wt, self.counter, self.step)]
+            self._launch()
+            for t, s0 in zip((self.params, self.m, self.v, self.w16, self.wt, self.counter, self.step), saved):
+                t.copy_(s0)
+            torch.cuda.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph):
+                self._launch()
+        self.graph.replay()
+
+    def gradients(self):
+        """Forward and backward of the current batch without the Adam step: the
+        gradients of every member as [W1, b1, ..., W4, b4] (W1 without its padding)."""
+        self._launch(adam=False)
+        self.torch.cuda.synchronize()
+        out = []
+        for g in range(self.G):
+            gr = []
+            for layer in range(4):
+                o, rows, cols = self.lay['W%d' % layer]
+                w = self.grad[g, o:o + rows * cols].view(rows, cols)
+                gr.append(w[:, :DIMS[layer]].clone())
+                ob, nb = self.lay['b%d' % layer]
+                gr.append(self.grad[g, ob:ob + nb].clone())
+            out.append(gr)
+        return out
+
+    def export(self):
+        """Copy the trained parameters, moments and step count back into the members."""
+        torch = self.torch
+        torch.cuda.synchronize()
+        step = int(self.step.item()) - 1
+        for g, net in enumerate(self.members):
+            for layer in range(4):
+                o, rows, cols = self.lay['W%d' % layer]
+                k = DIMS[layer]
+                for dst, src in ((net.params, self.params), (net.m, self.m), (net.v, self.v)):
+                    dst[2 * layer].copy_(src[g, o:o + rows * cols].view(rows, cols)[:, :k])
+                ob, nb = self.lay['b%d' % layer]
+                for dst, src in ((net.params, self.params), (net.m, self.m), (net.v, self.v)):
+                    dst[2 * layer + 1].copy_(src[g, ob:ob + nb])
+            net.w16 = [_cast(torch, w.contiguous()) for w in net.params[0::2]]
+            net.step = step
+            net._blob = None
+
+
 @dataclass
 class Dataset:
     x: np.ndarray        # encoded inputs [n, 4]
@@ -405,20 +705,37 @@ def rel_rms(pred, ref, weights=None):
     return np.sqrt(((pred - ref) ** 2 * w).sum(axis=-1) / np.maximum((ref ** 2 * w).sum(axis=-1), 1e-30))
 
 
-def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
-    """Train an ensemble on a Dataset; returns Ensemble."""
+def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None, engine='grouped'):
+    """Train an ensemble on a Dataset; returns Ensemble.  engine 'grouped': all members
+    at once on the training engine (EnsembleTrainer, one graph replay per step);
+    'layerwise': member by member on mcw_mlp_gemm and the per-member kernels."""
     import torch
     y = ds.y.astype(np.float64)
     y_mean, y_std = y.mean(0), np.maximum(y.std(0), 1e-3)
     t_all = torch.from_numpy(((y - y_mean) / y_std).astype(np.float32)).cuda()
     x_all = _cast(torch, torch.from_numpy(ds.x).cuda())
     w_out = torch.from_numpy(output_weights()).cuda()
-    out = []
     n = ds.x.shape[0]
+    nets = []
     for k in range(members):
         net = SurrogateMLP(seed=seed * 100 + k)
         net.y_mean = torch.from_numpy(y_mean).cuda()
         net.y_std = torch.from_numpy(y_std).cuda()
+        nets.append(net)
+    if engine == 'grouped':
+        # every member's step in one captured graph of grouped launches
+        rngs = [np.random.default_rng(seed * 100 + k) for k in range(members)]
+        tr = EnsembleTrainer(nets, batch, torch.from_numpy(ds.x).cuda(), t_all, w_out, lr=lr)
+        for ep in range(epochs):
+            lr_ep = lr * (0.5 * (1 + math.cos(math.pi * ep / epochs)))
+            tr.set_epoch([r.permutation(n) for r in rngs], lr_ep)
+            for _ in range(n // batch):
+                tr.run_step()
+            if log and (ep % 50 == 0 or ep == epochs - 1):
+                log('epoch %d loss %s' % (ep, np.round(tr.loss.cpu().numpy(), 5).tolist()))
+        tr.export()
+        return Ensemble(nets)
+    for k, net in enumerate(nets):
         rng = np.random.default_rng(seed * 100 + k)
         for ep in range(epochs):
             perm = torch.from_numpy(rng.permutation(n)).cuda()
@@ -428,9 +745,8 @@ def train(ds, members=5, epochs=400, batch=256, lr=1e-3, seed=0, log=None):
                 loss = net.train_step(x_all[idx].contiguous(), t_all[idx].contiguous(), w_out, lr=lr_ep)
             if log and (ep % 50 == 0 or ep == epochs - 1):
                 log('member %d epoch %d loss %.5f' % (k, ep, float(loss)))
-        out.append(net)
     torch.cuda.synchronize()
-    return Ensemble(out)
+    return Ensemble(nets)
 
 
 def save(ensemble, path):
