@@ -45,6 +45,14 @@ SEED = 0x5EED0002
 # conversions (8), HG inversion (6), sin/cos/sqrt of the angles (6), rotation and
 # renormalisation (25), move, compensated path sum and boundary tests (15).
 ALG_INST_PER_EVENT = 100
+# algorithmic work per scatter event by pipe, as the survey of the reference's walk
+# counts it (five uniforms = 1.25 Philox4x32-10 blocks of 10 rounds x (2 wide
+# multiplies = 4 IMAD, 4 XOR/ADD, 2 key adds) = 125 integer ops; HG inversion,
+# rotation, move, path and tests 30 FP32 ops; log, sin, cos and 2 square roots 5 SFU
+# ops), and the per-SM rate of each pipe per clock (4 schedulers x 32 lanes for the
+# integer and FP32 pipes, 16 for the SFU)
+OPS_PER_EVENT = {'int': 125, 'fp32': 30, 'sfu': 5}
+PIPE_LANES_PER_SM = {'int': 128, 'fp32': 128, 'sfu': 16}
 RECORD_BYTES = 32
 
 
@@ -364,7 +372,7 @@ def run_pol(args):
 
 
 def run_surrogate(args):
-    """Surrogate workload: --surrogate-configs configs (16,384 by default) x 2e5 photons walked
+    """Surrogate workload: --surrogate-configs configs (4,096 by default, BASELINE config 4) x 2e5 photons walked
     on the GPU, 5-member ensemble trained on the tensor-core kernels, 512 held-out configs
     judged by 1e6- and 1e7-photon Monte Carlo; BRF/s of the network against plain Monte
     Carlo; then the inverse workload."""
@@ -393,6 +401,9 @@ def run_surrogate(args):
     err = S.rel_rms(pred_brf, ref_brf)
     err7 = S.rel_rms(pred_brf, ref7_brf)
     floor = S.rel_rms(ref2_brf, ref_brf) / np.sqrt(2)
+    # the network's own error against 1e6-photon Monte Carlo: that walk's noise (floor,
+    # from two independent 1e6-photon walks) removed in quadrature, per config
+    err_corr = np.sqrt(np.maximum(err ** 2 - floor ** 2, 0.0))
     err_small_mc = S.rel_rms(ds.brf[:n_hold], ref_brf)
     rate_net = S.inference_rate(ens)
     rate_mc = n_hold / t_ref
@@ -405,6 +416,9 @@ def run_surrogate(args):
             'mc_brf_per_s': rate_mc, 'speedup_vs_mc': rate_net / rate_mc,
             'rms_rel_brf_err_vs_1e6_mc': {'median': float(np.median(err)), 'mean': float(np.mean(err)),
                                           'p90': float(np.percentile(err, 90))},
+            'rms_rel_brf_err_vs_1e6_mc_noise_removed': {'median': float(np.median(err_corr)),
+                                                        'mean': float(np.mean(err_corr)),
+                                                        'p90': float(np.percentile(err_corr, 90))},
             'rms_rel_brf_err_vs_1e7_mc': {'median': float(np.median(err7)), 'mean': float(np.mean(err7)),
                                           'p90': float(np.percentile(err7, 90))},
             'mc_1e6_noise_floor': float(np.median(floor)),
@@ -460,6 +474,108 @@ def run_mlp(args):
     return 0
 
 
+def run_train(args):
+    """Surrogate training on the training engine: (a) one Adam step of a 5-member
+    ensemble at batch 256 (BASELINE config 4's batch), all members at once from one
+    captured CUDA graph, against the same step run member by member on the layer-wise
+    kernels; (b) forward + backward of one network over 65,536 rows (split-K weight
+    gradients) against the layer-wise autograd path.  FLOPs: 3 x 596,480 per row
+    (forward, input and weight gradients)."""
+    import torch
+    from monte_carlompi_gb300 import surrogate as S
+    peaks, src = measured_peaks()
+    peak = float(peaks.get('bf16_tflops_sustained') or peaks.get('bf16_tflops') or 1700.0)
+    flop_row = 3.0 * 2 * sum(a * b for a, b in zip(S.DIMS[:-1], S.DIMS[1:]))
+    rng = np.random.default_rng(0x5EED0004)
+    w = torch.from_numpy(S.output_weights()).cuda()
+    big = 65536
+    if args.train_part == 'big':
+        # only the 65,536-row forward + backward (a short case for a profiler)
+        xb = torch.from_numpy(rng.uniform(-1, 1, (big, 4)).astype(np.float32)).cuda()
+        tb = torch.from_numpy(rng.standard_normal((big, 649)).astype(np.float32)).cuda()
+        one = S.EnsembleTrainer([S.SurrogateMLP(seed=9)], big, xb, tb, w, use_graph=False)
+        one.set_epoch([np.arange(big)], 1e-3)
+        for _ in range(args.warmup + args.steps):
+            one._launch(adam=False)
+        torch.cuda.synchronize()
+        print(json.dumps({'workload': 'train', 'part': 'big', 'rows': big, 'launch_sets': args.warmup + args.steps}))
+        return 0
+    n_rows, members, batch = 16384 - 512, 5, 256
+    x = torch.from_numpy(rng.uniform(-1, 1, (n_rows, 4)).astype(np.float32)).cuda()
+    t = torch.from_numpy(rng.standard_normal((n_rows, 649)).astype(np.float32)).cuda()
+    nets = [S.SurrogateMLP(seed=k) for k in range(members)]
+    tr = S.EnsembleTrainer(nets, batch, x, t, w, lr=1e-3)
+    steps = min(max(args.steps, 10) * 10, n_rows // batch)
+    tr.set_epoch([rng.permutation(n_rows) for _ in nets], 1e-3)
+    for _ in range(args.warmup):
+        tr.run_step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tr.set_epoch([rng.permutation(n_rows) for _ in nets], 1e-3)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        tr.run_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_grouped = e0.elapsed_time(e1) / steps
+    # the same step member by member on the layer-wise kernels (host-launched)
+    x16 = S._cast(torch, x)
+    perm = torch.from_numpy(rng.permutation(n_rows)).cuda()
+    for _ in range(args.warmup):
+        for net in nets:
+            net.train_step(x16[perm[:batch]].contiguous(), t[perm[:batch]].contiguous(), w)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    reps = 20
+    for r in range(reps):
+        idx = perm[r * batch:(r + 1) * batch]
+        for net in nets:
+            net.train_step(x16[idx].contiguous(), t[idx].contiguous(), w)
+    torch.cuda.synchronize()
+    ms_layer = (time.perf_counter() - t0) * 1e3 / reps
+    # forward + backward of 65,536 rows, one network
+    xb = torch.from_numpy(rng.uniform(-1, 1, (big, 4)).astype(np.float32)).cuda()
+    tb = torch.from_numpy(rng.standard_normal((big, 649)).astype(np.float32)).cuda()
+    one = S.EnsembleTrainer([S.SurrogateMLP(seed=9)], big, xb, tb, w, use_graph=False)
+    one.set_epoch([np.arange(big)], 1e-3)
+    for _ in range(args.warmup):
+        one._launch(adam=False)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        one._launch(adam=False)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_big = e0.elapsed_time(e1) / args.steps
+    # the same through the layer-wise autograd path
+    params = [p.detach().clone().requires_grad_(True) for p in one.members[0].params]
+    y = S.mlp_apply(xb, params)
+    y.backward(torch.ones_like(y))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        y = S.mlp_apply(xb, params)
+        y.backward(torch.ones_like(y))
+    torch.cuda.synchronize()
+    ms_big_layer = (time.perf_counter() - t0) * 1e3 / 2
+    tflops = flop_row * big / (ms_big / 1e3) / 1e12
+    line = {'metric': 'surrogate training: ensemble Adam step time', 'workload': 'train',
+            'value': ms_grouped, 'unit': 'ms per 5-member step (batch 256)', 'higher_is_better': False,
+            'steps': args.steps, 'warmup': args.warmup, 'dtype': 'bf16 (fp32 accumulate, fp32 Adam)',
+            'data': 'synthetic',
+            'config': {'net': '4-256-256-256-649 SiLU', 'members': members, 'batch': batch,
+                       'engine': 'grouped tcgen05 GEMMs fed by TMA, one CUDA graph per step '
+                                 '(16 launches for all members)'},
+            'layerwise_ms_per_step': ms_layer, 'speedup_vs_layerwise': ms_layer / ms_grouped,
+            'fwd_bwd_65536': {'ms': ms_big, 'layerwise_ms': ms_big_layer, 'speedup': ms_big_layer / ms_big,
+                              'tflops': tflops, 'splits': one.splits},
+            'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s',
+                         'frac': tflops / peak, 'peak_source': src + ' (bf16 sustained)',
+                         'kernel': '65,536-row forward + backward'}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_inverse(ens, walker, n_obs):
     """Inverse configuration: observed BRFs from 1e6-photon MC at hidden r_eff
     (log-uniform 50-1500 um, known lambda, theta0, depth) plus 1% Gaussian noise; Gauss-Newton
@@ -474,37 +590,53 @@ def run_inverse(ens, walker, n_obs):
     t_obs = _t.perf_counter() - t0
     obs = obs * (1 + 0.01 * np.random.default_rng(0x5EED0051).standard_normal(obs.shape))
     known = raw[:, 1:]
-    res = I.retrieve(ens, walker, obs, known)
+    noise = dict(obs_photons=1000000, obs_noise=0.01)
+    # residuals weighted by their inverse noise variance; where the ensemble spread of the
+    # retrieved r_eff exceeds 2%, the answer is corrected by walks at it (the surrogate's
+    # Jacobian, Monte Carlo residuals)
+    res = I.retrieve(ens, walker, obs, known, criterion='r_eff', fallback='correct', **noise)
     err = np.abs(res['r_eff'] / raw[:, 0] - 1)
-    # the same with the fallback decided on the spread of the retrieved r_eff
-    res_r = I.retrieve(ens, walker, obs, known, criterion='r_eff')
+    # the same with Monte Carlo Gauss-Newton (central differences) as the fallback
+    res_r = I.retrieve(ens, walker, obs, known, criterion='r_eff', fallback='gn', **noise)
     err_r = np.abs(res_r['r_eff'] / raw[:, 0] - 1)
+    # the surrogate alone (no walk)
+    s_net = I.surrogate_gn(ens, obs, known, **noise)[0]
+    err_net = np.abs(np.exp(s_net) / raw[:, 0] - 1)
     # the same retrieval with plain Monte Carlo only, on a subset
     n_sub = min(64, n_obs)
     t0 = _t.perf_counter()
-    s_mc, evals = I.mc_retrieve(walker, obs[:n_sub], known[:n_sub])
+    s_mc, evals = I.mc_retrieve(walker, obs[:n_sub], known[:n_sub], **noise)
     t_mc = _t.perf_counter() - t0
     err_mc = np.abs(np.exp(s_mc) / raw[:n_sub, 0] - 1)
     t_sur = res['seconds_net'] + res['seconds_mc']
     net_evals = n_obs * (16 + 6 + 1)
     return {'observations': n_obs, 'obs_photons': 1000000, 'noise': 0.01,
+            'weights': 'inverse noise variance per bin: counting noise of the 1e6-photon observation '
+                       '+ 1% noise + ensemble variance',
             'flagged_for_mc': float(res['flagged'].mean()),
             'r_eff_rel_err': {'median': float(np.median(err)), 'p90': float(np.percentile(err, 90))},
             'r_eff_rel_err_unflagged_median':
                 float(np.median(err[~res['flagged']])) if np.any(~res['flagged']) else None,
+            'posterior_width_median': float(np.median(res['sigma_noise'])),
             'seconds': {'surrogate_gn': res['seconds_net'], 'mc_fallback': res['seconds_mc']},
             'seconds_per_retrieval': t_sur / n_obs,
             'brf_evals': {'surrogate': net_evals, 'mc_fallback': res['mc_brf_evals']},
             'mc_only': {'subset': n_sub, 'method': '16-point grid + 4 Gauss-Newton iterations, 1e6-photon '
-                                                    'BRFs, central-difference Jacobians',
+                                                    'BRFs, central-difference Jacobians, same weights',
                         'r_eff_rel_err_median': float(np.median(err_mc)),
+                        'r_eff_rel_err_p90': float(np.percentile(err_mc, 90)),
                         'surrogate_path_err_median_same_subset': float(np.median(err[:n_sub])),
+                        'surrogate_path_err_p90_same_subset': float(np.percentile(err[:n_sub], 90)),
                         'seconds_per_retrieval': t_mc / n_sub, 'brf_evals': evals},
             'speedup_per_retrieval_vs_mc': (t_mc / n_sub) / (t_sur / n_obs),
             'seconds_obs_generation': t_obs,
-            'criterion': 'BRF ensemble spread > 2%',
+            'criterion': 'ensemble spread of the retrieved r_eff > 2%; fallback: walks at the answer '
+                         '(2 iterations, surrogate Jacobian)',
+            'surrogate_only_r_eff_rel_err': {'median': float(np.median(err_net)),
+                                             'p90': float(np.percentile(err_net, 90))},
             'r_eff_criterion': {
-                'criterion': 'ensemble spread of the retrieved r_eff > 2%',
+                'criterion': 'ensemble spread of the retrieved r_eff > 2%; fallback: Monte Carlo '
+                             'Gauss-Newton (3 iterations, central differences)',
                 'flagged_for_mc': float(res_r['flagged'].mean()),
                 'r_eff_rel_err': {'median': float(np.median(err_r)), 'p90': float(np.percentile(err_r, 90))},
                 'r_eff_rel_err_unflagged_median':
@@ -663,8 +795,17 @@ def run_ours(args):
         sm_max = float(peaks.get('sm_max_mhz') or 2070.0)
         ev_per_launch = events_all / walks / world
         kern_s = t_kern / walks
-        achieved = ev_per_launch * ALG_INST_PER_EVENT / kern_s / 1e12
-        peak = 152 * 4 * 32 * sm_max * 1e6 / 1e12
+        ev_rate = ev_per_launch / kern_s
+        pipes = {}
+        for pipe, ops in OPS_PER_EVENT.items():
+            pk = 152 * PIPE_LANES_PER_SM[pipe] * sm_max * 1e6 / 1e12
+            pipes[pipe] = {'achieved': ev_rate * ops / 1e12, 'peak': pk, 'frac': ev_rate * ops / 1e12 / pk,
+                           'ops_per_event': ops}
+        limiting = max(pipes, key=lambda q: pipes[q]['frac'])
+        achieved = pipes[limiting]['achieved']
+        peak = pipes[limiting]['peak']
+        issue_peak = 152 * 4 * 32 * sm_max * 1e6 / 1e12
+        achieved_100 = ev_rate * ALG_INST_PER_EVENT / 1e12
         rec_gbs = (n * RECORD_BYTES) / kern_s / 1e9
         tb = committed_traffic()
         line = {
@@ -689,12 +830,16 @@ def run_ours(args):
                     'path': 'Walker.walk -> mcw_walk, records written into pinned host memory, '
                             'tallies copied back; host wall clock per call'},
             'roofline': {
-                'bound': 'issue', 'achieved': achieved, 'peak': peak, 'unit': 'Tinst/s',
+                'bound': 'issue (%s pipe)' % limiting, 'achieved': achieved, 'peak': peak, 'unit': 'Tops/s',
                 'frac': achieved / peak,
                 'traffic': (tb * n) if tb else None,
-                'basis': '%d algorithmic thread-instructions per scatter event; peak = 152 SMs x '
-                         '4 schedulers x 32 lanes x %.0f MHz (sm_max_mhz, %s)' % (
-                             ALG_INST_PER_EVENT, sm_max, src),
+                'basis': 'max over pipes of events/s x algorithmic ops per event (int 125, fp32 30, sfu 5) '
+                         'against the pipe rate (152 SMs x lanes per clock x %.0f MHz, sm_max_mhz, %s)' % (
+                             sm_max, src),
+                'pipes': pipes,
+                'issue_100': {'achieved': achieved_100, 'peak': issue_peak, 'frac': achieved_100 / issue_peak,
+                              'basis': '%d thread-instructions per scatter event against the issue rate '
+                                       '(152 x 4 x 32 lanes x sm_max_mhz)' % ALG_INST_PER_EVENT},
                 'hbm': {'achieved': rec_gbs, 'peak': peaks.get('hbm_gbs'), 'unit': 'GB/s',
                         'frac': rec_gbs / float(peaks.get('hbm_gbs') or 6800.0),
                         'bytes': 'records, 32 B/photon'},
@@ -718,8 +863,11 @@ def main():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--repeats', type=int, default=0,
                     help='walks per timed step (0: enough for about 2 s of timed work)')
-    ap.add_argument('--workload', default='walk', choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol', 'lone'])
-    ap.add_argument('--surrogate-configs', type=int, default=16384)
+    ap.add_argument('--workload', default='walk',
+                    choices=['walk', 'sweep', 'surrogate', 'mlp', 'pol', 'lone', 'train'])
+    ap.add_argument('--train-part', default='all', choices=['all', 'big'],
+                    help="train workload: 'big' runs only the 65,536-row forward + backward")
+    ap.add_argument('--surrogate-configs', type=int, default=4096)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
     args = ap.parse_args()
@@ -735,6 +883,8 @@ def main():
         return run_pol(args)
     if args.workload == 'lone':
         return run_lone(args)
+    if args.workload == 'train':
+        return run_train(args)
     return run_ours(args)
 
 

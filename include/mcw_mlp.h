@@ -154,7 +154,10 @@ int mcw_mlp_loss_grouped(const float *y, int64_t ldy, int64_t stride_y, const fl
                          int64_t stride_g16t, float *loss, void *stream);
 
 /* Column sums of up to four gradient matrices (bias gradients):
- * out[g * stride_out + out_offset + j] = sum over i < m of g[g * stride + i * ld + j], j < n. */
+ * out[g * stride_out + out_offset + j] = sum over i < m of g[g * stride + i * ld + j], j < n.
+ * With partial (n_layers * groups * ceil(m / rows_per_chunk) * max n floats) and
+ * 0 < rows_per_chunk < m, the rows are summed in chunks in parallel and the chunks'
+ * sums added in order (the result does not depend on the launch either way). */
 typedef struct {
     const float *g;
     int64_t ld, stride;
@@ -164,7 +167,7 @@ typedef struct {
 } McwColsumLayer;
 
 int mcw_mlp_colsum_grouped(const McwColsumLayer *layers, int32_t n_layers, int32_t groups, int32_t m, float *out,
-                           int64_t stride_out, void *stream);
+                           int64_t stride_out, float *partial, int32_t rows_per_chunk, void *stream);
 
 /* A block of the flat parameters whose bf16 copy is also kept transposed:
  * wt[offset_t + c * ld_t + o] = w[offset + o * cols + c] for o < rows, c < cols. */

@@ -220,7 +220,8 @@ def load(path=None):
         'mcw_mlp_reduce_splits': ([vp, i64, i64, i64, vp, i64, i64, i32, i32, i32, i32, vp], ctypes.c_int),
         'mcw_mlp_loss_grouped': ([vp, i64, i64, vp, i64, i64, vp, i32, i32, i32, vp, i64, i64, vp, i64,
                                   vp, i64, i64, vp, vp], ctypes.c_int),
-        'mcw_mlp_colsum_grouped': ([ctypes.POINTER(ColsumLayerC), i32, i32, i32, vp, i64, vp], ctypes.c_int),
+        'mcw_mlp_colsum_grouped': ([ctypes.POINTER(ColsumLayerC), i32, i32, i32, vp, i64, vp, i32, vp],
+                                   ctypes.c_int),
         'mcw_mlp_adam_grouped': ([vp, vp, vp, vp, vp, i64, i32, vp, vp, ctypes.c_float, ctypes.c_float,
                                   ctypes.c_float, vp, i64, ctypes.POINTER(TransposeBlockC), i32, vp],
                                  ctypes.c_int),

@@ -225,7 +225,12 @@ __global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ T
     asm volatile("tcgen05.fence::after_thread_sync;\n");
 
     if (ok) {
-        const int m = m0 + warp * 32 + lane;
+        // epilogue: lane l of warp w holds row m0 + 32w + l of each 32-column block;
+        // the pipeline's shared memory (free now) gives every warp a 32 x 33 staging
+        // tile, so row-major loads and stores go one row (128 bytes) per instruction
+        float *tile = reinterpret_cast<float *>(smem + (size_t)warp * (32 * 33 * 4));
+        const int rbase = m0 + warp * 32;
+        const int m = rbase + lane;
         const bool row_ok = m < p.m;
         const bool have_acc = nch > 0;
 #pragma unroll 1
@@ -244,7 +249,7 @@ __global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ T
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             const int nb = n0 + c0;
-            if (!row_ok || nb >= p.n) continue;
+            if (nb >= p.n) break;                                   // warp-uniform
             const int cnt = min(32, p.n - nb);
             float z[32];
 #pragma unroll
@@ -256,54 +261,66 @@ __global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ T
                     if (j < cnt) z[j] += __ldg(b + j);
             }
             if (kEpi == MCW_EPI_DSILU) {
-                const float *ax = p.aux + (size_t)g * p.s_aux + (size_t)m * p.ld_aux + nb;
-                float a[32];
+                // the pre-activations, row by row into the tile, then column j of lane's row
+                const float *ax = p.aux + (size_t)g * p.s_aux + nb + lane;
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) {
+                    const int row = rbase + r;
+                    tile[r * 33 + lane] = (row < p.m && lane < cnt) ? __ldg(ax + (size_t)row * p.ld_aux) : 0.f;
+                }
+                __syncwarp();
 #pragma unroll
-                for (int j = 0; j < 32; ++j) a[j] = j < cnt ? __ldg(ax + j) : 0.f;
-#pragma unroll
-                for (int j = 0; j < 32; ++j) z[j] *= dsilu(a[j]);
+                for (int j = 0; j < 32; ++j) z[j] *= dsilu(tile[lane * 33 + j]);
+                __syncwarp();
             }
             // f32 output: the product (F32, BIAS_F32, split partials) or the kept
             // pre-activation / gradient (c2 of BIAS_SILU and DSILU)
             float *c32 = nullptr;
-            if (kEpi == MCW_EPI_F32)
-                c32 = static_cast<float *>(p.c) + (size_t)sp * p.s_split + (size_t)g * p.s_c + (size_t)m * p.ldc + nb;
-            else if (kEpi == MCW_EPI_BIAS_F32)
-                c32 = static_cast<float *>(p.c) + (size_t)g * p.s_c + (size_t)m * p.ldc + nb;
-            else if (p.c2)
-                c32 = static_cast<float *>(p.c2) + (size_t)g * p.s_c2 + (size_t)m * p.ldc2 + nb;
+            long long ld32 = 0;
+            if (kEpi == MCW_EPI_F32) {
+                c32 = static_cast<float *>(p.c) + (size_t)sp * p.s_split + (size_t)g * p.s_c;
+                ld32 = p.ldc;
+            } else if (kEpi == MCW_EPI_BIAS_F32) {
+                c32 = static_cast<float *>(p.c) + (size_t)g * p.s_c;
+                ld32 = p.ldc;
+            } else if (p.c2) {
+                c32 = static_cast<float *>(p.c2) + (size_t)g * p.s_c2;
+                ld32 = p.ldc2;
+            }
             if (c32) {
-                if (cnt == 32 && (reinterpret_cast<uintptr_t>(c32) & 15) == 0) {
 #pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        reinterpret_cast<float4 *>(c32)[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (j < cnt) c32[j] = z[j];
+                for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = z[j];
+                __syncwarp();
+                float *dst = c32 + nb + lane;
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) {
+                    const int row = rbase + r;
+                    if (row < p.m && lane < cnt) dst[(size_t)row * ld32] = tile[r * 33 + lane];
                 }
+                __syncwarp();
             }
             if (kEpi == MCW_EPI_BIAS_SILU || kEpi == MCW_EPI_DSILU) {
-                __align__(16) __nv_bfloat16 h[32];
+                float h[32];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) h[j] = __float2bfloat16(kEpi == MCW_EPI_BIAS_SILU ? silu(z[j]) : z[j]);
-                __nv_bfloat16 *c16 = static_cast<__nv_bfloat16 *>(p.c) + (size_t)g * p.s_c + (size_t)m * p.ldc + nb;
-                if (cnt == 32 && (reinterpret_cast<uintptr_t>(c16) & 15) == 0) {
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) reinterpret_cast<uint4 *>(c16)[q] = reinterpret_cast<const uint4 *>(h)[q];
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j)
-                        if (j < cnt) c16[j] = h[j];
-                }
-                if (p.ct) {
+                for (int j = 0; j < 32; ++j) h[j] = kEpi == MCW_EPI_BIAS_SILU ? silu(z[j]) : z[j];
+                if (p.ct && row_ok) {
                     // transposed copy [n, m]: for each column the warp's lanes write 32
                     // consecutive rows
                     __nv_bfloat16 *t16 = static_cast<__nv_bfloat16 *>(p.ct) + (size_t)g * p.s_ct + m;
 #pragma unroll
                     for (int j = 0; j < 32; ++j)
-                        if (j < cnt) t16[(size_t)(nb + j) * p.ldct] = h[j];
+                        if (j < cnt) t16[(size_t)(nb + j) * p.ldct] = __float2bfloat16(h[j]);
                 }
+#pragma unroll
+                for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = h[j];
+                __syncwarp();
+                __nv_bfloat16 *dst = static_cast<__nv_bfloat16 *>(p.c) + (size_t)g * p.s_c + nb + lane;
+#pragma unroll 4
+                for (int r = 0; r < 32; ++r) {
+                    const int row = rbase + r;
+                    if (row < p.m && lane < cnt) dst[(size_t)row * p.ldc] = __float2bfloat16(tile[r * 33 + lane]);
+                }
+                __syncwarp();
             }
         }
     } else if (threadIdx.x == 0) {
@@ -392,25 +409,44 @@ struct ColsumTable {
     int n_layers;
 };
 
-__global__ void colsum_grouped_kernel(const ColsumTable tab, int m, float *out, long long s_out) {
-    const ColsumLayer L = tab.l[blockIdx.y];
-    const int g = blockIdx.z;
+// One pass over rows [row0, row1) of every (layer, group): 8 row lanes per column,
+// their partial sums combined in a fixed order.  blockIdx.y is the row chunk; the
+// result goes to out (one chunk) or to partial[((z * chunks + chunk) * ldp) + col].
+__global__ void colsum_grouped_kernel(const ColsumTable tab, int groups, int m, int rows_per_chunk, float *out,
+                                      long long s_out, float *partial, int ldp) {
+    const int layer = blockIdx.z / groups, g = blockIdx.z % groups;
+    const ColsumLayer L = tab.l[layer];
     const int col = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int row0 = threadIdx.x >> 5;
+    const int row_lane = threadIdx.x >> 5;
+    const int r0 = blockIdx.y * rows_per_chunk, r1 = min(m, r0 + rows_per_chunk);
     __shared__ float part[8][32];
     float acc = 0.f;
     if (col < L.n) {
         const float *s = L.src + (size_t)g * L.s_g + col;
-        for (int r = row0; r < m; r += 8) acc += s[(size_t)r * L.ld];
+        for (int r = r0 + row_lane; r < r1; r += 8) acc += s[(size_t)r * L.ld];
     }
-    part[row0][threadIdx.x & 31] = acc;
+    part[row_lane][threadIdx.x & 31] = acc;
     __syncthreads();
-    if (row0 == 0 && col < L.n) {
-        float s = 0.f;
+    if (row_lane == 0 && col < L.n) {
+        float t = 0.f;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) s += part[q][threadIdx.x];
-        out[(size_t)g * s_out + L.off + col] = s;
+        for (int q = 0; q < 8; ++q) t += part[q][threadIdx.x];
+        if (partial) partial[((size_t)blockIdx.z * gridDim.y + blockIdx.y) * ldp + col] = t;
+        else out[(size_t)g * s_out + L.off + col] = t;
     }
+}
+
+// Second pass: the chunks' partial sums added in order.
+__global__ void colsum_finish_kernel(const ColsumTable tab, int groups, int chunks, const float *partial, int ldp,
+                                     float *out, long long s_out) {
+    const int layer = blockIdx.z / groups, g = blockIdx.z % groups;
+    const ColsumLayer L = tab.l[layer];
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= L.n) return;
+    const float *p = partial + (size_t)blockIdx.z * chunks * ldp + col;
+    float t = 0.f;
+    for (int c = 0; c < chunks; ++c) t += p[(size_t)c * ldp];
+    out[(size_t)g * s_out + L.off + col] = t;
 }
 
 // Transposed bf16 copies of weight blocks written by Adam (the B operands of the
@@ -623,7 +659,7 @@ int mcw_mlp_loss_grouped(const float *y, int64_t ldy, int64_t stride_y, const fl
 }
 
 int mcw_mlp_colsum_grouped(const McwColsumLayer *layers, int32_t n_layers, int32_t groups, int32_t m, float *out,
-                           int64_t stride_out, void *stream) {
+                           int64_t stride_out, float *partial, int32_t rows_per_chunk, void *stream) {
     if (!layers || n_layers < 1 || n_layers > 4 || groups < 1 || m < 0 || !out) return MCW_MLP_ERR_ARG;
     ColsumTable tab;
     memset(&tab, 0, sizeof(tab));
@@ -639,8 +675,16 @@ int mcw_mlp_colsum_grouped(const McwColsumLayer *layers, int32_t n_layers, int32
     }
     tab.n_layers = n_layers;
     if (nmax == 0) return 0;
-    colsum_grouped_kernel<<<dim3((nmax + 31) / 32, n_layers, groups), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        tab, m, out, stride_out);
+    const bool split = partial && rows_per_chunk > 0 && rows_per_chunk < m;
+    const int rpc = split ? rows_per_chunk : (m > 0 ? m : 1);
+    const int chunks = (m + rpc - 1) / rpc > 0 ? (m + rpc - 1) / rpc : 1;
+    if (chunks > 65535 || (long long)n_layers * groups > 65535) return MCW_MLP_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    colsum_grouped_kernel<<<dim3((nmax + 31) / 32, chunks, n_layers * groups), 256, 0, s>>>(
+        tab, groups, m, rpc, out, stride_out, split ? partial : nullptr, nmax);
+    if (split)
+        colsum_finish_kernel<<<dim3((nmax + 127) / 128, 1, n_layers * groups), 128, 0, s>>>(
+            tab, groups, chunks, partial, nmax, out, stride_out);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
 }
 

@@ -440,6 +440,11 @@ class EnsembleTrainer:
         self.gt = [torch.zeros((G, H, B), dtype=bf16, device=dev) for _ in range(3)] + \
                   [torch.zeros((G, OUT_PITCH, B), dtype=bf16, device=dev)]
         self.splits = _dw_splits(B)
+        # bias gradients of large batches: rows summed in chunks of 1,024, then in order
+        self.colsum_rows = 1024 if B > 2048 else 0
+        n_chunks = (B + 1023) // 1024
+        self.colsum_part = torch.zeros(4 * G * n_chunks * OUT_PITCH, dtype=f32, device=dev) \
+            if self.colsum_rows else None
         if self.splits > 1:
             largest = max(rows * cols for (_, rows, cols) in (self.lay['W%d' % q] for q in range(4)))
             self.part = torch.zeros((self.splits, G, largest), dtype=f32, device=dev)
@@ -545,8 +550,9 @@ class EnsembleTrainer:
             self._check(L.mcw_mlp_gemm_grouped(ctypes.byref(c), st), 'backward GEMM')
             if i in self.reduce_after:
                 self._check(L.mcw_mlp_reduce_splits(*self.reduce_after[i], st), 'mcw_mlp_reduce_splits')
-        self._check(L.mcw_mlp_colsum_grouped(self.colsum_layers, 4, G, B, self.grad.data_ptr(), self.P, st),
-                    'mcw_mlp_colsum_grouped')
+        self._check(L.mcw_mlp_colsum_grouped(self.colsum_layers, 4, G, B, self.grad.data_ptr(), self.P,
+                                             self.colsum_part.data_ptr() if self.colsum_part is not None else None,
+                                             self.colsum_rows, st), 'mcw_mlp_colsum_grouped')
         if not adam:
             return
         self._check(L.mcw_mlp_adam_grouped(self.params.data_ptr(), self.grad.data_ptr(), self.m.data_ptr(),
