@@ -263,11 +263,14 @@ __global__ void __launch_bounds__(128) gemm_tma_kernel(const __grid_constant__ T
             if (kEpi == MCW_EPI_DSILU) {
                 // the pre-activations, row by row into the tile, then column j of lane's row
                 const float *ax = p.aux + (size_t)g * p.s_aux + nb + lane;
-#pragma unroll 4
+                float av[32];   // all 32 loads in flight before the first store
+#pragma unroll
                 for (int r = 0; r < 32; ++r) {
                     const int row = rbase + r;
-                    tile[r * 33 + lane] = (row < p.m && lane < cnt) ? __ldg(ax + (size_t)row * p.ld_aux) : 0.f;
+                    av[r] = (row < p.m && lane < cnt) ? __ldg(ax + (size_t)row * p.ld_aux) : 0.f;
                 }
+#pragma unroll
+                for (int r = 0; r < 32; ++r) tile[r * 33 + lane] = av[r];
                 __syncwarp();
 #pragma unroll
                 for (int j = 0; j < 32; ++j) z[j] *= dsilu(tile[lane * 33 + j]);
@@ -359,40 +362,55 @@ __global__ void reduce_splits_kernel(const float *src, long long s_split, long l
     }
 }
 
-// Weighted squared error of `groups` outputs, 32 x 32 tiles: loss[g] += sum w_j d^2 /
-// (m n); the gradient 2 w_j d / (m n) as f32 and bf16 [m, n] and bf16 transposed
-// [n, m] (through a shared-memory tile, so both stores are coalesced).
+// Weighted squared error of `groups` outputs: each block takes a strip of 32 columns x
+// kLossRows rows in 32 x 32 tiles; loss[g] += sum w_j d^2 / (m n) (one atomic per block);
+// the gradient 2 w_j d / (m n) as f32 and bf16 [m, n] and bf16 transposed [n, m]
+// (through a shared-memory tile, so both stores are coalesced).
+constexpr int kLossRows = 256;
+
 __global__ void loss_grouped_kernel(const float *y, long long ldy, long long s_y, const float *t, long long ldt,
                                     long long s_t, const float *w, int m, int n, float *g32, long long ldg,
                                     long long s_g32, __nv_bfloat16 *g16, long long s_g16, __nv_bfloat16 *g16t,
                                     long long ldgt, long long s_g16t, float *loss) {
     __shared__ __nv_bfloat16 tile[32][33];
+    __shared__ float wsum[8];
     const int g = blockIdx.z;
-    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
+    const int c0 = blockIdx.x * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
     const float scale = 1.f / ((float)m * (float)n);
+    const int c = c0 + tx;
+    const float wc = (c < n) ? (w ? w[c] : 1.f) : 0.f;
     float l = 0.f;
-    for (int rr = ty; rr < 32; rr += 8) {
-        const int r = r0 + rr, c = c0 + tx;
-        __nv_bfloat16 h = __float2bfloat16(0.f);
-        if (r < m && c < n) {
-            const float d = y[(size_t)g * s_y + (size_t)r * ldy + c] - t[(size_t)g * s_t + (size_t)r * ldt + c];
-            const float wc = w ? w[c] : 1.f;
-            l += wc * d * d * scale;
-            const float gv = 2.f * wc * d * scale;
-            g32[(size_t)g * s_g32 + (size_t)r * ldg + c] = gv;
-            h = __float2bfloat16(gv);
-            g16[(size_t)g * s_g16 + (size_t)r * ldg + c] = h;
+    for (int r0 = blockIdx.y * kLossRows; r0 < min(m, (blockIdx.y + 1) * kLossRows); r0 += 32) {
+        for (int rr = ty; rr < 32; rr += 8) {
+            const int r = r0 + rr;
+            __nv_bfloat16 h = __float2bfloat16(0.f);
+            if (r < m && c < n) {
+                const float d = y[(size_t)g * s_y + (size_t)r * ldy + c] - t[(size_t)g * s_t + (size_t)r * ldt + c];
+                l += wc * d * d * scale;
+                const float gv = 2.f * wc * d * scale;
+                g32[(size_t)g * s_g32 + (size_t)r * ldg + c] = gv;
+                h = __float2bfloat16(gv);
+                g16[(size_t)g * s_g16 + (size_t)r * ldg + c] = h;
+            }
+            tile[rr][tx] = h;
         }
-        tile[rr][tx] = h;
-    }
-    __syncthreads();
-    for (int cc = ty; cc < 32; cc += 8) {
-        const int c = c0 + cc, r = r0 + tx;
-        if (c < n && r < m) g16t[(size_t)g * s_g16t + (size_t)c * ldgt + r] = tile[tx][cc];
+        __syncthreads();
+        for (int cc = ty; cc < 32; cc += 8) {
+            const int cw = c0 + cc, r = r0 + tx;
+            if (cw < n && r < m) g16t[(size_t)g * s_g16t + (size_t)cw * ldgt + r] = tile[tx][cc];
+        }
+        __syncthreads();
     }
     for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
-    if (tx == 0 && l != 0.f) atomicAdd(loss + g, l);
+    if (tx == 0) wsum[ty] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float b = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) b += wsum[q];
+        if (b != 0.f) atomicAdd(loss + g, b);
+    }
 }
 
 // Bias gradients: out[g * s_out + off_l + j] = sum_i G_l[g][i][j] for the layers of
@@ -651,7 +669,7 @@ int mcw_mlp_loss_grouped(const float *y, int64_t ldy, int64_t stride_y, const fl
                          int64_t stride_g16t, float *loss, void *stream) {
     if (!y || !t || !g32 || !g16 || !g16t || !loss || groups < 1 || m < 0 || n < 0) return MCW_MLP_ERR_ARG;
     if (m == 0 || n == 0) return 0;
-    const dim3 grid((n + 31) / 32, (m + 31) / 32, groups);
+    const dim3 grid((n + 31) / 32, (m + kLossRows - 1) / kLossRows, groups);
     loss_grouped_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(
         y, ldy, stride_y, t, ldt, stride_t, w, m, n, g32, ldg, stride_g32, static_cast<__nv_bfloat16 *>(g16),
         stride_g16, static_cast<__nv_bfloat16 *>(g16t), ldgt, stride_g16t, loss);

@@ -626,6 +626,20 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
 #endif
 constexpr int kLaneSteps = MCW_BLOCK_LANE_STEPS;          // steps per lane in a chunk
 constexpr int kChunkSteps = 32 * kLaneSteps;              // steps per chunk (one warp)
+#ifndef MCW_LONG_WALK
+#define MCW_LONG_WALK 8192
+#endif
+// with MCW_LONG_LANE_STEPS=4, a pass that starts past kLongWalk steps uses chunks of 32
+// lanes x 4 steps (1,024 steps per pass): fewer cycles per step for the longest walks,
+// decided by the photon's own step count, so records do not depend on where it is
+// walked.  Off by default: measured on one GB300, it made the 64-config sweep 3% faster
+// (16% from 256 steps on) and the 1e6-photon launch 3% (8%) slower, its registers being
+// live in the main loop
+constexpr int kLongWalk = MCW_LONG_WALK;
+#ifndef MCW_LONG_LANE_STEPS
+#define MCW_LONG_LANE_STEPS 2
+#endif
+constexpr int kLongLaneSteps = MCW_LONG_LANE_STEPS;
 constexpr int kPassChunks = 8;                            // chunks per block pass
 constexpr int kPassSteps = kPassChunks * kChunkSteps;     // steps per block pass
 constexpr int kCtaWalkThreads = 32 * kPassChunks;         // the drain kernel's block: a warp per chunk
@@ -697,19 +711,21 @@ __device__ __forceinline__ PassFrame pass_frame(const Photon &Q, bool reflected)
 
 // One lane's steps of a chunk: their rotations (then their composed rotations),
 // optical paths, and per step the absorption, reflectance and species bits.
+template <int LS>
 struct LaneSteps {
-    float4 qs[kLaneSteps];
-    float dtau[kLaneSteps];
+    float4 qs[LS];
+    float dtau[LS];
     unsigned absm, reflm, impm;
 };
 
-// Draw steps s0 .. s0 + kLaneSteps - 1 of photon Q; lamb: the first of them takes
+// Draw steps s0 .. s0 + LS - 1 of photon Q; lamb: the first of them takes
 // the Lambertian direction about the vertical (the first step after a bottom
 // reflection, :1238-1250).
-__device__ __forceinline__ void lane_draw(LaneSteps &L, const Photon &Q, uint32_t s0, bool lamb, const WalkArgs &a) {
+template <int LS>
+__device__ __forceinline__ void lane_draw(LaneSteps<LS> &L, const Photon &Q, uint32_t s0, bool lamb, const WalkArgs &a) {
     L.absm = L.reflm = L.impm = 0;
 #pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
+    for (int t = 0; t < LS; ++t) {
         const uint32_t n = s0 + (uint32_t)t;
         const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
         const float4 uu = step_uniforms(r);
@@ -729,18 +745,20 @@ __device__ __forceinline__ void lane_draw(LaneSteps &L, const Photon &Q, uint32_
     }
 }
 
-__device__ __forceinline__ float4 lane_product(const LaneSteps &L) {
+template <int LS>
+__device__ __forceinline__ float4 lane_product(const LaneSteps<LS> &L) {
     float4 q = L.qs[0];
 #pragma unroll
-    for (int t = 1; t < kLaneSteps; ++t) q = qmul(q, L.qs[t]);
+    for (int t = 1; t < LS; ++t) q = qmul(q, L.qs[t]);
     return q;
 }
 
 // x: the rotation up to the lane's first step; the lane's rotations become the
 // composed rotations of its steps.
-__device__ __forceinline__ void lane_prefixes(LaneSteps &L, float4 x) {
+template <int LS>
+__device__ __forceinline__ void lane_prefixes(LaneSteps<LS> &L, float4 x) {
 #pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
+    for (int t = 0; t < LS; ++t) {
         x = qmul(x, L.qs[t]);
         L.qs[t] = x;
     }
@@ -757,10 +775,11 @@ __device__ __forceinline__ float3 pass_dir(const PassFrame &F, const float4 p) {
 }
 
 // Each step's vertical move, and the lane's sums of the moves and path increments.
-__device__ __forceinline__ void lane_moves(const LaneSteps &L, const PassFrame &F, float inv_ext,
-                                           float (&dz)[kLaneSteps], float &zs, float &ps) {
+template <int LS>
+__device__ __forceinline__ void lane_moves(const LaneSteps<LS> &L, const PassFrame &F, float inv_ext,
+                                           float (&dz)[LS], float &zs, float &ps) {
 #pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
+    for (int t = 0; t < LS; ++t) {
         const float4 p = L.qs[t];
         const float c0 = __fmul_rn(2.f, fmaf(p.y, p.w, __fmul_rn(p.x, p.z)));
         const float c1 = __fmul_rn(2.f, fmaf(p.z, p.w, -__fmul_rn(p.x, p.y)));
@@ -776,17 +795,18 @@ __device__ __forceinline__ void lane_moves(const LaneSteps &L, const PassFrame &
 // step: the step (ts), the event bits, z after and before the step, the path up to
 // it.  zx, px: the moves and path before the lane's first step of the pass.
 struct LaneEvent {
-    int first, ts;        // first: the event step, kLaneSteps if none
+    int first, ts;        // first: the event step, LS if none
     unsigned what;        // 1 top, 2 bottom, 4 species impurity, 8 reflectance draw passed
     float zk, zp, pk;
 };
 
-__device__ __forceinline__ LaneEvent lane_event(const LaneSteps &L, const float (&dz)[kLaneSteps], const Photon &Q,
+template <int LS>
+__device__ __forceinline__ LaneEvent lane_event(const LaneSteps<LS> &L, const float (&dz)[LS], const Photon &Q,
                                                 float zx, float px) {
-    LaneEvent E{kLaneSteps, kLaneSteps - 1, 0u, 0.f, 0.f, 0.f};
+    LaneEvent E{LS, LS - 1, 0u, 0.f, 0.f, 0.f};
     float zl = 0.f, pl = 0.f;
 #pragma unroll
-    for (int t = 0; t < kLaneSteps; ++t) {
+    for (int t = 0; t < LS; ++t) {
         const float zp = t == 0 ? __fadd_rn(Q.z, zx) : __fadd_rn(Q.z, __fadd_rn(zx, zl));
         const float inc = __fmul_rn(L.dtau[t], Q.inv_ext);
         zl = t == 0 ? dz[t] : __fadd_rn(zl, dz[t]);
@@ -796,7 +816,7 @@ __device__ __forceinline__ LaneEvent lane_event(const LaneSteps &L, const float 
         const bool bot = zk < -Q.tau;
         const bool absb = !top && !bot && ((L.absm >> t) & 1u);
         const bool event = top || bot || absb;
-        if (E.first == kLaneSteps && (event || t == kLaneSteps - 1)) {
+        if (E.first == LS && (event || t == LS - 1)) {
             if (event) E.first = t;
             E.ts = t;
             E.what = (top ? 1u : 0u) | (bot ? 2u : 0u) | (((L.impm >> t) & 1u) << 2) | (((L.reflm >> t) & 1u) << 3);
@@ -809,11 +829,12 @@ __device__ __forceinline__ LaneEvent lane_event(const LaneSteps &L, const float 
 }
 
 // The direction (x, y, z) and path increment (w) of the lane's step ts.
-__device__ __forceinline__ float4 lane_step_dir(const LaneSteps &L, const PassFrame &F, int ts, float inv_ext) {
+template <int LS>
+__device__ __forceinline__ float4 lane_step_dir(const LaneSteps<LS> &L, const PassFrame &F, int ts, float inv_ext) {
     float4 p = L.qs[0];
     float dt = L.dtau[0];
 #pragma unroll
-    for (int t = 1; t < kLaneSteps; ++t)
+    for (int t = 1; t < LS; ++t)
         if (t == ts) { p = L.qs[t]; dt = L.dtau[t]; }
     const float3 d = pass_dir(F, p);
     return make_float4(d.x, d.y, d.z, __fmul_rn(dt, inv_ext));
@@ -856,36 +877,37 @@ __device__ __forceinline__ int pass_end(Photon &Q, int adv, bool ev, const float
 // One block pass over photon Q, held alike by every lane of the warp, the chunks
 // walked one after the other until the first with an event.  Q is updated alike
 // on every lane; returns the end condition.  Warp-collective.
+template <int LS>
 __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
     const bool reflected = (Q.flags & kFlagReflect) != 0;
     const PassFrame F = pass_frame(Q, reflected);
     float4 W = q_identity();               // rotation of the earlier chunks
     float Wz = 0.f, Wp = 0.f;              // their vertical moves and path increments
     for (int c = 0;; ++c) {
-        LaneSteps L;
-        lane_draw(L, Q, (uint32_t)Q.i + 1u + (uint32_t)(kChunkSteps * c + kLaneSteps * lane),
+        LaneSteps<LS> L;
+        lane_draw<LS>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * c + LS * lane),
                   reflected && c == 0 && lane == 0, a);
-        const float4 qi = warp_scan_q(lane_product(L), lane);
+        const float4 qi = warp_scan_q(lane_product<LS>(L), lane);
         float4 xl = shfl_q(qi, (lane + 31) & 31);
         if (lane == 0) xl = q_identity();
-        lane_prefixes(L, qmul(W, xl));
-        float dz[kLaneSteps], zs, ps;
-        lane_moves(L, F, Q.inv_ext, dz, zs, ps);
+        lane_prefixes<LS>(L, qmul(W, xl));
+        float dz[LS], zs, ps;
+        lane_moves<LS>(L, F, Q.inv_ext, dz, zs, ps);
         warp_scan_2(zs, ps, lane);
         float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
         if (lane == 0) { zx = 0.f; px = 0.f; }
-        const LaneEvent E = lane_event(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
-        const unsigned ev = __ballot_sync(0xffffffffu, E.first < kLaneSteps);
+        const LaneEvent E = lane_event<LS>(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
+        const unsigned ev = __ballot_sync(0xffffffffu, E.first < LS);
         if (ev || c == kPassChunks - 1) {
             const int e = ev ? __ffs(ev) - 1 : 31;
-            const float4 d = lane_step_dir(L, F, E.ts, Q.inv_ext);
+            const float4 d = lane_step_dir<LS>(L, F, E.ts, Q.inv_ext);
             const float4 dir = make_float4(__shfl_sync(0xffffffffu, d.x, e), __shfl_sync(0xffffffffu, d.y, e),
                                            __shfl_sync(0xffffffffu, d.z, e), __shfl_sync(0xffffffffu, d.w, e));
             const int ts = __shfl_sync(0xffffffffu, E.ts, e);
             const float ze = __shfl_sync(0xffffffffu, E.zk, e), zp = __shfl_sync(0xffffffffu, E.zp, e);
             const float pe = __shfl_sync(0xffffffffu, E.pk, e);
             const unsigned what = __shfl_sync(0xffffffffu, E.what, e);
-            return pass_end(Q, kChunkSteps * c + kLaneSteps * e + ts + 1, ev != 0, dir, ze, zp, pe, what);
+            return pass_end(Q, (32 * LS) * c + LS * e + ts + 1, ev != 0, dir, ze, zp, pe, what);
         }
         W = qmul(W, shfl_q(qi, 31));
         Wz = __fadd_rn(Wz, __shfl_sync(0xffffffffu, zs, 31));
@@ -906,22 +928,23 @@ struct CtaPassShared {
 // One block pass over photon Q, held alike by every thread of a block of
 // kCtaWalkThreads, warp w taking chunk w: the same arithmetic as block_pass.  Q is
 // updated alike on every thread; returns the end condition.  Block-collective.
+template <int LS>
 __device__ __forceinline__ int cta_pass(Photon &Q, const WalkArgs &a, CtaPassShared &S, int warp, int lane) {
     const bool reflected = (Q.flags & kFlagReflect) != 0;
     const PassFrame F = pass_frame(Q, reflected);
-    LaneSteps L;
-    lane_draw(L, Q, (uint32_t)Q.i + 1u + (uint32_t)(kChunkSteps * warp + kLaneSteps * lane),
+    LaneSteps<LS> L;
+    lane_draw<LS>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * warp + LS * lane),
               reflected && warp == 0 && lane == 0, a);
-    const float4 qi = warp_scan_q(lane_product(L), lane);
+    const float4 qi = warp_scan_q(lane_product<LS>(L), lane);
     if (lane == 31) S.wq[warp] = qi;
     __syncthreads();
     float4 W = q_identity();
     for (int c = 0; c < warp; ++c) W = qmul(W, S.wq[c]);
     float4 xl = shfl_q(qi, (lane + 31) & 31);
     if (lane == 0) xl = q_identity();
-    lane_prefixes(L, qmul(W, xl));
-    float dz[kLaneSteps], zs, ps;
-    lane_moves(L, F, Q.inv_ext, dz, zs, ps);
+    lane_prefixes<LS>(L, qmul(W, xl));
+    float dz[LS], zs, ps;
+    lane_moves<LS>(L, F, Q.inv_ext, dz, zs, ps);
     warp_scan_2(zs, ps, lane);
     if (lane == 31) S.wzp[warp] = make_float2(zs, ps);
     __syncthreads();
@@ -933,8 +956,8 @@ __device__ __forceinline__ int cta_pass(Photon &Q, const WalkArgs &a, CtaPassSha
     }
     float zx = __shfl_up_sync(0xffffffffu, zs, 1), px = __shfl_up_sync(0xffffffffu, ps, 1);
     if (lane == 0) { zx = 0.f; px = 0.f; }
-    const LaneEvent E = lane_event(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
-    const unsigned ev = __ballot_sync(0xffffffffu, E.first < kLaneSteps);
+    const LaneEvent E = lane_event<LS>(L, dz, Q, __fadd_rn(Wz, zx), __fadd_rn(Wp, px));
+    const unsigned ev = __ballot_sync(0xffffffffu, E.first < LS);
     if (lane == 0) S.wev[warp] = ev ? __ffs(ev) - 1 : 32;
     __syncthreads();
     int ec = kPassChunks - 1, el = 31;
@@ -944,9 +967,9 @@ __device__ __forceinline__ int cta_pass(Photon &Q, const WalkArgs &a, CtaPassSha
         if (l < 32) { ec = c; el = l; any = true; }
     }
     if (warp == ec && lane == el) {
-        S.dir = lane_step_dir(L, F, E.ts, Q.inv_ext);
+        S.dir = lane_step_dir<LS>(L, F, E.ts, Q.inv_ext);
         S.zzp = make_float4(E.zk, E.zp, E.pk, __uint_as_float(E.what));
-        S.adv = kChunkSteps * ec + kLaneSteps * el + E.ts + 1;
+        S.adv = (32 * LS) * ec + LS * el + E.ts + 1;
     }
     __syncthreads();
     const float4 zzp = S.zzp;
@@ -1202,7 +1225,11 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         for (unsigned pend = bmask; pend; pend &= pend - 1) {
             const int src = __ffs(pend) - 1;
             Photon Q = shfl_photon(P, src);
-            const int c = block_pass(Q, a, lane);
+            int c;
+            if constexpr (kLongLaneSteps != kLaneSteps)
+                c = Q.i >= kLongWalk ? block_pass<kLongLaneSteps>(Q, a, lane) : block_pass<kLaneSteps>(Q, a, lane);
+            else
+                c = block_pass<kLaneSteps>(Q, a, lane);
             if (lane == src) {
                 P.i = Q.i;
                 P.flags = Q.flags;
@@ -1296,7 +1323,11 @@ __global__ void __launch_bounds__(kCtaWalkThreads) drain_kernel(const WalkArgs a
         int cond = 0;
         bool over = false;
         for (uint32_t pass = 1; cond == 0; ++pass) {
-            cond = cta_pass(P, a, S.pass, warp, lane);
+            if constexpr (kLongLaneSteps != kLaneSteps)
+                cond = P.i >= kLongWalk ? cta_pass<kLongLaneSteps>(P, a, S.pass, warp, lane)
+                                        : cta_pass<kLaneSteps>(P, a, S.pass, warp, lane);
+            else
+                cond = cta_pass<kLaneSteps>(P, a, S.pass, warp, lane);
             if ((pass & 63u) == 0u) {
                 // time budget (watchdog; never a truncation in normal runs)
                 if (threadIdx.x == 0)

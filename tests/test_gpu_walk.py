@@ -402,6 +402,59 @@ def test_f32_block_mode_statistics_match_oracle(walker):
         assert abs(a.mean() - b.mean()) < 4 * se, (a.mean(), b.mean(), se)
 
 
+def _very_long_walks(n):
+    """Single-scattering albedo 0.9999 over tau 1e4 at normal incidence (r_eff 50 um,
+    1.0 um): about 2% of the walks pass 8,192 steps (up to ~5e4), where block passes
+    switch to chunks of 32 lanes x 4 steps."""
+    lo, hi = ssp.grid_for(1.0, 0.085)
+    ice = ssp.synthetic_ice_table(50.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    cfg = WalkConfig(n_photon=n, wvl0=1.0, half_width=0.085, theta0_deg=0.0, tau_tot=1e4,
+                     lambertian_reflectance=0.5, ssa_ice_override=0.9999)
+    return cfg, ice, imp
+
+
+def test_f32_very_long_walks_same_records_with_and_without_drain(walker):
+    """Walks past 8,192 steps take 4-step block passes in the warp and in the drain
+    kernel alike: records and tallies do not depend on where a photon is walked."""
+    cfg, ice, imp = _very_long_walks(20000)
+    walker.set_tables([ice], imp)
+    saved = walker.get_launch()
+    try:
+        walker.set_launch(256, 0, 8, 0)
+        a = walker.walk([cfg], 21, mode='f32')
+        walker.set_launch(256, 0, 8, 256)
+        b = walker.walk([cfg], 21, mode='f32')
+        walker.set_launch(128, 1, 4, 8192)
+        c = walker.walk([cfg], 21, mode='f32')
+    finally:
+        walker.set_launch(**saved)
+    assert int((a.records['n_scat'] > 8192).sum()) >= 100
+    assert np.array_equal(a.records, b.records) and np.array_equal(a.tallies, b.tallies)
+    assert np.array_equal(a.records, c.records) and np.array_equal(a.tallies, c.tallies)
+
+
+def test_f32_very_long_walks_statistics_match_oracle(walker):
+    """The same slab against the oracle's step-by-step FP64 walk of the reference
+    algorithm: condition fractions, exit histogram, mean n_scat and path length, and the
+    share of walks past 8,192 steps."""
+    cfg, ice, imp = _very_long_walks(40000)
+    walker.set_tables([ice], imp)
+    rec = walker.walk([cfg], 17, mode='f32').records
+    ref = oracle_run(cfg, ice, imp, 71)
+    condition_fractions_agree(rec['condition'], ref['condition'])
+    top_g, top_r = rec['condition'] == 1, ref['condition'] == 1
+    x2, dof, p = chi2_two_sample(exit_histogram(rec['theta_n'][top_g], rec['phi_n'][top_g]),
+                                 exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r]))
+    assert p > 1e-4, (x2, dof, p)
+    for a, b in ((rec['n_scat'].astype(np.float64), ref['n_scat'].astype(np.float64)),
+                 (rec['path_length'].astype(np.float64), ref['path_length'])):
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se, (a.mean(), b.mean(), se)
+    fa, fb = np.mean(rec['n_scat'] > 8192), np.mean(ref['n_scat'] > 8192)
+    assert abs(fa - fb) < 4 * np.sqrt(fb * (1 - fb) * 2 / rec.size) + 1e-9, (fa, fb)
+
+
 def test_records_into_pinned_host_memory(walker):
     """Pinned host buffers are written by the walk directly (no copy after the kernel);
     their records equal those copied into pageable memory, in both modes."""
