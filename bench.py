@@ -767,6 +767,7 @@ def run_ours(args):
         w.walk([cfg], SEED + 2000 + k, mode='f32', records='host', out=host_rec)
     barrier()
     e2e_t, h2d, d2h = [], 0, 0
+    e2e_dev, e2e_kern, e2e_lib = [], [], []
     e2e_calls = args.steps * min(repeats, 20)
     for k in range(e2e_calls):
         flush.zero_()
@@ -775,6 +776,9 @@ def run_ours(args):
         r = w.walk([cfg], SEED + 3000 + k, mode='f32', records='host', out=host_rec)
         e2e_t.append(time.perf_counter() - t0)
         h2d, d2h = r.stats['h2d_bytes'], r.stats['d2h_bytes']
+        e2e_dev.append(r.stats['device_ms'])
+        e2e_kern.append(r.stats['kernel_ms'])
+        e2e_lib.append(r.stats['total_ms'])
     barrier()
     _abi.load().mcw_host_free(host_ptr)
 
@@ -827,12 +831,19 @@ def run_ours(args):
             'e2e': {'value': N_PER_GPU * world * e2e_calls / t_e2e, 'unit': 'photons/s',
                     'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h),
                     'calls': e2e_calls,
+                    'ms_per_call': {'host_wall': 1e3 * t_e2e / e2e_calls,
+                                    'library_call': float(np.median(e2e_lib)),
+                                    'device': float(np.median(e2e_dev)),
+                                    'kernel': float(np.median(e2e_kern))},
                     'path': 'Walker.walk -> mcw_walk, records written into pinned host memory, '
                             'tallies copied back; host wall clock per call'},
             'roofline': {
                 'bound': 'issue (%s pipe)' % limiting, 'achieved': achieved, 'peak': peak, 'unit': 'Tops/s',
                 'frac': achieved / peak,
                 'traffic': (tb * n) if tb else None,
+                'traffic_note': 'DRAM bytes inside one launch (ncu, profiles/walk_f32_traffic.json): tables '
+                                'and launch data; the 32 MB of records (32 B per photon) stay in L2 during '
+                                'the launch and are written back after it, so the write-back is not counted',
                 'basis': 'max over pipes of events/s x algorithmic ops per event (int 125, fp32 30, sfu 5) '
                          'against the pipe rate (152 SMs x lanes per clock x %.0f MHz, sm_max_mhz, %s)' % (
                              sm_max, src),

@@ -354,11 +354,15 @@ __device__ __forceinline__ float3 pole_dir(const float sg, const float ct, const
 // are evaluated together and selected, so the step is one straight dependency
 // chain; only the rare bottom-reflection draw branches.
 template <bool kImpurity>
-__device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm) {
+// may_first: this step can be a photon's first (photons start on a round edge, so only
+// a round's step 0 can; a constant at every call, so the first-step selects of the
+// other steps compile away).
+__device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm,
+                                    const bool may_first) {
     P.i += 1;
     const float4 uu = step_uniforms(r);
     const float u1 = uu.x, u2 = uu.y, u3 = uu.z;
-    const bool first = (P.i == 1);
+    const bool first = may_first && (P.i == 1);
     const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
 
@@ -463,9 +467,10 @@ __device__ __forceinline__ bool impurity_draw(uint64_t rid, uint32_t n, float p_
     return ((float)r2.x * kTwo32Inv) < p_imp;
 }
 
-__device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool imp, const bool renorm) {
+__device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool imp, const bool renorm,
+                                         const bool may_first) {
     P.i += 1;
-    const bool first = (P.i == 1);
+    const bool first = may_first && (P.i == 1);
     const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
     const float dtau = (first && lam_surface) ? 0.f : s.dtau;
@@ -577,7 +582,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
                 st.sp = ys[u].x, st.cp = ys[u].y, st.dtau = ys[u].z, st.u4 = ys[u].w;
                 const bool alive = cond == 0;
                 Photon Q = P;
-                const int c = step_post(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1);
+                const int c = step_post(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
                 P.i = alive ? Q.i : P.i;
                 P.mux = alive ? Q.mux : P.mux;
                 P.muy = alive ? Q.muy : P.muy;
@@ -1205,7 +1210,7 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
                 // a lane whose photon ended earlier in the round keeps its final state
                 const bool alive = cond == 0;
                 Photon Q = P;
-                const int c = step<kImpurity>(Q, a, rb[k], k == kStepsPerRound - 1);
+                const int c = step<kImpurity>(Q, a, rb[k], k == kStepsPerRound - 1, k == 0);
                 // a finished photon's record uses i, the direction and the path only;
                 // its z, flags and path compensation are never read again
                 P.i = alive ? Q.i : P.i;
