@@ -28,10 +28,11 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NO_FMAD = {'walk_replay.cu', 'ssp_lut.cu'}
 # the FP32 production walk: flush denormals, approximate division and square root
 FAST_F32 = {'walk_f32.cu': ['-ftz=true', '-prec-div=false', '-prec-sqrt=false']}
-# tuning builds: extra -D flags for the FP32 walk (e.g. MCW_DEFINES="-DMCW_BLOCK_WALK=128");
+# tuning builds: extra -D flags for the FP32 walk and the fused inference kernel
+# (e.g. MCW_DEFINES="-DMCW_BLOCK_WALK=128");
 # its object goes to a directory of its own, the other units are shared with the default build
 DEFINES = os.environ.get('MCW_DEFINES', '').split()
-DEFINE_UNITS = {'walk_f32.cu'}
+DEFINE_UNITS = {'walk_f32.cu', 'mlp_fused.cu'}
 
 
 def nvcc():

@@ -48,12 +48,19 @@ constexpr int FK1 = 16;                 // layer-1 K, zero-padded
 #ifndef MCW_FUSED_EPI_WARPS
 #define MCW_FUSED_EPI_WARPS 8
 #endif
+#ifndef MCW_FUSED_TILES
+#define MCW_FUSED_TILES 1
+#endif
 #ifndef MCW_FUSED_CTAS_PER_SM
-#define MCW_FUSED_CTAS_PER_SM 2
+#define MCW_FUSED_CTAS_PER_SM (MCW_FUSED_TILES == 1 ? 2 : 1)
 #endif
 constexpr int kSlots = MCW_FUSED_SLOTS;              // weight ring depth
 constexpr int kEpiWarps = MCW_FUSED_EPI_WARPS;       // 8 or 16
 constexpr int kCtasPerSm = MCW_FUSED_CTAS_PER_SM;
+// 128-row tiles a CTA carries at once, each with its own accumulator and activation
+// tile: the MMAs of one tile's next layer run while the other tile's epilogue does
+constexpr int kTiles = MCW_FUSED_TILES;
+static_assert(kTiles == 1 || kTiles == 2, "one or two tiles per CTA");
 constexpr int kGroups = kEpiWarps / 4;               // column groups per accumulator lane quarter
 constexpr int kProducerWarp = kEpiWarps, kMmaWarp = kEpiWarps + 1;
 constexpr int kThreads = 32 * (kEpiWarps + 2);
@@ -81,9 +88,10 @@ constexpr int kBiasBytes = kBiasFloats * 4;
 constexpr int kHidCols = FH / kGroups;                // hidden columns per epilogue warp
 constexpr int kOutCols = kOutN / kGroups;             // output-block columns per epilogue warp
 static_assert(kEpiWarps % 4 == 0 && kHidCols % 32 == 0 && kOutCols % 32 == 0, "epilogue split");
-static_assert(kActBytes + kRingBytes + kStageBytes + kBiasBytes <= 227 * 1024, "shared memory");
-constexpr size_t kSmemBytes = (size_t)kActBytes + kRingBytes + kStageBytes + kBiasBytes;
-constexpr uint32_t kTmemCols = 256;
+static_assert(kTiles * kActBytes + kRingBytes + kStageBytes + kBiasBytes <= 227 * 1024, "shared memory");
+constexpr size_t kSmemBytes = (size_t)kTiles * kActBytes + kRingBytes + kStageBytes + kBiasBytes;
+constexpr uint32_t kTmemCols = 256 * kTiles;
+constexpr int kSeqChunks = kTiles * kNumChunks;       // weight chunks a CTA consumes
 constexpr unsigned long long kWaitNs = 2000000000ull;
 constexpr uint32_t kSuspendNs = 1000000;              // a waiting thread sleeps until the phase completes or 1 ms
 // F32 += BF16 x BF16, both K-major; N >> 3 in bits 17-22, M >> 4 in bits 24-28
@@ -93,7 +101,16 @@ __host__ __device__ constexpr uint32_t idesc(int n) {
 
 static_assert(kHidK * FH * 2 == kChunkBytes && kOutK * kOutN * 2 == kChunkBytes, "chunk sizes");
 static_assert(kW1Bytes + (kNumChunks - 1) * kChunkBytes == MCW_MLP_PACK_BYTES, "packed blob layout");
-static_assert(kXBytes <= kStageBytes, "the input tile lives in the stage region");
+static_assert(kTiles * kXBytes <= kStageBytes, "the input tiles live in the stage region");
+
+// The i-th weight chunk a CTA consumes: per layer the chunks of tile 0, then those of
+// tile 1 (the order in which the MMA warp issues the layers of its tiles).
+__host__ __device__ constexpr int chunk_at(int i) {
+    return i < kTiles ? 0
+         : i < kTiles * (1 + kHidChunks) ? 1 + (i - kTiles) % kHidChunks
+         : i < kTiles * (1 + 2 * kHidChunks) ? 1 + kHidChunks + (i - kTiles * (1 + kHidChunks)) % kHidChunks
+         : 1 + 2 * kHidChunks + (i - kTiles * (1 + 2 * kHidChunks)) % (kOutBlocks * kOutChunks);
+}
 
 __host__ __device__ constexpr size_t chunk_offset(int i) { return i == 0 ? 0 : kW1Bytes + (size_t)(i - 1) * kChunkBytes; }
 __host__ __device__ constexpr uint32_t chunk_bytes(int i) { return i == 0 ? kW1Bytes : kChunkBytes; }
@@ -368,8 +385,8 @@ __device__ __forceinline__ void epilogue_out_half(uint32_t tlane, int blk, const
 
 struct Bars {
     uint64_t full[kSlots], empty[kSlots];   // weight ring
-    uint64_t accf[2], acce[2];    // accumulator halves: full (MMA -> epilogue), empty (epilogue -> MMA)
-    uint64_t act;                 // input / activation tile written (epilogue -> MMA)
+    uint64_t accf[kTiles][2], acce[kTiles][2];  // accumulator halves per tile: full (MMA -> epilogue), empty
+    uint64_t act[kTiles];         // input / activation tile written (epilogue -> MMA)
     uint64_t fin;                 // every MMA of the CTA complete
 };
 
@@ -379,17 +396,17 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                                                                 const unsigned char *blob, void *y, int ldy,
                                                                 unsigned int *err) {
     extern __shared__ __align__(128) unsigned char smem[];
-    unsigned char *act = smem;                                   // 64 KB activation tile
-    unsigned char *ring = smem + kActBytes;                      // 2 x 16 KB weight chunks
-    unsigned char *stage_all = smem + kActBytes + kRingBytes;    // 16 KB output stage ...
-    unsigned char *xt = stage_all;                               // ... and, for layer 1, the input tile
+    unsigned char *act0 = smem;                                  // 64 KB activation tile per tile
+    unsigned char *ring = smem + kTiles * kActBytes;             // 2 x 16 KB weight chunks
+    unsigned char *stage_all = ring + kRingBytes;                // 16 KB output stage ...
+    unsigned char *xt0 = stage_all;                              // ... and, for layer 1, the input tiles
     float *sbias = reinterpret_cast<float *>(stage_all + kStageBytes);   // b1 | b2 | b3 | b4 (padded)
     __shared__ __align__(8) Bars bars;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
     volatile int *abort = &abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * FM;
+    const int m0 = blockIdx.x * FM * kTiles;
 
     if (warp == kMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
@@ -402,11 +419,13 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
             bar_init(&bars.full[i], 1);
             bar_init(&bars.empty[i], 1);
         }
-        for (int i = 0; i < 2; ++i) {
-            bar_init(&bars.accf[i], 1);
-            bar_init(&bars.acce[i], kEpiThreads);
+        for (int t = 0; t < kTiles; ++t) {
+            for (int i = 0; i < 2; ++i) {
+                bar_init(&bars.accf[t][i], 1);
+                bar_init(&bars.acce[t][i], kEpiThreads);
+            }
+            bar_init(&bars.act[t], kEpiThreads);
         }
-        bar_init(&bars.act, kEpiThreads);
         bar_init(&bars.fin, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
@@ -418,10 +437,11 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
     if (warp == kProducerWarp) {
         if (lane == 0) {
             int issued = 0;
-            for (int i = 0; i < kNumChunks; ++i) {
+            for (int i = 0; i < kSeqChunks; ++i) {
                 const int slot = i % kSlots;
                 if (i >= kSlots && !wait_bar(&bars.empty[slot], (uint32_t)(i / kSlots - 1) & 1u, abort)) break;
-                load_chunk(ring + slot * kChunkBytes, blob + chunk_offset(i), chunk_bytes(i), &bars.full[slot]);
+                const int c = chunk_at(i);
+                load_chunk(ring + slot * kChunkBytes, blob + chunk_offset(c), chunk_bytes(c), &bars.full[slot]);
                 issued = i + 1;
             }
             // the last copy into each slot has landed before the CTA can leave
@@ -430,9 +450,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
         }
     } else if (warp == kMmaWarp) {
         if (lane == 0) {
-            const uint32_t act_a = smem_u32(act), ring_a = smem_u32(ring), x_a = smem_u32(xt);
+            const uint32_t ring_a = smem_u32(ring);
             int chunk = 0;
-            uint32_t act_phase = 0;
+            uint32_t act_phase[kTiles];
+            for (int t = 0; t < kTiles; ++t) act_phase[t] = 0u;
             bool ok = true;
             auto take = [&](void) -> uint32_t {      // wait for the next chunk; its shared address
                 const int slot = chunk % kSlots;
@@ -444,51 +465,58 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                 commit(&bars.empty[chunk % kSlots]);
                 ++chunk;
             };
-            // layer 1: input tile x W1
-            ok = wait_bar(&bars.act, act_phase, abort);
-            act_phase ^= 1u;
-            asm volatile("tcgen05.fence::after_thread_sync;\n");
-            if (ok) {
+            auto wait_act = [&](int t) {             // tile t's input / activations written
+                ok = ok && wait_bar(&bars.act[t], act_phase[t], abort);
+                act_phase[t] ^= 1u;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+            };
+            // layer 1 of each tile: input tile x W1
+            for (int t = 0; t < kTiles && ok; ++t) {
+                wait_act(t);
+                if (!ok) break;
                 const uint32_t w = take();
-                if (ok) {
-                    mma_steps(tmem, x_a, FK1, 0, w, FK1, 1, idesc(FH), false);
-                    release();
-                    commit(&bars.accf[0]);
-                }
+                if (!ok) break;
+                mma_steps(tmem + (uint32_t)(t * 256), smem_u32(xt0 + t * kXBytes), FK1, 0, w, FK1, 1, idesc(FH), false);
+                release();
+                commit(&bars.accf[t][0]);
             }
-            // layers 2 and 3: eight chunks of 32 k each
+            // layers 2 and 3: eight chunks of 32 k each, tile by tile (one tile's MMAs run
+            // while the other's epilogue writes its activations)
             for (int layer = 0; layer < 2 && ok; ++layer) {
-                ok = wait_bar(&bars.act, act_phase, abort);
-                act_phase ^= 1u;
-                asm volatile("tcgen05.fence::after_thread_sync;\n");
-                for (int c = 0; c < kHidChunks && ok; ++c) {
-                    const uint32_t w = take();
-                    if (!ok) break;
-                    mma_steps(tmem, act_a, FH, c * (kHidK / 16), w, kHidK, kHidK / 16, idesc(FH), c > 0);
-                    release();
+                for (int t = 0; t < kTiles && ok; ++t) {
+                    wait_act(t);
+                    const uint32_t act_a = smem_u32(act0 + t * kActBytes);
+                    for (int c = 0; c < kHidChunks && ok; ++c) {
+                        const uint32_t w = take();
+                        if (!ok) break;
+                        mma_steps(tmem + (uint32_t)(t * 256), act_a, FH, c * (kHidK / 16), w, kHidK, kHidK / 16,
+                                  idesc(FH), c > 0);
+                        release();
+                    }
+                    if (ok) commit(&bars.accf[t][0]);
                 }
-                if (ok) commit(&bars.accf[0]);
             }
-            // output layer: six 128-column blocks alternating between accumulator halves
-            if (ok) {
-                ok = wait_bar(&bars.act, act_phase, abort);
-                asm volatile("tcgen05.fence::after_thread_sync;\n");
-            }
-            for (int j = 0; j < kOutBlocks && ok; ++j) {
-                const int h = j & 1;
-                if (j >= 2) {
-                    ok = wait_bar(&bars.acce[h], (uint32_t)((j >> 1) - 1) & 1u, abort);
-                    asm volatile("tcgen05.fence::after_thread_sync;\n");
-                    if (!ok) break;
+            // output layer: six 128-column blocks per tile alternating between the halves
+            // of the tile's accumulator
+            for (int t = 0; t < kTiles && ok; ++t) {
+                wait_act(t);
+                const uint32_t act_a = smem_u32(act0 + t * kActBytes);
+                for (int j = 0; j < kOutBlocks && ok; ++j) {
+                    const int h = j & 1;
+                    if (j >= 2) {
+                        ok = wait_bar(&bars.acce[t][h], (uint32_t)((j >> 1) - 1) & 1u, abort);
+                        asm volatile("tcgen05.fence::after_thread_sync;\n");
+                        if (!ok) break;
+                    }
+                    for (int c = 0; c < kOutChunks && ok; ++c) {
+                        const uint32_t w = take();
+                        if (!ok) break;
+                        mma_steps(tmem + (uint32_t)(t * 256 + h * kOutN), act_a, FH, c * (kOutK / 16), w, kOutK,
+                                  kOutK / 16, idesc(kOutN), c > 0);
+                        release();
+                    }
+                    if (ok) commit(&bars.accf[t][h]);
                 }
-                for (int c = 0; c < kOutChunks && ok; ++c) {
-                    const uint32_t w = take();
-                    if (!ok) break;
-                    mma_steps(tmem + (uint32_t)(h * kOutN), act_a, FH, c * (kOutK / 16), w, kOutK, kOutK / 16,
-                              idesc(kOutN), c > 0);
-                    release();
-                }
-                if (ok) commit(&bars.accf[h]);
             }
             // every MMA issued by this thread has completed before the memory is freed
             commit(&bars.fin);
@@ -497,10 +525,9 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
     } else {
         // epilogue warps
         const int quarter = warp & 3, group = warp >> 2;   // lane quarter, column group
-        const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16);
         unsigned char *stage = stage_all + warp * kStageWarp;
-        const int row0 = m0 + quarter * 32;
-        uint32_t accf_phase[2] = {0u, 0u};
+        uint32_t accf_phase[kTiles][2];
+        for (int t = 0; t < kTiles; ++t) accf_phase[t][0] = accf_phase[t][1] = 0u;
         // biases into shared memory (b4 zero past column 648), then the epilogue warps meet
         for (int i = threadIdx.x; i < kBiasFloats; i += kEpiThreads) {
             float v;
@@ -511,45 +538,55 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
             sbias[i] = v;
         }
         asm volatile("bar.sync 1, %0;\n" :: "n"(kEpiThreads) : "memory");
-        if (threadIdx.x < FM) {
-            const int r = threadIdx.x, gm = m0 + r;
-            float xin[FIN];
+        for (int t = 0; t < kTiles; ++t) {
+            if (threadIdx.x < FM) {
+                const int r = threadIdx.x, gm = m0 + t * FM + r;
+                float xin[FIN];
 #pragma unroll
-            for (int k = 0; k < FIN; ++k) xin[k] = gm < m ? x[(size_t)gm * FIN + k] : 0.f;
-            const __nv_bfloat162 p0 = __floats2bfloat162_rn(xin[0], xin[1]);
-            const __nv_bfloat162 p1 = __floats2bfloat162_rn(xin[2], xin[3]);
-            *reinterpret_cast<uint4 *>(xt + core_off(r, 0, FK1)) = make_uint4(
-                *reinterpret_cast<const uint32_t *>(&p0), *reinterpret_cast<const uint32_t *>(&p1), 0u, 0u);
-            *reinterpret_cast<uint4 *>(xt + core_off(r, 8, FK1)) = make_uint4(0u, 0u, 0u, 0u);
+                for (int k = 0; k < FIN; ++k) xin[k] = gm < m ? x[(size_t)gm * FIN + k] : 0.f;
+                const __nv_bfloat162 p0 = __floats2bfloat162_rn(xin[0], xin[1]);
+                const __nv_bfloat162 p1 = __floats2bfloat162_rn(xin[2], xin[3]);
+                unsigned char *xt = xt0 + t * kXBytes;
+                *reinterpret_cast<uint4 *>(xt + core_off(r, 0, FK1)) = make_uint4(
+                    *reinterpret_cast<const uint32_t *>(&p0), *reinterpret_cast<const uint32_t *>(&p1), 0u, 0u);
+                *reinterpret_cast<uint4 *>(xt + core_off(r, 8, FK1)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n");
+            arrive(&bars.act[t]);
         }
-        asm volatile("fence.proxy.async.shared::cta;\n");
-        arrive(&bars.act);
         const float *hb[3] = {sbias, sbias + 256, sbias + 512};
         bool ok = true;
         for (int layer = 0; layer < 3 && ok; ++layer) {
-            ok = wait_bar(&bars.accf[0], accf_phase[0], abort);
-            accf_phase[0] ^= 1u;
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;\n");
-            epilogue_hidden(tlane, hb[layer], act, quarter, group, lane);
-            asm volatile("fence.proxy.async.shared::cta;\n");
-            asm volatile("tcgen05.fence::before_thread_sync;\n");
-            arrive(&bars.act);
+            for (int t = 0; t < kTiles && ok; ++t) {
+                ok = wait_bar(&bars.accf[t][0], accf_phase[t][0], abort);
+                accf_phase[t][0] ^= 1u;
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(t * 256);
+                epilogue_hidden(tlane, hb[layer], act0 + t * kActBytes, quarter, group, lane);
+                asm volatile("fence.proxy.async.shared::cta;\n");
+                asm volatile("tcgen05.fence::before_thread_sync;\n");
+                arrive(&bars.act[t]);
+            }
         }
-        for (int j = 0; j < kOutBlocks && ok; ++j) {
-            const int h = j & 1;
-            ok = wait_bar(&bars.accf[h], accf_phase[h], abort);
-            accf_phase[h] ^= 1u;
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;\n");
-            if (kHalf)
-                epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<__half *>(y), ldy,
-                                  m, row0, group, lane);
-            else
-                epilogue_out(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<float *>(y), ldy, m,
-                             row0, group, lane);
-            asm volatile("tcgen05.fence::before_thread_sync;\n");
-            arrive(&bars.acce[h]);
+        for (int t = 0; t < kTiles && ok; ++t) {
+            const uint32_t tlane = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(t * 256);
+            const int row0 = m0 + t * FM + quarter * 32;
+            for (int j = 0; j < kOutBlocks && ok; ++j) {
+                const int h = j & 1;
+                ok = wait_bar(&bars.accf[t][h], accf_phase[t][h], abort);
+                accf_phase[t][h] ^= 1u;
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                if (kHalf)
+                    epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<__half *>(y),
+                                      ldy, m, row0, group, lane);
+                else
+                    epilogue_out(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<float *>(y), ldy,
+                                 m, row0, group, lane);
+                asm volatile("tcgen05.fence::before_thread_sync;\n");
+                arrive(&bars.acce[t][h]);
+            }
         }
     }
 
@@ -601,7 +638,7 @@ int forward(const float *x, int32_t m, const float *b1, const float *b2, const f
                           : reinterpret_cast<const void *>(mlp_fused_kernel<false>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
     if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
-    const unsigned grid = (unsigned)((m + FM - 1) / FM);
+    const unsigned grid = (unsigned)((m + FM * kTiles - 1) / (FM * kTiles));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const unsigned char *wb = static_cast<const unsigned char *>(blob);
     if (half) mlp_fused_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err);
