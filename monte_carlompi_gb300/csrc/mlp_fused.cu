@@ -131,7 +131,29 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+#ifndef MCW_FUSED_SILU_TANH
+#define MCW_FUSED_SILU_TANH 1
+#endif
 __device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// SiLU of a pair of pre-activations.  With MCW_FUSED_SILU_TANH (the default):
+// z sigmoid(z) = h + h tanh(h), h = z / 2, one hardware tanh per value (relative
+// error about 2^-11, below the bf16 rounding of the stored activation) and packed
+// FP32 pair operations; otherwise z / (1 + exp(-z)) per value.
+__device__ __forceinline__ float2 silu2(const float2 z) {
+#if MCW_FUSED_SILU_TANH
+    const float2 h = __fmul2_rn(z, make_float2(0.5f, 0.5f));
+    return __ffma2_rn(h, make_float2(tanh_approx(h.x), tanh_approx(h.y)), h);
+#else
+    return make_float2(silu(z.x), silu(z.y));
+#endif
+}
 
 // Byte offset of element (row, k) in a K-major core-matrix tile whose rows are kdim long.
 __host__ __device__ __forceinline__ uint32_t core_off(int row, int k, int kdim) {
@@ -242,9 +264,10 @@ __device__ __forceinline__ void silu_store32(const uint32_t (&r)[32], const floa
         uint32_t packed[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const __nv_bfloat162 two =
-                __floats2bfloat162_rn(silu(__uint_as_float(r[q * 8 + 2 * e]) + bv[2 * e]),
-                                      silu(__uint_as_float(r[q * 8 + 2 * e + 1]) + bv[2 * e + 1]));
+            const float2 a = silu2(__fadd2_rn(
+                make_float2(__uint_as_float(r[q * 8 + 2 * e]), __uint_as_float(r[q * 8 + 2 * e + 1])),
+                make_float2(bv[2 * e], bv[2 * e + 1])));
+            const __nv_bfloat162 two = __floats2bfloat162_rn(a.x, a.y);
             packed[e] = *reinterpret_cast<const uint32_t *>(&two);
         }
         *reinterpret_cast<uint4 *>(act + core_off(row, c0 + q * 8, FH)) =
@@ -330,47 +353,54 @@ __device__ __forceinline__ void epilogue_out(uint32_t tlane, int blk, const floa
     }
 }
 
-// The same in fp16: this warp's 64 columns (both 32-column halves of its share) are
-// packed into half2 first, so a stage row again holds 128 bytes and each output row
-// leaves as 128-byte runs.  Row pitch ldy (halves) is a multiple of 8.
+// The same in fp16: this warp's kOutCols (64 or 32) columns are packed into half2
+// first, so a stage row holds 128 (64) bytes and each output row leaves as runs of
+// that length.  Row pitch ldy (halves) is a multiple of 8.
 __device__ __forceinline__ void epilogue_out_half(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
                                                   __half *y, int ldy, int m, int row0, int group, int lane) {
-    static_assert(kOutCols == 64, "fp16 output: 64 columns per warp");
+    static_assert(kOutCols == 64 || kOutCols == 32, "fp16 output: 32 or 64 columns per warp");
+    constexpr int kHalves = kOutCols / 32;                // 32-column halves of the warp's share
+    constexpr int kLanesPerRow = kOutCols * 2 / 16;       // 16-byte pieces of a row: 8 or 4
+    constexpr int kRowsPerStore = 32 / kLanesPerRow;      // rows one store instruction covers: 4 or 8
     const int c0 = group * kOutCols;
     const int nb = blk * kOutN + c0;
     if (nb >= FO) return;
-    uint32_t hp[32];
+    uint32_t hp[16 * kHalves];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < kHalves; ++h) {
         float v[32];
         tmem_ld32(tlane + (uint32_t)(c0 + 32 * h), v);
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const float4 b = *reinterpret_cast<const float4 *>(b4 + nb + 32 * h + 4 * q);
-            const __half2 lo = __floats2half2_rn(v[4 * q] + b.x, v[4 * q + 1] + b.y);
-            const __half2 hi = __floats2half2_rn(v[4 * q + 2] + b.z, v[4 * q + 3] + b.w);
+            const float2 zl = __fadd2_rn(make_float2(v[4 * q], v[4 * q + 1]), make_float2(b.x, b.y));
+            const float2 zh = __fadd2_rn(make_float2(v[4 * q + 2], v[4 * q + 3]), make_float2(b.z, b.w));
+            const __half2 lo = __floats2half2_rn(zl.x, zl.y);
+            const __half2 hi = __floats2half2_rn(zh.x, zh.y);
             hp[16 * h + 2 * q] = *reinterpret_cast<const uint32_t *>(&lo);
             hp[16 * h + 2 * q + 1] = *reinterpret_cast<const uint32_t *>(&hi);
         }
     }
-    const bool full = nb + 64 <= FO;
+    const bool full = nb + kOutCols <= FO;
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
         __syncwarp();
         if ((lane >> 3) == p) {
             uint4 *dst = reinterpret_cast<uint4 *>(stage + (lane & 7) * kStagePitch);
 #pragma unroll
-            for (int q = 0; q < 8; ++q) dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+            for (int q = 0; q < 4 * kHalves; ++q)
+                dst[q] = make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
         }
         __syncwarp();
         const int rbase = row0 + 8 * p;
         if (full) {
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int r = (lane >> 3) + 4 * k;
-                const uint4 val = *reinterpret_cast<const uint4 *>(stage + r * kStagePitch + (lane & 7) * 16);
+            for (int k = 0; k < 8 / kRowsPerStore; ++k) {
+                const int r = lane / kLanesPerRow + kRowsPerStore * k;
+                const int piece = lane % kLanesPerRow;
+                const uint4 val = *reinterpret_cast<const uint4 *>(stage + r * kStagePitch + piece * 16);
                 if (rbase + r < m)
-                    *reinterpret_cast<uint4 *>(y + (size_t)(rbase + r) * ldy + nb + (lane & 7) * 8) = val;
+                    *reinterpret_cast<uint4 *>(y + (size_t)(rbase + r) * ldy + nb + piece * 8) = val;
             }
         } else if (nb + lane < FO) {       // the ragged block: columns 640 .. 648
 #pragma unroll
