@@ -187,7 +187,7 @@ def _random_net(seed):
     return net
 
 
-@pytest.mark.parametrize('m', [1, 127, 128, 129, 1000, 4097])
+@pytest.mark.parametrize('m', [1, 127, 128, 129, 1000, 4097, 65536 + 77])
 def test_fused_forward_matches_layerwise_and_float64(m):
     """mcw_mlp_forward (one tcgen05 kernel, activations in shared memory) against float64
     with the same bf16 roundings, and against the layer-by-layer GEMM forward."""
