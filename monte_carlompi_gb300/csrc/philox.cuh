@@ -32,9 +32,11 @@ __host__ __device__ inline PhiloxKeys philox_schedule(uint64_t seed) {
 }
 
 __device__ __forceinline__ uint4 philox_round(uint4 c, uint32_t k0, uint32_t k1) {
-    uint32_t hi0 = __umulhi(kPhiloxM0, c.x), lo0 = kPhiloxM0 * c.x;
-    uint32_t hi1 = __umulhi(kPhiloxM1, c.z), lo1 = kPhiloxM1 * c.z;
-    return make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    // each 32 x 32 -> 64-bit product as one wide multiply
+    const uint64_t p0 = (uint64_t)kPhiloxM0 * c.x;
+    const uint64_t p1 = (uint64_t)kPhiloxM1 * c.z;
+    return make_uint4((uint32_t)(p1 >> 32) ^ c.y ^ k0, (uint32_t)p1, (uint32_t)(p0 >> 32) ^ c.w ^ k1,
+                      (uint32_t)p0);
 }
 
 // Philox with a precomputed key schedule.
