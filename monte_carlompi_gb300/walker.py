@@ -83,6 +83,7 @@ class Walker:
         self._ctx = h
         self.device = device
         self._tables_keep = []
+        self._cfg_cache = (None, None)   # (field values of the last configs, their C array)
 
     def close(self):
         if getattr(self, '_ctx', None):
@@ -150,7 +151,7 @@ class Walker:
         if mode not in MODES:
             raise ValueError('mode must be one of %s' % ', '.join(sorted(MODES)))
         mode_c, dtype = MODES[mode]
-        cfg = configs_to_c(configs)
+        cfg = self._configs_c(configs)
         n = len(configs)
         total = int(sum(max(int(c.n_photon), 0) for c in configs))
         tallies = np.zeros(n, _abi.TALLY)
@@ -158,9 +159,9 @@ class Walker:
         rec = None
         if records == 'host':
             rec = out if out is not None else np.empty(total, dtype)
-            if rec.dtype != dtype or rec.size < total or not rec.flags['C_CONTIGUOUS']:
+            if rec.dtype != dtype or rec.size < total or not rec.flags.c_contiguous:
                 raise ValueError('out must be a contiguous %s array of >= %d records' % (dtype, total))
-            ptr, where = rec.ctypes.data, _abi.RECORDS_HOST
+            ptr, where = rec.__array_interface__['data'][0], _abi.RECORDS_HOST
         elif records == 'device':
             if device_ptr is None:
                 raise ValueError('records="device" needs device_ptr')
@@ -173,6 +174,14 @@ class Walker:
                                 tallies.ctypes.data, ctypes.byref(stats))
         _abi.check(rc, self._ctx)
         return WalkResult(rec, tallies, stats.as_dict())
+
+    def _configs_c(self, configs):
+        """The configs as a C array; a call on configs with the same field values as
+        the previous call reuses its array (the library only reads it)."""
+        key = tuple(tuple(vars(c).values()) for c in configs)
+        if key != self._cfg_cache[0]:
+            self._cfg_cache = (key, configs_to_c(configs))
+        return self._cfg_cache[1]
 
     def autotune(self, configs, seed=1):
         cfg = configs_to_c(configs)
