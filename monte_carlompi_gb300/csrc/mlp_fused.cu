@@ -23,11 +23,14 @@
 // checks a CTA-wide abort flag; a timeout sets bit 1 of the error flag read by
 // mcw_mlp_status, lets copies and MMAs in flight finish (bounded), frees the tensor
 // memory and leaves.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 
 #include "../../include/mcw_mlp.h"
 
@@ -81,6 +84,14 @@ constexpr int kRingBytes = kSlots * kChunkBytes;
 constexpr int kStagePitch = 36 * 4;                   // stage row: 32 floats + 16 B pad (no bank conflicts)
 constexpr int kStageWarp = 8 * kStagePitch;           // 8 rows per warp
 constexpr int kStageBytes = kEpiWarps * kStageWarp < 4096 ? 4096 : kEpiWarps * kStageWarp;
+#ifndef MCW_FUSED_TMA_OUT
+#define MCW_FUSED_TMA_OUT 1
+#endif
+// fp16 output through tensor stores: a warp's stage is 1 KB (8 rows x 128 bytes in the
+// tensor map's 128-byte swizzle), 1024-byte aligned; columns [0, kTmaCols) go through the
+// tensor map, the ragged rest (640 .. 648) through plain stores
+constexpr int kStageTma = 1024;
+constexpr int kTmaCols = (FO / 64) * 64;
 // biases in shared memory: b1, b2, b3 (256 each), b4 zero-padded to the six 128-column blocks
 constexpr int kB4Pad = 6 * 128;
 constexpr int kBiasFloats = 3 * 256 + kB4Pad;
@@ -102,6 +113,8 @@ __host__ __device__ constexpr uint32_t idesc(int n) {
 static_assert(kHidK * FH * 2 == kChunkBytes && kOutK * kOutN * 2 == kChunkBytes, "chunk sizes");
 static_assert(kW1Bytes + (kNumChunks - 1) * kChunkBytes == MCW_MLP_PACK_BYTES, "packed blob layout");
 static_assert(kTiles * kXBytes <= kStageBytes, "the input tiles live in the stage region");
+static_assert(kEpiWarps * kStageTma <= kStageBytes && (kTiles * kActBytes + kRingBytes) % 1024 == 0,
+              "tensor-store stages: 1 KB per epilogue warp, 1024-byte aligned");
 
 // The i-th weight chunk a CTA consumes: per layer the chunks of tile 0, then those of
 // tile 1 (the order in which the MMA warp issues the layers of its tiles).
@@ -413,6 +426,78 @@ __device__ __forceinline__ void epilogue_out_half(uint32_t tlane, int blk, const
     __syncwarp();
 }
 
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];\n"
+                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// the thread's tensor stores have read their shared-memory sources
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// the thread's tensor stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+
+// fp16 output through tensor stores: this warp's 64 columns, 8 rows at a time through its
+// 1 KB stage (16-byte chunk c of row r at r * 128 + (c ^ r) * 16, the map's 128-byte
+// swizzle, so the stage writes are free of bank conflicts), one tensor store per 8 rows
+// issued by lane 0; the warp goes on while the store drains.  The ragged block
+// (columns 640 .. 648) is written with plain stores from the same stage.
+__device__ __forceinline__ void epilogue_out_half_tma(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
+                                                      const CUtensorMap *ymap, __half *y, int ldy, int m, int row0,
+                                                      int group, int lane) {
+    static_assert(kOutCols == 64, "tensor stores: 64 columns (128 bytes) per warp");
+    const int c0 = group * kOutCols;
+    const int nb = blk * kOutN + c0;
+    if (nb >= FO) return;
+    uint32_t hp[32];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        float v[32];
+        tmem_ld32(tlane + (uint32_t)(c0 + 32 * h), v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float4 b = *reinterpret_cast<const float4 *>(b4 + nb + 32 * h + 4 * q);
+            const float2 zl = __fadd2_rn(make_float2(v[4 * q], v[4 * q + 1]), make_float2(b.x, b.y));
+            const float2 zh = __fadd2_rn(make_float2(v[4 * q + 2], v[4 * q + 3]), make_float2(b.z, b.w));
+            const __half2 lo = __floats2half2_rn(zl.x, zl.y);
+            const __half2 hi = __floats2half2_rn(zh.x, zh.y);
+            hp[16 * h + 2 * q] = *reinterpret_cast<const uint32_t *>(&lo);
+            hp[16 * h + 2 * q + 1] = *reinterpret_cast<const uint32_t *>(&hi);
+        }
+    }
+    const bool full = nb + kOutCols <= kTmaCols;
+    const int r = lane & 7;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        if (lane == 0) bulk_wait_read();          // the stage's last tensor store has read it
+        __syncwarp();
+        if ((lane >> 3) == p) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                *reinterpret_cast<uint4 *>(stage + r * 128 + ((q ^ r) << 4)) =
+                    make_uint4(hp[4 * q], hp[4 * q + 1], hp[4 * q + 2], hp[4 * q + 3]);
+        }
+        const int rbase = row0 + 8 * p;
+        if (full) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+                tma_store_2d(ymap, smem_u32(stage), nb, rbase);
+                bulk_commit();
+            }
+        } else {
+            __syncwarp();
+            if (nb + lane < FO) {
+#pragma unroll
+                for (int rr = 0; rr < 8; ++rr)
+                    if (rbase + rr < m)
+                        y[(size_t)(rbase + rr) * ldy + nb + lane] = *reinterpret_cast<const __half *>(
+                            stage + rr * 128 + (((lane >> 3) ^ rr) << 4) + (lane & 7) * 2);
+            }
+        }
+    }
+    __syncwarp();
+}
+
 struct Bars {
     uint64_t full[kSlots], empty[kSlots];   // weight ring
     uint64_t accf[kTiles][2], acce[kTiles][2];  // accumulator halves per tile: full (MMA -> epilogue), empty
@@ -424,8 +509,10 @@ template <bool kHalf>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const float *x, int m, const float *b1,
                                                                 const float *b2, const float *b3, const float *b4,
                                                                 const unsigned char *blob, void *y, int ldy,
-                                                                unsigned int *err) {
-    extern __shared__ __align__(128) unsigned char smem[];
+                                                                unsigned int *err,
+                                                                const __grid_constant__ CUtensorMap ymap,
+                                                                int use_tma) {
+    extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *act0 = smem;                                  // 64 KB activation tile per tile
     unsigned char *ring = smem + kTiles * kActBytes;             // 2 x 16 KB weight chunks
     unsigned char *stage_all = ring + kRingBytes;                // 16 KB output stage ...
@@ -608,7 +695,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                 accf_phase[t][h] ^= 1u;
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n");
-                if (kHalf)
+                if (kHalf && use_tma)
+                    epilogue_out_half_tma(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage_all + warp * kStageTma,
+                                          &ymap, static_cast<__half *>(y), ldy, m, row0, group, lane);
+                else if (kHalf)
                     epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<__half *>(y),
                                       ldy, m, row0, group, lane);
                 else
@@ -618,6 +708,7 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                 arrive(&bars.acce[t][h]);
             }
         }
+        if (kHalf && use_tma && lane == 0) bulk_wait_all();   // this warp's tensor stores are done
     }
 
     asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -655,6 +746,37 @@ using namespace mcw;
 
 namespace {
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// fp16 output [m, kTmaCols] at row pitch ldy halves, box 64 x 8, 128-byte swizzle; false
+// when the driver entry point is missing or the layout breaks a tensor-map rule.
+bool make_out_map(CUtensorMap *map, void *y, int m, int ldy) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || (reinterpret_cast<uintptr_t>(y) & 15) || (ldy & 7) || ldy < kTmaCols) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)kTmaCols, (cuuint64_t)m};
+    const cuuint64_t strides[1] = {(cuuint64_t)ldy * 2};
+    const cuuint32_t box[2] = {64, 8};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3, const float *b4,
             const void *blob, void *y, int32_t ldy, bool half, void *stream) {
     const int align = half ? 8 : 4;   // 16-byte row starts
@@ -671,8 +793,13 @@ int forward(const float *x, int32_t m, const float *b1, const float *b2, const f
     const unsigned grid = (unsigned)((m + FM * kTiles - 1) / (FM * kTiles));
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const unsigned char *wb = static_cast<const unsigned char *>(blob);
-    if (half) mlp_fused_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err);
-    else mlp_fused_kernel<false><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err);
+    CUtensorMap ymap;
+    memset(&ymap, 0, sizeof(ymap));
+    const int use_tma = (half && MCW_FUSED_TMA_OUT && make_out_map(&ymap, y, m, ldy)) ? 1 : 0;
+    if (half)
+        mlp_fused_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err, ymap, use_tma);
+    else
+        mlp_fused_kernel<false><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err, ymap, 0);
     return cudaGetLastError() == cudaSuccess ? 0 : MCW_MLP_ERR_CUDA;
 }
 
