@@ -449,15 +449,22 @@ __device__ __forceinline__ void epilogue_out_half_tma(uint32_t tlane, int blk, c
     const int nb = blk * kOutN + c0;
     if (nb >= FO) return;
     uint32_t hp[32];
+    // both 32-column loads in flight before the one wait
+    uint32_t ra[2][32];
+    tmem_ld32_issue(tlane + (uint32_t)c0, ra[0]);
+    tmem_ld32_issue(tlane + (uint32_t)(c0 + 32), ra[1]);
+    tmem_ld_wait(ra[0]);
+    tmem_ld_wait(ra[1]);
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        float v[32];
-        tmem_ld32(tlane + (uint32_t)(c0 + 32 * h), v);
+        const uint32_t (&v)[32] = ra[h];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const float4 b = *reinterpret_cast<const float4 *>(b4 + nb + 32 * h + 4 * q);
-            const float2 zl = __fadd2_rn(make_float2(v[4 * q], v[4 * q + 1]), make_float2(b.x, b.y));
-            const float2 zh = __fadd2_rn(make_float2(v[4 * q + 2], v[4 * q + 3]), make_float2(b.z, b.w));
+            const float2 zl = __fadd2_rn(make_float2(__uint_as_float(v[4 * q]), __uint_as_float(v[4 * q + 1])),
+                                         make_float2(b.x, b.y));
+            const float2 zh = __fadd2_rn(make_float2(__uint_as_float(v[4 * q + 2]), __uint_as_float(v[4 * q + 3])),
+                                         make_float2(b.z, b.w));
             const __half2 lo = __floats2half2_rn(zl.x, zl.y);
             const __half2 hi = __floats2half2_rn(zh.x, zh.y);
             hp[16 * h + 2 * q] = *reinterpret_cast<const uint32_t *>(&lo);

@@ -792,18 +792,26 @@ def output_weights():
     return np.concatenate([w, [10.0]]).astype(np.float32)
 
 
-def inference_rate(ensemble, batch=65536, reps=20):
-    """BRF predictions per second of one member on the tensor-core kernels (CUDA events)."""
+def inference_rate(ensemble, batch=65536, reps=20, members=None):
+    """BRF predictions per second on the fused tensor-core kernel (CUDA events): every member
+    of the ensemble (the mean and spread of a prediction need them all) forwards the same
+    batch; the L2 is flushed before each timed repetition (median over reps)."""
     import torch
-    m = ensemble.members[0]
+    ms = ensemble.members if members is None else ensemble.members[:members]
     x = torch.rand((batch, 4), device='cuda') * 2 - 1
     for _ in range(3):
-        m.predict_std(x)
+        for m in ms:
+            m.predict_std(x)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device='cuda')
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record()
+    times = []
     for _ in range(reps):
-        m.predict_std(x)
-    e1.record()
-    torch.cuda.synchronize()
-    return batch * reps / (e0.elapsed_time(e1) / 1e3)
+        flush.zero_()
+        e0.record()
+        for m in ms:
+            m.predict_std(x)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    del flush
+    return batch / (float(np.median(times)) / 1e3)

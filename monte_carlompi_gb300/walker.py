@@ -161,7 +161,7 @@ class Walker:
             rec = out if out is not None else np.empty(total, dtype)
             if rec.dtype != dtype or rec.size < total or not rec.flags.c_contiguous:
                 raise ValueError('out must be a contiguous %s array of >= %d records' % (dtype, total))
-            ptr, where = rec.__array_interface__['data'][0], _abi.RECORDS_HOST
+            ptr, where = rec.ctypes.data, _abi.RECORDS_HOST   # (__array_interface__ costs ~8 us here)
         elif records == 'device':
             if device_ptr is None:
                 raise ValueError('records="device" needs device_ptr')
