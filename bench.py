@@ -197,7 +197,7 @@ def sweep_workload():
     return cfgs, tables, imp
 
 
-def run_sweep(args):
+def run_sweep(args, emit=True):
     """Batched sweep in one graph-captured launch vs one launch per config."""
     import torch
     from monte_carlompi_gb300.walker import Walker
@@ -247,8 +247,9 @@ def run_sweep(args):
             'wall_ms': {'per_config_loop': wp, 'batched_graph': wb, 'speedup': wp / wb,
                         'note': 'host wall clock of the 64 Walker.walk calls against one graph launch, '
                                 'each returning with its tallies on the host'}}
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def run_lone(args):
@@ -381,7 +382,7 @@ def run_pol(args):
     return 0
 
 
-def run_surrogate(args):
+def run_surrogate(args, emit=True):
     """Surrogate workload: --surrogate-configs configs (4,096 by default, BASELINE config 4) x 2e5 photons walked
     on the GPU, 5-member ensemble trained on the tensor-core kernels, 512 held-out configs
     judged by 1e6- and 1e7-photon Monte Carlo; BRF/s of the network against plain Monte
@@ -442,12 +443,13 @@ def run_surrogate(args):
             'ensemble_spread_median': float(np.median(spread)),
             'seconds': {'data': t_data, 'train': t_train, 'judge_mc': t_ref},
             'inverse': inv}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     w.close()
-    return 0
+    return line
 
 
-def run_mlp(args):
+def run_mlp(args, emit=True):
     """Surrogate network inference on the fused tcgen05 kernel (mcw_mlp_forward): BRF/s,
     TFLOP/s of the four layers against the measured bf16 peak, and the output stream
     (f32 rows of 652) against the measured HBM copy bandwidth."""
@@ -485,7 +487,7 @@ def run_mlp(args):
     gbs = out_bytes / (ms / 1e3) / 1e9
     peak = float(peaks.get('bf16_tflops') or 1900.0)
     hbm = float(peaks.get('hbm_gbs') or 6800.0)
-    print(json.dumps({'metric': METRIC, 'workload': 'mlp', 'value': batch / (ms / 1e3), 'unit': 'BRF/s',
+    line = {'metric': METRIC, 'workload': 'mlp', 'value': batch / (ms / 1e3), 'unit': 'BRF/s',
                       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms, 'dtype': 'bf16',
                       'gpu_launches': args.steps,
                       'config': {'batch': batch, 'net': '4-256-256-256-649 SiLU',
@@ -497,8 +499,10 @@ def run_mlp(args):
                       'roofline': {'bound': 'tensor', 'achieved': tflops, 'peak': peak, 'unit': 'TFLOP/s',
                                    'frac': tflops / peak, 'peak_source': src,
                                    'hbm': {'achieved': gbs, 'peak': hbm, 'unit': 'GB/s', 'frac': gbs / hbm,
-                                           'bytes': 'x in + y out (fp16, row pitch 656)'}}}))
-    return 0
+                                           'bytes': 'x in + y out (fp16, row pitch 656)'}}}
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def run_train(args):
@@ -885,11 +889,54 @@ def run_ours(args):
         }
         if not args.no_cpu_baseline:
             line['cpu_baseline'] = cpu_baseline()
+        if world == 1 and not args.no_extras:
+            line['extras'] = extras(args)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
     w.close()
     return 0
+
+
+def extras(args):
+    """The other workloads, run after the walk's timed region and summarised in its line:
+    the 64-config sweep, fused inference, and the surrogate (training, its error against
+    Monte Carlo, inference rate, the inverse).  A workload that fails records its error."""
+    out = {}
+
+    def keep(d, keys):
+        return {k: d[k] for k in keys if k in d}
+
+    try:
+        s = run_sweep(args, emit=False)
+        out['sweep'] = keep(s, ['value', 'unit', 'batched_graph_ms', 'per_config_launches_ms',
+                                'speedup_vs_per_config', 'wall_ms', 'scatter_events_per_s'])
+        out['sweep']['config'] = s['config']['workload']
+    except Exception as e:  # noqa: BLE001  (a failed extra must not lose the walk's line)
+        out['sweep'] = {'error': repr(e)}
+    try:
+        m = run_mlp(args, emit=False)
+        out['mlp'] = keep(m, ['value', 'unit', 'ms_per_step'])
+        out['mlp']['roofline'] = keep(m['roofline'], ['bound', 'achieved', 'peak', 'unit', 'frac'])
+        out['mlp']['config'] = m['config']
+    except Exception as e:  # noqa: BLE001
+        out['mlp'] = {'error': repr(e)}
+    try:
+        g = run_surrogate(args, emit=False)
+        out['surrogate'] = keep(g, ['value', 'unit', 'brf_per_s_one_member', 'mc_brf_per_s', 'speedup_vs_mc',
+                                    'rms_rel_brf_err_vs_1e6_mc', 'rms_rel_brf_err_vs_1e6_mc_noise_removed',
+                                    'rms_rel_brf_err_vs_1e7_mc', 'mc_1e6_noise_floor', 'seconds', 'config'])
+        inv = g.get('inverse') or {}
+        out['surrogate']['inverse'] = keep(inv, ['observations', 'r_eff_rel_err', 'flagged_for_mc',
+                                                 'seconds_per_retrieval', 'speedup_per_retrieval_vs_mc',
+                                                 'criterion'])
+        if 'mc_only' in inv:
+            out['surrogate']['inverse']['mc_only'] = keep(inv['mc_only'], [
+                'subset', 'r_eff_rel_err_median', 'surrogate_path_err_median_same_subset',
+                'seconds_per_retrieval'])
+    except Exception as e:  # noqa: BLE001
+        out['surrogate'] = {'error': repr(e)}
+    return out
 
 
 def main():
@@ -908,15 +955,20 @@ def main():
     ap.add_argument('--surrogate-configs', type=int, default=4096)
     ap.add_argument('--surrogate-epochs', type=int, default=300)
     ap.add_argument('--inverse-configs', type=int, default=4096)
+    ap.add_argument('--no-extras', action='store_true',
+                    help='walk workload: skip the other workloads summarised under "extras"')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
     if args.workload == 'sweep':
-        return run_sweep(args)
+        run_sweep(args)
+        return 0
     if args.workload == 'surrogate':
-        return run_surrogate(args)
+        run_surrogate(args)
+        return 0
     if args.workload == 'mlp':
-        return run_mlp(args)
+        run_mlp(args)
+        return 0
     if args.workload == 'pol':
         return run_pol(args)
     if args.workload == 'lone':
