@@ -383,7 +383,7 @@ def run_pol(args):
 
 
 def run_surrogate(args, emit=True):
-    """Surrogate workload: --surrogate-configs configs (4,096 by default, BASELINE config 4) x 2e5 photons walked
+    """Surrogate workload: --surrogate-configs configs (4,096 by default, the surrogate-training workload) x 2e5 photons walked
     on the GPU, 5-member ensemble trained on the tensor-core kernels, 512 held-out configs
     judged by 1e6- and 1e7-photon Monte Carlo; BRF/s of the network against plain Monte
     Carlo; then the inverse workload."""
@@ -507,7 +507,7 @@ def run_mlp(args, emit=True):
 
 def run_train(args):
     """Surrogate training on the training engine: (a) one Adam step of a 5-member
-    ensemble at batch 256 (BASELINE config 4's batch), all members at once from one
+    ensemble at batch 256 (the surrogate-training batch), all members at once from one
     captured CUDA graph, against the same step run member by member on the layer-wise
     kernels; (b) forward + backward of one network over 65,536 rows (split-K weight
     gradients) against the layer-wise autograd path.  FLOPs: 3 x 596,480 per row
