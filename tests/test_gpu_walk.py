@@ -541,6 +541,50 @@ def test_batch_first_config_equals_single_run(walker):
                                   single.records['condition'])
 
 
+SWEEP_SAMPLE = [   # (r_eff um, lambda0 um, theta0 deg, depth m): configs of the 64-config sweep's grid
+    (100.0, 1.30, 0.0, 0.10), (400.0, 1.60, 45.0, 0.02), (1500.0, 1.10, 60.0, 1.0),
+    (50.0, 1.70, 30.0, 0.02), (200.0, 0.95, 0.0, 0.02), (800.0, 1.40, 60.0, 0.10)]
+
+
+def test_sweep_configs_match_oracle_in_one_graph_launch(walker):
+    """Six configs of the batched sweep (each its own grain-size table, wavelength, zenith
+    and depth) walked together by one captured graph launch, each against the oracle at
+    the same N: condition fractions within 4 sigma, the 648-bin exit histogram
+    (two-sample chi-square, p > 1e-4) and mean n_scat within 4 sigma."""
+    import torch
+    n = 40000
+    tables, cfgs = [], []
+    for j, (r, wvl, th, depth) in enumerate(SWEEP_SAMPLE):
+        tables.append(ssp.synthetic_ice_table(r, 600, 2100))
+        cfgs.append(WalkConfig(n_photon=n, wvl0=wvl, half_width=0.085, theta0_deg=th,
+                               tau_tot=depth * ssp.ext_cff_mss_sphere(r) * 300.0,
+                               lambertian_reflectance=0.5, ice_table=j, rds_snw=r))
+    imp = ssp.synthetic_impurity_table(600, 2100)
+    walker.set_tables(tables, imp)
+    buf = torch.zeros(n * len(cfgs) * _abi.RECORD32.itemsize, dtype=torch.uint8, device='cuda')
+    g = walker.graph(cfgs, device_ptr=buf.data_ptr())
+    try:
+        g.launch(5)
+        res = g.launch(6)
+    finally:
+        g.close()
+    torch.cuda.synchronize()
+    rec = buf.cpu().numpy().view(_abi.RECORD32)
+    for j, cfg in enumerate(cfgs):
+        got = rec[j * n:(j + 1) * n]
+        assert np.all(got['config'] == j)
+        assert int(res.tallies[j]['n_cond'][1:].sum()) == n
+        ref = oracle_run(cfg, tables[j], imp, 600 + j)
+        condition_fractions_agree(got['condition'], ref['condition'])
+        top_g, top_r = got['condition'] == 1, ref['condition'] == 1
+        x2, dof, p = chi2_two_sample(exit_histogram(got['theta_n'][top_g], got['phi_n'][top_g]),
+                                     exit_histogram(ref['theta_n'][top_r], ref['phi_n'][top_r]))
+        assert p > 1e-4, (j, x2, dof, p)
+        a, b = got['n_scat'].astype(np.float64), ref['n_scat'].astype(np.float64)
+        se = np.sqrt(a.var() / a.size + b.var() / b.size)
+        assert abs(a.mean() - b.mean()) < 4 * se, (j, a.mean(), b.mean(), se)
+
+
 def test_graph_replays_equal_walks(walker):
     cfg, ice, imp = cfg2_geometry(200000)
     cfgs = [cfg, dataclasses.replace(cfg, theta0_deg=30.0, n_photon=100000)]
