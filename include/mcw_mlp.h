@@ -102,6 +102,17 @@ int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2,
 int mcw_mlp_forward_f16(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
                         const float *b4, const void *blob, void *y, int32_t ldy, void *stream);
 
+/* The biases of one network, b1 | b2 | b3 | b4, as one f32 row. */
+#define MCW_MLP_BIAS_FLOATS (3 * MCW_MLP_HIDDEN + MCW_MLP_OUT)
+
+/* mcw_mlp_forward_f16 of `members` networks (an ensemble) on the same inputs, in one
+ * launch: member e's biases at bias + e * MCW_MLP_BIAS_FLOATS, its packed weights at
+ * blob + e * MCW_MLP_PACK_BYTES, its outputs at y + e * m * ldy halves (ldy as
+ * mcw_mlp_forward_f16).  Each member's outputs equal those of mcw_mlp_forward_f16 bit
+ * for bit.  No reference counterpart (the ensemble's spread judges the surrogate). */
+int mcw_mlp_forward_ensemble_f16(const float *x, int32_t m, int32_t members, const float *bias, const void *blob,
+                                 void *y, int32_t ldy, void *stream);
+
 /* ---- training engine: one Adam step of an ensemble in a fixed sequence of launches.
  * "groups" are independent problems of the same shape (ensemble members) whose
  * operands lie stride_* elements apart; strides and leading dimensions count

@@ -134,9 +134,11 @@ ENGINE_MMA_SYNC, ENGINE_TCGEN05 = 0, 1
 # entry points of include/mcw_mlp.h
 MLP_EXPORTS = ['mcw_mlp_gemm', 'mcw_mlp_colsum', 'mcw_mlp_loss', 'mcw_mlp_adam', 'mcw_mlp_cast_bf16',
                'mcw_mlp_status', 'mcw_mlp_pack', 'mcw_mlp_forward', 'mcw_mlp_forward_f16',
+               'mcw_mlp_forward_ensemble_f16',
                'mcw_mlp_gemm_grouped', 'mcw_mlp_reduce_splits', 'mcw_mlp_loss_grouped',
                'mcw_mlp_colsum_grouped', 'mcw_mlp_adam_grouped', 'mcw_mlp_gather', 'mcw_mlp_advance']
 MLP_PACK_BYTES = 5 * 256 * 256 * 2 + 256 * 16 * 2
+MLP_BIAS_FLOATS = 3 * 256 + 649
 
 RECORD32 = np.dtype([('condition', np.int32), ('n_scat', np.int32), ('wvn', np.float32),
                      ('theta_n', np.float32), ('phi_n', np.float32),
@@ -216,6 +218,7 @@ def load(path=None):
         'mcw_mlp_pack': ([vp, vp, vp, vp, vp, vp], ctypes.c_int),
         'mcw_mlp_forward': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
         'mcw_mlp_forward_f16': ([vp, i32, vp, vp, vp, vp, vp, vp, i32, vp], ctypes.c_int),
+        'mcw_mlp_forward_ensemble_f16': ([vp, i32, i32, vp, vp, vp, i32, vp], ctypes.c_int),
         'mcw_mlp_gemm_grouped': ([ctypes.POINTER(GemmGroupedC), vp], ctypes.c_int),
         'mcw_mlp_reduce_splits': ([vp, i64, i64, i64, vp, i64, i64, i32, i32, i32, i32, vp], ctypes.c_int),
         'mcw_mlp_loss_grouped': ([vp, i64, i64, vp, i64, i64, vp, i32, i32, i32, vp, i64, i64, vp, i64,

@@ -430,6 +430,11 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t sr
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];\n"
                  :: "l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y) : "memory");
 }
+// A tensor store of the ensemble's output map {columns, rows, member}: box {64, 8, 1}.
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];\n"
+                 :: "l"(reinterpret_cast<uint64_t>(map)), "r"(src), "r"(x), "r"(y), "r"(z) : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
 // the thread's tensor stores have read their shared-memory sources
 __device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
@@ -441,9 +446,10 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 // swizzle, so the stage writes are free of bank conflicts), one tensor store per 8 rows
 // issued by lane 0; the warp goes on while the store drains.  The ragged block
 // (columns 640 .. 648) is written with plain stores from the same stage.
+template <bool kEnsemble>
 __device__ __forceinline__ void epilogue_out_half_tma(uint32_t tlane, int blk, const float *b4, unsigned char *stage,
                                                       const CUtensorMap *ymap, __half *y, int ldy, int m, int row0,
-                                                      int group, int lane) {
+                                                      int member, int group, int lane) {
     static_assert(kOutCols == 64, "tensor stores: 64 columns (128 bytes) per warp");
     const int c0 = group * kOutCols;
     const int nb = blk * kOutN + c0;
@@ -488,7 +494,10 @@ __device__ __forceinline__ void epilogue_out_half_tma(uint32_t tlane, int blk, c
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             __syncwarp();
             if (lane == 0) {
-                tma_store_2d(ymap, smem_u32(stage), nb, rbase);
+                if (kEnsemble)
+                    tma_store_3d(ymap, smem_u32(stage), nb, rbase, member);
+                else
+                    tma_store_2d(ymap, smem_u32(stage), nb, rbase);
                 bulk_commit();
             }
         } else {
@@ -512,13 +521,13 @@ struct Bars {
     uint64_t fin;                 // every MMA of the CTA complete
 };
 
-template <bool kHalf>
-__global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const float *x, int m, const float *b1,
-                                                                const float *b2, const float *b3, const float *b4,
-                                                                const unsigned char *blob, void *y, int ldy,
-                                                                unsigned int *err,
-                                                                const __grid_constant__ CUtensorMap ymap,
-                                                                int use_tma) {
+// kEnsemble: the instance that carries several networks (tiles per member, member
+// strides); the one-network instance has none of that arithmetic.
+template <bool kHalf, bool kEnsemble>
+__device__ __forceinline__ void mlp_fused_body(const float *x, int m, const float *b1, const float *b2,
+                                               const float *b3, const float *b4, const unsigned char *blob, void *y,
+                                               int ldy, unsigned int *err, const CUtensorMap *ymap, int use_tma,
+                                               int tiles, int bias_stride, long long blob_stride) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *act0 = smem;                                  // 64 KB activation tile per tile
     unsigned char *ring = smem + kTiles * kActBytes;             // 2 x 16 KB weight chunks
@@ -530,7 +539,11 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
     __shared__ int abort_flag;
     volatile int *abort = &abort_flag;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * FM * kTiles;
+    // networks of an ensemble: CTA blockIdx.x carries tile (blockIdx.x % tiles) of member
+    // (blockIdx.x / tiles), whose biases lie bias_stride floats and whose packed weights
+    // blob_stride bytes after the previous member's, its output rows m * ldy after them
+    // (member is recomputed where it is used, so it holds no register through the kernel)
+    const int m0 = (kEnsemble ? (int)blockIdx.x % tiles : (int)blockIdx.x) * FM * kTiles;
 
     if (warp == kMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
@@ -565,7 +578,10 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                 const int slot = i % kSlots;
                 if (i >= kSlots && !wait_bar(&bars.empty[slot], (uint32_t)(i / kSlots - 1) & 1u, abort)) break;
                 const int c = chunk_at(i);
-                load_chunk(ring + slot * kChunkBytes, blob + chunk_offset(c), chunk_bytes(c), &bars.full[slot]);
+                load_chunk(ring + slot * kChunkBytes,
+                           blob + (kEnsemble ? (size_t)((int)blockIdx.x / tiles) * (size_t)blob_stride : 0) +
+                               chunk_offset(c),
+                           chunk_bytes(c), &bars.full[slot]);
                 issued = i + 1;
             }
             // the last copy into each slot has landed before the CTA can leave
@@ -653,13 +669,16 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
         uint32_t accf_phase[kTiles][2];
         for (int t = 0; t < kTiles; ++t) accf_phase[t][0] = accf_phase[t][1] = 0u;
         // biases into shared memory (b4 zero past column 648), then the epilogue warps meet
-        for (int i = threadIdx.x; i < kBiasFloats; i += kEpiThreads) {
-            float v;
-            if (i < 256) v = b1[i];
-            else if (i < 512) v = b2[i - 256];
-            else if (i < 768) v = b3[i - 512];
-            else v = i - 768 < FO ? b4[i - 768] : 0.f;
-            sbias[i] = v;
+        {
+            const size_t bo = kEnsemble ? (size_t)((int)blockIdx.x / tiles) * (size_t)bias_stride : 0;
+            for (int i = threadIdx.x; i < kBiasFloats; i += kEpiThreads) {
+                float v;
+                if (i < 256) v = b1[bo + i];
+                else if (i < 512) v = b2[bo + i - 256];
+                else if (i < 768) v = b3[bo + i - 512];
+                else v = i - 768 < FO ? b4[bo + i - 768] : 0.f;
+                sbias[i] = v;
+            }
         }
         asm volatile("bar.sync 1, %0;\n" :: "n"(kEpiThreads) : "memory");
         for (int t = 0; t < kTiles; ++t) {
@@ -702,15 +721,19 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
                 accf_phase[t][h] ^= 1u;
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n");
+                // this member's output rows (plain stores; the tensor map takes the member as a coordinate)
+                const int member = kEnsemble ? (int)blockIdx.x / tiles : 0;
+                const size_t yoff = kEnsemble ? (size_t)member * (size_t)m * (size_t)ldy : 0;
                 if (kHalf && use_tma)
-                    epilogue_out_half_tma(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage_all + warp * kStageTma,
-                                          &ymap, static_cast<__half *>(y), ldy, m, row0, group, lane);
+                    epilogue_out_half_tma<kEnsemble>(tlane + (uint32_t)(h * kOutN), j, sbias + 768,
+                                                     stage_all + warp * kStageTma,
+                                          ymap, static_cast<__half *>(y) + yoff, ldy, m, row0, member, group, lane);
                 else if (kHalf)
-                    epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<__half *>(y),
-                                      ldy, m, row0, group, lane);
+                    epilogue_out_half(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage,
+                                      static_cast<__half *>(y) + yoff, ldy, m, row0, group, lane);
                 else
-                    epilogue_out(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<float *>(y), ldy,
-                                 m, row0, group, lane);
+                    epilogue_out(tlane + (uint32_t)(h * kOutN), j, sbias + 768, stage, static_cast<float *>(y) + yoff,
+                                 ldy, m, row0, group, lane);
                 asm volatile("tcgen05.fence::before_thread_sync;\n");
                 arrive(&bars.acce[t][h]);
             }
@@ -726,6 +749,26 @@ __global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const f
         asm volatile("tcgen05.fence::after_thread_sync;\n");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" :: "r"(tmem), "r"(kTmemCols));
     }
+}
+
+// One network: CTA blockIdx.x carries rows 128 blockIdx.x ...
+template <bool kHalf>
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_kernel(const float *x, int m, const float *b1,
+                                                                const float *b2, const float *b3, const float *b4,
+                                                                const unsigned char *blob, void *y, int ldy,
+                                                                unsigned int *err,
+                                                                const __grid_constant__ CUtensorMap ymap,
+                                                                int use_tma) {
+    mlp_fused_body<kHalf, false>(x, m, b1, b2, b3, b4, blob, y, ldy, err, &ymap, use_tma, (int)gridDim.x, 0, 0);
+}
+
+// An ensemble: fp16 outputs, tiles CTAs per member (mlp_fused_body).
+__global__ void __launch_bounds__(kThreads, kCtasPerSm) mlp_fused_ensemble_kernel(
+        const float *x, int m, const float *b1, const float *b2, const float *b3, const float *b4,
+        const unsigned char *blob, void *y, int ldy, unsigned int *err, const __grid_constant__ CUtensorMap ymap,
+        int use_tma, int tiles, int bias_stride, long long blob_stride) {
+    mlp_fused_body<true, true>(x, m, b1, b2, b3, b4, blob, y, ldy, err, &ymap, use_tma, tiles, bias_stride,
+                               blob_stride);
 }
 
 // Rows [row0, row0 + rows_out) and k [k0, k0 + kdim) of W [n, k_in] (row-major bf16) as a
@@ -770,40 +813,55 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// fp16 output [m, kTmaCols] at row pitch ldy halves, box 64 x 8, 128-byte swizzle; false
-// when the driver entry point is missing or the layout breaks a tensor-map rule.
-bool make_out_map(CUtensorMap *map, void *y, int m, int ldy) {
+// fp16 output [m, kTmaCols] at row pitch ldy halves, box 64 x 8, and for an ensemble
+// [members, m, kTmaCols] (members m * ldy halves apart), box 64 x 8 x 1, so that a box
+// passing row m - 1 of a member is clipped there; 128-byte swizzle.  False when the
+// driver entry point is missing or the layout breaks a tensor-map rule.
+bool make_out_map(CUtensorMap *map, void *y, int m, int ldy, int members) {
     EncodeTiledFn fn = encode_fn();
-    if (!fn || (reinterpret_cast<uintptr_t>(y) & 15) || (ldy & 7) || ldy < kTmaCols) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)kTmaCols, (cuuint64_t)m};
-    const cuuint64_t strides[1] = {(cuuint64_t)ldy * 2};
-    const cuuint32_t box[2] = {64, 8};
-    const cuuint32_t estr[2] = {1, 1};
-    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+    if (!fn || (reinterpret_cast<uintptr_t>(y) & 15) || (ldy & 7) || ldy < kTmaCols || members < 1) return false;
+    const cuuint32_t rank = members > 1 ? 3 : 2;
+    const cuuint64_t dims[3] = {(cuuint64_t)kTmaCols, (cuuint64_t)m, (cuuint64_t)members};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldy * 2, (cuuint64_t)m * (cuuint64_t)ldy * 2};
+    const cuuint32_t box[3] = {64, 8, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, rank, y, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_NONE,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// members networks (1 for one network) on the same inputs: member e's biases bias_stride
+// floats and its packed weights blob_stride bytes after member e - 1's, its outputs at
+// y + e * m * ldy.
 int forward(const float *x, int32_t m, const float *b1, const float *b2, const float *b3, const float *b4,
-            const void *blob, void *y, int32_t ldy, bool half, void *stream) {
+            const void *blob, void *y, int32_t ldy, bool half, void *stream, int members = 1, int bias_stride = 0,
+            long long blob_stride = 0) {
     const int align = half ? 8 : 4;   // 16-byte row starts
     if (!x || !b1 || !b2 || !b3 || !b4 || !blob || !y || m < 0 || ldy < FO || (ldy % align) != 0)
         return MCW_MLP_ERR_ARG;
     if ((((uintptr_t)blob | (uintptr_t)y) & 15) != 0) return MCW_MLP_ERR_ARG;
+    if (members < 1 || (members > 1 && (bias_stride < 0 || blob_stride <= 0 || (blob_stride & 15) != 0)))
+        return MCW_MLP_ERR_ARG;
     if (m == 0) return 0;
     unsigned int *err = tc_err_flag();
     if (!err) return MCW_MLP_ERR_CUDA;
-    const void *fn = half ? reinterpret_cast<const void *>(mlp_fused_kernel<true>)
+    const void *fn = half ? (members > 1 ? reinterpret_cast<const void *>(mlp_fused_ensemble_kernel)
+                                         : reinterpret_cast<const void *>(mlp_fused_kernel<true>))
                           : reinterpret_cast<const void *>(mlp_fused_kernel<false>);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes);
     if (e != cudaSuccess) return MCW_MLP_ERR_CUDA;
-    const unsigned grid = (unsigned)((m + FM * kTiles - 1) / (FM * kTiles));
+    const int tiles = (m + FM * kTiles - 1) / (FM * kTiles);
+    if ((long long)tiles * members > 0x7fffffffLL) return MCW_MLP_ERR_ARG;
+    const unsigned grid = (unsigned)(tiles * members);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     const unsigned char *wb = static_cast<const unsigned char *>(blob);
     CUtensorMap ymap;
     memset(&ymap, 0, sizeof(ymap));
-    const int use_tma = (half && MCW_FUSED_TMA_OUT && make_out_map(&ymap, y, m, ldy)) ? 1 : 0;
-    if (half)
+    const int use_tma = (half && MCW_FUSED_TMA_OUT && make_out_map(&ymap, y, m, ldy, members)) ? 1 : 0;
+    if (half && members > 1)
+        mlp_fused_ensemble_kernel<<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err, ymap,
+                                                                     use_tma, tiles, bias_stride, blob_stride);
+    else if (half)
         mlp_fused_kernel<true><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err, ymap, use_tma);
     else
         mlp_fused_kernel<false><<<grid, kThreads, kSmemBytes, s>>>(x, m, b1, b2, b3, b4, wb, y, ldy, err, ymap, 0);
@@ -842,6 +900,13 @@ int mcw_mlp_forward(const float *x, int32_t m, const float *b1, const float *b2,
 int mcw_mlp_forward_f16(const float *x, int32_t m, const float *b1, const float *b2, const float *b3,
                         const float *b4, const void *blob, void *y, int32_t ldy, void *stream) {
     return forward(x, m, b1, b2, b3, b4, blob, y, ldy, true, stream);
+}
+
+int mcw_mlp_forward_ensemble_f16(const float *x, int32_t m, int32_t members, const float *bias, const void *blob,
+                                 void *y, int32_t ldy, void *stream) {
+    if (!bias || members < 1) return MCW_MLP_ERR_ARG;
+    return forward(x, m, bias, bias + 256, bias + 512, bias + 768, blob, y, ldy, true, stream, members,
+                   MCW_MLP_BIAS_FLOATS, (long long)MCW_MLP_PACK_BYTES);
 }
 
 }  // extern "C"

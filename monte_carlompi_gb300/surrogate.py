@@ -141,6 +141,22 @@ def forward_fused(torch, x, w16, biases, blob, half=False):
     return y[:, :DIMS[-1]]
 
 
+def forward_ensemble(torch, x, blob, bias, members):
+    """Inference of an ensemble's members on the same inputs in one launch
+    (mcw_mlp_forward_ensemble_f16): blob holds the members' packed weights one after the
+    other (members x MLP_PACK_BYTES), bias their biases (float32 [members, 1417], b1 | b2 |
+    b3 | b4); returns fp16 [members, m, 649] views of the output rows, each member's equal
+    to forward_fused(half=True) of that member."""
+    x = x.contiguous().float()
+    m = x.shape[0]
+    y = torch.empty((members, m, Y_PITCH_F16), dtype=torch.float16, device=x.device)
+    rc = _abi.load().mcw_mlp_forward_ensemble_f16(_ptr(x), m, members, _ptr(bias), _ptr(blob), _ptr(y),
+                                                  Y_PITCH_F16, _stream(torch))
+    if rc:
+        raise _abi.McwError(rc, 'mcw_mlp_forward_ensemble_f16 failed (m=%d, members=%d)' % (m, members))
+    return y[:, :, :DIMS[-1]]
+
+
 def forward_cached(torch, x16, w16, biases, keep=True):
     """Forward pass on the tensor-core kernels; returns (y fp32, cache for backward).
     keep=False (inference) skips storing the FP32 pre-activations."""
@@ -674,16 +690,34 @@ class Ensemble:
 
     def __init__(self, members):
         self.members = members
+        self._pack = None         # (key, blob of every member's packed weights, their biases)
+
+    def packed(self):
+        """The members' packed weights one after the other and their biases as rows
+        (float32 [members, 1417]), rebuilt when any member's weights change."""
+        import torch
+        key = tuple((m.step, tuple(w.data_ptr() for w in m.w16), tuple(b.data_ptr() for b in m.params[1::2]))
+                    for m in self.members)
+        if self._pack is None or self._pack[0] != key:
+            blob = torch.cat([m.packed() for m in self.members])
+            bias = torch.stack([torch.cat([b.float().reshape(-1) for b in m.params[1::2]]) for m in self.members])
+            self._pack = (key, blob, bias.contiguous())
+        return self._pack[1], self._pack[2]
+
+    def predict_std(self, x):
+        """Every member's standardised outputs for encoded inputs x (torch CUDA float32
+        [n, 4]) in one launch of the fused kernel: fp16 [members, n, 649]."""
+        import torch
+        blob, bias = self.packed()
+        return forward_ensemble(torch, x, blob, bias, len(self.members))
 
     def predict_members(self, raw):
         """Each member's BRF [members, n, 648] and albedo [members, n]."""
         import torch
         x = torch.from_numpy(encode(*np.asarray(raw, np.float64).T)).cuda()
-        outs = []
-        for m in self.members:
-            ys = m.predict_std(x).double() * m.y_std + m.y_mean
-            outs.append(ys.cpu().numpy())
-        outs = np.stack(outs)
+        ys = self.predict_std(x)
+        outs = np.stack([(ys[k].double() * m.y_std + m.y_mean).cpu().numpy()
+                         for k, m in enumerate(self.members)])
         brfs, albs = zip(*[from_target(o) for o in outs])
         return np.stack(brfs), np.stack(albs)
 
@@ -795,21 +829,21 @@ def output_weights():
 def inference_rate(ensemble, batch=65536, reps=20, members=None):
     """BRF predictions per second on the fused tensor-core kernel (CUDA events): every member
     of the ensemble (the mean and spread of a prediction need them all) forwards the same
-    batch; the L2 is flushed before each timed repetition (median over reps)."""
+    batch in one launch (mcw_mlp_forward_ensemble_f16); with members=k, the first k members
+    one launch each.  The L2 is flushed before each timed repetition (median over reps)."""
     import torch
     ms = ensemble.members if members is None else ensemble.members[:members]
     x = torch.rand((batch, 4), device='cuda') * 2 - 1
+    run = ensemble.predict_std if members is None else (lambda v: [m.predict_std(v) for m in ms])
     for _ in range(3):
-        for m in ms:
-            m.predict_std(x)
+        run(x)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device='cuda')
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     times = []
     for _ in range(reps):
         flush.zero_()
         e0.record()
-        for m in ms:
-            m.predict_std(x)
+        run(x)
         e1.record()
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))

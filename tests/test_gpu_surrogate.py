@@ -211,6 +211,32 @@ def test_fused_forward_matches_layerwise_and_float64(m):
     assert (y - y_layer).abs().max().item() < 5e-3 * scale
 
 
+@pytest.mark.parametrize('m', [1000, 1001, 4096])
+def test_ensemble_forward_equals_member_forwards(m):
+    """One launch over three members (mcw_mlp_forward_ensemble_f16) gives each member the
+    bits of its own forward (mcw_mlp_forward_f16), at a row count that is a multiple of the
+    128-row tile, one that is not, and one that is not a multiple of the 8-row output box;
+    the padding columns and rows of the next member are not written."""
+    nets = [_random_net(30 + k) for k in range(3)]
+    ens = surrogate.Ensemble(nets)
+    x = (torch.rand(m, 4, generator=torch.Generator().manual_seed(5)) * 2 - 1).cuda()
+    blob, bias = ens.packed()
+    y = torch.full((3, m, surrogate.Y_PITCH_F16), 3.0, dtype=torch.float16, device='cuda')
+    rc = _abi.load().mcw_mlp_forward_ensemble_f16(surrogate._ptr(x), m, 3, surrogate._ptr(bias),
+                                                  surrogate._ptr(blob), surrogate._ptr(y), surrogate.Y_PITCH_F16,
+                                                  surrogate._stream(torch))
+    assert rc == 0
+    for k, net in enumerate(nets):
+        ref = net.predict_std(x)
+        torch.cuda.synchronize()
+        assert torch.equal(y[k, :, :649], ref), k
+    assert (y[:, :, 649:] == 3.0).all()
+    assert torch.equal(ens.predict_std(x), y[:, :, :649])
+    assert _abi.load().mcw_mlp_forward_ensemble_f16(surrogate._ptr(x), m, 0, surrogate._ptr(bias),
+                                                    surrogate._ptr(blob), surrogate._ptr(y), surrogate.Y_PITCH_F16,
+                                                    surrogate._stream(torch)) == -1
+
+
 def test_fused_forward_leading_dimension_and_repack():
     """Rows land at stride ldy without touching the padding columns or the rows past m;
     after an Adam step the packed weights are rebuilt so inference follows the new weights."""
