@@ -641,6 +641,10 @@ def run_inverse(ens, walker, n_obs):
     obs = obs * (1 + 0.01 * np.random.default_rng(0x5EED0051).standard_normal(obs.shape))
     known = raw[:, 1:]
     noise = dict(obs_photons=1000000, obs_noise=0.01)
+    # warm-up (untimed): the first float64 tensor operations of a fresh process take seconds
+    # on this PyTorch build (their kernels are compiled for the GPU on first use)
+    I.retrieve(ens, walker, obs[:32], known[:32], criterion='r_eff', fallback='correct', **noise)
+    I.retrieve(ens, walker, obs[:32], known[:32], criterion='r_eff', fallback='gn', **noise)
     # residuals weighted by their inverse noise variance; where the ensemble spread of the
     # retrieved r_eff exceeds 2%, the answer is corrected by walks at it (the surrogate's
     # Jacobian, Monte Carlo residuals)
