@@ -376,18 +376,14 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
     float sp, cp;
     __sincosf(kTwoPiF * (u2 - 0.5f), &sp, &cp);
 
-    // after a bottom reflection the direction is drawn about the vertical: the
-    // pole case of mu = (0, 0, 1)
-    const float mx = lamb ? 0.f : P.mux;
-    const float my = lamb ? 0.f : P.muy;
-    const float mz = lamb ? 1.f : P.muz;
-    const float s2 = horiz2(mx, my);
-    float3 g = rotate(mx, my, mz, s2, ct, st, cp, sp, renorm);
-    // pole: the direction is exactly vertical (rare: a branch)
-    if (!(s2 > 0.f)) g = pole_dir(copysignf(1.f, mz), ct, st, cp, sp);
-    const float nx = first ? mx : g.x;
-    const float ny = first ? my : g.y;
-    const float nz = first ? mz : g.z;
+    const float s2 = horiz2(P.mux, P.muy);
+    float3 g = rotate(P.mux, P.muy, P.muz, s2, ct, st, cp, sp, renorm);
+    // the pole case (rare: a branch): the direction is exactly vertical, or it is drawn
+    // about the vertical after a bottom reflection (the pole case of mu = (0, 0, 1))
+    if (lamb || !(s2 > 0.f)) g = pole_dir(lamb ? 1.f : copysignf(1.f, P.muz), ct, st, cp, sp);
+    const float nx = first ? P.mux : g.x;     // a first step is never after a reflection
+    const float ny = first ? P.muy : g.y;
+    const float nz = first ? P.muz : g.z;
 
     const float z0 = P.z;
     // zn = dtau nz + z0 and the path increment dtau / (ext rho) as one pair
@@ -479,13 +475,14 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     // pole case of mu = (0, 0, 1) and is selected afterwards, so only that select
     // sits on the chain between steps.  Same values as step().
     const float s2 = horiz2(P.mux, P.muy);
-    const float3 g = rotate(P.mux, P.muy, P.muz, s2, s.ct_hg, s.st_hg, s.cp, s.sp, renorm);
-    const float3 pd = pole_dir(copysignf(1.f, P.muz), s.ct_hg, s.st_hg, s.cp, s.sp);
-    const float3 ld = pole_dir(1.f, s.ct_l, s.st_l, s.cp, s.sp);
-    const bool pole = !(s2 > 0.f);
-    const float nx = first ? P.mux : (lamb ? ld.x : (pole ? pd.x : g.x));
-    const float ny = first ? P.muy : (lamb ? ld.y : (pole ? pd.y : g.y));
-    const float nz = first ? P.muz : (lamb ? ld.z : (pole ? pd.z : g.z));
+    float3 g = rotate(P.mux, P.muy, P.muz, s2, s.ct_hg, s.st_hg, s.cp, s.sp, renorm);
+    // the first step, a reflected direction and the pole are rare: a branch
+    if (first || lamb || !(s2 > 0.f)) {
+        if (first) g = make_float3(P.mux, P.muy, P.muz);
+        else if (lamb) g = pole_dir(1.f, s.ct_l, s.st_l, s.cp, s.sp);
+        else g = pole_dir(copysignf(1.f, P.muz), s.ct_hg, s.st_hg, s.cp, s.sp);
+    }
+    const float nx = g.x, ny = g.y, nz = g.z;
     const float z0 = P.z;
     const float2 zi = __ffma2_rn(make_float2(dtau, dtau), make_float2(nz, P.inv_ext), make_float2(z0, 0.f));
     float zn = zi.x;
