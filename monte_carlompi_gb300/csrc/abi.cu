@@ -418,6 +418,9 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &l
     wa.keys = philox_schedule(seed);
     wa.drain_count = &cn->drain_count;
     wa.drain_next = &cn->drain_next;
+    wa.deep = 1;
+    for (const DevConfig &c : plan.cfgs)
+        if (!(c.tau_tot_d >= kDeepTau)) wa.deep = 0;
     return wa;
 }
 

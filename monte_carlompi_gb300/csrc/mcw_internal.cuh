@@ -141,7 +141,12 @@ struct WalkArgs {
     int32_t drain_from;
     uint32_t drain_cap;          // slots in drain (grid * block)
     const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
+    int32_t deep;                // every config's optical depth >= kDeepTau: the kernel instance
+                                 // whose steps branch on the (rare) bottom crossing; same records
 };
+
+// Optical depth from which a slab counts as deep for WalkArgs::deep.
+constexpr double kDeepTau = 32.0;
 
 struct ReplayArgs {
     const DevConfig *cfgs;

@@ -347,16 +347,51 @@ __device__ __forceinline__ float3 pole_dir(const float sg, const float ct, const
     return make_float3(__fmul_rn(st, cp), __fmul_rn(__fmul_rn(sg, st), sp), __fmul_rn(sg, ct));
 }
 
+// The end of a step's move (monte_carlo3D.py:1390-1466): the exit correction of the path
+// at the top or bottom (:1390-1459), the clamp at the bottom and the reflectance draw of
+// a Lambertian bottom (:1422, :1453; the step's absorption word, since a step that
+// reaches the bottom is never tested for absorption), else the absorption test
+// (:1461-1466).  Returns the end condition (0: walking on, or reflected).  kDeep: the
+// bottom branch is rare in the warp and is a branch; otherwise every alternative is
+// evaluated and selected.  Both give the same values.
+template <bool kDeep>
+__device__ __forceinline__ int boundary(Photon &P, float &zn, const float z0, const float inc, const float u4,
+                                        const float coalb, const bool top, const bool bot, const bool first,
+                                        const bool imp) {
+    if (kDeep) {
+        P.flags &= ~kFlagReflect;
+        if (bot) {
+            P.path = fmaf(-__fdividef(zn + P.tau, zn - z0), inc, P.path);
+            zn = -P.tau;
+            const bool refl = (P.flags & kFlagLamBottom) && u4 < P.R;
+            if (refl) P.flags |= kFlagReflect;
+            return refl ? 0 : (first ? 3 : 2);
+        }
+        if (top) P.path = fmaf(-__fdividef(zn, zn - z0), inc, P.path);
+        return top ? 1 : ((u4 < coalb) ? (imp ? 5 : 4) : 0);
+    }
+    const float2 fd = __fadd2_rn(make_float2(zn, zn), make_float2(P.tau, -z0));
+    const float frac = __fdividef(top ? zn : fd.x, fd.y);
+    if (top || bot) P.path = fmaf(-frac, inc, P.path);
+    zn = bot ? -P.tau : zn;
+    const bool refl = bot && (P.flags & kFlagLamBottom) && u4 < P.R;
+    P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
+    const bool absorb = u4 < coalb;
+    return top ? 1 : (bot ? (refl ? 0 : (first ? 3 : 2)) : (absorb ? (imp ? 5 : 4) : 0));
+}
+
 // One scatter event (monte_carlo3D.py:1213-1466) with its step block r =
 // Philox(step P.i + 1, photon) already computed.  Returns the end condition
 // (0 = still walking).  The alternatives of the reference's branches (first
 // step, Lambertian direction, pole, general rotation; top, bottom, absorption)
 // are evaluated together and selected, so the step is one straight dependency
 // chain; only the rare bottom-reflection draw branches.
-template <bool kImpurity>
+template <bool kImpurity, bool kDeep>
 // may_first: this step can be a photon's first (photons start on a round edge, so only
 // a round's step 0 can; a constant at every call, so the first-step selects of the
-// other steps compile away).
+// other steps compile away).  kDeep: every slab of the launch is optically deep, so a
+// bottom crossing is rare in a warp and takes a branch; otherwise selects.  The values
+// are the same either way.
 __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm,
                                     const bool may_first) {
     P.i += 1;
@@ -409,18 +444,11 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
 
     const bool top = zn > 0.f;                                  // :1390-1397
     const bool bot = zn < -P.tau;                               // :1399-1459
-    const float2 fd = __fadd2_rn(make_float2(zn, zn), make_float2(P.tau, -z0));
-    const float frac = __fdividef(top ? zn : fd.x, fd.y);
-    if (top || bot) P.path = fmaf(-frac, inc, P.path);
-    zn = bot ? -P.tau : zn;
     // r.w is the absorption draw; a step that reaches the bottom is never tested
     // for absorption (the reference's elif chain), so there it is the
     // Lambertian-bottom reflectance draw (:1422, :1453)
     const float u4 = uu.w;
-    const bool refl = bot && (P.flags & kFlagLamBottom) && u4 < P.R;
-    P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
-    const bool absorb = u4 < coalb;                             // :1461-1466
-    const int cond = top ? 1 : (bot ? (refl ? 0 : (first ? 3 : 2)) : (absorb ? (imp ? 5 : 4) : 0));
+    const int cond = boundary<kDeep>(P, zn, z0, inc, u4, coalb, top, bot, first, imp);
     P.mux = nx;
     P.muy = ny;
     P.muz = nz;
@@ -463,6 +491,7 @@ __device__ __forceinline__ bool impurity_draw(uint64_t rid, uint32_t n, float p_
     return ((float)r2.x * kTwo32Inv) < p_imp;
 }
 
+template <bool kDeep>
 __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool imp, const bool renorm,
                                          const bool may_first) {
     P.i += 1;
@@ -496,14 +525,7 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     const float coalb = imp ? P.coalb_imp : P.coalb_ice;       // 1 - R on a Lambertian surface
     const bool top = zn > 0.f;
     const bool bot = zn < -P.tau;
-    const float2 fd = __fadd2_rn(make_float2(zn, zn), make_float2(P.tau, -z0));
-    const float frac = __fdividef(top ? zn : fd.x, fd.y);
-    if (top || bot) P.path = fmaf(-frac, inc, P.path);
-    zn = bot ? -P.tau : zn;
-    const bool refl = bot && (P.flags & kFlagLamBottom) && s.u4 < P.R;
-    P.flags = (P.flags & ~kFlagReflect) | (refl ? kFlagReflect : 0u);
-    const bool absorb = s.u4 < coalb;
-    const int cond = top ? 1 : (bot ? (refl ? 0 : (first ? 3 : 2)) : (absorb ? (imp ? 5 : 4) : 0));
+    const int cond = boundary<kDeep>(P, zn, z0, inc, s.u4, coalb, top, bot, first, imp);
     P.mux = nx;
     P.muy = ny;
     P.muz = nz;
@@ -521,7 +543,7 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
 // condition.  S is a multiple of kStepsPerRound and rounds start at a multiple of
 // it, so renormalisation falls on the same steps as in the dense rounds and the
 // records are bit-identical.
-template <bool kImpurity>
+template <bool kImpurity, bool kDeep>
 __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsigned act, const int n_act,
                                             const int lane, const unsigned lt_mask, const WalkArgs &a) {
     // 1 <= n_act <= kSparseWarp; S = 2^ls
@@ -579,7 +601,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
                 st.sp = ys[u].x, st.cp = ys[u].y, st.dtau = ys[u].z, st.u4 = ys[u].w;
                 const bool alive = cond == 0;
                 Photon Q = P;
-                const int c = step_post(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
+                const int c = step_post<kDeep>(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
                 P.i = alive ? Q.i : P.i;
                 P.mux = alive ? Q.mux : P.mux;
                 P.muy = alive ? Q.muy : P.muy;
@@ -1084,7 +1106,8 @@ __device__ __noinline__ void finish_batch(const FinishSlot *fin, WarpTally &tall
     }
 }
 
-template <bool kImpurity>
+// kDeep: every slab of the launch is optically deep (WalkArgs::deep; see boundary()).
+template <bool kImpurity, bool kDeep>
 __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -1195,7 +1218,7 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         const int n_act = __popc(act);
         int cond = 0;
         if (n_act <= kSparseWarp) {
-            if (n_act > 0) cond = sparse_round<kImpurity>(P, q, act, n_act, lane, lt_mask, a);
+            if (n_act > 0) cond = sparse_round<kImpurity, kDeep>(P, q, act, n_act, lane, lt_mask, a);
         } else if (me_active) {
             uint4 rb[kStepsPerRound];
             const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
@@ -1207,7 +1230,7 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
                 // a lane whose photon ended earlier in the round keeps its final state
                 const bool alive = cond == 0;
                 Photon Q = P;
-                const int c = step<kImpurity>(Q, a, rb[k], k == kStepsPerRound - 1, k == 0);
+                const int c = step<kImpurity, kDeep>(Q, a, rb[k], k == kStepsPerRound - 1, k == 0);
                 // a finished photon's record uses i, the direction and the path only;
                 // its z, flags and path compensation are never read again
                 P.i = alive ? Q.i : P.i;
@@ -1389,10 +1412,14 @@ cudaError_t allow_smem() {
     if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> g(m);
     if (done.count(dev)) return cudaSuccess;
-    e = cudaFuncSetAttribute(walk_f32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(walk_f32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess) done.insert(dev);
+    for (const void *fn : {reinterpret_cast<const void *>(walk_f32_kernel<false, false>),
+                           reinterpret_cast<const void *>(walk_f32_kernel<true, false>),
+                           reinterpret_cast<const void *>(walk_f32_kernel<false, true>),
+                           reinterpret_cast<const void *>(walk_f32_kernel<true, true>)}) {
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess) return e;
+    }
+    done.insert(dev);
     return e;
 }
 
@@ -1416,9 +1443,10 @@ int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity) {
         if (it != cache.end()) return it->second;
     }
     int n = 0;
+    // the deep-slab instances have the same register count (checked with -Xptxas -v)
     const cudaError_t e = impurity
-        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<true>, block, smem)
-        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<false>, block, smem);
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<true, false>, block, smem)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, walk_f32_kernel<false, false>, block, smem);
     if (e != cudaSuccess) return 0;
     std::lock_guard<std::mutex> g(m);
     cache[key] = n;
@@ -1426,16 +1454,24 @@ int walk_f32_max_blocks_per_sm(int block, int n_cfg, bool impurity) {
 }
 
 bool walk_f32_is_kernel(const void *fn) {
-    return fn == reinterpret_cast<const void *>(walk_f32_kernel<false>) ||
-           fn == reinterpret_cast<const void *>(walk_f32_kernel<true>) ||
+    return fn == reinterpret_cast<const void *>(walk_f32_kernel<false, false>) ||
+           fn == reinterpret_cast<const void *>(walk_f32_kernel<true, false>) ||
+           fn == reinterpret_cast<const void *>(walk_f32_kernel<false, true>) ||
+           fn == reinterpret_cast<const void *>(walk_f32_kernel<true, true>) ||
            fn == reinterpret_cast<const void *>(drain_kernel);
 }
 
 cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s) {
     cudaError_t e = allow_smem();
     if (e != cudaSuccess) return e;
-    if (impurity) walk_f32_kernel<true><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
-    else walk_f32_kernel<false><<<grid, block, smem_bytes(block, a.n_cfg), s>>>(a);
+    const size_t smem = smem_bytes(block, a.n_cfg);
+    if (a.deep) {
+        if (impurity) walk_f32_kernel<true, true><<<grid, block, smem, s>>>(a);
+        else walk_f32_kernel<false, true><<<grid, block, smem, s>>>(a);
+    } else {
+        if (impurity) walk_f32_kernel<true, false><<<grid, block, smem, s>>>(a);
+        else walk_f32_kernel<false, false><<<grid, block, smem, s>>>(a);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess || a.drain_from <= 0 || !a.drain) return e;
     // the drain kernel: as many blocks as fit at once, each taking the handed-over
