@@ -80,6 +80,9 @@ struct Plan {
     int64_t total = 0;
     int32_t lut_total = 0;
     bool impurity = false;  // some config has imp_cnc > 0
+    // the deep-slab kernel instance (WalkArgs::deep): the configs with tau < kDeepTau
+    // hold at most a fifth of the expected scatter events (records do not depend on it)
+    bool deep = false;
 };
 
 struct Counters {
@@ -237,6 +240,20 @@ void make_claim_order(const mcw_ctx *ctx, const mcw_config *cfgs, Plan &plan) {
                      [&](int32_t a, int32_t b) { return key[a] > key[b]; });
     plan.claim_prefix.assign(n + 1, 0);
     for (int32_t k = 0; k < n; ++k) plan.claim_prefix[k + 1] = plan.claim_prefix[k] + plan.cfgs[plan.claim_cfg[k]].n_photon;
+    // deep-slab instance: the thin configs' share of the expected events (photons x
+    // expected walk length) is small; one config: its own depth
+    if (n == 1 || ctx->h_ice.empty()) {
+        plan.deep = true;
+        for (const DevConfig &c : plan.cfgs) plan.deep = plan.deep && c.tau_tot_d >= kDeepTau;
+    } else {
+        double thin = 0.0, all = 0.0;
+        for (int32_t i = 0; i < n; ++i) {
+            const double w = (double)plan.cfgs[i].n_photon * key[i];
+            all += w;
+            if (!(plan.cfgs[i].tau_tot_d >= kDeepTau)) thin += w;
+        }
+        plan.deep = thin <= 0.2 * all;
+    }
 }
 
 int make_plan(mcw_ctx *ctx, const mcw_config *cfgs, int32_t n_cfg, int32_t mode, Plan &plan) {
@@ -418,9 +435,7 @@ WalkArgs walk_args(const mcw_ctx *ctx, const Plan &plan, DevBuf &cfgs, DevBuf &l
     wa.keys = philox_schedule(seed);
     wa.drain_count = &cn->drain_count;
     wa.drain_next = &cn->drain_next;
-    wa.deep = 1;
-    for (const DevConfig &c : plan.cfgs)
-        if (!(c.tau_tot_d >= kDeepTau)) wa.deep = 0;
+    wa.deep = plan.deep ? 1 : 0;
     return wa;
 }
 

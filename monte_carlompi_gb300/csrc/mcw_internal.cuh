@@ -141,8 +141,9 @@ struct WalkArgs {
     int32_t drain_from;
     uint32_t drain_cap;          // slots in drain (grid * block)
     const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
-    int32_t deep;                // every config's optical depth >= kDeepTau: the kernel instance
-                                 // whose steps branch on the (rare) bottom crossing; same records
+    int32_t deep;                // slabs optically deep (tau >= kDeepTau) for most of the scatter
+                                 // events of the launch: the kernel instance whose steps branch on
+                                 // the (rare) bottom crossing; the records are the same either way
 };
 
 // Optical depth from which a slab counts as deep for WalkArgs::deep.
