@@ -582,9 +582,8 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
     __syncwarp();
     int cond = 0;
     if (me) {
-        // groups of kStepsPerRound steps, branch-free inside a group as in the dense
-        // rounds (a lane whose photon ended keeps its final state), so one step's
-        // rotation overlaps the previous step's boundary tests
+        // groups of kStepsPerRound steps (renormalised on a group's last step, as in the
+        // dense rounds)
         for (int k0 = 0; k0 < S; k0 += kStepsPerRound) {
             if (in_block_mode(P)) break;                        // block mode from kBlockWalk on
             const int t0 = (rank << ls) + k0;
@@ -594,23 +593,16 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
                 xs[u] = q.pbuf[2 * (t0 + u)];
                 ys[u] = q.pbuf[2 * (t0 + u) + 1];
             }
+            // each photon's lane leaves at its end condition (at most kSparseWarp lanes walk
+            // here, so the divergence costs little); the state is the one after that step,
+            // as in the dense rounds
 #pragma unroll
             for (int u = 0; u < kStepsPerRound; ++u) {
                 StepPre st;
                 st.ct_hg = xs[u].x, st.st_hg = xs[u].y, st.ct_l = xs[u].z, st.st_l = xs[u].w;
                 st.sp = ys[u].x, st.cp = ys[u].y, st.dtau = ys[u].z, st.u4 = ys[u].w;
-                const bool alive = cond == 0;
-                Photon Q = P;
-                const int c = step_post<kDeep>(Q, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
-                P.i = alive ? Q.i : P.i;
-                P.mux = alive ? Q.mux : P.mux;
-                P.muy = alive ? Q.muy : P.muy;
-                P.muz = alive ? Q.muz : P.muz;
-                P.path = alive ? Q.path : P.path;
-                P.flags = Q.flags;
-                P.z = Q.z;
-                P.pathc = Q.pathc;
-                cond = alive ? c : cond;
+                cond = step_post<kDeep>(P, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
+                if (cond != 0) break;
             }
             if (cond != 0) break;
         }
