@@ -577,7 +577,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
             if (kImpurity && (m0.w & kFlagImpurity))
                 imp_t = impurity_draw(((uint64_t)m0.y << 32) | m0.x, n, __uint_as_float(m2.y), a);
         }
-        impm |= (uint64_t)__ballot_sync(0xffffffffu, imp_t) << (32 * pass);
+        if (kImpurity) impm |= (uint64_t)__ballot_sync(0xffffffffu, imp_t) << (32 * pass);
     }
     __syncwarp();
     int cond = 0;
@@ -601,7 +601,9 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
                 StepPre st;
                 st.ct_hg = xs[u].x, st.st_hg = xs[u].y, st.ct_l = xs[u].z, st.st_l = xs[u].w;
                 st.sp = ys[u].x, st.cp = ys[u].y, st.dtau = ys[u].z, st.u4 = ys[u].w;
-                cond = step_post<kDeep>(P, st, (impm >> (t0 + u)) & 1u, u == kStepsPerRound - 1, u == 0);
+                // (a constant false in the instance without the species draw)
+                const bool imp = kImpurity && ((impm >> (t0 + u)) & 1u);
+                cond = step_post<kDeep>(P, st, imp, u == kStepsPerRound - 1, u == 0);
                 if (cond != 0) break;
             }
             if (cond != 0) break;
