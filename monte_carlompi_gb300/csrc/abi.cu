@@ -80,8 +80,9 @@ struct Plan {
     int64_t total = 0;
     int32_t lut_total = 0;
     bool impurity = false;  // some config has imp_cnc > 0
-    // the deep-slab kernel instance (WalkArgs::deep): the configs with tau < kDeepTau
-    // hold at most a fifth of the expected scatter events (records do not depend on it)
+    // the deep-slab kernel instance (WalkArgs::deep): no config is a Lambertian surface
+    // and the configs with tau < kDeepTau hold at most a fifth of the expected scatter
+    // events (records do not depend on it)
     bool deep = false;
 };
 
@@ -240,9 +241,14 @@ void make_claim_order(const mcw_ctx *ctx, const mcw_config *cfgs, Plan &plan) {
                      [&](int32_t a, int32_t b) { return key[a] > key[b]; });
     plan.claim_prefix.assign(n + 1, 0);
     for (int32_t k = 0; k < n; ++k) plan.claim_prefix[k + 1] = plan.claim_prefix[k] + plan.cfgs[plan.claim_cfg[k]].n_photon;
-    // deep-slab instance: the thin configs' share of the expected events (photons x
-    // expected walk length) is small; one config: its own depth
-    if (n == 1 || ctx->h_ice.empty()) {
+    // deep-slab instance: no config is a Lambertian surface, and the thin configs' share
+    // of the expected events (photons x expected walk length) is small; one config: its
+    // own depth
+    bool surface = false;
+    for (int32_t i = 0; i < n; ++i) surface = surface || cfgs[i].lambertian_surface;
+    if (surface) {
+        plan.deep = false;
+    } else if (n == 1 || ctx->h_ice.empty()) {
         plan.deep = true;
         for (const DevConfig &c : plan.cfgs) plan.deep = plan.deep && c.tau_tot_d >= kDeepTau;
     } else {

@@ -142,8 +142,9 @@ struct WalkArgs {
     uint32_t drain_cap;          // slots in drain (grid * block)
     const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
     int32_t deep;                // slabs optically deep (tau >= kDeepTau) for most of the scatter
-                                 // events of the launch: the kernel instance whose steps branch on
-                                 // the (rare) bottom crossing; the records are the same either way
+                                 // events of the launch and no Lambertian surface: the kernel
+                                 // instance whose steps branch on the (rare) bottom crossing and
+                                 // carry no surface tests; the records are the same either way
 };
 
 // Optical depth from which a slab counts as deep for WalkArgs::deep.

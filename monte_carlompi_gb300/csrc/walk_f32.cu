@@ -142,8 +142,10 @@ struct Photon {
 
 // A photon walks in block mode (block_pass) from kBlockWalk steps on, except on a
 // Lambertian surface (whose directions do not follow from the previous one).
+// kDeep: no config of the launch is a Lambertian surface (WalkArgs::deep).
+template <bool kDeep>
 __device__ __forceinline__ bool in_block_mode(const Photon &P) {
-    return P.cfg >= 0 && P.i >= kBlockWalk && !(P.flags & kFlagLamSurface);
+    return P.cfg >= 0 && P.i >= kBlockWalk && (kDeep || !(P.flags & kFlagLamSurface));
 }
 
 // A photon handed to the drain queue: kDrainSlot = 6 float4.
@@ -389,16 +391,16 @@ __device__ __forceinline__ int boundary(Photon &P, float &zn, const float z0, co
 template <bool kImpurity, bool kDeep>
 // may_first: this step can be a photon's first (photons start on a round edge, so only
 // a round's step 0 can; a constant at every call, so the first-step selects of the
-// other steps compile away).  kDeep: every slab of the launch is optically deep, so a
-// bottom crossing is rare in a warp and takes a branch; otherwise selects.  The values
-// are the same either way.
+// other steps compile away).  kDeep: the slabs of the launch are optically deep, so a
+// bottom crossing is rare in a warp and takes a branch (otherwise selects), and no config
+// is a Lambertian surface.  The values are the same either way.
 __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r, const bool renorm,
                                     const bool may_first) {
     P.i += 1;
     const float4 uu = step_uniforms(r);
     const float u1 = uu.x, u2 = uu.y, u3 = uu.z;
     const bool first = may_first && (P.i == 1);
-    const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
+    const bool lam_surface = !kDeep && (P.flags & kFlagLamSurface) != 0;   // none in the deep instance
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
 
     const float dtau = (first && lam_surface) ? 0.f : -__logf(u3);
@@ -496,7 +498,7 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
                                          const bool may_first) {
     P.i += 1;
     const bool first = may_first && (P.i == 1);
-    const bool lam_surface = (P.flags & kFlagLamSurface) != 0;
+    const bool lam_surface = !kDeep && (P.flags & kFlagLamSurface) != 0;   // none in the deep instance
     const bool lamb = !first && (lam_surface || (P.flags & kFlagReflect));
     const float dtau = (first && lam_surface) ? 0.f : s.dtau;
     // The HG rotation of the current direction does not wait for `lamb` (which
@@ -585,7 +587,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
         // groups of kStepsPerRound steps (renormalised on a group's last step, as in the
         // dense rounds)
         for (int k0 = 0; k0 < S; k0 += kStepsPerRound) {
-            if (in_block_mode(P)) break;                        // block mode from kBlockWalk on
+            if (in_block_mode<kDeep>(P)) break;                 // block mode from kBlockWalk on
             const int t0 = (rank << ls) + k0;
             float4 xs[kStepsPerRound], ys[kStepsPerRound];
 #pragma unroll
@@ -1100,7 +1102,8 @@ __device__ __noinline__ void finish_batch(const FinishSlot *fin, WarpTally &tall
     }
 }
 
-// kDeep: every slab of the launch is optically deep (WalkArgs::deep; see boundary()).
+// kDeep: the slabs of the launch are optically deep and none is a Lambertian surface
+// (WalkArgs::deep; see boundary()).
 template <bool kImpurity, bool kDeep>
 __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1183,7 +1186,7 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         // steps go to the queue, walked after this kernel with a thread block each
         // (a lane hands over at most one photon: it takes none afterwards)
         if (a.drain_from > 0 && exhausted && n_birth == 0) {
-            const bool leave = in_block_mode(P) && P.i >= a.drain_from;
+            const bool leave = in_block_mode<kDeep>(P) && P.i >= a.drain_from;
             const unsigned lm = __ballot_sync(0xffffffffu, leave);
             if (lm) {
                 unsigned base = 0;
@@ -1206,7 +1209,7 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         // ---- kStepsPerRound scatter events per active lane of a well-filled warp;
         // their Philox blocks are independent of the walk, so they are computed
         // together first.  A sparse warp runs sparse_round instead.
-        const unsigned bmask = __ballot_sync(0xffffffffu, in_block_mode(P));
+        const unsigned bmask = __ballot_sync(0xffffffffu, in_block_mode<kDeep>(P));
         const unsigned act = ~idle & ~bmask;
         const bool me_active = (act >> lane) & 1u;
         const int n_act = __popc(act);
