@@ -81,8 +81,8 @@ struct Plan {
     int32_t lut_total = 0;
     bool impurity = false;  // some config has imp_cnc > 0
     // the deep-slab kernel instance (WalkArgs::deep): no config is a Lambertian surface
-    // and the configs with tau < kDeepTau hold at most a fifth of the expected scatter
-    // events (records do not depend on it)
+    // or scatters isotropically, and the configs with tau < kDeepTau hold at most a fifth
+    // of the expected scatter events (records do not depend on it)
     bool deep = false;
 };
 
@@ -111,6 +111,9 @@ struct mcw_ctx {
     // host copy of the device tables (the claim order's estimate of walk lengths)
     std::vector<double> h_tab;
     std::vector<DevTable> h_ice;                   // offsets into h_tab (pointers unused)
+    // per ice table: every asymmetry parameter is of one sign and at least 1e-3 away from
+    // 0, so no photon scatters isotropically (the deep-slab instance's HG step)
+    std::vector<char> h_ice_aniso;
     // phase matrices of the polarised walk, one per ice table (n_rows 0 = none)
     DevBuf phasedata, phase_tables, phasedata32, phase_tables32, phase_seeds;
     std::vector<int32_t> phase_rows;
@@ -244,8 +247,17 @@ void make_claim_order(const mcw_ctx *ctx, const mcw_config *cfgs, Plan &plan) {
     // deep-slab instance: no config is a Lambertian surface, and the thin configs' share
     // of the expected events (photons x expected walk length) is small; one config: its
     // own depth
+    // and no photon scatters isotropically (the asymmetry parameter of every config away
+    // from 0: its override, or every value of its ice table)
     bool surface = false;
-    for (int32_t i = 0; i < n; ++i) surface = surface || cfgs[i].lambertian_surface;
+    for (int32_t i = 0; i < n; ++i) {
+        surface = surface || cfgs[i].lambertian_surface;
+        const double g = cfgs[i].g_override;
+        const bool aniso = std::isnan(g) ? (cfgs[i].ice_table >= 0 && cfgs[i].ice_table < (int32_t)ctx->h_ice_aniso.size() &&
+                                            ctx->h_ice_aniso[cfgs[i].ice_table])
+                                         : std::fabs(g) > 1e-3;
+        surface = surface || !aniso;
+    }
     if (surface) {
         plan.deep = false;
     } else if (n == 1 || ctx->h_ice.empty()) {
@@ -598,6 +610,15 @@ int mcw_set_tables(mcw_ctx *ctx, const mcw_ssp_table *ice, int32_t n_ice, const 
     CUDA_TRY(ctx, cudaMemcpy(ctx->ice_tables.p, tabs.data(), n_ice * sizeof(DevTable), cudaMemcpyHostToDevice));
     ctx->h_tab = host;
     ctx->h_ice = tabs;
+    ctx->h_ice_aniso.assign(n_ice, 0);
+    for (int32_t i = 0; i < n_ice; ++i) {
+        bool pos = true, neg = true;
+        for (int32_t k = 0; k < ice[i].n; ++k) {
+            pos = pos && ice[i].asm_prm[k] > 1e-3;
+            neg = neg && ice[i].asm_prm[k] < -1e-3;
+        }
+        ctx->h_ice_aniso[i] = (pos || neg) ? 1 : 0;
+    }
     ctx->imp = dimp;
     ctx->n_ice = n_ice;
     ctx->max_ice_n = 0;

@@ -142,9 +142,10 @@ struct WalkArgs {
     uint32_t drain_cap;          // slots in drain (grid * block)
     const DevPhase32 *phase;     // FP32 polarised walk: per ice table (records are mcw_record32p)
     int32_t deep;                // slabs optically deep (tau >= kDeepTau) for most of the scatter
-                                 // events of the launch and no Lambertian surface: the kernel
-                                 // instance whose steps branch on the (rare) bottom crossing and
-                                 // carry no surface tests; the records are the same either way
+                                 // events of the launch, no Lambertian surface and no isotropic
+                                 // scattering: the kernel instance whose steps branch on the
+                                 // (rare) bottom crossing and carry no surface or isotropic
+                                 // alternatives; the records are the same either way
 };
 
 // Optical depth from which a slab counts as deep for WalkArgs::deep.

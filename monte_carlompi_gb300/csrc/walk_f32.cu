@@ -300,9 +300,15 @@ __device__ __forceinline__ float4 step_uniforms(const uint4 r) {
 }
 
 // Henyey-Greenstein scattering cosine by inversion (monte_carlo3D.py:915), or
-// 1 - 2u when isotropic (hg_d == 0).
+// 1 - 2u when isotropic (hg_d == 0).  kAniso: no photon of the launch is isotropic
+// (WalkArgs::deep), the same value without the isotropic alternative.
+template <bool kAniso = false>
 __device__ __forceinline__ float hg_cos(const float u1, const float hg_a, const float hg_b, const float hg_c,
                                         const float hg_d, const float hg_e) {
+    if (kAniso) {
+        const float t = __fdividef(hg_b, fmaf(hg_d, u1, hg_c));
+        return __fmul_rn(hg_e, fmaf(-t, t, hg_a));
+    }
     const float2 d = __ffma2_rn(make_float2(hg_d, -2.f), make_float2(u1, u1), make_float2(hg_c, 1.f));
     const float t = __fdividef(hg_b, d.x);
     return (hg_d != 0.f) ? __fmul_rn(hg_e, fmaf(-t, t, hg_a)) : d.y;
@@ -407,7 +413,7 @@ __device__ __forceinline__ int step(Photon &P, const WalkArgs &a, const uint4 r,
 
     // scattering cosine: HG inversion (isotropic when hg_d == 0), or the
     // Lambertian cos = sqrt(u) after a bottom reflection
-    float ct = hg_cos(u1, P.hg_a, P.hg_b, P.hg_c, P.hg_d, P.hg_e);
+    float ct = hg_cos<kDeep>(u1, P.hg_a, P.hg_b, P.hg_c, P.hg_d, P.hg_e);
     if (lamb) ct = sqrtf(u1);                                   // rare: a branch, not a select
     const float st = sin_of(ct);
     float sp, cp;
@@ -473,12 +479,13 @@ struct StepPre {
 };
 
 // hg = (hg_a, hg_b, hg_c, hg_d) and hg_e of the photon (Photon::hg_*).
+template <bool kDeep>
 __device__ __forceinline__ StepPre step_pre(const uint4 r, const float4 hg, const float hg_e) {
     StepPre o;
     const float4 uu = step_uniforms(r);
     const float u1 = uu.x, u2 = uu.y, u3 = uu.z;
     o.dtau = -__logf(u3);
-    o.ct_hg = hg_cos(u1, hg.x, hg.y, hg.z, hg.w, hg_e);
+    o.ct_hg = hg_cos<kDeep>(u1, hg.x, hg.y, hg.z, hg.w, hg_e);
     o.st_hg = sin_of(o.ct_hg);
     o.ct_l = sqrtf(u1);
     o.st_l = sin_of(o.ct_l);
@@ -571,7 +578,7 @@ __device__ __forceinline__ int sparse_round(Photon &P, WarpQueues &q, const unsi
             const uint4 m0 = q.rmeta[3 * j], m1 = q.rmeta[3 * j + 1], m2 = q.rmeta[3 * j + 2];
             const uint32_t n = m0.z + 1u + (uint32_t)k;
             const uint4 r = philox10(make_uint4(n, kTagStep, m0.x, m0.y), a.keys);
-            const StepPre t = step_pre(r, make_float4(__uint_as_float(m1.x), __uint_as_float(m1.y),
+            const StepPre t = step_pre<kDeep>(r, make_float4(__uint_as_float(m1.x), __uint_as_float(m1.y),
                                                       __uint_as_float(m1.z), __uint_as_float(m1.w)),
                                        __uint_as_float(m2.x));
             q.pbuf[2 * e] = make_float4(t.ct_hg, t.st_hg, t.ct_l, t.st_l);
@@ -1102,8 +1109,8 @@ __device__ __noinline__ void finish_batch(const FinishSlot *fin, WarpTally &tall
     }
 }
 
-// kDeep: the slabs of the launch are optically deep and none is a Lambertian surface
-// (WalkArgs::deep; see boundary()).
+// kDeep: the slabs of the launch are optically deep, none is a Lambertian surface and no
+// photon scatters isotropically (WalkArgs::deep; see boundary()).
 template <bool kImpurity, bool kDeep>
 __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
