@@ -748,7 +748,8 @@ struct LaneSteps {
 // Draw steps s0 .. s0 + LS - 1 of photon Q; lamb: the first of them takes
 // the Lambertian direction about the vertical (the first step after a bottom
 // reflection, :1238-1250).
-template <int LS>
+// kImp: the launch has impurity configs; kDeep: the deep-slab instance (no isotropic photon).
+template <int LS, bool kImp, bool kDeep>
 __device__ __forceinline__ void lane_draw(LaneSteps<LS> &L, const Photon &Q, uint32_t s0, bool lamb, const WalkArgs &a) {
     L.absm = L.reflm = L.impm = 0;
 #pragma unroll
@@ -757,13 +758,13 @@ __device__ __forceinline__ void lane_draw(LaneSteps<LS> &L, const Photon &Q, uin
         const uint4 r = philox10(make_uint4(n, kTagStep, (uint32_t)Q.rid, (uint32_t)(Q.rid >> 32)), a.keys);
         const float4 uu = step_uniforms(r);
         L.dtau[t] = -__logf(uu.z);                                      // :1014
-        const bool imp = (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
+        const bool imp = kImp && (Q.flags & kFlagImpurity) && impurity_draw(Q.rid, n, Q.p_imp, a);
         // absorption as 1 - u < 1 - ssa (:1461-1466); on a bottom crossing the same
         // word is the reflectance draw
         L.absm |= (uu.w < (imp ? Q.coalb_imp : Q.coalb_ice) ? 1u : 0u) << t;
         L.reflm |= (uu.w < Q.R ? 1u : 0u) << t;
-        L.impm |= (imp ? 1u : 0u) << t;
-        const float ct = (lamb && t == 0) ? sqrtf(uu.x) : hg_cos(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
+        if (kImp) L.impm |= (imp ? 1u : 0u) << t;
+        const float ct = (lamb && t == 0) ? sqrtf(uu.x) : hg_cos<kDeep>(uu.x, Q.hg_a, Q.hg_b, Q.hg_c, Q.hg_d, Q.hg_e);
         const float ch = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fadd_rn(1.f, ct))));  // cos(theta / 2)
         const float sh = sqrtf(fmaxf(0.f, __fmul_rn(0.5f, __fsub_rn(1.f, ct))));  // sin(theta / 2)
         float sph, cph;                                                 // half the azimuth, uniform
@@ -904,7 +905,7 @@ __device__ __forceinline__ int pass_end(Photon &Q, int adv, bool ev, const float
 // One block pass over photon Q, held alike by every lane of the warp, the chunks
 // walked one after the other until the first with an event.  Q is updated alike
 // on every lane; returns the end condition.  Warp-collective.
-template <int LS>
+template <int LS, bool kImp, bool kDeep>
 __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane) {
     const bool reflected = (Q.flags & kFlagReflect) != 0;
     const PassFrame F = pass_frame(Q, reflected);
@@ -912,7 +913,7 @@ __device__ __forceinline__ int block_pass(Photon &Q, const WalkArgs &a, int lane
     float Wz = 0.f, Wp = 0.f;              // their vertical moves and path increments
     for (int c = 0;; ++c) {
         LaneSteps<LS> L;
-        lane_draw<LS>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * c + LS * lane),
+        lane_draw<LS, kImp, kDeep>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * c + LS * lane),
                   reflected && c == 0 && lane == 0, a);
         const float4 qi = warp_scan_q(lane_product<LS>(L), lane);
         float4 xl = shfl_q(qi, (lane + 31) & 31);
@@ -955,12 +956,12 @@ struct CtaPassShared {
 // One block pass over photon Q, held alike by every thread of a block of
 // kCtaWalkThreads, warp w taking chunk w: the same arithmetic as block_pass.  Q is
 // updated alike on every thread; returns the end condition.  Block-collective.
-template <int LS>
+template <int LS, bool kImp, bool kDeep>
 __device__ __forceinline__ int cta_pass(Photon &Q, const WalkArgs &a, CtaPassShared &S, int warp, int lane) {
     const bool reflected = (Q.flags & kFlagReflect) != 0;
     const PassFrame F = pass_frame(Q, reflected);
     LaneSteps<LS> L;
-    lane_draw<LS>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * warp + LS * lane),
+    lane_draw<LS, kImp, kDeep>(L, Q, (uint32_t)Q.i + 1u + (uint32_t)((32 * LS) * warp + LS * lane),
               reflected && warp == 0 && lane == 0, a);
     const float4 qi = warp_scan_q(lane_product<LS>(L), lane);
     if (lane == 31) S.wq[warp] = qi;
@@ -1256,9 +1257,10 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
             Photon Q = shfl_photon(P, src);
             int c;
             if constexpr (kLongLaneSteps != kLaneSteps)
-                c = Q.i >= kLongWalk ? block_pass<kLongLaneSteps>(Q, a, lane) : block_pass<kLaneSteps>(Q, a, lane);
+                c = Q.i >= kLongWalk ? block_pass<kLongLaneSteps, kImpurity, kDeep>(Q, a, lane)
+                                     : block_pass<kLaneSteps, kImpurity, kDeep>(Q, a, lane);
             else
-                c = block_pass<kLaneSteps>(Q, a, lane);
+                c = block_pass<kLaneSteps, kImpurity, kDeep>(Q, a, lane);
             if (lane == src) {
                 P.i = Q.i;
                 P.flags = Q.flags;
@@ -1330,6 +1332,7 @@ struct DrainBlock {
 // After the walk: every photon handed over to the drain queue is walked to its end
 // by a whole block (cta_pass), one photon after another; finished photons go
 // through warp 0's finish queue.  The queue is complete when this kernel starts.
+template <bool kImp, bool kDeep>
 __global__ void __launch_bounds__(kCtaWalkThreads) drain_kernel(const WalkArgs a) {
     __shared__ DrainBlock S;
     const int lane = threadIdx.x & 31;
@@ -1353,10 +1356,10 @@ __global__ void __launch_bounds__(kCtaWalkThreads) drain_kernel(const WalkArgs a
         bool over = false;
         for (uint32_t pass = 1; cond == 0; ++pass) {
             if constexpr (kLongLaneSteps != kLaneSteps)
-                cond = P.i >= kLongWalk ? cta_pass<kLongLaneSteps>(P, a, S.pass, warp, lane)
-                                        : cta_pass<kLaneSteps>(P, a, S.pass, warp, lane);
+                cond = P.i >= kLongWalk ? cta_pass<kLongLaneSteps, kImp, kDeep>(P, a, S.pass, warp, lane)
+                                        : cta_pass<kLaneSteps, kImp, kDeep>(P, a, S.pass, warp, lane);
             else
-                cond = cta_pass<kLaneSteps>(P, a, S.pass, warp, lane);
+                cond = cta_pass<kLaneSteps, kImp, kDeep>(P, a, S.pass, warp, lane);
             if ((pass & 63u) == 0u) {
                 // time budget (watchdog; never a truncation in normal runs)
                 if (threadIdx.x == 0)
@@ -1462,7 +1465,10 @@ bool walk_f32_is_kernel(const void *fn) {
            fn == reinterpret_cast<const void *>(walk_f32_kernel<true, false>) ||
            fn == reinterpret_cast<const void *>(walk_f32_kernel<false, true>) ||
            fn == reinterpret_cast<const void *>(walk_f32_kernel<true, true>) ||
-           fn == reinterpret_cast<const void *>(drain_kernel);
+           fn == reinterpret_cast<const void *>(drain_kernel<false, false>) ||
+           fn == reinterpret_cast<const void *>(drain_kernel<true, false>) ||
+           fn == reinterpret_cast<const void *>(drain_kernel<false, true>) ||
+           fn == reinterpret_cast<const void *>(drain_kernel<true, true>);
 }
 
 cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int block, int sm_count, cudaStream_t s) {
@@ -1483,12 +1489,20 @@ cudaError_t launch_walk_f32(const WalkArgs &a, bool impurity, int grid, int bloc
     static std::atomic<int> per_sm_cached{0};
     int per_sm = per_sm_cached.load();
     if (per_sm == 0) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drain_kernel, kCtaWalkThreads, 0);
+        // (the four instances hold the same block size and shared memory)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, drain_kernel<true, false>, kCtaWalkThreads, 0);
         if (e != cudaSuccess) return e;
         per_sm = std::max(1, per_sm);
         per_sm_cached.store(per_sm);
     }
-    drain_kernel<<<std::max(1, sm_count) * per_sm, kCtaWalkThreads, 0, s>>>(a);
+    const int dgrid = std::max(1, sm_count) * per_sm;
+    if (a.deep) {
+        if (impurity) drain_kernel<true, true><<<dgrid, kCtaWalkThreads, 0, s>>>(a);
+        else drain_kernel<false, true><<<dgrid, kCtaWalkThreads, 0, s>>>(a);
+    } else {
+        if (impurity) drain_kernel<true, false><<<dgrid, kCtaWalkThreads, 0, s>>>(a);
+        else drain_kernel<false, false><<<dgrid, kCtaWalkThreads, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 
