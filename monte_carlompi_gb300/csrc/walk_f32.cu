@@ -476,6 +476,17 @@ struct StepPre {
     float sp, cp;         // azimuth (:921), uniform on (-pi, pi)
     float dtau;           // optical path -ln u (:1014)
     float u4;             // absorption draw (:1020), or the bottom reflectance draw
+    __device__ __forceinline__ float2 lambertian() const { return make_float2(ct_l, st_l); }
+};
+
+// The same part for the dense rounds, the Lambertian cosine left to the rare
+// reflected step (taken from u1 there: the same sqrt of the same uniform).
+struct StepPreDense {
+    float ct_hg, st_hg, sp, cp, dtau, u4, u1;
+    __device__ __forceinline__ float2 lambertian() const {
+        const float c = sqrtf(u1);
+        return make_float2(c, sin_of(c));
+    }
 };
 
 // hg = (hg_a, hg_b, hg_c, hg_d) and hg_e of the photon (Photon::hg_*).
@@ -494,14 +505,27 @@ __device__ __forceinline__ StepPre step_pre(const uint4 r, const float4 hg, cons
     return o;
 }
 
+template <bool kDeep>
+__device__ __forceinline__ StepPreDense step_pre_dense(const uint4 r, const Photon &P) {
+    StepPreDense o;
+    const float4 uu = step_uniforms(r);
+    o.u1 = uu.x;
+    o.dtau = -__logf(uu.z);
+    o.ct_hg = hg_cos<kDeep>(uu.x, P.hg_a, P.hg_b, P.hg_c, P.hg_d, P.hg_e);
+    o.st_hg = sin_of(o.ct_hg);
+    __sincosf(kTwoPiF * (uu.y - 0.5f), &o.sp, &o.cp);
+    o.u4 = uu.w;
+    return o;
+}
+
 // Ice or impurity for step n (monte_carlo3D.py:1023, :1375-1383), as in step().
 __device__ __forceinline__ bool impurity_draw(uint64_t rid, uint32_t n, float p_imp, const WalkArgs &a) {
     const uint4 r2 = philox10(make_uint4(n, kTagSpecies, (uint32_t)rid, (uint32_t)(rid >> 32)), a.keys);
     return ((float)r2.x * kTwo32Inv) < p_imp;
 }
 
-template <bool kDeep>
-__device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool imp, const bool renorm,
+template <bool kDeep, class Pre>
+__device__ __forceinline__ int step_post(Photon &P, const Pre &s, const bool imp, const bool renorm,
                                          const bool may_first) {
     P.i += 1;
     const bool first = may_first && (P.i == 1);
@@ -517,7 +541,10 @@ __device__ __forceinline__ int step_post(Photon &P, const StepPre &s, const bool
     // the first step, a reflected direction and the pole are rare: a branch
     if (first || lamb || !(s2 > 0.f)) {
         if (first) g = make_float3(P.mux, P.muy, P.muz);
-        else if (lamb) g = pole_dir(1.f, s.ct_l, s.st_l, s.cp, s.sp);
+        else if (lamb) {
+            const float2 l = s.lambertian();
+            g = pole_dir(1.f, l.x, l.y, s.cp, s.sp);
+        }
         else g = pole_dir(copysignf(1.f, P.muz), s.ct_hg, s.st_hg, s.cp, s.sp);
     }
     const float nx = g.x, ny = g.y, nz = g.z;
@@ -1225,17 +1252,34 @@ __global__ void __launch_bounds__(256, 2) walk_f32_kernel(const WalkArgs a) {
         if (n_act <= kSparseWarp) {
             if (n_act > 0) cond = sparse_round<kImpurity, kDeep>(P, q, act, n_act, lane, lt_mask, a);
         } else if (me_active) {
-            uint4 rb[kStepsPerRound];
+            // the deep instance: the direction-independent part of the round's steps
+            // first, then their chains (step_post, the same values as step(): the HG
+            // cosine, azimuth and optical path of step k + 1 do not wait for the chain of
+            // step k behind its rare branches); otherwise the Philox blocks first, then step()
             const uint32_t glo = (uint32_t)P.rid, ghi = (uint32_t)(P.rid >> 32);
+            StepPreDense pre[kDeep ? kStepsPerRound : 1];
+            bool impk[kDeep ? kStepsPerRound : 1];
+            uint4 rb[kDeep ? 1 : kStepsPerRound];
 #pragma unroll
-            for (int k = 0; k < kStepsPerRound; ++k)
-                rb[k] = philox10(make_uint4((uint32_t)P.i + 1u + k, kTagStep, glo, ghi), a.keys);
+            for (int k = 0; k < kStepsPerRound; ++k) {
+                const uint32_t n = (uint32_t)P.i + 1u + k;
+                if constexpr (kDeep) {
+                    pre[k] = step_pre_dense<kDeep>(philox10(make_uint4(n, kTagStep, glo, ghi), a.keys), P);
+                    impk[k] = kImpurity && (P.flags & kFlagImpurity) && impurity_draw(P.rid, n, P.p_imp, a);
+                } else {
+                    rb[k] = philox10(make_uint4(n, kTagStep, glo, ghi), a.keys);
+                }
+            }
 #pragma unroll
             for (int k = 0; k < kStepsPerRound; ++k) {
                 // a lane whose photon ended earlier in the round keeps its final state
                 const bool alive = cond == 0;
                 Photon Q = P;
-                const int c = step<kImpurity, kDeep>(Q, a, rb[k], k == kStepsPerRound - 1, k == 0);
+                int c;
+                if constexpr (kDeep)
+                    c = step_post<kDeep>(Q, pre[k], impk[k], k == kStepsPerRound - 1, k == 0);
+                else
+                    c = step<kImpurity, kDeep>(Q, a, rb[k], k == kStepsPerRound - 1, k == 0);
                 // a finished photon's record uses i, the direction and the path only;
                 // its z, flags and path compensation are never read again
                 P.i = alive ? Q.i : P.i;
