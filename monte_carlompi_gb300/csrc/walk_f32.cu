@@ -390,10 +390,12 @@ __device__ __forceinline__ int boundary(Photon &P, float &zn, const float z0, co
 
 // One scatter event (monte_carlo3D.py:1213-1466) with its step block r =
 // Philox(step P.i + 1, photon) already computed.  Returns the end condition
-// (0 = still walking).  The alternatives of the reference's branches (first
-// step, Lambertian direction, pole, general rotation; top, bottom, absorption)
-// are evaluated together and selected, so the step is one straight dependency
-// chain; only the rare bottom-reflection draw branches.
+// (0 = still walking).  The first step and the general rotation are evaluated
+// together and selected; the Lambertian direction and the pole case are rare
+// branches; top, bottom and absorption are selected (the deep instance branches
+// on the rare bottom crossing, see boundary()).  The dense rounds of the other
+// instances walk with it; the deep instance's dense rounds and every sparse round
+// split it into step_pre / step_pre_dense and step_post, with the same values.
 template <bool kImpurity, bool kDeep>
 // may_first: this step can be a photon's first (photons start on a round edge, so only
 // a round's step 0 can; a constant at every call, so the first-step selects of the
