@@ -541,6 +541,30 @@ def test_batch_first_config_equals_single_run(walker):
                                   single.records['condition'])
 
 
+@pytest.mark.parametrize('imp_cnc', [0.0, 2e-6])
+@pytest.mark.parametrize('general', ['lambertian_surface', 'isotropic'])
+def test_f32_records_independent_of_kernel_instance(walker, imp_cnc, general):
+    """The deep-slab kernel instance (a branch on the bottom crossing, no surface or
+    isotropic alternatives, dense rounds split into the direction-independent part of
+    their steps and the chains) gives the same records and tallies as the general one.
+    A deep slab walked alone takes the deep instance; the same slab next to a
+    Lambertian-surface config, or next to an isotropically scattering one, takes the
+    general instance.  Both species-draw variants (2e-6: ~8% of the photons end on an
+    impurity and ~200 walk past the 256 steps of block mode; ~380 without impurities)."""
+    a, ice, imp = cfg2_geometry(40000)
+    a = dataclasses.replace(a, imp_cnc=imp_cnc)
+    other = (dataclasses.replace(a, lambertian_surface=True, n_photon=2000) if general == 'lambertian_surface'
+             else dataclasses.replace(a, g_override=0.0, n_photon=2000))
+    walker.set_tables([ice], imp)
+    alone = walker.walk([a], 17, mode='f32')
+    mixed = walker.walk([a, other], 17, mode='f32')
+    assert np.array_equal(mixed.records[:a.n_photon], alone.records)
+    for k in ('n_cond', 'q_cond_fx', 'n_events', 'bin_count', 'bin_wvn_fx', 'max_n_scat'):
+        assert np.array_equal(mixed.tallies[0][k], alone.tallies[0][k]), k
+    assert (int(alone.tallies[0]['n_cond'][5]) > 0) == (imp_cnc > 0)
+    assert int((alone.records['n_scat'] > 256).sum()) > 50
+
+
 SWEEP_SAMPLE = [   # (r_eff um, lambda0 um, theta0 deg, depth m): configs of the 64-config sweep's grid
     (100.0, 1.30, 0.0, 0.10), (400.0, 1.60, 45.0, 0.02), (1500.0, 1.10, 60.0, 1.0),
     (50.0, 1.70, 30.0, 0.02), (200.0, 0.95, 0.0, 0.02), (800.0, 1.40, 60.0, 0.10)]
