@@ -479,6 +479,50 @@ def test_records_into_pinned_host_memory(walker):
             lib.mcw_host_free(ptr)
 
 
+def test_pinned_host_records_with_drain_and_two_configs(walker):
+    """Pinned host records of the FP32 walk, written by the kernels themselves, cover
+    every photon: those finished by the drain kernel (weakly absorbing deep snow,
+    handover from 256 steps), two configs in config order (20,003 photons), and a cfg2
+    run of 100,000 photons; each against the same walk into pageable memory (records
+    copied after the kernels), tallies and stats alike."""
+    import ctypes
+    lo, hi = ssp.grid_for(1.0, 0.085)
+    ice = ssp.synthetic_ice_table(50.0, lo, hi)
+    imp = ssp.synthetic_impurity_table(lo, hi)
+    tau = 0.1 * ssp.ext_cff_mss_sphere(50.0) * 300.0
+    weak = WalkConfig(n_photon=3000, wvl0=1.0, half_width=0.085, theta0_deg=30.0, tau_tot=tau,
+                      lambertian_reflectance=0.5)
+    thin = dataclasses.replace(weak, n_photon=17003, tau_tot=4.0, theta0_deg=60.0)
+    c2, ice2, imp2 = cfg2_geometry(100000)
+    lib = _abi.load()
+    saved = walker.get_launch()
+    try:
+        for cfgs, tables, imp_t, launch in (([weak, thin], ice, imp, (256, 0, 8, 256)),
+                                            ([c2], ice2, imp2, (256, 2, 1, 0))):
+            walker.set_tables([tables], imp_t)
+            walker.set_launch(*launch)
+            n = sum(c.n_photon for c in cfgs)
+            nbytes = n * _abi.RECORD32.itemsize
+            ptr = ctypes.c_void_p()
+            _abi.check(lib.mcw_host_alloc(nbytes, ctypes.byref(ptr)), what='host alloc')
+            try:
+                pinned = np.frombuffer((ctypes.c_char * nbytes).from_address(ptr.value),
+                                       dtype=_abi.RECORD32, count=n)
+                for seed in (5, 6):
+                    pinned[:] = np.zeros(1, _abi.RECORD32)
+                    a = walker.walk(cfgs, seed, mode='f32', records='host', out=pinned)
+                    b = walker.walk(cfgs, seed, mode='f32')
+                    assert np.array_equal(pinned, b.records)
+                    assert np.array_equal(a.tallies, b.tallies)
+                    assert a.stats['d2h_bytes'] == b.stats['d2h_bytes']
+                if launch[3]:
+                    assert int(b.records['n_scat'].max()) > 4096   # the drain kernel walked some
+            finally:
+                lib.mcw_host_free(ptr)
+    finally:
+        walker.set_launch(**saved)
+
+
 def test_f32_tallies_agree_with_records(walker):
     cfg, ice, imp = cfg2_geometry(300000, depth=0.02, rds=1500.0)
     walker.set_tables([ice], imp)
